@@ -1,0 +1,375 @@
+/*
+ * lj_gpu.h -- C ABI of the GB300 (sm_103a) rendering hot path for lajolla.
+ *
+ * This is the drop-in boundary.  In the reference renderer the hot path sits
+ * behind three C++ seams:
+ *   - Image3 render(const Scene &scene)                     src/render.h:9
+ *   - intersect()/occluded() over Embree's rtcIntersect1 /
+ *     rtcOccluded1                                           src/intersection.h:39-44,
+ *                                                            src/intersection.cpp:7-85
+ *   - the BSDF / light / phase functors dispatched through
+ *     std::visit                                             src/material.cpp:90-119,
+ *                                                            src/light.cpp:56-77,
+ *                                                            src/phase_function.cpp:30-47
+ * Every entry point below replaces one of them; the comment on each names the
+ * reference interface it stands in for.
+ *
+ * Conventions (all entry points):
+ *   - return LJ_OK (0) on success, a negative LJ_ERR_* code on failure; no C++
+ *     exception ever crosses this boundary (the reference throws fl_exception,
+ *     src/flexception.h:8-24; here that becomes an error code plus
+ *     lj_gpu_last_error()).
+ *   - descriptors are read during the call and copied; the caller keeps
+ *     ownership of every pointer it passes in.
+ *   - all device memory is owned by an lj_ctx or lj_scene handle.
+ *   - a context is used from one host thread at a time; contexts are
+ *     independent of each other.
+ *   - "d_" pointers are device pointers (cudaMalloc'd or torch tensors),
+ *     everything else is host memory.  `stream` is a cudaStream_t (NULL = the
+ *     legacy default stream).
+ *   - every device loop is bounded (BVH stack depth, bounces, null
+ *     collisions); a kernel that reaches a bound writes a status word which
+ *     the host turns into LJ_ERR_DEVICE_LIMIT.
+ */
+#ifndef LJ_GPU_H
+#define LJ_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LJ_GPU_ABI_VERSION 1
+
+/* ---- error codes -------------------------------------------------------- */
+#define LJ_OK                 0
+#define LJ_ERR_INVALID_ARG   -1  /* null handle, bad size, bad enum, bad index */
+#define LJ_ERR_CUDA          -2  /* a CUDA runtime call failed                 */
+#define LJ_ERR_OUT_OF_MEMORY -3  /* device allocation or HBM budget exceeded   */
+#define LJ_ERR_UNSUPPORTED   -4  /* feature not available on this build        */
+#define LJ_ERR_DEVICE_LIMIT  -5  /* a bounded device loop hit its limit        */
+#define LJ_ERR_NO_DEVICE     -6  /* no CUDA device / wrong architecture        */
+#define LJ_ERR_QUEUE_FULL    -7  /* server admission queue is full             */
+#define LJ_ERR_NOT_FOUND     -8  /* unknown job id                             */
+#define LJ_ERR_TIMEOUT       -9  /* a host-side wait ran out of time           */
+#define LJ_ERR_CANCELLED    -10  /* the job was cancelled                      */
+
+typedef struct lj_ctx lj_ctx;
+typedef struct lj_scene lj_scene;
+typedef struct lj_server lj_server;
+
+/* ---- scene description (flat POD view of the reference's Scene) ---------- */
+
+/* Texture<T> variant, src/texture.h:80-113 (ConstantTexture, ImageTexture,
+ * CheckerboardTexture).  Scalar textures use value0[0] / value1[0]. */
+enum { LJ_TEX_CONST = 0, LJ_TEX_IMAGE = 1, LJ_TEX_CHECKER = 2 };
+typedef struct lj_texture_desc {
+    int32_t kind;
+    int32_t image_id;          /* LJ_TEX_IMAGE: index into lj_scene_desc.images */
+    float value0[3];           /* constant value / checkerboard color0          */
+    float value1[3];           /* checkerboard color1                           */
+    float uscale, vscale, uoffset, voffset;
+} lj_texture_desc;             /* 48 bytes */
+
+/* Material variant, same order as src/material.h:102-110. */
+enum {
+    LJ_MAT_LAMBERTIAN = 0,
+    LJ_MAT_ROUGHPLASTIC = 1,
+    LJ_MAT_ROUGHDIELECTRIC = 2,
+    LJ_MAT_DISNEY_DIFFUSE = 3,
+    LJ_MAT_DISNEY_METAL = 4,
+    LJ_MAT_DISNEY_GLASS = 5,
+    LJ_MAT_DISNEY_CLEARCOAT = 6,
+    LJ_MAT_DISNEY_SHEEN = 7,
+    LJ_MAT_DISNEY_BSDF = 8,
+    LJ_MAT_COUNT = 9
+};
+#define LJ_MAT_SLOTS 12
+/* Texture slot meaning per material type (struct member order of
+ * src/material.h:12-100):
+ *   LAMBERTIAN        0 reflectance
+ *   ROUGHPLASTIC      0 diffuse_reflectance 1 specular_reflectance 2 roughness
+ *   ROUGHDIELECTRIC   0 specular_reflectance 1 specular_transmittance 2 roughness
+ *   DISNEY_DIFFUSE    0 base_color 1 roughness 2 subsurface
+ *   DISNEY_METAL      0 base_color 1 roughness 2 anisotropic
+ *   DISNEY_GLASS      0 base_color 1 roughness 2 anisotropic
+ *   DISNEY_CLEARCOAT  0 clearcoat_gloss
+ *   DISNEY_SHEEN      0 base_color 1 sheen_tint
+ *   DISNEY_BSDF       0 base_color 1 specular_transmission 2 metallic
+ *                     3 subsurface 4 specular 5 roughness 6 specular_tint
+ *                     7 anisotropic 8 sheen 9 sheen_tint 10 clearcoat
+ *                     11 clearcoat_gloss
+ */
+typedef struct lj_material_desc {
+    int32_t type;
+    float eta;                 /* interior IOR / exterior IOR (plastic, dielectric, glass, bsdf) */
+    lj_texture_desc tex[LJ_MAT_SLOTS];
+} lj_material_desc;
+
+/* Shape variant, src/shape.h:21-54 (Sphere, TriangleMesh). */
+enum { LJ_SHAPE_MESH = 0, LJ_SHAPE_SPHERE = 1 };
+typedef struct lj_shape_desc {
+    int32_t kind;
+    int32_t material_id;
+    int32_t area_light_id;       /* -1 if not emissive */
+    int32_t interior_medium_id;  /* -1 = none */
+    int32_t exterior_medium_id;
+    int32_t num_vertices;
+    int32_t num_triangles;
+    int32_t pad0;
+    const float *positions;      /* num_vertices * 3 (FP32, as Embree receives them) */
+    const int32_t *indices;      /* num_triangles * 3 */
+    const float *normals;        /* num_vertices * 3 or NULL */
+    const float *uvs;            /* num_vertices * 2 or NULL */
+    float center[3];             /* sphere */
+    float radius;
+} lj_shape_desc;
+
+/* Light variant, src/light.h:15-36 (DiffuseAreaLight, Envmap). */
+enum { LJ_LIGHT_AREA = 0, LJ_LIGHT_ENVMAP = 1 };
+typedef struct lj_light_desc {
+    int32_t kind;
+    int32_t shape_id;            /* area light: emitting shape              */
+    float intensity[3];          /* area light radiance                     */
+    int32_t image_id;            /* envmap: RGB image (mip level 0)         */
+    float scale;                 /* envmap scale                            */
+    int32_t pad0;
+    double to_world[16];         /* envmap, row-major 4x4 */
+    double to_local[16];
+} lj_light_desc;
+
+/* RGB or single-channel FP32 image, row-major, channels interleaved. */
+typedef struct lj_image_desc {
+    int32_t width, height, channels, pad0;
+    const float *data;
+} lj_image_desc;
+
+/* Volume<T> variant, src/volume.h:12-30 (ConstantVolume, GridVolume). */
+enum { LJ_VOL_CONST = 0, LJ_VOL_GRID = 1 };
+typedef struct lj_volume_desc {
+    int32_t kind;
+    int32_t res[3];              /* x, y, z */
+    int32_t channels;            /* 1 or 3 */
+    float value[3];              /* constant volume */
+    float p_min[3], p_max[3];
+    float scale;
+    const float *data;           /* res.x*res.y*res.z*channels, x fastest */
+} lj_volume_desc;
+
+/* Medium variant, src/medium.h:10-22; PhaseFunction src/phase_function.h:9-16. */
+enum { LJ_MEDIUM_HOMOGENEOUS = 0, LJ_MEDIUM_HETEROGENEOUS = 1 };
+enum { LJ_PHASE_ISOTROPIC = 0, LJ_PHASE_HG = 1 };
+typedef struct lj_medium_desc {
+    int32_t kind;
+    int32_t phase_kind;
+    float g;
+    float sigma_a[3], sigma_s[3];
+    lj_volume_desc albedo, density;
+} lj_medium_desc;
+
+/* Camera, src/camera.h:9-25, and Filter variant src/filter.h:31-45. */
+enum { LJ_FILTER_BOX = 0, LJ_FILTER_TENT = 1, LJ_FILTER_GAUSSIAN = 2 };
+typedef struct lj_camera_desc {
+    double cam_to_world[16];     /* row-major */
+    double fov;                  /* degrees */
+    int32_t width, height;
+    int32_t filter_kind;
+    float filter_param;          /* box/tent width, gaussian stddev */
+    int32_t medium_id;
+    int32_t pad0;
+} lj_camera_desc;
+
+/* Integrator enum and RenderOptions, src/scene.h:13-31. */
+enum {
+    LJ_INTEGRATOR_DEPTH = 0,
+    LJ_INTEGRATOR_SHADING_NORMAL = 1,
+    LJ_INTEGRATOR_MEAN_CURVATURE = 2,
+    LJ_INTEGRATOR_RAY_DIFFERENTIAL = 3,
+    LJ_INTEGRATOR_MIPMAP_LEVEL = 4,
+    LJ_INTEGRATOR_PATH = 5,
+    LJ_INTEGRATOR_VOLPATH = 6
+};
+typedef struct lj_render_options {
+    int32_t integrator;
+    int32_t samples_per_pixel;
+    int32_t max_depth;           /* -1 = Russian roulette only (device cap LJ_MAX_BOUNCES) */
+    int32_t rr_depth;
+    int32_t vol_path_version;
+    int32_t max_null_collisions;
+} lj_render_options;
+
+typedef struct lj_scene_desc {
+    lj_camera_desc camera;
+    lj_render_options options;
+    int32_t num_shapes, num_materials, num_lights, num_media, num_images;
+    int32_t envmap_light_id;     /* -1 if none */
+    const lj_shape_desc *shapes;
+    const lj_material_desc *materials;
+    const lj_light_desc *lights;
+    const lj_medium_desc *media;
+    const lj_image_desc *images;
+} lj_scene_desc;
+
+/* Hard cap on path length when max_depth == -1 (the reference relies on
+ * Russian roulette alone; a device loop must be bounded). */
+#define LJ_MAX_BOUNCES 1024
+
+/* ---- context -------------------------------------------------------------- */
+
+/* Replaces rtcNewDevice (src/main.cpp:30) + parallel_init (src/main.cpp:31). */
+int lj_gpu_init(int device, lj_ctx **out);
+/* Replaces rtcReleaseDevice + parallel_cleanup (src/main.cpp:47-48). */
+void lj_gpu_shutdown(lj_ctx *ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char *lj_gpu_last_error(lj_ctx *ctx);
+int lj_gpu_abi_version(void);
+
+/* ---- scene ---------------------------------------------------------------- */
+
+/* Replaces Scene::Scene's Embree registration + rtcCommitScene + sampling
+ * table construction (src/scene.cpp:4-53).  Copies the description to the
+ * device and builds the BVH there (LBVH -> 8-wide compressed BVH). */
+int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *desc, lj_scene **out);
+/* Replaces Scene::~Scene / rtcReleaseScene (src/scene.cpp:55-59). */
+void lj_gpu_scene_destroy(lj_scene *scene);
+
+typedef struct lj_scene_info {
+    float bounds_lower[3], bounds_upper[3]; /* rtcGetSceneBounds (src/scene.cpp:29-34) */
+    double bsphere_radius;                  /* Scene::bounds.radius */
+    double bsphere_center[3];
+    int64_t num_triangles;                  /* all meshes */
+    int64_t num_prims;                      /* triangles + spheres */
+    int64_t num_wide_nodes;                 /* compressed 8-wide BVH nodes (80 B each) */
+    int64_t num_binary_nodes;               /* LBVH internal nodes */
+    int64_t device_bytes;                   /* HBM held by this scene */
+    double build_ms;                        /* device BVH build time */
+} lj_scene_info;
+int lj_gpu_scene_info(lj_scene *scene, lj_scene_info *out);
+
+/* ---- render -------------------------------------------------------------- */
+
+typedef struct lj_render_params {
+    uint64_t seed;               /* job seed; RNG is keyed on (seed, pixel, sample) */
+    int32_t spp;                 /* 0 = scene options.samples_per_pixel */
+    int32_t sample_offset;       /* first sample index (resume / split renders) */
+    int32_t max_paths_in_flight; /* 0 = library default (wavefront width) */
+    int32_t pad0;
+} lj_render_params;
+
+typedef struct lj_stats {
+    double device_ms;            /* kernel time of the render (CUDA events)   */
+    int64_t samples;             /* camera samples traced                     */
+    int64_t rays_closest;        /* closest-hit rays traced                   */
+    int64_t rays_shadow;         /* shadow rays traced                        */
+    int64_t path_segments;       /* shade-kernel invocations                  */
+    int64_t kernel_launches;     /* kernels launched by this call             */
+    int64_t null_collisions;     /* volpath: null-collision events            */
+    int64_t real_collisions;     /* volpath: real scattering events           */
+} lj_stats;
+
+/* Replaces Image3 render(const Scene&) (src/render.cpp:155-170).  Writes the
+ * W*H*3 FP32 image (the per-pixel mean over spp samples, HWC) into host
+ * memory `out_rgb`.  Host<->device copies are part of the call. */
+int lj_gpu_render(lj_scene *scene, const lj_render_params *params,
+                  float *out_rgb, lj_stats *stats);
+
+/* Same as lj_gpu_render but leaves the image in device memory `d_out_rgb`
+ * (W*H*3 floats) and runs asynchronously on `stream`; stats->device_ms is 0
+ * unless `stats` is non-NULL, in which case the call synchronizes. */
+int lj_gpu_render_device(lj_scene *scene, const lj_render_params *params,
+                         float *d_out_rgb, void *stream, lj_stats *stats);
+
+/* ---- batch kernels (oracle tests and microbenchmarks) -------------------- */
+
+/* Ray layout: 32 bytes, FP32, as RTCRay's first two float4s (rtcore_ray.h). */
+typedef struct lj_ray {
+    float org[3];
+    float tnear;
+    float dir[3];
+    float tfar;
+} lj_ray;
+
+/* Hit layout: 16 bytes.  prim = global primitive index (triangles of all
+ * meshes in shape order, then spheres), -1 on miss. u, v = barycentrics
+ * (Embree convention: p = (1-u-v) p0 + u p1 + v p2). */
+typedef struct lj_hit {
+    float t;
+    int32_t prim;
+    float u, v;
+} lj_hit;
+
+/* Replaces rtcIntersect1 (src/intersection.cpp:32) for n rays at once. */
+int lj_gpu_trace_closest(lj_scene *scene, const lj_ray *d_rays, lj_hit *d_hits,
+                         int64_t n, void *stream);
+/* Replaces rtcOccluded1 (src/intersection.cpp:83) for n rays at once;
+ * d_occluded[i] = 1 if any primitive lies in (tnear, tfar). */
+int lj_gpu_trace_any(lj_scene *scene, const lj_ray *d_rays, uint8_t *d_occluded,
+                     int64_t n, void *stream);
+/* Maps a global primitive index to (shape id, primitive id within shape). */
+int lj_gpu_prim_to_shape(lj_scene *scene, int32_t prim, int32_t *shape_id,
+                         int32_t *local_prim);
+
+/* 30-bit Morton codes (10 bits per axis) of triangle centroids over the
+ * centroid bounding box, and the stable sort order of those codes -- the
+ * first two stages of the LBVH build (replaces the BVH build behind
+ * rtcCommitScene, src/scene.cpp:27).  d_tri_vertices: n*9 floats
+ * (v0, v1, v2).  Outputs: d_codes[n] (unsorted, per triangle) and
+ * d_order[n] (triangle indices in ascending code order, ties by index). */
+int lj_gpu_morton_sort(lj_ctx *ctx, const float *d_tri_vertices, int64_t n,
+                       uint32_t *d_codes, uint32_t *d_order, void *stream);
+
+/* BSDF batch: replaces eval / sample_bsdf / pdf_sample_bsdf
+ * (src/material.cpp:90-119) for n independent queries in the local shading
+ * frame of a vertex whose geometric and shading normal are +z (the setup of
+ * the reference's src/tests/materials.cpp:55-60).
+ *   params:  n * LJ_BSDF_PARAMS floats per query, laid out per material type
+ *            as the texture slots above (RGB slots take 3 floats, scalar
+ *            slots 1 float, in slot order), followed by eta.
+ *   dir_in/dir_out: n*3, rnd: n*3 (uv, w).
+ *   eval -> out_value n*3; pdf -> out_pdf n; sample -> out_dir n*3,
+ *   out_eta n, out_roughness n, out_valid n (0/1). */
+#define LJ_BSDF_PARAMS 24
+enum { LJ_BSDF_OP_EVAL = 0, LJ_BSDF_OP_PDF = 1, LJ_BSDF_OP_SAMPLE = 2 };
+typedef struct lj_bsdf_batch {
+    int32_t material_type;
+    int32_t op;
+    int32_t transport_to_view;   /* 0 = TransportDirection::TO_LIGHT */
+    int32_t pad0;
+    const float *d_params;
+    const float *d_dir_in;
+    const float *d_dir_out;
+    const float *d_rnd;
+    float *d_out_value;
+    float *d_out_pdf;
+    float *d_out_dir;
+    float *d_out_eta;
+    float *d_out_roughness;
+    int32_t *d_out_valid;
+} lj_bsdf_batch;
+int lj_gpu_bsdf_batch(lj_ctx *ctx, const lj_bsdf_batch *batch, int64_t n, void *stream);
+
+/* Light batch: replaces sample_light + sample_point_on_light +
+ * pdf_point_on_light + light_pmf (src/scene.cpp:61-67, src/light.cpp:56-77)
+ * for n reference points of a scene.  rnd: n*4 (light_w, uv, shape_w) in the
+ * order src/path_tracing.h:98-100 consumes them.
+ * Outputs: light id, point n*3, normal n*3, pdf = light_pmf * pdf_point. */
+int lj_gpu_light_sample_batch(lj_scene *scene, const float *d_ref_points,
+                              const float *d_rnd, int32_t *d_out_light,
+                              float *d_out_point, float *d_out_normal,
+                              float *d_out_pdf, int64_t n, void *stream);
+
+/* Phase batch: replaces eval / sample_phase_function / pdf_sample_phase
+ * (src/phase_function.cpp:30-47) for Henyey-Greenstein (g) or isotropic
+ * (phase_kind).  out_value n (eval), out_pdf n, out_dir n*3 (sample). */
+int lj_gpu_phase_batch(lj_ctx *ctx, int32_t phase_kind, float g,
+                       const float *d_dir_in, const float *d_dir_out,
+                       const float *d_rnd, float *d_out_value, float *d_out_pdf,
+                       float *d_out_dir, int64_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LJ_GPU_H */

@@ -1,0 +1,428 @@
+"""Scene description + seeded synthetic scene generators.
+
+A `Scene` holds the flat, FP32 view of lajolla's `Scene` (src/scene.h:42-82)
+that the C ABI takes (`lj_scene_desc`, include/lj_gpu.h).  Every value a
+generator produces is float32-exact, so the same scene written out as Mitsuba
+XML + OBJ (`write_mitsuba`) parses in the reference renderer (whose parser
+reads numbers with std::stof, src/parsers/parse_scene.cpp:85-116) to exactly
+the same numbers the GPU path receives.
+
+Generators (seeded, deterministic):
+  cornell_box      5 wall quads + 2 y-rotated boxes + ceiling quad light
+                   (17, 12, 4), Lambertian albedos U[0.1, 0.8]^3, fov 40,
+                   box filter -- the 256x256 / 64 spp / max depth 6 workload.
+  triangle_soup    n triangles, centroids U[0,1]^3, vertex offsets N(0, 0.01)
+  random_rays      origins U[-0.5, 1.5]^3, directions uniform on S^2
+"""
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import abi
+
+
+def f32(x):
+    return float(np.float32(x))
+
+
+def look_at(pos, target, up):
+    """src/transform.cpp:64-90 (look_at), returned float32-exact (the parser
+    reads matrices with std::stof)."""
+    pos, target, up = (np.asarray(v, np.float64) for v in (pos, target, up))
+    d = target - pos
+    d = d / np.linalg.norm(d)
+    upn = up / np.linalg.norm(up)
+    left = np.cross(upn, d)
+    left = left / np.linalg.norm(left)
+    new_up = np.cross(d, left)
+    m = np.zeros((4, 4))
+    m[:3, 0] = left
+    m[:3, 1] = new_up
+    m[:3, 2] = d
+    m[:3, 3] = pos
+    m[3, 3] = 1
+    return m.astype(np.float32).astype(np.float64)
+
+
+def const_tex(v):
+    v = [v, v, v] if np.isscalar(v) else list(v)
+    return dict(kind=abi.LJ_TEX_CONST, value0=[f32(x) for x in v])
+
+
+def checker_tex(c0, c1, uscale=1.0, vscale=1.0):
+    c0 = [c0] * 3 if np.isscalar(c0) else list(c0)
+    c1 = [c1] * 3 if np.isscalar(c1) else list(c1)
+    return dict(kind=abi.LJ_TEX_CHECKER, value0=[f32(x) for x in c0],
+                value1=[f32(x) for x in c1], uscale=f32(uscale), vscale=f32(vscale))
+
+
+def lambertian(rgb):
+    return dict(type=abi.LJ_MAT_LAMBERTIAN, eta=1.0, tex=[const_tex(rgb)])
+
+
+def roughplastic(kd, ks=(1, 1, 1), roughness=0.1, eta=1.49 / 1.000277):
+    return dict(type=abi.LJ_MAT_ROUGHPLASTIC, eta=f32(eta),
+                tex=[const_tex(kd), const_tex(ks), const_tex(roughness)])
+
+
+def roughdielectric(ks=(1, 1, 1), kt=(1, 1, 1), roughness=0.1, eta=1.5046 / 1.000277):
+    return dict(type=abi.LJ_MAT_ROUGHDIELECTRIC, eta=f32(eta),
+                tex=[const_tex(ks), const_tex(kt), const_tex(roughness)])
+
+
+def disney_bsdf(base_color, specular_transmission=0.0, metallic=0.0, subsurface=0.0,
+                specular=0.5, roughness=0.5, specular_tint=0.0, anisotropic=0.0,
+                sheen=0.0, sheen_tint=0.5, clearcoat=0.0, clearcoat_gloss=1.0, eta=1.5):
+    vals = [specular_transmission, metallic, subsurface, specular, roughness, specular_tint,
+            anisotropic, sheen, sheen_tint, clearcoat, clearcoat_gloss]
+    return dict(type=abi.LJ_MAT_DISNEY_BSDF, eta=f32(eta),
+                tex=[const_tex(base_color)] + [const_tex(v) for v in vals])
+
+
+class Scene:
+    """Flat scene: numpy arrays + dicts, convertible to lj_scene_desc."""
+
+    def __init__(self, width, height, spp, max_depth, cam_to_world, fov,
+                 filter_kind=abi.LJ_FILTER_BOX, filter_param=1.0, rr_depth=5,
+                 integrator=abi.LJ_INTEGRATOR_PATH, vol_path_version=0,
+                 max_null_collisions=1000, camera_medium=-1):
+        self.width, self.height = int(width), int(height)
+        self.spp, self.max_depth, self.rr_depth = int(spp), int(max_depth), int(rr_depth)
+        self.integrator = integrator
+        self.vol_path_version = vol_path_version
+        self.max_null_collisions = max_null_collisions
+        self.cam_to_world = np.asarray(cam_to_world, np.float64)
+        self.fov = f32(fov)
+        self.filter_kind, self.filter_param = filter_kind, f32(filter_param)
+        self.camera_medium = camera_medium
+        self.shapes, self.materials, self.lights, self.media, self.images = [], [], [], [], []
+        self.envmap_light_id = -1
+
+    # -- building ---------------------------------------------------------
+    def add_material(self, m):
+        self.materials.append(m)
+        return len(self.materials) - 1
+
+    def add_mesh(self, positions, indices, material_id, normals=None, uvs=None,
+                 emission=None, interior_medium=-1, exterior_medium=-1):
+        sh = dict(kind=abi.LJ_SHAPE_MESH,
+                  positions=np.ascontiguousarray(positions, np.float32),
+                  indices=np.ascontiguousarray(indices, np.int32),
+                  normals=None if normals is None else np.ascontiguousarray(normals, np.float32),
+                  uvs=None if uvs is None else np.ascontiguousarray(uvs, np.float32),
+                  material_id=material_id, area_light_id=-1,
+                  interior_medium_id=interior_medium, exterior_medium_id=exterior_medium)
+        return self._add_shape(sh, emission)
+
+    def add_sphere(self, center, radius, material_id, emission=None,
+                   interior_medium=-1, exterior_medium=-1):
+        sh = dict(kind=abi.LJ_SHAPE_SPHERE, center=[f32(c) for c in center],
+                  radius=f32(radius), material_id=material_id, area_light_id=-1,
+                  interior_medium_id=interior_medium, exterior_medium_id=exterior_medium)
+        return self._add_shape(sh, emission)
+
+    def _add_shape(self, sh, emission):
+        sid = len(self.shapes)
+        if emission is not None:
+            sh["area_light_id"] = len(self.lights)
+            self.lights.append(dict(kind=abi.LJ_LIGHT_AREA, shape_id=sid,
+                                    intensity=[f32(e) for e in emission]))
+        self.shapes.append(sh)
+        return sid
+
+    @property
+    def num_triangles(self):
+        return sum(len(s["indices"]) for s in self.shapes if s["kind"] == abi.LJ_SHAPE_MESH)
+
+    # -- C ABI view -------------------------------------------------------
+    def desc(self):
+        """Returns (lj_scene_desc, keepalive); keep `keepalive` referenced
+        while the descriptor is in use."""
+        keep = []
+
+        def ptr(arr, ctype):
+            if arr is None:
+                return None
+            arr = np.ascontiguousarray(arr)
+            keep.append(arr)
+            return arr.ctypes.data_as(C.POINTER(ctype))
+
+        d = abi.lj_scene_desc()
+        cam = d.camera
+        for i, v in enumerate(self.cam_to_world.reshape(-1)):
+            cam.cam_to_world[i] = v
+        cam.fov = self.fov
+        cam.width, cam.height = self.width, self.height
+        cam.filter_kind, cam.filter_param = self.filter_kind, self.filter_param
+        cam.medium_id = self.camera_medium
+        o = d.options
+        o.integrator, o.samples_per_pixel = self.integrator, self.spp
+        o.max_depth, o.rr_depth = self.max_depth, self.rr_depth
+        o.vol_path_version, o.max_null_collisions = self.vol_path_version, self.max_null_collisions
+
+        shapes = (abi.lj_shape_desc * max(1, len(self.shapes)))()
+        for i, s in enumerate(self.shapes):
+            t = shapes[i]
+            t.kind, t.material_id, t.area_light_id = s["kind"], s["material_id"], s["area_light_id"]
+            t.interior_medium_id, t.exterior_medium_id = s["interior_medium_id"], s["exterior_medium_id"]
+            if s["kind"] == abi.LJ_SHAPE_MESH:
+                t.num_vertices, t.num_triangles = len(s["positions"]), len(s["indices"])
+                t.positions = ptr(s["positions"], C.c_float)
+                t.indices = ptr(s["indices"], C.c_int32)
+                t.normals = ptr(s["normals"], C.c_float)
+                t.uvs = ptr(s["uvs"], C.c_float)
+            else:
+                for k in range(3):
+                    t.center[k] = s["center"][k]
+                t.radius = s["radius"]
+        mats = (abi.lj_material_desc * max(1, len(self.materials)))()
+        for i, m in enumerate(self.materials):
+            mats[i].type, mats[i].eta = m["type"], m["eta"]
+            for k, tx in enumerate(m["tex"]):
+                td = mats[i].tex[k]
+                td.kind = tx.get("kind", abi.LJ_TEX_CONST)
+                td.image_id = tx.get("image_id", -1)
+                for c in range(3):
+                    td.value0[c] = tx.get("value0", [0, 0, 0])[c]
+                    td.value1[c] = tx.get("value1", [0, 0, 0])[c]
+                td.uscale, td.vscale = tx.get("uscale", 1.0), tx.get("vscale", 1.0)
+                td.uoffset, td.voffset = tx.get("uoffset", 0.0), tx.get("voffset", 0.0)
+        lights = (abi.lj_light_desc * max(1, len(self.lights)))()
+        for i, l in enumerate(self.lights):
+            t = lights[i]
+            t.kind = l["kind"]
+            t.shape_id = l.get("shape_id", -1)
+            for c in range(3):
+                t.intensity[c] = l.get("intensity", [0, 0, 0])[c]
+            t.image_id = l.get("image_id", -1)
+            t.scale = l.get("scale", 1.0)
+            tw = np.asarray(l.get("to_world", np.eye(4)), np.float64).reshape(-1)
+            tl = np.asarray(l.get("to_local", np.eye(4)), np.float64).reshape(-1)
+            for k in range(16):
+                t.to_world[k], t.to_local[k] = tw[k], tl[k]
+        images = (abi.lj_image_desc * max(1, len(self.images)))()
+        for i, im in enumerate(self.images):
+            im = np.ascontiguousarray(im, np.float32)
+            if im.ndim == 2:
+                im = im[:, :, None]
+            images[i].height, images[i].width, images[i].channels = im.shape
+            images[i].data = ptr(im, C.c_float)
+        media = (abi.lj_medium_desc * max(1, len(self.media)))()
+        for i, m in enumerate(self.media):
+            t = media[i]
+            t.kind, t.phase_kind, t.g = m["kind"], m.get("phase_kind", 0), m.get("g", 0.0)
+            for c in range(3):
+                t.sigma_a[c] = m.get("sigma_a", [0, 0, 0])[c]
+                t.sigma_s[c] = m.get("sigma_s", [0, 0, 0])[c]
+            for key in ("albedo", "density"):
+                v = m.get(key)
+                if v is None:
+                    continue
+                vd = getattr(t, key)
+                vd.kind = v["kind"]
+                if v["kind"] == abi.LJ_VOL_CONST:
+                    for c in range(3):
+                        vd.value[c] = v["value"][c]
+                    vd.channels = 3
+                else:
+                    data = np.ascontiguousarray(v["data"], np.float32)  # (z, y, x, ch)
+                    vd.res[0], vd.res[1], vd.res[2] = data.shape[2], data.shape[1], data.shape[0]
+                    vd.channels = data.shape[3]
+                    for c in range(3):
+                        vd.p_min[c], vd.p_max[c] = v["p_min"][c], v["p_max"][c]
+                    vd.data = ptr(data, C.c_float)
+                vd.scale = v.get("scale", 1.0)
+        d.num_shapes, d.num_materials = len(self.shapes), len(self.materials)
+        d.num_lights, d.num_media, d.num_images = len(self.lights), len(self.media), len(self.images)
+        d.envmap_light_id = self.envmap_light_id
+        d.shapes = C.cast(shapes, C.POINTER(abi.lj_shape_desc))
+        d.materials = C.cast(mats, C.POINTER(abi.lj_material_desc))
+        d.lights = C.cast(lights, C.POINTER(abi.lj_light_desc))
+        d.media = C.cast(media, C.POINTER(abi.lj_medium_desc))
+        d.images = C.cast(images, C.POINTER(abi.lj_image_desc))
+        keep += [shapes, mats, lights, images, media]
+        return d, keep
+
+    # -- Mitsuba XML for the reference renderer ---------------------------
+    def write_mitsuba(self, directory, name="scene"):
+        """Write <directory>/<name>.xml (+ OBJ meshes) in the subset of the
+        Mitsuba 0.5 format lajolla's parser reads
+        (src/parsers/parse_scene.cpp).  Supports what the generators emit:
+        path integrator, perspective sensor, box filter, diffuse /
+        roughplastic / roughdielectric BSDFs, OBJ meshes, spheres, area
+        emitters."""
+        os.makedirs(directory, exist_ok=True)
+        r = repr
+
+        def vec(v):
+            return ", ".join(r(float(x)) for x in v)
+
+        out = ['<?xml version="1.0" encoding="utf-8"?>', '<scene version="0.4.0">',
+               '  <integrator type="path">',
+               f'    <integer name="maxDepth" value="{self.max_depth}"/>',
+               f'    <integer name="rrDepth" value="{self.rr_depth}"/>', '  </integrator>',
+               '  <sensor type="perspective">',
+               f'    <float name="fov" value="{r(self.fov)}"/>',
+               '    <transform name="toWorld">',
+               '      <matrix value="' + " ".join(r(float(x)) for x in self.cam_to_world.reshape(-1)) + '"/>',
+               '    </transform>',
+               f'    <sampler type="independent"><integer name="sampleCount" value="{self.spp}"/></sampler>',
+               '    <film type="hdrfilm">',
+               f'      <integer name="width" value="{self.width}"/>',
+               f'      <integer name="height" value="{self.height}"/>']
+        if self.filter_kind == abi.LJ_FILTER_BOX:
+            out.append(f'      <rfilter type="box"><float name="width" value="{r(self.filter_param)}"/></rfilter>')
+        elif self.filter_kind == abi.LJ_FILTER_TENT:
+            out.append(f'      <rfilter type="tent"><float name="width" value="{r(self.filter_param)}"/></rfilter>')
+        else:
+            out.append(f'      <rfilter type="gaussian"><float name="stddev" value="{r(self.filter_param)}"/></rfilter>')
+        out += ['    </film>', '  </sensor>']
+        for i, m in enumerate(self.materials):
+            tx = m["tex"]
+            if m["type"] == abi.LJ_MAT_LAMBERTIAN:
+                out.append(f'  <bsdf type="diffuse" id="mat{i}"><rgb name="reflectance" value="{vec(tx[0]["value0"])}"/></bsdf>')
+            elif m["type"] == abi.LJ_MAT_ROUGHPLASTIC:
+                out += [f'  <bsdf type="roughplastic" id="mat{i}">',
+                        f'    <rgb name="diffuseReflectance" value="{vec(tx[0]["value0"])}"/>',
+                        f'    <rgb name="specularReflectance" value="{vec(tx[1]["value0"])}"/>',
+                        f'    <float name="alpha" value="{r(f32(tx[2]["value0"][0] ** 2))}"/>',
+                        f'    <float name="intIOR" value="{r(m["eta"])}"/>',
+                        '    <float name="extIOR" value="1"/>', '  </bsdf>']
+            elif m["type"] == abi.LJ_MAT_ROUGHDIELECTRIC:
+                out += [f'  <bsdf type="roughdielectric" id="mat{i}">',
+                        f'    <rgb name="specularReflectance" value="{vec(tx[0]["value0"])}"/>',
+                        f'    <rgb name="specularTransmittance" value="{vec(tx[1]["value0"])}"/>',
+                        f'    <float name="alpha" value="{r(f32(tx[2]["value0"][0] ** 2))}"/>',
+                        f'    <float name="intIOR" value="{r(m["eta"])}"/>',
+                        '    <float name="extIOR" value="1"/>', '  </bsdf>']
+            else:
+                raise ValueError("write_mitsuba: material type %d not supported" % m["type"])
+        for i, s in enumerate(self.shapes):
+            if s["kind"] == abi.LJ_SHAPE_MESH:
+                fn = os.path.join(directory, f"{name}_shape{i}.obj")
+                with open(fn, "w") as f:
+                    for p in s["positions"]:
+                        f.write("v %r %r %r\n" % tuple(float(x) for x in p))
+                    if s["normals"] is not None:
+                        for n in s["normals"]:
+                            f.write("vn %r %r %r\n" % tuple(float(x) for x in n))
+                    for t in s["indices"]:
+                        a, b, c = (int(x) + 1 for x in t)
+                        if s["normals"] is not None:
+                            f.write(f"f {a}//{a} {b}//{b} {c}//{c}\n")
+                        else:
+                            f.write(f"f {a} {b} {c}\n")
+                out.append('  <shape type="obj">')
+                out.append(f'    <string name="filename" value="{fn}"/>')
+                if s["normals"] is None:
+                    out.append('    <boolean name="faceNormals" value="true"/>')
+            else:
+                out.append('  <shape type="sphere">')
+                out.append(f'    <point name="center" x="{r(s["center"][0])}" y="{r(s["center"][1])}" z="{r(s["center"][2])}"/>')
+                out.append(f'    <float name="radius" value="{r(s["radius"])}"/>')
+            out.append(f'    <ref id="mat{s["material_id"]}"/>')
+            if s["area_light_id"] >= 0:
+                em = self.lights[s["area_light_id"]]["intensity"]
+                out.append(f'    <emitter type="area"><rgb name="radiance" value="{vec(em)}"/></emitter>')
+            out.append('  </shape>')
+        out.append('</scene>')
+        path = os.path.join(directory, f"{name}.xml")
+        with open(path, "w") as f:
+            f.write("\n".join(out) + "\n")
+        return path
+
+
+def _quad(p0, p1, p2, p3):
+    """Two triangles (p0,p1,p2), (p0,p2,p3); normal = (p1-p0) x (p2-p0)."""
+    return np.array([p0, p1, p2, p3], np.float32), np.array([[0, 1, 2], [0, 2, 3]], np.int32)
+
+
+def _box(center, size, angle_deg):
+    """Axis box rotated about +y; 12 outward-facing triangles."""
+    cx, cy, cz = center
+    sx, sy, sz = (s / 2 for s in size)
+    c, s = math.cos(math.radians(angle_deg)), math.sin(math.radians(angle_deg))
+
+    def P(x, y, z):
+        return [cx + c * x + s * z, cy + y, cz - s * x + c * z]
+
+    corners = {}
+    for ix in (-1, 1):
+        for iy in (-1, 1):
+            for iz in (-1, 1):
+                corners[(ix, iy, iz)] = P(ix * sx, iy * sy, iz * sz)
+    faces = [  # each CCW seen from outside
+        [(-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1)],      # +z
+        [(1, -1, -1), (-1, -1, -1), (-1, 1, -1), (1, 1, -1)],  # -z
+        [(1, -1, 1), (1, -1, -1), (1, 1, -1), (1, 1, 1)],      # +x
+        [(-1, -1, -1), (-1, -1, 1), (-1, 1, 1), (-1, 1, -1)],  # -x
+        [(-1, 1, 1), (1, 1, 1), (1, 1, -1), (-1, 1, -1)],      # +y
+        [(-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1)],  # -y
+    ]
+    pos, idx = [], []
+    for f in faces:
+        b = len(pos)
+        pos += [corners[k] for k in f]
+        idx += [[b, b + 1, b + 2], [b, b + 2, b + 3]]
+    return np.array(pos, np.float32), np.array(idx, np.int32)
+
+
+def cornell_box(seed=0, width=256, height=256, spp=64, max_depth=6, rr_depth=5):
+    """Seeded Cornell-like box: interior [-1,1] x [0,2] x [-1,1], open at +z."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(width, height, spp, max_depth,
+               look_at([0, 1, 3.4], [0, 1, 0], [0, 1, 0]), 40.0, rr_depth=rr_depth)
+
+    def albedo():
+        return [f32(x) for x in rng.uniform(0.1, 0.8, 3)]
+
+    walls = [
+        _quad([-1, 0, 1], [1, 0, 1], [1, 0, -1], [-1, 0, -1]),      # floor, normal +y
+        _quad([-1, 2, -1], [1, 2, -1], [1, 2, 1], [-1, 2, 1]),      # ceiling, normal -y
+        _quad([-1, 0, -1], [1, 0, -1], [1, 2, -1], [-1, 2, -1]),    # back, normal +z
+        _quad([-1, 0, 1], [-1, 0, -1], [-1, 2, -1], [-1, 2, 1]),    # left, normal +x
+        _quad([1, 0, -1], [1, 0, 1], [1, 2, 1], [1, 2, -1]),        # right, normal -x
+    ]
+    for pos, idx in walls:
+        sc.add_mesh(pos, idx, sc.add_material(lambertian(albedo())))
+    a1, a2 = (float(x) for x in rng.uniform(10, 35, 2))
+    for center, size, ang in (([-0.35, 0.6, -0.3], [0.6, 1.2, 0.6], a1),
+                              ([0.4, 0.3, 0.3], [0.6, 0.6, 0.6], -a2)):
+        pos, idx = _box(center, size, ang)
+        sc.add_mesh(pos, idx, sc.add_material(lambertian(albedo())))
+    lpos, lidx = _quad([-0.25, 1.98, -0.25], [0.25, 1.98, -0.25], [0.25, 1.98, 0.25], [-0.25, 1.98, 0.25])
+    sc.add_mesh(lpos, lidx, sc.add_material(lambertian([0.78, 0.78, 0.78])), emission=[17, 12, 4])
+    return sc
+
+
+def triangle_soup(seed, n_tris, offset_sigma=0.01):
+    """n triangles: centroids U[0,1]^3, each vertex = centroid + N(0, sigma)."""
+    rng = np.random.default_rng(seed)
+    cent = rng.uniform(0, 1, (n_tris, 1, 3))
+    v = (cent + rng.normal(0, offset_sigma, (n_tris, 3, 3))).astype(np.float32)
+    return v.reshape(-1, 3), np.arange(n_tris * 3, dtype=np.int32).reshape(-1, 3)
+
+
+def soup_scene(seed, n_tris):
+    """A scene wrapping a triangle soup (one Lambertian mesh, one light)."""
+    pos, idx = triangle_soup(seed, n_tris)
+    sc = Scene(64, 64, 1, 2, look_at([0.5, 0.5, 3], [0.5, 0.5, 0.5], [0, 1, 0]), 40.0)
+    m = sc.add_material(lambertian([0.5, 0.5, 0.5]))
+    sc.add_mesh(pos, idx, m)
+    return sc
+
+
+def random_rays(seed, n, tnear=0.0, tfar=np.inf):
+    """Rays as an (n, 8) float32 array in lj_ray layout."""
+    rng = np.random.default_rng(seed)
+    org = rng.uniform(-0.5, 1.5, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.empty((n, 8), np.float32)
+    r[:, 0:3] = org
+    r[:, 3] = tnear
+    r[:, 4:7] = d
+    r[:, 7] = tfar
+    return r
