@@ -324,14 +324,15 @@ int lj_gpu_morton_sort(lj_ctx *ctx, const float *d_tri_vertices, int64_t n,
  * (src/material.cpp:90-119) for n independent queries in the local shading
  * frame of a vertex whose geometric and shading normal are +z (the setup of
  * the reference's src/tests/materials.cpp:55-60).
- *   params:  n * LJ_BSDF_PARAMS floats per query, laid out per material type
- *            as the texture slots above (RGB slots take 3 floats, scalar
- *            slots 1 float, in slot order), followed by eta.
+ *   params:  n * lj_gpu_bsdf_param_count(type) floats: per query the
+ *            material's texture slots above packed in slot order (RGB slots
+ *            3 floats, scalar slots 1 float), followed by eta.
  *   dir_in/dir_out: n*3, rnd: n*3 (uv, w).
  *   eval -> out_value n*3; pdf -> out_pdf n; sample -> out_dir n*3,
  *   out_eta n, out_roughness n, out_valid n (0/1). */
-#define LJ_BSDF_PARAMS 24
 enum { LJ_BSDF_OP_EVAL = 0, LJ_BSDF_OP_PDF = 1, LJ_BSDF_OP_SAMPLE = 2 };
+/* Packed parameter count per query for a material type, -1 if unknown. */
+int lj_gpu_bsdf_param_count(int32_t material_type);
 typedef struct lj_bsdf_batch {
     int32_t material_type;
     int32_t op;

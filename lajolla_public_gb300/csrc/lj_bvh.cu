@@ -1,0 +1,643 @@
+// GPU BVH build and batch ray casting: replaces the Embree scene build behind
+// rtcCommitScene (src/scene.cpp:19-34, src/shapes/triangle_mesh.inl:1-22,
+// src/shapes/sphere.inl:151-162) and the rtcIntersect1 / rtcOccluded1 calls
+// (src/intersection.cpp:32, :83).
+//
+// Build pipeline (all on the device, one stream):
+//   1. primitive boxes + centroids, scene box and centroid box (block reduce
+//      + ordered-uint atomics)
+//   2. 30-bit Morton codes of centroids over the centroid box
+//   3. stable LSD radix sort of (code, primitive) -- 4 passes of 8 bits,
+//      warp-match ranking, no library sort
+//   4. Karras (HPG 2012) binary radix tree: one thread per internal node
+//   5. bottom-up boxes (atomic arrival counters, L2-coherent loads)
+//   6. level-synchronous collapse into the compressed 8-wide layout of
+//      lj_scene.cuh: greedy largest-area child expansion, octant slot
+//      assignment, 8-bit conservative quantization, leaves of <= 3 primitives
+//      stored contiguously in leaf order.
+#include <cfloat>
+#include <cmath>
+#include <vector>
+
+#include "lj_internal.h"
+#include "lj_trace.cuh"
+
+namespace lj {
+
+namespace {
+
+constexpr int kRsThreads = 256;
+constexpr int kRsItems = 8;
+constexpr int kRsTile = kRsThreads * kRsItems;
+
+__device__ __forceinline__ uint32_t f2o(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+__host__ __forceinline__ float o2f_host(uint32_t u) {
+    uint32_t v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    memcpy(&f, &v, 4);
+    return f;
+}
+
+// Block-wide min/max of 6 values (3 mins, 3 maxes) -> ordered-uint atomics.
+// blockDim.x must be a multiple of 32 and <= 1024.
+__device__ void block_minmax6(float v[6], uint32_t *dst) {
+    __shared__ float sh[32][6];
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            float x = __shfl_xor_sync(0xffffffffu, v[k], o);
+            v[k] = k < 3 ? fminf(v[k], x) : fmaxf(v[k], x);
+        }
+    }
+    if (lane == 0)
+        for (int k = 0; k < 6; k++) sh[warp][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int nw = blockDim.x >> 5;
+        for (int w = 1; w < nw; w++)
+            for (int k = 0; k < 6; k++) v[k] = k < 3 ? fminf(v[k], sh[w][k]) : fmaxf(v[k], sh[w][k]);
+        for (int k = 0; k < 3; k++) atomicMin(dst + k, f2o(v[k]));
+        for (int k = 3; k < 6; k++) atomicMax(dst + k, f2o(v[k]));
+    }
+}
+
+__global__ void k_init_bounds(uint32_t *b, int count) {
+    int i = threadIdx.x;
+    if (i < count) b[i] = (i % 6) < 3 ? f2o(FLT_MAX) : f2o(-FLT_MAX);
+}
+
+// bounds: [0..5] centroid min/max, [6..11] primitive box min/max
+__global__ void k_prim_bounds(BvhInput in, float4 *plo, float4 *phi, float4 *cent, uint32_t *bounds) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = in.num_tris + in.num_spheres;
+    float cb[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float bb[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    if (i < n) {
+        V3 l, h, c;
+        if (i < in.num_tris) {
+            int a = in.tri_vidx[i * 3], b = in.tri_vidx[i * 3 + 1], cc = in.tri_vidx[i * 3 + 2];
+            V3 p0{in.vpos[a * 3], in.vpos[a * 3 + 1], in.vpos[a * 3 + 2]};
+            V3 p1{in.vpos[b * 3], in.vpos[b * 3 + 1], in.vpos[b * 3 + 2]};
+            V3 p2{in.vpos[cc * 3], in.vpos[cc * 3 + 1], in.vpos[cc * 3 + 2]};
+            l = V3{fminf(p0.x, fminf(p1.x, p2.x)), fminf(p0.y, fminf(p1.y, p2.y)), fminf(p0.z, fminf(p1.z, p2.z))};
+            h = V3{fmaxf(p0.x, fmaxf(p1.x, p2.x)), fmaxf(p0.y, fmaxf(p1.y, p2.y)), fmaxf(p0.z, fmaxf(p1.z, p2.z))};
+            c = tri_centroid(p0, p1, p2);
+        } else {
+            const float *s = in.spheres + (size_t)(i - in.num_tris) * 4;
+            c = V3{s[0], s[1], s[2]};
+            float r = s[3];
+            l = V3{__fsub_rn(c.x, r), __fsub_rn(c.y, r), __fsub_rn(c.z, r)};
+            h = V3{__fadd_rn(c.x, r), __fadd_rn(c.y, r), __fadd_rn(c.z, r)};
+        }
+        plo[i] = make_float4(l.x, l.y, l.z, 0.f);
+        phi[i] = make_float4(h.x, h.y, h.z, 0.f);
+        cent[i] = make_float4(c.x, c.y, c.z, 0.f);
+        cb[0] = cb[3] = c.x; cb[1] = cb[4] = c.y; cb[2] = cb[5] = c.z;
+        bb[0] = l.x; bb[1] = l.y; bb[2] = l.z; bb[3] = h.x; bb[4] = h.y; bb[5] = h.z;
+    }
+    block_minmax6(cb, bounds);
+    __syncthreads();
+    block_minmax6(bb, bounds + 6);
+}
+
+__global__ void k_morton(const float4 *cent, int64_t n, const uint32_t *bounds, uint32_t *codes,
+                         uint32_t *idx) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    V3 lo{o2f(bounds[0]), o2f(bounds[1]), o2f(bounds[2])};
+    V3 hi{o2f(bounds[3]), o2f(bounds[4]), o2f(bounds[5])};
+    V3 sc{morton_scale(lo.x, hi.x), morton_scale(lo.y, hi.y), morton_scale(lo.z, hi.z)};
+    float4 c = cent[i];
+    codes[i] = morton3(V3{c.x, c.y, c.z}, lo, sc);
+    if (idx) idx[i] = (uint32_t)i;
+}
+
+__global__ void k_tri_centroids(const float *v, int64_t n, float4 *cent, uint32_t *bounds) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float cb[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    if (i < n) {
+        const float *t = v + i * 9;
+        V3 c = tri_centroid(V3{t[0], t[1], t[2]}, V3{t[3], t[4], t[5]}, V3{t[6], t[7], t[8]});
+        cent[i] = make_float4(c.x, c.y, c.z, 0.f);
+        cb[0] = cb[3] = c.x; cb[1] = cb[4] = c.y; cb[2] = cb[5] = c.z;
+    }
+    block_minmax6(cb, bounds);
+}
+
+// ---- radix sort ----------------------------------------------------------
+__global__ void k_rs_hist(const uint32_t *keys, int64_t n, int shift, uint32_t *hist, int tiles) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    int64_t base = (int64_t)blockIdx.x * kRsTile;
+#pragma unroll
+    for (int k = 0; k < kRsItems; k++) {
+        int64_t idx = base + k * kRsThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// single-block exclusive scan of `total` entries in place
+__global__ void k_rs_scan(uint32_t *hist, int64_t total) {
+    __shared__ uint32_t sums[1024];
+    int t = threadIdx.x;
+    int64_t chunk = (total + blockDim.x - 1) / blockDim.x;
+    int64_t b = t * chunk, e = b + chunk < total ? b + chunk : total;
+    uint32_t s = 0;
+    for (int64_t i = b; i < e; i++) s += hist[i];
+    sums[t] = s;
+    __syncthreads();
+    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+        uint32_t v = t >= off ? sums[t - off] : 0u;
+        __syncthreads();
+        sums[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = sums[t] - s;
+    for (int64_t i = b; i < e; i++) {
+        uint32_t v = hist[i];
+        hist[i] = run;
+        run += v;
+    }
+}
+
+__global__ void k_rs_scatter(const uint32_t *kin, const uint32_t *vin, uint32_t *kout, uint32_t *vout,
+                             int64_t n, int shift, const uint32_t *hist, int tiles) {
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_wc[kRsThreads / 32][257];
+    int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    s_base[tid] = hist[(size_t)tid * tiles + blockIdx.x];
+    int64_t base = (int64_t)blockIdx.x * kRsTile;
+    uint32_t lt_mask = (1u << lane) - 1u;
+    for (int round = 0; round < kRsItems; round++) {
+        for (int j = tid; j < (kRsThreads / 32) * 257; j += kRsThreads) (&s_wc[0][0])[j] = 0;
+        __syncthreads();
+        int64_t idx = base + round * kRsThreads + tid;
+        bool valid = idx < n;
+        uint32_t key = valid ? kin[idx] : 0u, val = valid ? vin[idx] : 0u;
+        uint32_t d = valid ? (key >> shift) & 255u : 256u;
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t rank = __popc(peers & lt_mask);
+        if (valid && lane == __ffs(peers) - 1) s_wc[warp][d] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t run = s_base[tid];
+            for (int w = 0; w < kRsThreads / 32; w++) {
+                uint32_t c = s_wc[w][tid];
+                s_wc[w][tid] = run;
+                run += c;
+            }
+            s_base[tid] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = s_wc[warp][d] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- Karras radix tree ---------------------------------------------------
+__device__ __forceinline__ int kdelta(const uint32_t *codes, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint32_t a = codes[i], b = codes[j];
+    if (a != b) return __clz(a ^ b);
+    return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+}
+
+__global__ void k_karras(const uint32_t *codes, int n, int2 *child, int2 *range, int *parent_int,
+                         int *parent_leaf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (kdelta(codes, n, i, i + 1) - kdelta(codes, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = kdelta(codes, n, i, i - d);
+    int lmax = 2;
+    while (kdelta(codes, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = kdelta(codes, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (kdelta(codes, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + min(d, 0);
+    int first = min(i, j), last = max(i, j);
+    int left = (first == gamma) ? ~gamma : gamma;
+    int right = (last == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    child[i] = make_int2(left, right);
+    range[i] = make_int2(first, last);
+    if (left < 0) parent_leaf[gamma] = i; else parent_int[gamma] = i;
+    if (right < 0) parent_leaf[gamma + 1] = i; else parent_int[gamma + 1] = i;
+}
+
+__global__ void k_bottom_up(int n, const int2 *child, const int *parent_int, const int *parent_leaf,
+                            const uint32_t *sorted, const float4 *plo, const float4 *phi, float4 *nlo,
+                            float4 *nhi, uint32_t *flags) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int p = parent_leaf[j];
+    int guard = 0;
+    while (p >= 0 && guard++ < 64 * 1024) {
+        __threadfence();
+        if (atomicAdd(&flags[p], 1u) == 0u) return;
+        int2 c = child[p];
+        float4 l0, h0, l1, h1;
+        if (c.x < 0) { uint32_t g = sorted[~c.x]; l0 = plo[g]; h0 = phi[g]; }
+        else { l0 = __ldcg(nlo + c.x); h0 = __ldcg(nhi + c.x); }
+        if (c.y < 0) { uint32_t g = sorted[~c.y]; l1 = plo[g]; h1 = phi[g]; }
+        else { l1 = __ldcg(nlo + c.y); h1 = __ldcg(nhi + c.y); }
+        __stcg(nlo + p, make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.f));
+        __stcg(nhi + p, make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.f));
+        p = parent_int[p];
+    }
+}
+
+// ---- collapse to the compressed 8-wide layout ----------------------------
+struct CollapseArgs {
+    const int2 *child;      // binary internal nodes
+    const int2 *range;
+    const float4 *nlo, *nhi;
+    const uint32_t *sorted;   // sorted position -> global prim
+    const float4 *plo, *phi;  // per global prim
+    BvhInput in;
+    uint4 *nodes;
+    float4 *prims;
+    int *node_counter, *prim_counter;
+    const int2 *qin;        // (binary node encoded, wide node index)
+    const int *qin_count;
+    int2 *qout;
+    int *qout_count;
+};
+
+struct ChildInfo {
+    int enc;            // >= 0 internal binary node, < 0 leaf (~sorted index)
+    int first, count;
+    float lo[3], hi[3];
+};
+
+__device__ void child_info(const CollapseArgs &a, int enc, ChildInfo &c) {
+    c.enc = enc;
+    float4 l, h;
+    if (enc < 0) {
+        int j = ~enc;
+        uint32_t g = a.sorted[j];
+        l = a.plo[g];
+        h = a.phi[g];
+        c.first = j;
+        c.count = 1;
+    } else {
+        l = a.nlo[enc];
+        h = a.nhi[enc];
+        int2 r = a.range[enc];
+        c.first = r.x;
+        c.count = r.y - r.x + 1;
+    }
+    c.lo[0] = l.x; c.lo[1] = l.y; c.lo[2] = l.z;
+    c.hi[0] = h.x; c.hi[1] = h.y; c.hi[2] = h.z;
+}
+
+__device__ float half_area(const ChildInfo &c) {
+    float dx = c.hi[0] - c.lo[0], dy = c.hi[1] - c.lo[1], dz = c.hi[2] - c.lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ void write_prim(const CollapseArgs &a, int sorted_pos, int slot) {
+    uint32_t g = a.sorted[sorted_pos];
+    float4 *dst = a.prims + (size_t)slot * kPrimF4;
+    if ((int)g < a.in.num_tris) {
+        int i0 = a.in.tri_vidx[g * 3], i1 = a.in.tri_vidx[g * 3 + 1], i2 = a.in.tri_vidx[g * 3 + 2];
+        V3 p0{a.in.vpos[i0 * 3], a.in.vpos[i0 * 3 + 1], a.in.vpos[i0 * 3 + 2]};
+        V3 p1{a.in.vpos[i1 * 3], a.in.vpos[i1 * 3 + 1], a.in.vpos[i1 * 3 + 2]};
+        V3 p2{a.in.vpos[i2 * 3], a.in.vpos[i2 * 3 + 1], a.in.vpos[i2 * 3 + 2]};
+        V3 e1 = xsub(p1, p0), e2 = xsub(p2, p0);
+        dst[0] = make_float4(p0.x, p0.y, p0.z, __int_as_float((int)g));
+        dst[1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+        dst[2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+    } else {
+        const float *s = a.in.spheres + (size_t)((int)g - a.in.num_tris) * 4;
+        dst[0] = make_float4(s[0], s[1], s[2], __int_as_float((int)g));
+        dst[1] = make_float4(s[3], 0.0f, 0.0f, 1.0f);
+        dst[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+__global__ void k_collapse(CollapseArgs a) {
+    int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= *a.qin_count) return;
+    int2 q = a.qin[item];
+    ChildInfo ch[8];
+    int cnt;
+    if (q.x < 0) {
+        child_info(a, q.x, ch[0]);
+        cnt = 1;
+    } else {
+        int2 c = a.child[q.x];
+        child_info(a, c.x, ch[0]);
+        child_info(a, c.y, ch[1]);
+        cnt = 2;
+    }
+    // greedy expansion of the largest child that must stay internal
+    while (cnt < 8) {
+        int best = -1;
+        float best_area = -1.0f;
+        for (int k = 0; k < cnt; k++) {
+            if (ch[k].enc >= 0 && ch[k].count > 3) {
+                float ar = half_area(ch[k]);
+                if (ar > best_area) { best_area = ar; best = k; }
+            }
+        }
+        if (best < 0) break;
+        int2 c = a.child[ch[best].enc];
+        child_info(a, c.y, ch[cnt]);
+        child_info(a, c.x, ch[best]);
+        cnt++;
+    }
+    // node box
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int k = 0; k < cnt; k++)
+        for (int ax = 0; ax < 3; ax++) {
+            lo[ax] = fminf(lo[ax], ch[k].lo[ax]);
+            hi[ax] = fmaxf(hi[ax], ch[k].hi[ax]);
+        }
+    // octant slot assignment: slot s prefers children offset toward
+    // (+x if s&4, +y if s&2, +z if s&1); greedy on the 8x8 cost table.
+    float pc[3] = {(lo[0] + hi[0]) * 0.5f, (lo[1] + hi[1]) * 0.5f, (lo[2] + hi[2]) * 0.5f};
+    int slot_of[8], child_in_slot[8];
+    for (int k = 0; k < 8; k++) { slot_of[k] = -1; child_in_slot[k] = -1; }
+    for (int round = 0; round < cnt; round++) {
+        float best = FLT_MAX;
+        int bc = -1, bs = -1;
+        for (int k = 0; k < cnt; k++) {
+            if (slot_of[k] >= 0) continue;
+            float ox = (ch[k].lo[0] + ch[k].hi[0]) * 0.5f - pc[0];
+            float oy = (ch[k].lo[1] + ch[k].hi[1]) * 0.5f - pc[1];
+            float oz = (ch[k].lo[2] + ch[k].hi[2]) * 0.5f - pc[2];
+            for (int s = 0; s < 8; s++) {
+                if (child_in_slot[s] >= 0) continue;
+                float cost = -((s & 4 ? ox : -ox) + (s & 2 ? oy : -oy) + (s & 1 ? oz : -oz));
+                if (cost < best) { best = cost; bc = k; bs = s; }
+            }
+        }
+        slot_of[bc] = bs;
+        child_in_slot[bs] = bc;
+    }
+    int n_int = 0, n_prims = 0;
+    for (int k = 0; k < cnt; k++) {
+        if (ch[k].count > 3) n_int++;
+        else n_prims += ch[k].count;
+    }
+    int child_base = n_int ? atomicAdd(a.node_counter, n_int) : 0;
+    int prim_base = n_prims ? atomicAdd(a.prim_counter, n_prims) : 0;
+    int qbase = n_int ? atomicAdd(a.qout_count, n_int) : 0;
+    // quantization frame: per-axis power-of-two scale with 255 * s >= extent
+    uint32_t ebits[3];
+    float sc[3];
+    for (int ax = 0; ax < 3; ax++) {
+        float ext = hi[ax] - lo[ax];
+        int e = ext > 0.0f ? (int)ceilf(log2f(ext / 255.0f)) : -126;
+        e = max(-126, min(127, e));
+        float s = ldexpf(1.0f, e);
+        while (lo[ax] + 255.0f * s < hi[ax] && e < 127) { e++; s = ldexpf(1.0f, e); }
+        ebits[ax] = (uint32_t)(e + 127);
+        sc[ax] = s;
+    }
+    uint32_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint32_t qlo[3][8], qhi[3][8];
+    uint32_t imask = 0;
+    int int_rank = 0, prim_off = 0;
+    for (int s = 0; s < 8; s++) {
+        for (int ax = 0; ax < 3; ax++) { qlo[ax][s] = 0; qhi[ax][s] = 0; }
+        int k = child_in_slot[s];
+        if (k < 0) continue;
+        const ChildInfo &c = ch[k];
+        for (int ax = 0; ax < 3; ax++) {
+            float fl = floorf((c.lo[ax] - lo[ax]) / sc[ax]);
+            float fh = ceilf((c.hi[ax] - lo[ax]) / sc[ax]);
+            int ql = (int)fmaxf(0.0f, fminf(255.0f, fl));
+            int qh = (int)fmaxf(0.0f, fminf(255.0f, fh));
+            while (ql > 0 && lo[ax] + (float)ql * sc[ax] > c.lo[ax]) ql--;
+            while (qh < 255 && lo[ax] + (float)qh * sc[ax] < c.hi[ax]) qh++;
+            if (qh <= ql) { if (qh < 255) qh = ql + 1; else ql = qh - 1; }
+            qlo[ax][s] = (uint32_t)ql;
+            qhi[ax][s] = (uint32_t)qh;
+        }
+        if (c.count > 3) {
+            meta[s] = (1u << 5) | (24u + (uint32_t)s);
+            imask |= 1u << s;
+            int2 e = make_int2(c.enc, child_base + int_rank);
+            a.qout[qbase + int_rank] = e;
+            int_rank++;
+        } else {
+            uint32_t unary = c.count == 1 ? 1u : (c.count == 2 ? 3u : 7u);
+            meta[s] = (unary << 5) | (uint32_t)prim_off;
+            for (int m = 0; m < c.count; m++) write_prim(a, c.first + m, prim_base + prim_off + m);
+            prim_off += c.count;
+        }
+    }
+    auto pack = [](const uint32_t *b) {
+        return b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24);
+    };
+    uint4 *dst = a.nodes + (size_t)q.y * kWideNodeU4;
+    dst[0] = make_uint4(__float_as_uint(lo[0]), __float_as_uint(lo[1]), __float_as_uint(lo[2]),
+                        ebits[0] | (ebits[1] << 8) | (ebits[2] << 16) | (imask << 24));
+    dst[1] = make_uint4((uint32_t)child_base, (uint32_t)prim_base, pack(meta), pack(meta + 4));
+    dst[2] = make_uint4(pack(qlo[0]), pack(qlo[0] + 4), pack(qlo[1]), pack(qlo[1] + 4));
+    dst[3] = make_uint4(pack(qlo[2]), pack(qlo[2] + 4), pack(qhi[0]), pack(qhi[0] + 4));
+    dst[4] = make_uint4(pack(qhi[1]), pack(qhi[1] + 4), pack(qhi[2]), pack(qhi[2] + 4));
+}
+
+__global__ void k_set_int(int *p, int v) { *p = v; }
+
+__global__ void k_trace_closest(DevBvh bvh, const float4 *rays, float4 *hits, int64_t n, int *status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
+    TraceHit h{0.0f, -1, 0.0f, 0.0f};
+    int ovf = 0;
+    bool f = trace_bvh<false>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
+    hits[i] = f ? make_float4(h.t, __int_as_float(h.prim), h.u, h.v)
+                : make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f);
+    if (ovf) atomicOr(status, kStatusStackOverflow);
+}
+
+__global__ void k_trace_any(DevBvh bvh, const float4 *rays, uint8_t *occ, int64_t n, int *status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
+    TraceHit h{0.0f, -1, 0.0f, 0.0f};
+    int ovf = 0;
+    bool f = trace_bvh<true>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
+    occ[i] = f ? 1 : 0;
+    if (ovf) atomicOr(status, kStatusStackOverflow);
+}
+
+inline int grid_for(int64_t n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+size_t radix_hist_entries(int64_t n) {
+    int64_t tiles = (n + kRsTile - 1) / kRsTile;
+    return (size_t)256 * (size_t)(tiles > 0 ? tiles : 1);
+}
+
+int radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tmp_keys, uint32_t *tmp_vals,
+                     uint32_t *hist, int64_t n, cudaStream_t s, std::string *err) {
+    if (n <= 1) return 0;
+    int tiles = (int)((n + kRsTile - 1) / kRsTile);
+    uint32_t *ki = keys, *vi = vals, *ko = tmp_keys, *vo = tmp_vals;
+    for (int shift = 0; shift < 32; shift += 8) {
+        k_rs_hist<<<tiles, kRsThreads, 0, s>>>(ki, n, shift, hist, tiles);
+        k_rs_scan<<<1, 1024, 0, s>>>(hist, (int64_t)256 * tiles);
+        k_rs_scatter<<<tiles, kRsThreads, 0, s>>>(ki, vi, ko, vo, n, shift, hist, tiles);
+        std::swap(ki, ko);
+        std::swap(vi, vo);
+    }
+    LJ_CUDA_TRY(cudaGetLastError());
+    return 0;   // four passes: the result is back in keys / vals
+}
+
+int morton_codes_tris(const float *tri_vertices, int64_t n, uint32_t *codes, uint32_t *bounds,
+                      cudaStream_t s, std::string *err) {
+    float4 *cent = nullptr;
+    LJ_CUDA_TRY(cudaMallocAsync(&cent, (size_t)n * sizeof(float4), s));
+    k_init_bounds<<<1, 32, 0, s>>>(bounds, 6);
+    k_tri_centroids<<<grid_for(n, 256), 256, 0, s>>>(tri_vertices, n, cent, bounds);
+    k_morton<<<grid_for(n, 256), 256, 0, s>>>(cent, n, bounds, codes, nullptr);
+    LJ_CUDA_TRY(cudaGetLastError());
+    LJ_CUDA_TRY(cudaFreeAsync(cent, s));
+    return 0;
+}
+
+int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *err) {
+    const int n = in.num_tris + in.num_spheres;
+    out->num_nodes = 0;
+    out->num_binary = 0;
+    if (n == 0) return 0;
+    cudaEvent_t e0, e1;
+    LJ_CUDA_TRY(cudaEventCreate(&e0));
+    LJ_CUDA_TRY(cudaEventCreate(&e1));
+    LJ_CUDA_TRY(cudaEventRecord(e0, s));
+
+    // scratch (freed at the end of the build)
+    float4 *plo, *phi, *cent, *nlo, *nhi;
+    uint32_t *bounds, *codes, *idx, *tk, *tv, *hist, *flags;
+    int2 *child, *range, *q0, *q1;
+    int *parent_int, *parent_leaf, *counters;
+    const int ni = n > 1 ? n - 1 : 1;
+    size_t hist_n = radix_hist_entries(n);
+    LJ_CUDA_TRY(cudaMallocAsync(&plo, sizeof(float4) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&phi, sizeof(float4) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&cent, sizeof(float4) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&nlo, sizeof(float4) * ni, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&nhi, sizeof(float4) * ni, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&bounds, sizeof(uint32_t) * 16, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&codes, sizeof(uint32_t) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&idx, sizeof(uint32_t) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&tk, sizeof(uint32_t) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&tv, sizeof(uint32_t) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&hist, sizeof(uint32_t) * hist_n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&flags, sizeof(uint32_t) * ni, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&child, sizeof(int2) * ni, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&range, sizeof(int2) * ni, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&q0, sizeof(int2) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&q1, sizeof(int2) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&parent_int, sizeof(int) * ni, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&parent_leaf, sizeof(int) * n, s));
+    LJ_CUDA_TRY(cudaMallocAsync(&counters, sizeof(int) * 4, s));
+    // outputs
+    LJ_CUDA_TRY(cudaMalloc(&out->nodes, sizeof(uint4) * kWideNodeU4 * (size_t)ni));
+    LJ_CUDA_TRY(cudaMalloc(&out->prims, sizeof(float4) * kPrimF4 * (size_t)n));
+
+    k_init_bounds<<<1, 32, 0, s>>>(bounds, 12);
+    k_prim_bounds<<<grid_for(n, 256), 256, 0, s>>>(in, plo, phi, cent, bounds);
+    k_morton<<<grid_for(n, 256), 256, 0, s>>>(cent, n, bounds, codes, idx);
+    if (radix_sort_pairs(codes, idx, tk, tv, hist, n, s, err)) return -2;
+    LJ_CUDA_TRY(cudaMemsetAsync(parent_int, 0xff, sizeof(int) * ni, s));
+    LJ_CUDA_TRY(cudaMemsetAsync(parent_leaf, 0xff, sizeof(int) * n, s));
+    LJ_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(uint32_t) * ni, s));
+    if (n > 1) {
+        k_karras<<<grid_for(n - 1, 256), 256, 0, s>>>(codes, n, child, range, parent_int, parent_leaf);
+        k_bottom_up<<<grid_for(n, 256), 256, 0, s>>>(n, child, parent_int, parent_leaf, idx, plo, phi,
+                                                      nlo, nhi, flags);
+    }
+    // collapse, level by level
+    int h_root[2] = {n > 1 ? 0 : ~0, 0};
+    LJ_CUDA_TRY(cudaMemcpyAsync(q0, h_root, sizeof(int2), cudaMemcpyHostToDevice, s));
+    int h_counters[4] = {1, 0, 1, 0};   // node counter, prim counter, qin count, qout count
+    LJ_CUDA_TRY(cudaMemcpyAsync(counters, h_counters, sizeof(h_counters), cudaMemcpyHostToDevice, s));
+    CollapseArgs a;
+    a.child = child; a.range = range; a.nlo = nlo; a.nhi = nhi; a.sorted = idx;
+    a.plo = plo; a.phi = phi; a.in = in; a.nodes = out->nodes; a.prims = out->prims;
+    a.node_counter = counters; a.prim_counter = counters + 1;
+    int qcount = 1;
+    int2 *qin = q0, *qout = q1;
+    int *cin = counters + 2, *cout = counters + 3;
+    for (int level = 0; level < 4096 && qcount > 0; level++) {
+        k_set_int<<<1, 1, 0, s>>>(cout, 0);
+        a.qin = qin; a.qin_count = cin; a.qout = qout; a.qout_count = cout;
+        k_collapse<<<grid_for(qcount, 128), 128, 0, s>>>(a);
+        LJ_CUDA_TRY(cudaMemcpyAsync(&qcount, cout, sizeof(int), cudaMemcpyDeviceToHost, s));
+        LJ_CUDA_TRY(cudaStreamSynchronize(s));
+        std::swap(qin, qout);
+        std::swap(cin, cout);
+    }
+    int h_final[2];
+    LJ_CUDA_TRY(cudaMemcpyAsync(h_final, counters, sizeof(h_final), cudaMemcpyDeviceToHost, s));
+    uint32_t hb[12];
+    LJ_CUDA_TRY(cudaMemcpyAsync(hb, bounds, sizeof(hb), cudaMemcpyDeviceToHost, s));
+    LJ_CUDA_TRY(cudaEventRecord(e1, s));
+    LJ_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    out->build_ms = ms;
+    out->num_nodes = h_final[0];
+    out->num_binary = n - 1;
+    for (int k = 0; k < 3; k++) {
+        out->lo[k] = o2f_host(hb[6 + k]);
+        out->hi[k] = o2f_host(hb[9 + k]);
+    }
+    cudaFreeAsync(plo, s); cudaFreeAsync(phi, s); cudaFreeAsync(cent, s);
+    cudaFreeAsync(nlo, s); cudaFreeAsync(nhi, s); cudaFreeAsync(bounds, s);
+    cudaFreeAsync(codes, s); cudaFreeAsync(idx, s); cudaFreeAsync(tk, s); cudaFreeAsync(tv, s);
+    cudaFreeAsync(hist, s); cudaFreeAsync(flags, s); cudaFreeAsync(child, s);
+    cudaFreeAsync(range, s); cudaFreeAsync(q0, s); cudaFreeAsync(q1, s);
+    cudaFreeAsync(parent_int, s); cudaFreeAsync(parent_leaf, s); cudaFreeAsync(counters, s);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (h_final[1] != n) {
+        if (err) *err = "BVH collapse placed " + std::to_string(h_final[1]) + " of " + std::to_string(n) + " primitives";
+        return -5;
+    }
+    LJ_CUDA_TRY(cudaGetLastError());
+    return 0;
+}
+
+int launch_trace_closest(const DevBvh &bvh, const void *rays, void *hits, int64_t n, int *d_status,
+                         cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_trace_closest<<<grid_for(n, 128), 128, 0, s>>>(bvh, (const float4 *)rays, (float4 *)hits, n, d_status);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+int launch_trace_any(const DevBvh &bvh, const void *rays, uint8_t *occ, int64_t n, int *d_status,
+                     cudaStream_t s) {
+    if (n <= 0) return 0;
+    k_trace_any<<<grid_for(n, 128), 128, 0, s>>>(bvh, (const float4 *)rays, occ, n, d_status);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
+}  // namespace lj

@@ -1,0 +1,48 @@
+// Host-side handle types behind the opaque lj_ctx / lj_scene of lj_gpu.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lj_gpu.h"
+#include "lj_internal.h"
+
+struct lj_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    int *d_status = nullptr;      // device status word (bounded-loop flags)
+    // grow-only scratch for the Morton / radix-sort entry point
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+};
+
+// Wavefront buffers owned by a scene, grown on demand (lj_path.cu).
+struct PathBuffers {
+    size_t capacity = 0;
+    void *block = nullptr;
+    size_t bytes = 0;
+};
+
+struct lj_scene {
+    lj_ctx *ctx = nullptr;
+    lj::DevScene dev{};
+    std::vector<void *> allocs;   // device allocations freed on destroy
+    lj_scene_info info{};
+    lj_render_options options{};
+    int width = 0, height = 0;
+    int num_spheres = 0;
+    std::vector<int> shape_prim_base;   // shape -> first global prim
+    std::vector<int> prim_shape_host;   // global prim -> shape
+    PathBuffers path;
+    bool has_media = false;
+};
+
+namespace lj {
+int set_error(lj_ctx *ctx, int code, const std::string &msg);
+// lj_path.cu
+int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, cudaStream_t s,
+                lj_stats *stats, bool sync_stats);
+}  // namespace lj

@@ -1,0 +1,65 @@
+// Host-side declarations shared by the .cu translation units of liblj_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "lj_scene.cuh"
+
+namespace lj {
+
+// Status word bits written by bounded device loops.
+enum : int {
+    kStatusStackOverflow = 1,
+    kStatusBounceCap = 2,
+    kStatusNullCollisionCap = 4,
+    kStatusQueueOverflow = 8,
+};
+
+#define LJ_CUDA_TRY(expr)                                                      \
+    do {                                                                       \
+        cudaError_t _e = (expr);                                               \
+        if (_e != cudaSuccess) {                                               \
+            if (err) *err = std::string(#expr) + ": " + cudaGetErrorString(_e); \
+            return -2;                                                         \
+        }                                                                      \
+    } while (0)
+
+// ---- radix sort (lj_bvh.cu) ----
+// Stable LSD sort of (key, value) pairs on bits [0, 32) of the key, 8 bits
+// per pass.  tmp_keys/tmp_vals: n entries; hist: radix_hist_entries(n).
+size_t radix_hist_entries(int64_t n);
+int radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tmp_keys, uint32_t *tmp_vals,
+                     uint32_t *hist, int64_t n, cudaStream_t s, std::string *err);
+
+// Morton codes of triangle centroids (n x 9 floats) over their centroid box.
+// `bounds_scratch`: 8 uint32.
+int morton_codes_tris(const float *tri_vertices, int64_t n, uint32_t *codes,
+                      uint32_t *bounds_scratch, cudaStream_t s, std::string *err);
+
+// ---- BVH build (lj_bvh.cu) ----
+struct BvhInput {
+    const float *vpos;      // device, global vertex positions
+    const int *tri_vidx;    // device, 3 per triangle
+    const float *spheres;   // device, 4 floats (c, r) per sphere (prims num_tris ..)
+    int num_tris, num_spheres;
+};
+struct BvhOutput {
+    uint4 *nodes = nullptr;     // device, owned by the scene
+    float4 *prims = nullptr;    // device
+    int num_nodes = 0;
+    int num_binary = 0;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // scene AABB (rtcGetSceneBounds)
+    double build_ms = 0;
+};
+int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *err);
+
+// ---- batch trace (lj_bvh.cu) ----
+int launch_trace_closest(const DevBvh &bvh, const void *rays, void *hits, int64_t n,
+                         int *d_status, cudaStream_t s);
+int launch_trace_any(const DevBvh &bvh, const void *rays, uint8_t *occ, int64_t n,
+                     int *d_status, cudaStream_t s);
+
+}  // namespace lj

@@ -1,0 +1,180 @@
+// Ray traversal of the compressed 8-wide BVH: the GPU replacement of
+// rtcIntersect1 / rtcOccluded1 (src/intersection.cpp:32, :83).
+//
+// Node groups follow the hit-mask scheme of Ylitie, Karras and Laine,
+// "Efficient Incoherent Ray Traversal on GPUs Through Compressed Wide BVHs"
+// (HPG 2017): a group is (base index, 32-bit mask); bits 24-31 mark hit
+// internal children, placed at slot ^ (7 - ray octant) so that popping the
+// highest bit first visits children roughly front to back; bits 0-23 mark
+// hit leaf primitives (prim_base + bit).  Each node is five 128-bit loads.
+//
+// Primitive hits use the exact-rounding Moller-Trumbore test of
+// lj_common.cuh (bit-identical to the CPU oracle) and, for spheres, the
+// reference's user-geometry semantics (src/shapes/sphere.inl:40-106: nearest
+// root in [tnear, tfar)).
+#pragma once
+
+#include "lj_common.cuh"
+#include "lj_scene.cuh"
+
+namespace lj {
+
+struct TraceHit {
+    float t;
+    int prim;
+    float u, v;
+};
+
+// Sphere: returns t in [tnear, tfar) of the nearest root, or -1.  FP32 with
+// the "closest point" discriminant (no catastrophic cancellation for rays
+// starting far from a small sphere).
+LJ_D float sphere_hit(V3 c, float r, V3 o, V3 d, float tnear, float tfar) {
+    V3 v = o - c;
+    float A = dot(d, d);
+    float b = dot(d, v);               // B / 2
+    V3 f = v - d * (b / A);            // vector from center to closest point
+    float disc = r * r - dot(f, f);    // (discriminant / 4) / A
+    if (disc < 0.0f) return -1.0f;
+    float q = -(b + copysignf(sqrtf(A * disc), b));
+    float C = dot(v, v) - r * r;
+    float t0, t1;
+    if (q == 0.0f) {
+        t0 = t1 = -b / A;
+    } else {
+        t0 = C / q;
+        t1 = q / A;
+    }
+    if (t0 > t1) { float tmp = t0; t0 = t1; t1 = tmp; }
+    float t = -1.0f;
+    if (t0 >= tnear && t0 < tfar) t = t0;
+    if (t1 >= tnear && t1 < tfar && t < 0.0f) t = t1;
+    return (t >= tnear && t < tfar) ? t : -1.0f;
+}
+
+LJ_D uint32_t extract_byte(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
+
+// Returns true on hit.  kAny: stop at the first hit (occlusion query).
+// `hit` is updated with the closest hit; tfar shrinks as hits are found.
+// *overflow is set if the traversal stack was exhausted (bounded loop).
+template <bool kAny>
+LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, TraceHit &hit,
+                    int *overflow) {
+    if (bvh.num_nodes == 0) return false;
+    // direction components of exactly zero would give inf * 0 in the slab test
+    const float tiny = 1e-30f;
+    V3 dd = V3{fabsf(d.x) < tiny ? copysignf(tiny, d.x) : d.x,
+               fabsf(d.y) < tiny ? copysignf(tiny, d.y) : d.y,
+               fabsf(d.z) < tiny ? copysignf(tiny, d.z) : d.z};
+    V3 inv = V3{1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z};
+    const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
+    const uint32_t oct_xor = 7u - oct;
+    const bool negx = inv.x < 0.0f, negy = inv.y < 0.0f, negz = inv.z < 0.0f;
+
+    uint2 stack[kTraversalStack];
+    int sp = 0;
+    bool found = false;
+    // virtual parent: one internal child in slot 0 pointing at node 0
+    uint2 ngroup = make_uint2(0u, (1u << (24u + (0u ^ oct_xor))) | 1u);
+    // every iteration visits one node or one primitive group; a well-formed
+    // tree needs far fewer than this, a corrupt one stops here with a flag
+    const int kMaxIterations = 1 << 22;
+    for (int iter = 0;; iter++) {
+        if (iter >= kMaxIterations) {
+            *overflow = 1;
+            break;
+        }
+        uint2 tgroup = make_uint2(0u, 0u);
+        if (ngroup.y > 0x00ffffffu) {
+            uint32_t k = 31u - __clz(ngroup.y & 0xff000000u);
+            uint32_t slot = (k - 24u) ^ oct_xor;
+            uint32_t imask = ngroup.y & 0xffu;
+            uint32_t child = ngroup.x + __popc(imask & ((1u << slot) - 1u));
+            ngroup.y &= ~(1u << k);
+            if (ngroup.y > 0x00ffffffu) {
+                if (sp < kTraversalStack) stack[sp++] = ngroup;
+                else *overflow = 1;
+            }
+            const uint4 *np = bvh.nodes + (size_t)child * kWideNodeU4;
+            uint4 c0 = __ldg(np + 0), c1 = __ldg(np + 1), c2 = __ldg(np + 2),
+                  c3 = __ldg(np + 3), c4 = __ldg(np + 4);
+            float px = __uint_as_float(c0.x), py = __uint_as_float(c0.y), pz = __uint_as_float(c0.z);
+            float sx = __uint_as_float((c0.w & 0xffu) << 23);
+            float sy = __uint_as_float(((c0.w >> 8) & 0xffu) << 23);
+            float sz = __uint_as_float(((c0.w >> 16) & 0xffu) << 23);
+            uint32_t nimask = c0.w >> 24;
+            // plane t = q * a + b
+            float ax = sx * inv.x, bx = (px - o.x) * inv.x;
+            float ay = sy * inv.y, by = (py - o.y) * inv.y;
+            float az = sz * inv.z, bz = (pz - o.z) * inv.z;
+            uint32_t node_hits = 0, prim_hits = 0;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                uint32_t meta = extract_byte(i < 4 ? c1.z : c1.w, i & 3);
+                if (meta == 0u) continue;
+                uint32_t lox = extract_byte(i < 4 ? c2.x : c2.y, i & 3);
+                uint32_t loy = extract_byte(i < 4 ? c2.z : c2.w, i & 3);
+                uint32_t loz = extract_byte(i < 4 ? c3.x : c3.y, i & 3);
+                uint32_t hix = extract_byte(i < 4 ? c3.z : c3.w, i & 3);
+                uint32_t hiy = extract_byte(i < 4 ? c4.x : c4.y, i & 3);
+                uint32_t hiz = extract_byte(i < 4 ? c4.z : c4.w, i & 3);
+                float nx = fmaf((float)(negx ? hix : lox), ax, bx);
+                float fx = fmaf((float)(negx ? lox : hix), ax, bx);
+                float ny = fmaf((float)(negy ? hiy : loy), ay, by);
+                float fy = fmaf((float)(negy ? loy : hiy), ay, by);
+                float nz = fmaf((float)(negz ? hiz : loz), az, bz);
+                float fz = fmaf((float)(negz ? loz : hiz), az, bz);
+                // a few ulps of slack keep hits on box faces from being culled
+                float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, tnear)) * (1.0f - 2.0e-7f);
+                float tmax = fminf(fminf(fx, fy), fminf(fz, tfar * (1.0f + 2.0e-7f))) * (1.0f + 2.0e-7f);
+                if (tmin <= tmax) {
+                    uint32_t off = meta & 0x1fu;
+                    if (off >= 24u) node_hits |= 1u << (24u + ((uint32_t)i ^ oct_xor));
+                    else prim_hits |= ((meta >> 5) & 7u) << off;
+                }
+            }
+            ngroup = make_uint2(c1.x, node_hits | nimask);
+            tgroup = make_uint2(c1.y, prim_hits);
+        } else {
+            tgroup = ngroup;
+            ngroup = make_uint2(0u, 0u);
+        }
+        while (tgroup.y != 0u) {
+            int b = __ffs(tgroup.y) - 1;
+            tgroup.y &= tgroup.y - 1u;
+            const float4 *pp = bvh.prims + (size_t)(tgroup.x + (uint32_t)b) * kPrimF4;
+            float4 f0 = __ldg(pp + 0), f1 = __ldg(pp + 1);
+            if (f1.w == 0.0f) {
+                float4 f2 = __ldg(pp + 2);
+                float t, u, v;
+                if (tri_intersect(V3{f0.x, f0.y, f0.z}, V3{f1.x, f1.y, f1.z}, V3{f2.x, f2.y, f2.z}, o,
+                                  d, tnear, tfar, t, u, v)) {
+                    found = true;
+                    if (kAny) return true;
+                    tfar = t;
+                    hit.t = t;
+                    hit.u = u;
+                    hit.v = v;
+                    hit.prim = __float_as_int(f0.w);
+                }
+            } else {
+                float t = sphere_hit(V3{f0.x, f0.y, f0.z}, f1.x, o, d, tnear, tfar);
+                if (t >= 0.0f) {
+                    found = true;
+                    if (kAny) return true;
+                    tfar = t;
+                    hit.t = t;
+                    hit.u = 0.0f;   // sphere uv is recomputed from the hit point
+                    hit.v = 0.0f;
+                    hit.prim = __float_as_int(f0.w);
+                }
+            }
+        }
+        if (ngroup.y <= 0x00ffffffu) {
+            if (sp == 0) break;
+            ngroup = stack[--sp];
+        }
+    }
+    return found;
+}
+
+}  // namespace lj

@@ -1,0 +1,220 @@
+"""Python binding of liblj_gpu.so (include/lj_gpu.h) -- the GPU hot path.
+
+This is the host-side mirror of the reference's render interface:
+  GpuScene(scene)              ~ Scene::Scene (src/scene.cpp:4-53): upload +
+                                 device BVH build
+  GpuScene.render(...)         ~ Image3 render(const Scene&) (src/render.cpp:155-170)
+  GpuScene.trace_closest(...)  ~ rtcIntersect1 per ray (src/intersection.cpp:32)
+  GpuScene.trace_any(...)      ~ rtcOccluded1 per ray (src/intersection.cpp:83)
+Errors raise LjError (the reference throws fl_exception, src/flexception.h).
+
+There is no CPU fallback: if the CUDA library is missing or no GB300-class
+device is present, construction raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "liblj_gpu.so")
+
+_lib = None
+
+
+class LjError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("lj_gpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load liblj_gpu.so (building it first if needed).  Raises if it cannot."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            from . import build as _build
+            _build.build()
+        L = C.CDLL(LIB_PATH)
+        vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int32
+        L.lj_gpu_init.argtypes = [C.c_int, C.POINTER(vp)]
+        L.lj_gpu_shutdown.argtypes = [vp]
+        L.lj_gpu_last_error.argtypes = [vp]
+        L.lj_gpu_last_error.restype = C.c_char_p
+        L.lj_gpu_abi_version.restype = C.c_int
+        L.lj_gpu_scene_create.argtypes = [vp, C.POINTER(abi.lj_scene_desc), C.POINTER(vp)]
+        L.lj_gpu_scene_destroy.argtypes = [vp]
+        L.lj_gpu_scene_info.argtypes = [vp, C.POINTER(abi.lj_scene_info)]
+        L.lj_gpu_render.argtypes = [vp, C.POINTER(abi.lj_render_params), vp, C.POINTER(abi.lj_stats)]
+        L.lj_gpu_render_device.argtypes = [vp, C.POINTER(abi.lj_render_params), vp, vp,
+                                           C.POINTER(abi.lj_stats)]
+        L.lj_gpu_trace_closest.argtypes = [vp, vp, vp, i64, vp]
+        L.lj_gpu_trace_any.argtypes = [vp, vp, vp, i64, vp]
+        L.lj_gpu_prim_to_shape.argtypes = [vp, i32, C.POINTER(i32), C.POINTER(i32)]
+        L.lj_gpu_morton_sort.argtypes = [vp, vp, i64, vp, vp, vp]
+        L.lj_gpu_bsdf_param_count.argtypes = [i32]
+        L.lj_gpu_bsdf_batch.argtypes = [vp, C.POINTER(abi.lj_bsdf_batch), i64, vp]
+        L.lj_gpu_light_sample_batch.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp]
+        L.lj_gpu_phase_batch.argtypes = [vp, i32, C.c_float, vp, vp, vp, vp, vp, vp, i64, vp]
+        _lib = L
+    return _lib
+
+
+def _ptr(t):
+    """Device pointer of a torch tensor (or None)."""
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+class Context:
+    def __init__(self, device=0):
+        self.h = C.c_void_p()
+        rc = lib().lj_gpu_init(device, C.byref(self.h))
+        if rc != abi.LJ_OK:
+            raise LjError(rc, "lj_gpu_init failed (no CUDA device of compute capability >= 10.0?)")
+        self.device = device
+
+    def check(self, rc):
+        if rc != abi.LJ_OK:
+            raise LjError(rc, lib().lj_gpu_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            lib().lj_gpu_shutdown(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- stateless batch kernels (torch CUDA tensors in, torch tensors out) --
+    def morton_sort(self, tri_vertices, stream=None):
+        import torch
+        n = tri_vertices.shape[0]
+        codes = torch.empty(n, dtype=torch.int32, device=tri_vertices.device)
+        order = torch.empty(n, dtype=torch.int32, device=tri_vertices.device)
+        self.check(lib().lj_gpu_morton_sort(self.h, _ptr(tri_vertices), n, _ptr(codes), _ptr(order),
+                                            stream))
+        return codes, order
+
+    def bsdf(self, material_type, op, params, dir_in, dir_out=None, rnd=None, to_view=False, stream=None):
+        import torch
+        n = dir_in.shape[0]
+        dev = dir_in.device
+        b = abi.lj_bsdf_batch()
+        b.material_type, b.op, b.transport_to_view = material_type, op, 1 if to_view else 0
+        out = {}
+        b.d_params, b.d_dir_in = params.data_ptr(), dir_in.data_ptr()
+        if dir_out is not None:
+            b.d_dir_out = dir_out.data_ptr()
+        if rnd is not None:
+            b.d_rnd = rnd.data_ptr()
+        if op == abi.LJ_BSDF_OP_EVAL:
+            out["value"] = torch.empty((n, 3), dtype=torch.float32, device=dev)
+            b.d_out_value = out["value"].data_ptr()
+        elif op == abi.LJ_BSDF_OP_PDF:
+            out["pdf"] = torch.empty(n, dtype=torch.float32, device=dev)
+            b.d_out_pdf = out["pdf"].data_ptr()
+        else:
+            out["dir"] = torch.empty((n, 3), dtype=torch.float32, device=dev)
+            out["eta"] = torch.empty(n, dtype=torch.float32, device=dev)
+            out["roughness"] = torch.empty(n, dtype=torch.float32, device=dev)
+            out["valid"] = torch.empty(n, dtype=torch.int32, device=dev)
+            b.d_out_dir, b.d_out_eta = out["dir"].data_ptr(), out["eta"].data_ptr()
+            b.d_out_roughness, b.d_out_valid = out["roughness"].data_ptr(), out["valid"].data_ptr()
+        self.check(lib().lj_gpu_bsdf_batch(self.h, C.byref(b), n, stream))
+        return out
+
+    def phase(self, kind, g, dir_in, dir_out, rnd, stream=None):
+        import torch
+        n = dir_in.shape[0]
+        dev = dir_in.device
+        val = torch.empty(n, dtype=torch.float32, device=dev)
+        pdf = torch.empty(n, dtype=torch.float32, device=dev)
+        d = torch.empty((n, 3), dtype=torch.float32, device=dev)
+        self.check(lib().lj_gpu_phase_batch(self.h, kind, g, _ptr(dir_in), _ptr(dir_out), _ptr(rnd),
+                                            _ptr(val), _ptr(pdf), _ptr(d), n, stream))
+        return val, pdf, d
+
+
+class GpuScene:
+    """A scene resident on the device (BVH built there)."""
+
+    def __init__(self, ctx, scene):
+        self.ctx = ctx
+        self.scene = scene
+        desc, keep = scene.desc()
+        self.h = C.c_void_p()
+        ctx.check(lib().lj_gpu_scene_create(ctx.h, C.byref(desc), C.byref(self.h)))
+        del keep
+
+    def close(self):
+        if self.h:
+            lib().lj_gpu_scene_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        inf = abi.lj_scene_info()
+        self.ctx.check(lib().lj_gpu_scene_info(self.h, C.byref(inf)))
+        return inf
+
+    def render(self, seed=0, spp=0, sample_offset=0, max_paths_in_flight=0):
+        """Host-memory render (includes device->host copy).  Returns (image HxWx3 float32, stats)."""
+        sc = self.scene
+        out = np.zeros((sc.height, sc.width, 3), np.float32)
+        p = abi.lj_render_params(seed=seed, spp=spp, sample_offset=sample_offset,
+                                 max_paths_in_flight=max_paths_in_flight)
+        st = abi.lj_stats()
+        self.ctx.check(lib().lj_gpu_render(self.h, C.byref(p), out.ctypes.data_as(C.c_void_p), C.byref(st)))
+        return out, st
+
+    def render_device(self, out, seed=0, spp=0, sample_offset=0, max_paths_in_flight=0, stream=None,
+                      stats=True):
+        """Render into a device tensor `out` (H*W*3 float32)."""
+        p = abi.lj_render_params(seed=seed, spp=spp, sample_offset=sample_offset,
+                                 max_paths_in_flight=max_paths_in_flight)
+        st = abi.lj_stats() if stats else None
+        self.ctx.check(lib().lj_gpu_render_device(self.h, C.byref(p), _ptr(out), stream,
+                                                  C.byref(st) if st is not None else None))
+        return st
+
+    def trace_closest(self, rays, stream=None):
+        """rays: (n, 8) float32 CUDA tensor -> (n, 4) hits (t, prim bits, u, v)."""
+        import torch
+        n = rays.shape[0]
+        hits = torch.empty((n, 4), dtype=torch.float32, device=rays.device)
+        self.ctx.check(lib().lj_gpu_trace_closest(self.h, _ptr(rays), _ptr(hits), n, stream))
+        return hits
+
+    def trace_any(self, rays, stream=None):
+        import torch
+        n = rays.shape[0]
+        occ = torch.empty(n, dtype=torch.uint8, device=rays.device)
+        self.ctx.check(lib().lj_gpu_trace_any(self.h, _ptr(rays), _ptr(occ), n, stream))
+        return occ
+
+    def light_sample(self, ref_points, rnd, stream=None):
+        import torch
+        n = ref_points.shape[0]
+        dev = ref_points.device
+        lid = torch.empty(n, dtype=torch.int32, device=dev)
+        pt = torch.empty((n, 3), dtype=torch.float32, device=dev)
+        nr = torch.empty((n, 3), dtype=torch.float32, device=dev)
+        pdf = torch.empty(n, dtype=torch.float32, device=dev)
+        self.ctx.check(lib().lj_gpu_light_sample_batch(self.h, _ptr(ref_points), _ptr(rnd), _ptr(lid),
+                                                       _ptr(pt), _ptr(nr), _ptr(pdf), n, stream))
+        return lid, pt, nr, pdf
+
+    def prim_to_shape(self, prim):
+        s, l = C.c_int32(), C.c_int32()
+        self.ctx.check(lib().lj_gpu_prim_to_shape(self.h, int(prim), C.byref(s), C.byref(l)))
+        return s.value, l.value

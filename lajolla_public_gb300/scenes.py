@@ -287,14 +287,14 @@ class Scene:
                 out += [f'  <bsdf type="roughplastic" id="mat{i}">',
                         f'    <rgb name="diffuseReflectance" value="{vec(tx[0]["value0"])}"/>',
                         f'    <rgb name="specularReflectance" value="{vec(tx[1]["value0"])}"/>',
-                        f'    <float name="alpha" value="{r(f32(tx[2]["value0"][0] ** 2))}"/>',
+                        f'    <float name="roughness" value="{r(tx[2]["value0"][0])}"/>',
                         f'    <float name="intIOR" value="{r(m["eta"])}"/>',
                         '    <float name="extIOR" value="1"/>', '  </bsdf>']
             elif m["type"] == abi.LJ_MAT_ROUGHDIELECTRIC:
                 out += [f'  <bsdf type="roughdielectric" id="mat{i}">',
                         f'    <rgb name="specularReflectance" value="{vec(tx[0]["value0"])}"/>',
                         f'    <rgb name="specularTransmittance" value="{vec(tx[1]["value0"])}"/>',
-                        f'    <float name="alpha" value="{r(f32(tx[2]["value0"][0] ** 2))}"/>',
+                        f'    <float name="roughness" value="{r(tx[2]["value0"][0])}"/>',
                         f'    <float name="intIOR" value="{r(m["eta"])}"/>',
                         '    <float name="extIOR" value="1"/>', '  </bsdf>']
             else:

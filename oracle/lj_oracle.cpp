@@ -1455,12 +1455,13 @@ static V3 path_tracing(const Scene &sc, int x, int y, Rng &rng, bool yx_order) {
         V2 luv{rng.next(), rng.next()};
         double lw = rng.next();
         double sw = rng.next();
-        int lid = sample_1d(sc.light_dist, lw);
-        const LightS &light = sc.lights[lid];
-        PN pl = sample_point_on_light(sc, light, vx.position, luv, sw);
         V3 C1{};
         double w1 = 0;
-        {
+        // a scene without lights has no NEE (the reference asserts there)
+        int lid = sc.lights.empty() ? -1 : sample_1d(sc.light_dist, lw);
+        if (lid >= 0) {
+            const LightS &light = sc.lights[lid];
+            PN pl = sample_point_on_light(sc, light, vx.position, luv, sw);
             double G = 0;
             V3 dl;
             if (light.kind != LJ_LIGHT_ENVMAP) {

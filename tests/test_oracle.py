@@ -1,0 +1,119 @@
+"""The oracle (C++ restatement, oracle/lj_oracle.cpp) pinned against golden
+vectors and renders produced by the reference's own code
+(tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+import ljtest
+from lajolla_public_gb300 import abi, scenes
+from oracle import ljo
+from golden import make_golden
+
+
+def test_pcg_matches_reference():
+    g = ljtest.golden("pcg")
+    for i, s in enumerate(g["streams"]):
+        raw = ljo.pcg(int(s), 0x31e241f862a1fb5e, g["raw"].shape[1])
+        np.testing.assert_array_equal(raw, g["raw"][i])
+        np.testing.assert_array_equal(raw.astype(np.float64) / 2.0 ** 32, g["real"][i])
+
+
+def test_table_dist_matches_reference():
+    g = ljtest.golden("table")
+    L = ljo.lib()
+    f1, u1 = np.ascontiguousarray(g["f1"]), np.ascontiguousarray(g["u1"])
+    idx = np.zeros(len(u1), np.int32)
+    pmf = np.zeros(len(u1))
+    L.ljo_table1d(ljo._p(f1), len(f1), ljo._p(u1), len(u1), ljo._p(idx), ljo._p(pmf))
+    np.testing.assert_array_equal(idx, g["idx1"].astype(np.int32))
+    np.testing.assert_allclose(pmf, g["pmf1"], rtol=1e-14, atol=0)
+    f2 = np.ascontiguousarray(g["f2"])
+    u2 = np.ascontiguousarray(g["u2"])
+    xy = np.zeros((len(u2), 2))
+    pdf = np.zeros(len(u2))
+    h, w = f2.shape
+    L.ljo_table2d(ljo._p(f2), w, h, ljo._p(u2), len(u2), ljo._p(xy), ljo._p(pdf))
+    np.testing.assert_allclose(xy, g["xy2"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(pdf, g["pdf2"], rtol=1e-13, atol=0)
+
+
+def test_bsdf_matches_reference():
+    g = ljtest.golden("bsdf")
+    rec, out = g["inputs"], g["outputs"]
+    for t in (0, 1, 2):
+        sel = rec[:, 0] == t
+        r, o = rec[sel], out[sel]
+        params = np.array([ljtest.bsdf_params(x)[1] for x in r], np.float32)
+        wi, wo, rnd = r[:, 9:12], r[:, 12:15], r[:, 15:18]
+        ev = ljo.bsdf(t, abi.LJ_BSDF_OP_EVAL, params, wi, wo)
+        evv = ljo.bsdf(t, abi.LJ_BSDF_OP_EVAL, params, wi, wo, to_view=True)
+        pd = ljo.bsdf(t, abi.LJ_BSDF_OP_PDF, params, wi, wo)
+        sm = ljo.bsdf(t, abi.LJ_BSDF_OP_SAMPLE, params, wi, rnd=rnd)
+        np.testing.assert_allclose(ev["value"], o[:, 0:3], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(evv["value"], o[:, 3:6], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(pd["pdf"], o[:, 6], rtol=1e-12, atol=1e-14)
+        np.testing.assert_array_equal(sm["valid"], o[:, 7].astype(np.int32))
+        v = sm["valid"] == 1
+        np.testing.assert_allclose(sm["dir"][v], o[v, 8:11], rtol=1e-12, atol=1e-13)
+        np.testing.assert_allclose(sm["eta"][v], o[v, 11], rtol=1e-12)
+        np.testing.assert_allclose(sm["roughness"][v], o[v, 12], rtol=1e-12)
+
+
+def test_phase_matches_reference():
+    g = ljtest.golden("phase")
+    r, o = g["inputs"], g["outputs"]
+    for gval in np.unique(r[:, 0]):
+        sel = r[:, 0] == gval
+        val, pdf, d = ljo.phase(abi.LJ_PHASE_HG, float(gval), r[sel, 1:4], r[sel, 4:7], r[sel, 7:9])
+        np.testing.assert_allclose(val, o[sel, 0], rtol=1e-12)
+        np.testing.assert_allclose(pdf, o[sel, 1], rtol=1e-12)
+        np.testing.assert_allclose(d, o[sel, 2:5], rtol=1e-10, atol=1e-12)
+
+
+def test_light_sampling_matches_reference():
+    g = ljtest.golden("light")
+    sc = ljtest.light_scene(g["env"], g["to_world"])
+    o = ljo.OracleScene(sc)
+    r, out = g["inputs"], g["outputs"]
+    lid, pt, nr, pdf = o.light_sample(r[:, 0:3], r[:, [3, 4, 5, 6]])
+    np.testing.assert_array_equal(lid, out[:, 0].astype(np.int32))
+    np.testing.assert_allclose(pt, out[:, 1:4], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(nr, out[:, 4:7], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(pdf, out[:, 7], rtol=1e-9)
+
+
+@pytest.mark.parametrize("case", sorted(make_golden.RENDER_CASES))
+def test_render_matches_reference_sample_for_sample(case):
+    """Tile-mode RNG reproduces the reference renderer's own image exactly
+    (up to its FP32 PFM output rounding)."""
+    ref = ljtest.golden("renders")[case]
+    sc = make_golden.RENDER_CASES[case]()
+    img = ljo.OracleScene(sc).render(mode="tile", yx_order=True)
+    np.testing.assert_allclose(img, ref, rtol=2e-7, atol=2e-7)
+
+
+def test_morton_sort_is_stable_and_sorted():
+    pos, idx = scenes.triangle_soup(5, 20000)
+    tri = pos[idx].reshape(-1, 9)
+    tri[100] = tri[7]          # duplicate codes -> order by index
+    codes, order = ljo.morton(tri)
+    assert codes.max() < (1 << 30)
+    s = codes[order]
+    assert np.all(np.diff(s.astype(np.int64)) >= 0)
+    ties = np.diff(s.astype(np.int64)) == 0
+    assert np.all(np.diff(order.astype(np.int64))[ties] > 0)
+    np.testing.assert_array_equal(np.sort(order), np.arange(len(tri)))
+
+
+def test_bvh_matches_brute_force_cpu():
+    """The oracle's own BVH traversal agrees with brute force (CPU twin of
+    the GPU trace parity test)."""
+    sc = scenes.soup_scene(3, 3000)
+    o = ljo.OracleScene(sc)
+    rays = scenes.random_rays(4, 4000)
+    t0, p0, _, _, ties = o.trace_closest(rays, brute=True)
+    t1, p1, _, _, _ = o.trace_closest(rays, brute=False)
+    ok = (p0 == p1) | (ties > 1)
+    assert ok.all()
+    np.testing.assert_array_equal(t0[p0 >= 0], t1[p0 >= 0])
+    np.testing.assert_array_equal(o.trace_any(rays, brute=True), o.trace_any(rays, brute=False))
