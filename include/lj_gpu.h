@@ -220,7 +220,8 @@ typedef struct lj_scene_desc {
 
 /* Replaces rtcNewDevice (src/main.cpp:30) + parallel_init (src/main.cpp:31). */
 int lj_gpu_init(int device, lj_ctx **out);
-/* Replaces rtcReleaseDevice + parallel_cleanup (src/main.cpp:47-48). */
+/* Replaces rtcReleaseDevice + parallel_cleanup (src/main.cpp:47-48).
+ * Destroys the context's remaining scenes: their handles are invalid after. */
 void lj_gpu_shutdown(lj_ctx *ctx);
 /* Message of the last failing call on this context ("" if none). */
 const char *lj_gpu_last_error(lj_ctx *ctx);
@@ -250,13 +251,26 @@ int lj_gpu_scene_info(lj_scene *scene, lj_scene_info *out);
 
 /* ---- render -------------------------------------------------------------- */
 
+/* lj_render_params.flags */
+#define LJ_RENDER_PROFILE 1      /* time each kernel class with CUDA events (adds event records) */
+
 typedef struct lj_render_params {
     uint64_t seed;               /* job seed; RNG is keyed on (seed, pixel, sample) */
     int32_t spp;                 /* 0 = scene options.samples_per_pixel */
     int32_t sample_offset;       /* first sample index (resume / split renders) */
     int32_t max_paths_in_flight; /* 0 = library default (wavefront width) */
-    int32_t pad0;
+    int32_t flags;               /* LJ_RENDER_* bits */
 } lj_render_params;
+
+/* Kernel classes of the wavefront, for LJ_RENDER_PROFILE. */
+enum {
+    LJ_KERNEL_CAMERA = 0,        /* ray generation                      */
+    LJ_KERNEL_TRACE = 1,         /* closest-hit traversal               */
+    LJ_KERNEL_SHADE = 2,         /* shading / NEE / BSDF sampling       */
+    LJ_KERNEL_SHADOW = 3,        /* shadow any-hit traversal            */
+    LJ_KERNEL_OTHER = 4,         /* resolve, scale, queue bookkeeping   */
+    LJ_KERNEL_CLASSES = 5
+};
 
 typedef struct lj_stats {
     double device_ms;            /* kernel time of the render (CUDA events)   */
@@ -267,6 +281,8 @@ typedef struct lj_stats {
     int64_t kernel_launches;     /* kernels launched by this call             */
     int64_t null_collisions;     /* volpath: null-collision events            */
     int64_t real_collisions;     /* volpath: real scattering events           */
+    double class_ms[LJ_KERNEL_CLASSES];        /* LJ_RENDER_PROFILE only */
+    int64_t class_launches[LJ_KERNEL_CLASSES]; /* LJ_RENDER_PROFILE only */
 } lj_stats;
 
 /* Replaces Image3 render(const Scene&) (src/render.cpp:155-170).  Writes the
@@ -310,6 +326,12 @@ int lj_gpu_trace_any(lj_scene *scene, const lj_ray *d_rays, uint8_t *d_occluded,
 /* Maps a global primitive index to (shape id, primitive id within shape). */
 int lj_gpu_prim_to_shape(lj_scene *scene, int32_t prim, int32_t *shape_id,
                          int32_t *local_prim);
+/* Instrumented traversal (a separate, slower kernel; for byte accounting):
+ * for n rays, the total number of 80-byte wide nodes fetched and 48-byte leaf
+ * primitive records tested by closest-hit (any_hit = 0) or any-hit traversal.
+ * No reference counterpart (Embree exposes no traversal counters). */
+int lj_gpu_trace_counters(lj_scene *scene, const lj_ray *d_rays, int64_t n, int32_t any_hit,
+                          int64_t *nodes_fetched, int64_t *prims_tested);
 
 /* 30-bit Morton codes (10 bits per axis) of triangle centroids over the
  * centroid bounding box, and the stable sort order of those codes -- the

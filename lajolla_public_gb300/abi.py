@@ -125,16 +125,24 @@ class lj_scene_info(C.Structure):
                 ("device_bytes", C.c_int64), ("build_ms", C.c_double)]
 
 
+LJ_RENDER_PROFILE = 1
+(LJ_KERNEL_CAMERA, LJ_KERNEL_TRACE, LJ_KERNEL_SHADE, LJ_KERNEL_SHADOW, LJ_KERNEL_OTHER) = range(5)
+LJ_KERNEL_CLASSES = 5
+KERNEL_CLASS_NAMES = ["camera", "trace", "shade", "shadow", "other"]
+
+
 class lj_render_params(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("spp", C.c_int32), ("sample_offset", C.c_int32),
-                ("max_paths_in_flight", C.c_int32), ("pad0", C.c_int32)]
+                ("max_paths_in_flight", C.c_int32), ("flags", C.c_int32)]
 
 
 class lj_stats(C.Structure):
     _fields_ = [("device_ms", C.c_double), ("samples", C.c_int64),
                 ("rays_closest", C.c_int64), ("rays_shadow", C.c_int64),
                 ("path_segments", C.c_int64), ("kernel_launches", C.c_int64),
-                ("null_collisions", C.c_int64), ("real_collisions", C.c_int64)]
+                ("null_collisions", C.c_int64), ("real_collisions", C.c_int64),
+                ("class_ms", C.c_double * LJ_KERNEL_CLASSES),
+                ("class_launches", C.c_int64 * LJ_KERNEL_CLASSES)]
 
 
 class lj_ray(C.Structure):

@@ -120,7 +120,7 @@ int lj_gpu_bsdf_batch(lj_ctx *ctx, const lj_bsdf_batch *b, int64_t n, void *stre
     if (b->op == LJ_BSDF_OP_SAMPLE) ok = ok && b->d_rnd && b->d_out_dir;
     if (!ok) return set_error(ctx, LJ_ERR_INVALID_ARG, "bsdf_batch: missing buffer for this op");
     cudaSetDevice(ctx->device);
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
     k_bsdf_batch<<<blocks(n), 256, 0, s>>>(*b, bsdf_param_count(b->material_type), n);
     if (cudaGetLastError() != cudaSuccess) return set_error(ctx, LJ_ERR_CUDA, "bsdf_batch launch failed");
     return LJ_OK;
@@ -133,7 +133,7 @@ int lj_gpu_light_sample_batch(lj_scene *sc, const float *ref, const float *rnd, 
     if (sc->dev.num_lights == 0) return set_error(sc->ctx, LJ_ERR_INVALID_ARG, "light_sample_batch: scene has no lights");
     if (n == 0) return LJ_OK;
     cudaSetDevice(sc->ctx->device);
-    cudaStream_t s = stream ? (cudaStream_t)stream : sc->ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
     k_light_batch<<<blocks(n), 256, 0, s>>>(sc->dev, ref, rnd, out_light, out_point, out_normal, out_pdf, n);
     if (cudaGetLastError() != cudaSuccess) return set_error(sc->ctx, LJ_ERR_CUDA, "light_sample_batch launch failed");
     return LJ_OK;
@@ -146,7 +146,7 @@ int lj_gpu_phase_batch(lj_ctx *ctx, int32_t kind, float g, const float *d_dir_in
     if (n > 0 && !d_dir_in) return LJ_ERR_INVALID_ARG;
     if (n == 0) return LJ_OK;
     cudaSetDevice(ctx->device);
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
     k_phase_batch<<<blocks(n), 256, 0, s>>>(kind, g, d_dir_in, d_dir_out, d_rnd, d_out_value, d_out_pdf,
                                             d_out_dir, n);
     if (cudaGetLastError() != cudaSuccess) return set_error(ctx, LJ_ERR_CUDA, "phase_batch launch failed");

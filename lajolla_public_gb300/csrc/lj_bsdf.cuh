@@ -338,7 +338,8 @@ LJ_HD BsdfSample dclearcoat_sample(float gloss, const BsdfVertex &v, V3 wi, floa
     if (dot(v.ng, wi) < 0.0f) return no_sample();
     Frame f = upper_frame(v, wi);
     float ag = cc_alpha(gloss), a2 = ag * ag;
-    float ce = sqrtf(fmaxf(0.0f, (1.0f - powf(a2, 1.0f - u0)) / (1.0f - a2)));
+    // (1 - a2^(1 - u0)) written as -expm1((1 - u0) log a2): no cancellation
+    float ce = sqrtf(fmaxf(0.0f, -expm1f((1.0f - u0) * logf(a2)) / (1.0f - a2)));
     float se = sqrtf(fmaxf(0.0f, 1.0f - ce * ce));
     float sp, cp;
     sincosf(kTwoPi * u1, &sp, &cp);

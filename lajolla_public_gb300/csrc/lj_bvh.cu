@@ -485,9 +485,39 @@ __global__ void k_trace_any(DevBvh bvh, const float4 *rays, uint8_t *occ, int64_
     if (ovf) atomicOr(status, kStatusStackOverflow);
 }
 
+template <bool kAny>
+__global__ void k_trace_count(DevBvh bvh, const float4 *rays, int64_t n, unsigned long long *counts,
+                              int *status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t nn = 0, np = 0;
+    if (i < n) {
+        float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
+        TraceHit h{0.0f, -1, 0.0f, 0.0f};
+        int ovf = 0;
+        trace_bvh<kAny, true>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf, &nn, &np);
+        if (ovf) atomicOr(status, kStatusStackOverflow);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        nn += __shfl_xor_sync(0xffffffffu, nn, o);
+        np += __shfl_xor_sync(0xffffffffu, np, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(counts, (unsigned long long)nn);
+        atomicAdd(counts + 1, (unsigned long long)np);
+    }
+}
+
 inline int grid_for(int64_t n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
+
+int launch_trace_counters(const DevBvh &bvh, const void *rays, int64_t n, bool any,
+                          unsigned long long *d_counts, int *d_status, cudaStream_t s) {
+    if (n <= 0) return 0;
+    if (any) k_trace_count<true><<<grid_for(n, 128), 128, 0, s>>>(bvh, (const float4 *)rays, n, d_counts, d_status);
+    else k_trace_count<false><<<grid_for(n, 128), 128, 0, s>>>(bvh, (const float4 *)rays, n, d_counts, d_status);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
 
 size_t radix_hist_entries(int64_t n) {
     int64_t tiles = (n + kRsTile - 1) / kRsTile;

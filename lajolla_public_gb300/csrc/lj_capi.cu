@@ -242,6 +242,7 @@ void lj_gpu_shutdown(lj_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    while (!ctx->scenes.empty()) lj_gpu_scene_destroy(ctx->scenes.back());
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->d_status) cudaFree(ctx->d_status);
     cudaStreamDestroy(ctx->stream);
@@ -540,14 +541,17 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
         err = "scene upload: stream synchronize failed";
         return fail(LJ_ERR_CUDA);
     }
+    ctx->scenes.push_back(sc);
     *out = sc;
     return LJ_OK;
 }
 
 void lj_gpu_scene_destroy(lj_scene *sc) {
     if (!sc) return;
+    auto &live = sc->ctx->scenes;
+    live.erase(std::remove(live.begin(), live.end(), sc), live.end());
     cudaSetDevice(sc->ctx->device);
-    cudaStreamSynchronize(sc->ctx->stream);
+    cudaDeviceSynchronize();   // kernels on any stream may still read the scene
     for (void *p : sc->allocs) cudaFree(p);
     if (sc->path.block) cudaFree(sc->path.block);
     delete sc;
@@ -583,7 +587,7 @@ static int check_status(lj_ctx *ctx, cudaStream_t s, const char *what) {
 
 int lj_gpu_trace_closest(lj_scene *sc, const lj_ray *d_rays, lj_hit *d_hits, int64_t n, void *stream) {
     if (!sc || n < 0 || (n > 0 && (!d_rays || !d_hits))) return LJ_ERR_INVALID_ARG;
-    cudaStream_t s = stream ? (cudaStream_t)stream : sc->ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
     cudaSetDevice(sc->ctx->device);
     if (launch_trace_closest(sc->dev.bvh, d_rays, d_hits, n, sc->ctx->d_status, s))
         return set_error(sc->ctx, LJ_ERR_CUDA, "trace_closest launch failed");
@@ -592,11 +596,30 @@ int lj_gpu_trace_closest(lj_scene *sc, const lj_ray *d_rays, lj_hit *d_hits, int
 
 int lj_gpu_trace_any(lj_scene *sc, const lj_ray *d_rays, uint8_t *d_occluded, int64_t n, void *stream) {
     if (!sc || n < 0 || (n > 0 && (!d_rays || !d_occluded))) return LJ_ERR_INVALID_ARG;
-    cudaStream_t s = stream ? (cudaStream_t)stream : sc->ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
     cudaSetDevice(sc->ctx->device);
     if (launch_trace_any(sc->dev.bvh, d_rays, d_occluded, n, sc->ctx->d_status, s))
         return set_error(sc->ctx, LJ_ERR_CUDA, "trace_any launch failed");
     return LJ_OK;
+}
+
+int lj_gpu_trace_counters(lj_scene *sc, const lj_ray *d_rays, int64_t n, int32_t any_hit,
+                          int64_t *nodes_fetched, int64_t *prims_tested) {
+    if (!sc || n < 0 || (n > 0 && !d_rays) || !nodes_fetched || !prims_tested) return LJ_ERR_INVALID_ARG;
+    cudaSetDevice(sc->ctx->device);
+    cudaStream_t s = sc->ctx->stream;
+    unsigned long long *d = nullptr, h[2] = {0, 0};
+    if (cudaMallocAsync(&d, sizeof(h), s) != cudaSuccess)
+        return set_error(sc->ctx, LJ_ERR_OUT_OF_MEMORY, "trace_counters: allocation failed");
+    cudaMemsetAsync(d, 0, sizeof(h), s);
+    int rc = launch_trace_counters(sc->dev.bvh, d_rays, n, any_hit != 0, d, sc->ctx->d_status, s);
+    cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s);
+    cudaFreeAsync(d, s);
+    if (rc || cudaStreamSynchronize(s) != cudaSuccess)
+        return set_error(sc->ctx, LJ_ERR_CUDA, "trace_counters failed");
+    *nodes_fetched = (int64_t)h[0];
+    *prims_tested = (int64_t)h[1];
+    return check_status(sc->ctx, s, "trace_counters");
 }
 
 int lj_gpu_morton_sort(lj_ctx *ctx, const float *d_tri_vertices, int64_t n, uint32_t *d_codes,
@@ -605,7 +628,7 @@ int lj_gpu_morton_sort(lj_ctx *ctx, const float *d_tri_vertices, int64_t n, uint
     if (n > (int64_t)1 << 31) return set_error(ctx, LJ_ERR_INVALID_ARG, "morton_sort: n too large");
     if (n == 0) return LJ_OK;
     cudaSetDevice(ctx->device);
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
     std::string err;
     // scratch: bounds (64 B), sorted keys (n), tmp keys (n), tmp vals (n), histogram
     size_t hist = radix_hist_entries(n);

@@ -17,6 +17,8 @@ struct lj_ctx {
     // grow-only scratch for the Morton / radix-sort entry point
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
+    // live scenes of this context: lj_gpu_shutdown destroys what is left
+    std::vector<struct lj_scene *> scenes;
 };
 
 // Wavefront buffers owned by a scene, grown on demand (lj_path.cu).

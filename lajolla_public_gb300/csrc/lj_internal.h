@@ -61,5 +61,8 @@ int launch_trace_closest(const DevBvh &bvh, const void *rays, void *hits, int64_
                          int *d_status, cudaStream_t s);
 int launch_trace_any(const DevBvh &bvh, const void *rays, uint8_t *occ, int64_t n,
                      int *d_status, cudaStream_t s);
+// instrumented traversal: d_counts[0] += nodes fetched, d_counts[1] += prims tested
+int launch_trace_counters(const DevBvh &bvh, const void *rays, int64_t n, bool any,
+                          unsigned long long *d_counts, int *d_status, cudaStream_t s);
 
 }  // namespace lj

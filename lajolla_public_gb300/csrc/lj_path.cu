@@ -18,6 +18,7 @@
 // sample order, so the image is deterministic.
 #include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "lj_host.h"
 #include "lj_shade.cuh"
@@ -417,22 +418,51 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
         cudaEventRecord(e0, s);
     }
     int64_t launches = 0;
+    // LJ_RENDER_PROFILE: an event pair around every kernel, grouped by class
+    const bool profile = timed && (params->flags & LJ_RENDER_PROFILE);
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    auto mark_begin = [&](int cls) {
+        if (!profile) return;
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, s);
+        marks.push_back({cls, {a, b}});
+    };
+    auto mark_end = [&]() {
+        if (profile) cudaEventRecord(marks.back().second.second, s);
+    };
+    int64_t class_launches[LJ_KERNEL_CLASSES] = {0, 0, 0, 0, 0};
     for (int sb = 0; sb < spp; sb += nsamp) {
         int ns = std::min(nsamp, spp - sb);
         int Pb = num_pixels * ns;
         k_set_counts<<<1, 1, 0, s>>>(q.counts, Pb);
+        mark_begin(LJ_KERNEL_CAMERA);
         k_camera<<<(Pb + 255) / 256, 256, 0, s>>>(sc, ps, q, Pb, num_pixels, params->sample_offset + sb,
                                                   params->seed);
+        mark_end();
         launches += 2;
+        class_launches[LJ_KERNEL_OTHER]++;
+        class_launches[LJ_KERNEL_CAMERA]++;
         int curq = 0;
         for (int pass = 0; pass < passes; pass++) {
             k_zero2<<<1, 1, 0, s>>>(q.counts, curq ^ 1, 2);
+            mark_begin(LJ_KERNEL_TRACE);
             k_trace_queue<<<g_trace, 128, 0, s>>>(sc.bvh, q.ray[curq], q.hit, q.counts + curq, q.stats + 0,
                                                   ctx->d_status);
+            mark_end();
+            mark_begin(LJ_KERNEL_SHADE);
             k_shade<<<g_shade, 128, 0, s>>>(sc, ps, q, curq, spread0, ctx->d_status);
+            mark_end();
+            mark_begin(LJ_KERNEL_SHADOW);
             k_trace_shadow<<<g_shadow, 128, 0, s>>>(sc.bvh, q.sray, q.spath, q.scontrib, q.counts + 2, ps.L,
                                                     q.stats + 1, ctx->d_status);
+            mark_end();
             launches += 4;
+            class_launches[LJ_KERNEL_OTHER]++;
+            class_launches[LJ_KERNEL_TRACE]++;
+            class_launches[LJ_KERNEL_SHADE]++;
+            class_launches[LJ_KERNEL_SHADOW]++;
             curq ^= 1;
             if (scene->options.max_depth == -1 && (pass & 7) == 7) {
                 int c = 0;
@@ -443,10 +473,12 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
         }
         k_resolve<<<(num_pixels + 255) / 256, 256, 0, s>>>(ps.L, num_pixels, ns, d_out);
         launches++;
+        class_launches[LJ_KERNEL_OTHER]++;
     }
     int64_t nfl = 3 * (int64_t)num_pixels;
     k_scale<<<(int)((nfl + 255) / 256), 256, 0, s>>>(d_out, nfl, 1.0f / spp);
     launches++;
+    class_launches[LJ_KERNEL_OTHER]++;
     LJ_CUDA_TRY(cudaGetLastError());
     if (timed) {
         cudaEventRecord(e1, s);
@@ -463,6 +495,22 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
         stats->rays_shadow = (int64_t)st[1];
         stats->path_segments = (int64_t)st[2];
         stats->kernel_launches = launches;
+        for (int c = 0; c < LJ_KERNEL_CLASSES; c++) {
+            stats->class_launches[c] = class_launches[c];
+            stats->class_ms[c] = 0.0;
+        }
+        for (auto &m : marks) {
+            float kms = 0;
+            cudaEventElapsedTime(&kms, m.second.first, m.second.second);
+            stats->class_ms[m.first] += kms;
+            cudaEventDestroy(m.second.first);
+            cudaEventDestroy(m.second.second);
+        }
+        if (profile) {
+            double other = ms;
+            for (int c = 0; c < LJ_KERNEL_OTHER; c++) other -= stats->class_ms[c];
+            stats->class_ms[LJ_KERNEL_OTHER] = other > 0 ? other : 0;
+        }
         int status = 0;
         LJ_CUDA_TRY(cudaMemcpy(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
         if (status) {
@@ -487,7 +535,7 @@ int lj_gpu_render_device(lj_scene *scene, const lj_render_params *params, float 
     cudaSetDevice(scene->ctx->device);
     if (scene->options.integrator != LJ_INTEGRATOR_PATH)
         return set_error(scene->ctx, LJ_ERR_UNSUPPORTED, "render: integrator not available in this build");
-    cudaStream_t s = stream ? (cudaStream_t)stream : scene->ctx->stream;
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
     if (stats) memset(stats, 0, sizeof(*stats));
     return render_path(scene, params, d_out_rgb, s, stats, stats != nullptr);
 }

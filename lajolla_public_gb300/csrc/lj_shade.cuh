@@ -277,19 +277,27 @@ LJ_D PN sample_point_on_shape(const DevScene &sc, const ShapeRec &sh, V3 ref, fl
         V3 off{r_ * cp, r_ * sp, z};
         return PN{c + off * r, off};
     }
+    // Same cone sampling as sphere.inl:164-212, written without cancellation
+    // for FP32: om = 1 - cos_max, 1 - ce^2 = u om (2 - u om), and the point is
+    // ref + w * ds with ds the near root along the sampled direction w.
     float dc = sqrtf(dc2);
     Frame fr = frame_from_n((c - ref) / dc);
     float sin_max_sq = r * r / dc2;
     float cos_max = sqrtf(fmaxf(0.0f, 1.0f - sin_max_sq));
-    float ce = (1.0f - u0) + u0 * cos_max;
-    float se = sqrtf(fmaxf(0.0f, 1.0f - ce * ce));
-    float ds = dc * ce - sqrtf(fmaxf(0.0f, r * r - dc2 * se * se));
-    float ca = (dc2 + r * r - ds * ds) / (2.0f * dc * r);
-    float sa = sqrtf(fmaxf(0.0f, 1.0f - ca * ca));
+    float om = sin_max_sq / (1.0f + cos_max);
+    float ce = 1.0f - u0 * om;
+    float se = sqrtf(fmaxf(0.0f, u0 * om * (2.0f - u0 * om)));
+    // r^2 - dc^2 se^2 = dc^2 om (1 - u0) (2 - om (1 + u0))
+    float disc = om * (1.0f - u0) * (2.0f - om * (1.0f + u0));
+    float ds = dc * (ce - sqrtf(fmaxf(0.0f, disc)));
     float sp, cp;
     sincosf(u1 * kTwoPi, &sp, &cp);
-    V3 n = -to_world(fr, V3{sa * cp, sa * sp, ca});
-    return PN{n * r + c, n};
+    // the reference's normal -(sa cos, sa sin, ca) puts the point at azimuth
+    // phi + pi as seen from ref
+    V3 wdir = to_world(fr, V3{-se * cp, -se * sp, ce});
+    V3 p = ref + wdir * ds;
+    V3 n = (p - c) / r;
+    return PN{p, n};
 }
 LJ_D float pdf_point_on_shape(const ShapeRec &sh, const PN &pn, V3 ref) {
     if (sh.kind == 0) return 1.0f / sh.total_area;

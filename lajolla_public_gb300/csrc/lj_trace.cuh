@@ -25,30 +25,43 @@ struct TraceHit {
     float u, v;
 };
 
-// Sphere: returns t in [tnear, tfar) of the nearest root, or -1.  FP32 with
-// the "closest point" discriminant (no catastrophic cancellation for rays
-// starting far from a small sphere).
+// Sphere: returns t in [tnear, tfar) of the nearest root, or -1.  Spheres are
+// rare primitives, so this runs in FP64 exactly like the reference's user-
+// geometry callback (src/shapes/sphere.inl:15-106: FP32 ray widened to FP64,
+// the stable quadratic of solve_quadratic), with explicit round-to-nearest
+// intrinsics so no contraction changes a rounding: t is bit-identical to the
+// CPU oracle's.
+LJ_D double ddot(double ax, double ay, double az, double bx, double by, double bz) {
+    return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
+}
 LJ_D float sphere_hit(V3 c, float r, V3 o, V3 d, float tnear, float tfar) {
-    V3 v = o - c;
-    float A = dot(d, d);
-    float b = dot(d, v);               // B / 2
-    V3 f = v - d * (b / A);            // vector from center to closest point
-    float disc = r * r - dot(f, f);    // (discriminant / 4) / A
-    if (disc < 0.0f) return -1.0f;
-    float q = -(b + copysignf(sqrtf(A * disc), b));
-    float C = dot(v, v) - r * r;
-    float t0, t1;
-    if (q == 0.0f) {
-        t0 = t1 = -b / A;
+    double vx = __dsub_rn((double)o.x, (double)c.x), vy = __dsub_rn((double)o.y, (double)c.y),
+           vz = __dsub_rn((double)o.z, (double)c.z);
+    double dx = d.x, dy = d.y, dz = d.z, rr = r;
+    double A = ddot(dx, dy, dz, dx, dy, dz);
+    double B = __dmul_rn(2.0, ddot(dx, dy, dz, vx, vy, vz));
+    double C = __dsub_rn(ddot(vx, vy, vz, vx, vy, vz), __dmul_rn(rr, rr));
+    double t0, t1;
+    if (A == 0.0) {
+        if (B == 0.0) return -1.0f;
+        t0 = t1 = __ddiv_rn(-C, B);
     } else {
-        t0 = C / q;
-        t1 = q / A;
+        double disc = __dsub_rn(__dmul_rn(B, B), __dmul_rn(__dmul_rn(4.0, A), C));
+        if (disc < 0.0) return -1.0f;
+        double rd = __dsqrt_rn(disc);
+        if (B >= 0.0) {
+            t0 = __ddiv_rn(__dsub_rn(-B, rd), __dmul_rn(2.0, A));
+            t1 = __ddiv_rn(__dmul_rn(2.0, C), __dsub_rn(-B, rd));
+        } else {
+            t0 = __ddiv_rn(__dmul_rn(2.0, C), __dadd_rn(-B, rd));
+            t1 = __ddiv_rn(__dadd_rn(-B, rd), __dmul_rn(2.0, A));
+        }
     }
-    if (t0 > t1) { float tmp = t0; t0 = t1; t1 = tmp; }
-    float t = -1.0f;
-    if (t0 >= tnear && t0 < tfar) t = t0;
-    if (t1 >= tnear && t1 < tfar && t < 0.0f) t = t1;
-    return (t >= tnear && t < tfar) ? t : -1.0f;
+    if (t0 > t1) { double tmp = t0; t0 = t1; t1 = tmp; }
+    double tn = tnear, tf = tfar, t = -1.0;
+    if (t0 >= tn && t0 < tf) t = t0;
+    if (t1 >= tn && t1 < tf && t < 0.0) t = t1;
+    return (t >= tn && t < tf) ? (float)t : -1.0f;
 }
 
 LJ_D uint32_t extract_byte(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
@@ -56,9 +69,11 @@ LJ_D uint32_t extract_byte(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
 // Returns true on hit.  kAny: stop at the first hit (occlusion query).
 // `hit` is updated with the closest hit; tfar shrinks as hits are found.
 // *overflow is set if the traversal stack was exhausted (bounded loop).
-template <bool kAny>
+// kCount: also count fetched nodes and tested primitives (instrumented
+// variant used only for byte accounting).
+template <bool kAny, bool kCount = false>
 LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, TraceHit &hit,
-                    int *overflow) {
+                    int *overflow, uint32_t *n_nodes = nullptr, uint32_t *n_prims = nullptr) {
     if (bvh.num_nodes == 0) return false;
     // direction components of exactly zero would give inf * 0 in the slab test
     const float tiny = 1e-30f;
@@ -94,6 +109,7 @@ LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, Trac
                 if (sp < kTraversalStack) stack[sp++] = ngroup;
                 else *overflow = 1;
             }
+            if (kCount) (*n_nodes)++;
             const uint4 *np = bvh.nodes + (size_t)child * kWideNodeU4;
             uint4 c0 = __ldg(np + 0), c1 = __ldg(np + 1), c2 = __ldg(np + 2),
                   c3 = __ldg(np + 3), c4 = __ldg(np + 4);
@@ -141,6 +157,7 @@ LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, Trac
         while (tgroup.y != 0u) {
             int b = __ffs(tgroup.y) - 1;
             tgroup.y &= tgroup.y - 1u;
+            if (kCount) (*n_prims)++;
             const float4 *pp = bvh.prims + (size_t)(tgroup.x + (uint32_t)b) * kPrimF4;
             float4 f0 = __ldg(pp + 0), f1 = __ldg(pp + 1);
             if (f1.w == 0.0f) {

@@ -13,6 +13,7 @@ device is present, construction raises.
 """
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -54,6 +55,7 @@ def lib():
         L.lj_gpu_trace_any.argtypes = [vp, vp, vp, i64, vp]
         L.lj_gpu_prim_to_shape.argtypes = [vp, i32, C.POINTER(i32), C.POINTER(i32)]
         L.lj_gpu_morton_sort.argtypes = [vp, vp, i64, vp, vp, vp]
+        L.lj_gpu_trace_counters.argtypes = [vp, vp, i64, i32, C.POINTER(i64), C.POINTER(i64)]
         L.lj_gpu_bsdf_param_count.argtypes = [i32]
         L.lj_gpu_bsdf_batch.argtypes = [vp, C.POINTER(abi.lj_bsdf_batch), i64, vp]
         L.lj_gpu_light_sample_batch.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp]
@@ -74,13 +76,17 @@ class Context:
         if rc != abi.LJ_OK:
             raise LjError(rc, "lj_gpu_init failed (no CUDA device of compute capability >= 10.0?)")
         self.device = device
+        self._scenes = weakref.WeakSet()
 
     def check(self, rc):
         if rc != abi.LJ_OK:
             raise LjError(rc, lib().lj_gpu_last_error(self.h).decode())
 
     def close(self):
+        """Destroys the context and every scene still open on it."""
         if self.h:
+            for s in list(self._scenes):
+                s.close()
             lib().lj_gpu_shutdown(self.h)
             self.h = C.c_void_p()
 
@@ -148,13 +154,17 @@ class GpuScene:
         self.scene = scene
         desc, keep = scene.desc()
         self.h = C.c_void_p()
+        if not ctx.h:
+            raise LjError(abi.LJ_ERR_INVALID_ARG, "context is closed")
         ctx.check(lib().lj_gpu_scene_create(ctx.h, C.byref(desc), C.byref(self.h)))
+        ctx._scenes.add(self)
         del keep
 
     def close(self):
-        if self.h:
+        # a closed context has already destroyed its scenes
+        if self.h and self.ctx.h:
             lib().lj_gpu_scene_destroy(self.h)
-            self.h = C.c_void_p()
+        self.h = C.c_void_p()
 
     def __del__(self):
         try:
@@ -178,10 +188,12 @@ class GpuScene:
         return out, st
 
     def render_device(self, out, seed=0, spp=0, sample_offset=0, max_paths_in_flight=0, stream=None,
-                      stats=True):
-        """Render into a device tensor `out` (H*W*3 float32)."""
+                      stats=True, profile=False):
+        """Render into a device tensor `out` (H*W*3 float32).  profile=True
+        times each kernel class with CUDA events (stats.class_ms)."""
         p = abi.lj_render_params(seed=seed, spp=spp, sample_offset=sample_offset,
-                                 max_paths_in_flight=max_paths_in_flight)
+                                 max_paths_in_flight=max_paths_in_flight,
+                                 flags=abi.LJ_RENDER_PROFILE if profile else 0)
         st = abi.lj_stats() if stats else None
         self.ctx.check(lib().lj_gpu_render_device(self.h, C.byref(p), _ptr(out), stream,
                                                   C.byref(st) if st is not None else None))
@@ -213,6 +225,13 @@ class GpuScene:
         self.ctx.check(lib().lj_gpu_light_sample_batch(self.h, _ptr(ref_points), _ptr(rnd), _ptr(lid),
                                                        _ptr(pt), _ptr(nr), _ptr(pdf), n, stream))
         return lid, pt, nr, pdf
+
+    def trace_counters(self, rays, any_hit=False):
+        """(nodes fetched, primitives tested) over a batch of rays."""
+        nn, npr = C.c_int64(), C.c_int64()
+        self.ctx.check(lib().lj_gpu_trace_counters(self.h, _ptr(rays), rays.shape[0], 1 if any_hit else 0,
+                                                   C.byref(nn), C.byref(npr)))
+        return nn.value, npr.value
 
     def prim_to_shape(self, prim):
         s, l = C.c_int32(), C.c_int32()

@@ -414,6 +414,134 @@ def soup_scene(seed, n_tris):
     return sc
 
 
+def value_noise_2d(rng, nx, nz, octaves=5, base_cells=8):
+    """Seeded fractal value noise on an (nz, nx) grid in [0, 1]: random
+    lattice values, smoothstep-interpolated, octaves summed with gain 1/2."""
+    h = np.zeros((nz, nx))
+    amp, total = 1.0, 0.0
+    xs, zs = np.linspace(0, 1, nx), np.linspace(0, 1, nz)
+    for o in range(octaves):
+        cells = base_cells * (2 ** o)
+        lat = rng.uniform(0, 1, (cells + 2, cells + 2))
+        fx, fz = xs * cells, zs * cells
+        ix, iz = np.floor(fx).astype(int), np.floor(fz).astype(int)
+        tx, tz = fx - ix, fz - iz
+        tx, tz = tx * tx * (3 - 2 * tx), tz * tz * (3 - 2 * tz)
+        a = lat[iz[:, None], ix[None, :]]
+        b = lat[iz[:, None], ix[None, :] + 1]
+        c = lat[iz[:, None] + 1, ix[None, :]]
+        d = lat[iz[:, None] + 1, ix[None, :] + 1]
+        top = a + (b - a) * tx[None, :]
+        bot = c + (d - c) * tx[None, :]
+        h += amp * (top + (bot - top) * tz[:, None])
+        total += amp
+        amp *= 0.5
+    return h / total
+
+
+def terrain_mesh(rng, nx, nz, size_x, size_z, height):
+    """(nx x nz) quads -> 2 nx nz triangles, smooth vertex normals."""
+    vx, vz = nx + 1, nz + 1
+    hgt = value_noise_2d(rng, vx, vz) * height
+    xs = np.linspace(-size_x / 2, size_x / 2, vx)
+    zs = np.linspace(-size_z / 2, size_z / 2, vz)
+    X, Z = np.meshgrid(xs, zs)
+    pos = np.stack([X, hgt, Z], axis=-1).reshape(-1, 3).astype(np.float32)
+    gz, gx = np.gradient(hgt, zs, xs)
+    n = np.stack([-gx, np.ones_like(gx), -gz], axis=-1).reshape(-1, 3)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    i = np.arange(nz)[:, None] * vx + np.arange(nx)[None, :]
+    i = i.reshape(-1)
+    # counter-clockwise seen from +y: normal (e1 x e2) points up
+    t0 = np.stack([i, i + vx, i + 1], axis=1)
+    t1 = np.stack([i + 1, i + vx, i + vx + 1], axis=1)
+    idx = np.concatenate([t0, t1], axis=0).astype(np.int32)
+    return pos, idx, n.astype(np.float32)
+
+
+def icosphere(subdiv):
+    """Unit icosphere: 20 * 4^subdiv triangles, outward winding."""
+    t = (1 + 5 ** 0.5) / 2
+    v = [[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+         [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]]
+    f = [[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+         [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5], [2, 4, 11],
+         [6, 2, 10], [8, 6, 7], [9, 8, 1]]
+    verts = [np.array(p, np.float64) / np.linalg.norm(p) for p in v]
+    faces = f
+    for _ in range(subdiv):
+        cache = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [[a, ab, ca], [b, bc, ab], [c, ca, bc], [ab, bc, ca]]
+        faces = nf
+    return np.array(verts, np.float64), np.array(faces, np.int32)
+
+
+def sky_envmap(rng, w, h, sun_peak=5e3):
+    """Procedural HDR lat-long sky (y up, lajolla's mapping envmap.inl:7-20):
+    blue-to-white gradient over a dark ground plus a Gaussian sun lobe."""
+    u = (np.arange(w) + 0.5) / w
+    v = (np.arange(h) + 0.5) / h
+    az, el = u * 2 * np.pi, v * np.pi
+    dirs = np.stack([np.sin(az)[None, :] * np.sin(el)[:, None],
+                     np.cos(el)[:, None] * np.ones((1, w)),
+                     -np.cos(az)[None, :] * np.sin(el)[:, None]], axis=-1)
+    up = np.clip(dirs[..., 1], 0, 1)
+    horizon = np.array([0.9, 0.85, 0.8])
+    zenith = np.array([0.2, 0.35, 0.8])
+    sky = horizon * (1 - up[..., None]) + zenith * up[..., None]
+    sky = np.where(dirs[..., 1:2] > 0, sky, np.array([0.05, 0.04, 0.03]))
+    sun_el = np.radians(rng.uniform(25, 50))
+    sun_az = rng.uniform(0, 2 * np.pi)
+    sd = np.array([np.sin(sun_az) * np.sin(np.pi / 2 - sun_el), np.cos(np.pi / 2 - sun_el),
+                   -np.cos(sun_az) * np.sin(np.pi / 2 - sun_el)])
+    cosang = np.clip(dirs @ sd, -1, 1)
+    lobe = np.exp(-(1 - cosang) / (1 - np.cos(np.radians(1.5))))
+    sky = sky * 2 + sun_peak * lobe[..., None] * np.array([1.0, 0.95, 0.85])
+    return sky.astype(np.float32)
+
+
+def terrain_scene(seed=0, width=1920, height=1080, spp=256, max_depth=8, grid=(2048, 1024),
+                  n_spheres=64, sphere_subdiv=5, env_size=(1024, 512)):
+    """Seeded large-mesh scene: fractal terrain + icospheres with Disney BSDFs
+    (roughness U[0.05,1], metallic Bernoulli(0.3), base color U[0,1]^3) under
+    a procedural HDR envmap sampled through the 2D table."""
+    rng = np.random.default_rng(seed)
+    sx, sz, hh = 40.0, 20.0, 3.0
+    sc = Scene(width, height, spp, max_depth,
+               look_at([0, 7.5, 16], [0, 1.0, -2], [0, 1, 0]), 50.0)
+
+    def disney():
+        return disney_bsdf(rng.uniform(0, 1, 3), metallic=float(rng.uniform() < 0.3),
+                           roughness=rng.uniform(0.05, 1.0))
+    pos, idx, nrm = terrain_mesh(rng, grid[0], grid[1], sx, sz, hh)
+    sc.add_mesh(pos, idx, sc.add_material(disney()), normals=nrm)
+    hmap = pos.reshape(grid[1] + 1, grid[0] + 1, 3)
+    uv, uf = icosphere(sphere_subdiv)
+    for _ in range(n_spheres):
+        r = rng.uniform(0.25, 0.8)
+        gx, gz = rng.integers(0, grid[0] + 1), rng.integers(0, grid[1] // 2 + 1) + grid[1] // 4
+        c = hmap[gz, gx] + np.array([0, r * 0.9, 0])
+        p = (uv * r + c).astype(np.float32)
+        sc.add_mesh(p, uf, sc.add_material(disney()), normals=uv.astype(np.float32))
+    sc.images.append(sky_envmap(rng, env_size[0], env_size[1]))
+    sc.lights.append(dict(kind=abi.LJ_LIGHT_ENVMAP, image_id=len(sc.images) - 1, scale=1.0,
+                          to_world=np.eye(4), to_local=np.eye(4)))
+    sc.envmap_light_id = len(sc.lights) - 1
+    return sc
+
+
 def random_rays(seed, n, tnear=0.0, tfar=np.inf):
     """Rays as an (n, 8) float32 array in lj_ray layout."""
     rng = np.random.default_rng(seed)

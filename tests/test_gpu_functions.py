@@ -3,10 +3,15 @@ by the reference's own functions (Lambertian, RoughPlastic, RoughDielectric,
 HG phase, light sampling) and against the oracle restatement (the Disney
 family, whose reference bodies are homework stubs -- parity unpinned there).
 
-Tolerance (FP32 vs the reference's FP64 on identical inputs): relative error
-<= 1e-5 for at least 99% of the values of each output, and <= 1e-3 relative
-(or 1e-6 absolute) for all of them -- the remaining tail comes from FP32
-conditioning (grazing Fresnel, near-specular GGX peaks)."""
+Tolerances (FP32 device code vs the reference's FP64 on identical inputs):
+  scalar / RGB outputs (BSDF value, pdf, eta, phase value):
+      |gpu - ref| <= 1e-5 |ref| + 1e-7   for at least 99% of the values,
+      |gpu - ref| <= 1e-3 |ref| + 1e-6   for all of them;
+  unit-vector outputs (sampled directions, normals), Euclidean error:
+      <= 1e-5 for at least 99%, <= 1e-3 for all;
+  points: the unit-vector rule scaled by max(1, |ref|).
+The tails come from FP32 conditioning (grazing Fresnel, near-specular GGX
+peaks, values of order 1e-7 next to O(1) intermediates)."""
 import numpy as np
 import pytest
 import torch
@@ -17,20 +22,26 @@ from oracle import ljo
 
 pytestmark = pytest.mark.gpu
 
-REL = 1e-5
-FRAC = 0.99
-REL_MAX = 1e-3
-ABS_FLOOR = 1e-6
 
-
-def check_close(got, want, name, rel=REL, frac=FRAC, rel_max=REL_MAX, floor=ABS_FLOOR):
+def check_close(got, want, name, rtol=1e-5, atol=1e-7, frac=0.99, rtol_all=1e-3, atol_all=1e-6):
     got = np.asarray(got, np.float64).reshape(-1)
     want = np.asarray(want, np.float64).reshape(-1)
-    err = np.abs(got - want) / np.maximum(np.abs(want), floor)
     assert np.isfinite(got).all(), name
-    ok = (err <= rel).mean()
-    assert ok >= frac, "%s: only %.4f within %g (max %g)" % (name, ok, rel, err.max())
-    assert err.max() <= rel_max, "%s: max rel err %g" % (name, err.max())
+    d = np.abs(got - want)
+    ok = (d <= rtol * np.abs(want) + atol).mean()
+    worst = (d / (rtol_all * np.abs(want) + atol_all)).max()
+    assert ok >= frac, "%s: only %.4f within rtol %g atol %g" % (name, ok, rtol, atol)
+    assert worst <= 1.0, "%s: an error exceeds rtol %g atol %g by %.3gx" % (name, rtol_all, atol_all, worst)
+
+
+def check_vectors(got, want, name, tol=1e-5, frac=0.99, tol_all=1e-3):
+    got = np.asarray(got, np.float64).reshape(-1, 3)
+    want = np.asarray(want, np.float64).reshape(-1, 3)
+    assert np.isfinite(got).all(), name
+    scale = np.maximum(1.0, np.linalg.norm(want, axis=1))
+    err = np.linalg.norm(got - want, axis=1) / scale
+    assert (err <= tol).mean() >= frac, "%s: only %.4f within %g (max %g)" % (name, (err <= tol).mean(), tol, err.max())
+    assert err.max() <= tol_all, "%s: max error %g" % (name, err.max())
 
 
 def cu(a):
@@ -56,7 +67,7 @@ def test_bsdf_vs_reference_golden(ctx):
         valid = sm["valid"].cpu().numpy()
         assert (valid == o[:, 7].astype(np.int32)).mean() >= 0.995
         v = (valid == 1) & (o[:, 7] == 1)
-        check_close(sm["dir"].cpu().numpy()[v], o[v, 8:11], "sample dir type %d" % t, floor=1e-3)
+        check_vectors(sm["dir"].cpu().numpy()[v], o[v, 8:11], "sample dir type %d" % t)
         check_close(sm["eta"].cpu().numpy()[v], o[v, 11], "sample eta type %d" % t)
         check_close(sm["roughness"].cpu().numpy()[v], o[v, 12], "sample roughness type %d" % t)
 
@@ -103,7 +114,7 @@ def test_disney_vs_oracle_restatement(ctx, t):
     valid = s["valid"].cpu().numpy()
     assert (valid == want_s["valid"]).mean() >= 0.995
     v = (valid == 1) & (want_s["valid"] == 1)
-    check_close(s["dir"].cpu().numpy()[v], want_s["dir"][v], "disney dir %d" % t, floor=1e-3)
+    check_vectors(s["dir"].cpu().numpy()[v], want_s["dir"][v], "disney dir %d" % t)
 
 
 def test_bsdf_sample_pdf_consistency_reference_method(ctx):
@@ -135,9 +146,9 @@ def test_phase_vs_reference_golden(ctx):
     for gval in np.unique(r[:, 0]):
         sel = r[:, 0] == gval
         val, pdf, d = ctx.phase(abi.LJ_PHASE_HG, float(gval), cu(r[sel, 1:4]), cu(r[sel, 4:7]), cu(r[sel, 7:9]))
-        check_close(val.cpu().numpy(), o[sel, 0], "hg eval g=%g" % gval, rel_max=2e-3)
-        check_close(pdf.cpu().numpy(), o[sel, 1], "hg pdf g=%g" % gval, rel_max=2e-3)
-        check_close(d.cpu().numpy(), o[sel, 2:5], "hg dir g=%g" % gval, floor=1e-3, rel_max=5e-3)
+        check_close(val.cpu().numpy(), o[sel, 0], "hg eval g=%g" % gval)
+        check_close(pdf.cpu().numpy(), o[sel, 1], "hg pdf g=%g" % gval)
+        check_vectors(d.cpu().numpy(), o[sel, 2:5], "hg dir g=%g" % gval)
 
 
 def test_light_sampling_vs_reference_golden(ctx):
@@ -149,6 +160,6 @@ def test_light_sampling_vs_reference_golden(ctx):
     lid = lid.cpu().numpy()
     same = lid == out[:, 0].astype(np.int32)
     assert same.mean() >= 0.99
-    check_close(pt.cpu().numpy()[same], out[same, 1:4], "light point", floor=1e-3, rel_max=5e-3)
-    check_close(nr.cpu().numpy()[same], out[same, 4:7], "light normal", floor=1e-3, rel_max=5e-3)
-    check_close(pdf.cpu().numpy()[same], out[same, 7], "light pdf", rel_max=5e-3)
+    check_vectors(pt.cpu().numpy()[same], out[same, 1:4], "light point")
+    check_vectors(nr.cpu().numpy()[same], out[same, 4:7], "light normal")
+    check_close(pdf.cpu().numpy()[same], out[same, 7], "light pdf")
