@@ -55,6 +55,7 @@ extern "C" {
 #define LJ_ERR_NOT_FOUND     -8  /* unknown job id                             */
 #define LJ_ERR_TIMEOUT       -9  /* a host-side wait ran out of time           */
 #define LJ_ERR_CANCELLED    -10  /* the job was cancelled                      */
+#define LJ_ERR_SIZE_LIMIT   -11  /* request larger than a fixed-size buffer    */
 
 typedef struct lj_ctx lj_ctx;
 typedef struct lj_scene lj_scene;
@@ -341,6 +342,21 @@ int lj_gpu_trace_counters(lj_scene *scene, const lj_ray *d_rays, int64_t n, int3
  * d_order[n] (triangle indices in ascending code order, ties by index). */
 int lj_gpu_morton_sort(lj_ctx *ctx, const float *d_tri_vertices, int64_t n,
                        uint32_t *d_codes, uint32_t *d_order, void *stream);
+
+/* Same results as lj_gpu_morton_sort, for callers that cannot allocate
+ * device memory when they call it (no counterpart in the reference, which
+ * has no GPU path).  It takes no context and calls no allocator: its working
+ * memory is one fixed 2 MiB array inside this library, held on every GPU
+ * that loads the library until the process exits.  Hence the limit:
+ * n <= LJ_NOALLOC_MORTON_MAX_TRIANGLES, else LJ_ERR_SIZE_LIMIT (nothing is
+ * queued).  The first call on each device looks up the array's device
+ * address (with that device current) and caches it; make that first call
+ * before any stream capture begins.  Every call reuses the same array, so
+ * calls that overlap on the GPU race: order them (same stream, or events).
+ * Errors are returned as codes only (there is no context for a message). */
+#define LJ_NOALLOC_MORTON_MAX_TRIANGLES 65536
+int lj_gpu_morton_sort_noalloc(const float *d_tri_vertices, int64_t n, uint32_t *d_codes,
+                               uint32_t *d_order, void *stream);
 
 /* BSDF batch: replaces eval / sample_bsdf / pdf_sample_bsdf
  * (src/material.cpp:90-119) for n independent queries in the local shading

@@ -16,6 +16,8 @@ LJ_ERR_QUEUE_FULL = -7
 LJ_ERR_NOT_FOUND = -8
 LJ_ERR_TIMEOUT = -9
 LJ_ERR_CANCELLED = -10
+LJ_ERR_SIZE_LIMIT = -11
+LJ_NOALLOC_MORTON_MAX_TRIANGLES = 65536
 
 LJ_TEX_CONST, LJ_TEX_IMAGE, LJ_TEX_CHECKER = 0, 1, 2
 (LJ_MAT_LAMBERTIAN, LJ_MAT_ROUGHPLASTIC, LJ_MAT_ROUGHDIELECTRIC, LJ_MAT_DISNEY_DIFFUSE,

@@ -552,6 +552,14 @@ int morton_codes_tris(const float *tri_vertices, int64_t n, uint32_t *codes, uin
     return 0;
 }
 
+int morton_codes_tris_into(const float *tri_vertices, int64_t n, uint32_t *codes, uint32_t *bounds,
+                           float4 *cent, cudaStream_t s) {
+    k_init_bounds<<<1, 32, 0, s>>>(bounds, 6);
+    k_tri_centroids<<<grid_for(n, 256), 256, 0, s>>>(tri_vertices, n, cent, bounds);
+    k_morton<<<grid_for(n, 256), 256, 0, s>>>(cent, n, bounds, codes, nullptr);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
+
 int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *err) {
     const int n = in.num_tris + in.num_spheres;
     out->num_nodes = 0;

@@ -38,6 +38,9 @@ int radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tmp_keys, uint32_
 // `bounds_scratch`: 8 uint32.
 int morton_codes_tris(const float *tri_vertices, int64_t n, uint32_t *codes,
                       uint32_t *bounds_scratch, cudaStream_t s, std::string *err);
+// Same, with the caller's centroid buffer (n float4): allocates nothing.
+int morton_codes_tris_into(const float *tri_vertices, int64_t n, uint32_t *codes, uint32_t *bounds,
+                           float4 *cent, cudaStream_t s);
 
 // ---- BVH build (lj_bvh.cu) ----
 struct BvhInput {
