@@ -184,7 +184,9 @@ int check_desc(const lj_scene_desc *d, std::string &msg) {
         } else {
             msg = "shape " + std::to_string(i) + ": unknown kind"; return -1;
         }
-        if (s.material_id < 0 || s.material_id >= d->num_materials) {
+        // material -1: an index-matching surface (volumetric integrator only)
+        if (s.material_id < -1 || s.material_id >= d->num_materials ||
+            (s.material_id == -1 && d->options.integrator != LJ_INTEGRATOR_VOLPATH)) {
             msg = "shape " + std::to_string(i) + ": material id out of range"; return -1;
         }
         if (s.area_light_id >= d->num_lights) { msg = "shape " + std::to_string(i) + ": light id out of range"; return -1; }

@@ -542,6 +542,82 @@ def terrain_scene(seed=0, width=1920, height=1080, spp=256, max_depth=8, grid=(2
     return sc
 
 
+def value_noise_3d(rng, n, octaves=5, base_cells=4):
+    """Seeded fractal value noise on an n^3 grid (z, y, x) in [0, 1]."""
+    g = np.linspace(0, 1, n)
+    out = np.zeros((n, n, n), np.float32)
+    amp, total = 1.0, 0.0
+    for o in range(octaves):
+        cells = base_cells * (2 ** o)
+        lat = rng.uniform(0, 1, (cells + 2,) * 3).astype(np.float32)
+        f = g * cells
+        i = np.floor(f).astype(int)
+        t = (f - i).astype(np.float32)
+        t = t * t * (3 - 2 * t)
+        acc = np.zeros((n, n, n), np.float32)
+        for dz in (0, 1):
+            wz = t if dz else 1 - t
+            for dy in (0, 1):
+                wy = t if dy else 1 - t
+                for dx in (0, 1):
+                    wx = t if dx else 1 - t
+                    v = lat[(i + dz)[:, None, None], (i + dy)[None, :, None], (i + dx)[None, None, :]]
+                    acc += v * (wz[:, None, None] * wy[None, :, None] * wx[None, None, :])
+        out += amp * acc
+        total += amp
+        amp *= 0.5
+    return out / total
+
+
+def volume_scene(seed=0, width=512, height=512, spp=256, max_depth=64, grid=256, max_density=20.0,
+                 sigma_t_scale=(1.05, 0.9, 0.8), albedo=(0.952, 0.889, 0.75), g=0.7,
+                 eta=1.33, roughness=0.1):
+    """Seeded volumetric scene: a heterogeneous chromatic medium (5-octave
+    value noise scaled to `max_density`, sigma_t = scale * noise as a
+    3-channel density, constant albedo, HG g) inside a rough dielectric
+    sphere, over a diffuse plane, lit by one sphere area light."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(width, height, spp, max_depth, look_at([0, 1.4, 4.2], [0, 0.9, 0], [0, 1, 0]), 35.0,
+               integrator=abi.LJ_INTEGRATOR_VOLPATH, vol_path_version=6)
+    noise = value_noise_3d(rng, grid)
+    noise = noise - noise.min()
+    noise = noise / noise.max() * max_density
+    dens = (noise[..., None] * np.asarray(sigma_t_scale, np.float32)).astype(np.float32)
+    c, r = np.array([0.0, 1.0, 0.0]), 1.0
+    sc.media.append(dict(kind=abi.LJ_MEDIUM_HETEROGENEOUS, phase_kind=abi.LJ_PHASE_HG, g=f32(g),
+                         albedo=dict(kind=abi.LJ_VOL_CONST, value=[f32(a) for a in albedo]),
+                         density=dict(kind=abi.LJ_VOL_GRID, data=dens, p_min=[f32(x) for x in c - r],
+                                      p_max=[f32(x) for x in c + r])))
+    diel = sc.add_material(roughdielectric([1, 1, 1], [1, 1, 1], roughness, eta))
+    sc.add_sphere(c, r, diel, interior_medium=0, exterior_medium=-1)
+    floor_m = sc.add_material(lambertian([0.6, 0.6, 0.6]))
+    fpos, fidx = _quad([-6, 0, 6], [6, 0, 6], [6, 0, -6], [-6, 0, -6])
+    sc.add_mesh(fpos, fidx, floor_m)
+    lm = sc.add_material(lambertian([0.0, 0.0, 0.0]))
+    sc.add_sphere([2.0, 3.5, 1.5], 0.5, lm, emission=[30, 28, 25])
+    return sc
+
+
+def homogeneous_box_scene(width=32, height=32, spp=16, max_depth=16, sigma_a=(0.3, 0.6, 0.9),
+                          sigma_s=(1.2, 0.8, 0.5), g=0.5, index_matched=True):
+    """Small test scene: a chromatic homogeneous medium inside a unit box
+    (index-matching if `index_matched`, else a rough dielectric), over a
+    diffuse floor, lit by a quad light."""
+    sc = Scene(width, height, spp, max_depth, look_at([0, 1.2, 3.5], [0, 0.6, 0], [0, 1, 0]), 40.0,
+               integrator=abi.LJ_INTEGRATOR_VOLPATH, vol_path_version=6)
+    sc.media.append(dict(kind=abi.LJ_MEDIUM_HOMOGENEOUS, phase_kind=abi.LJ_PHASE_HG, g=f32(g),
+                         sigma_a=[f32(x) for x in sigma_a], sigma_s=[f32(x) for x in sigma_s]))
+    pos, idx = _box([0, 0.6, 0], [1.0, 1.0, 1.0], 20.0)
+    m = -1 if index_matched else sc.add_material(roughdielectric([1, 1, 1], [1, 1, 1], 0.2, 1.33))
+    sc.add_mesh(pos, idx, m, interior_medium=0, exterior_medium=-1)
+    fm = sc.add_material(lambertian([0.5, 0.5, 0.5]))
+    fpos, fidx = _quad([-3, 0, 3], [3, 0, 3], [3, 0, -3], [-3, 0, -3])
+    sc.add_mesh(fpos, fidx, fm)
+    lpos, lidx = _quad([-0.5, 2.5, -0.5], [0.5, 2.5, -0.5], [0.5, 2.5, 0.5], [-0.5, 2.5, 0.5])
+    sc.add_mesh(lpos, lidx, sc.add_material(lambertian([0, 0, 0])), emission=[8, 8, 8])
+    return sc
+
+
 def random_rays(seed, n, tnear=0.0, tfar=np.inf):
     """Rays as an (n, 8) float32 array in lj_ray layout."""
     rng = np.random.default_rng(seed)

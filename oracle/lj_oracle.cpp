@@ -832,6 +832,24 @@ struct CameraS {
 struct PrimRef {
     int shape, local;
 };
+// Volume<Spectrum> (src/volume.h:12-30): constant or grid (trilinear).
+struct VolS {
+    int kind = LJ_VOL_CONST;
+    V3 value;
+    int res[3] = {1, 1, 1};
+    V3 pmin, pmax;
+    double scale = 1;
+    std::vector<V3> data;
+    V3 max_data;
+};
+// Medium (src/medium.h:10-22) + phase function (src/phase_function.h:9-16)
+struct MediumS {
+    int kind = LJ_MEDIUM_HOMOGENEOUS;
+    int phase = LJ_PHASE_ISOTROPIC;
+    double g = 0;
+    V3 sigma_a, sigma_s;
+    VolS albedo, density;
+};
 
 struct Scene {
     CameraS cam;
@@ -842,6 +860,8 @@ struct Scene {
     std::vector<LightS> lights;
     std::vector<MatS> mats;
     std::vector<Mip3> images;
+    std::vector<MediumS> media;
+    int camera_medium = -1;
     int envmap = -1;
     Table1D light_dist;
     double bradius = 0;
@@ -946,11 +966,51 @@ static double light_power(const Scene &sc, const LightS &l) {
     return kPi * sc.bradius * sc.bradius * l.dist.total / ((double)l.dist.w * l.dist.h);
 }
 
+static VolS vol_from(const lj_volume_desc &v) {
+    VolS o;
+    o.kind = v.kind;
+    o.scale = v.scale;
+    if (v.kind == LJ_VOL_CONST) {
+        o.value = V3{v.value[0], v.value[1], v.value[2]};
+        o.max_data = o.value;
+        return o;
+    }
+    for (int k = 0; k < 3; k++) o.res[k] = v.res[k];
+    o.pmin = V3{v.p_min[0], v.p_min[1], v.p_min[2]};
+    o.pmax = V3{v.p_max[0], v.p_max[1], v.p_max[2]};
+    size_t n = (size_t)v.res[0] * v.res[1] * v.res[2];
+    o.data.resize(n);
+    o.max_data = V3{0, 0, 0};
+    for (size_t i = 0; i < n; i++) {
+        // load_volume (src/volume.cpp:66-104): 1-channel data is replicated
+        V3 x = v.channels == 3 ? V3{v.data[i * 3], v.data[i * 3 + 1], v.data[i * 3 + 2]}
+                               : V3{v.data[i], v.data[i], v.data[i]};
+        o.data[i] = x;
+        o.max_data = vmax(o.max_data, x);
+    }
+    return o;
+}
+
 static Scene *build_scene(const lj_scene_desc *d) {
     auto sc = std::make_unique<Scene>();
     sc->cam = make_camera(d->camera);
     sc->opt = d->options;
     sc->envmap = d->envmap_light_id;
+    sc->camera_medium = d->camera.medium_id;
+    for (int i = 0; i < d->num_media; i++) {
+        const lj_medium_desc &m = d->media[i];
+        MediumS ms;
+        ms.kind = m.kind;
+        ms.phase = m.phase_kind;
+        ms.g = m.g;
+        ms.sigma_a = V3{m.sigma_a[0], m.sigma_a[1], m.sigma_a[2]};
+        ms.sigma_s = V3{m.sigma_s[0], m.sigma_s[1], m.sigma_s[2]};
+        if (m.kind == LJ_MEDIUM_HETEROGENEOUS) {
+            ms.albedo = vol_from(m.albedo);
+            ms.density = vol_from(m.density);
+        }
+        sc->media.push_back(std::move(ms));
+    }
     for (int i = 0; i < d->num_images; i++) {
         const lj_image_desc &im = d->images[i];
         Img3 img;
@@ -1542,6 +1602,321 @@ static V3 path_tracing(const Scene &sc, int x, int y, Rng &rng, bool yx_order) {
     return radiance;
 }
 
+// ======================= volumetric path tracing (v6) =======================
+// Restates handouts/homework2.tex (the reference's vol_path_tracing bodies,
+// src/vol_path_tracing.h:6-64, are stubs): the v3 loop (:303-440) with
+// index-matching surfaces, v4 NEE through index-matching surfaces + MIS
+// (:441-584), v5 surface lighting (:585-620), v6 delta / ratio tracking with
+// chromatic majorants and one-sample MIS over channels (:621-816).
+// Choices where the handout is silent (mirrored exactly by the GPU code):
+//   - RR probability min(max(beta) / eta_scale, 0.95), from bounce rr_depth
+//   - rays leaving a surface start at the scene epsilon, rays leaving a
+//     medium scattering point at 0
+//   - spectral pdfs enter MIS weights through their channel average
+//   - a BSDF event is a scattering event for MIS (never_scatter = false)
+//   - NEE at a surface uses the BSDF in place of the phase function
+//   - a BSDF transmission updates the medium with the new direction
+
+// GridVolume lookup, src/volume.h:44-81
+static V3 vol_lookup(const VolS &v, V3 p) {
+    if (v.kind == LJ_VOL_CONST) return v.value;
+    V3 pn = (p - v.pmin) / (v.pmax - v.pmin);
+    if (pn.x < 0 || pn.x > 1 || pn.y < 0 || pn.y > 1 || pn.z < 0 || pn.z > 1) return V3{};
+    pn.x *= (double)(v.res[0] - 1);
+    pn.y *= (double)(v.res[1] - 1);
+    pn.z *= (double)(v.res[2] - 1);
+    int x0 = std::clamp((int)pn.x, 0, v.res[0] - 1), y0 = std::clamp((int)pn.y, 0, v.res[1] - 1),
+        z0 = std::clamp((int)pn.z, 0, v.res[2] - 1);
+    int x1 = std::clamp(x0 + 1, 0, v.res[0] - 1), y1 = std::clamp(y0 + 1, 0, v.res[1] - 1),
+        z1 = std::clamp(z0 + 1, 0, v.res[2] - 1);
+    double dx = pn.x - x0, dy = pn.y - y0, dz = pn.z - z0;
+    auto at = [&](int x, int y, int z) { return v.data[((size_t)z * v.res[1] + y) * v.res[0] + x]; };
+    V3 r = at(x0, y0, z0) * ((1 - dx) * (1 - dy) * (1 - dz)) + at(x1, y0, z0) * (dx * (1 - dy) * (1 - dz)) +
+           at(x0, y1, z0) * ((1 - dx) * dy * (1 - dz)) + at(x1, y1, z0) * (dx * dy * (1 - dz)) +
+           at(x0, y0, z1) * ((1 - dx) * (1 - dy) * dz) + at(x1, y0, z1) * (dx * (1 - dy) * dz) +
+           at(x0, y1, z1) * ((1 - dx) * dy * dz) + at(x1, y1, z1) * (dx * dy * dz);
+    return r * v.scale;
+}
+// slab test against the grid's box, src/volume.h:124-144
+static bool vol_intersect(const VolS &v, const Ray &r) {
+    if (v.kind == LJ_VOL_CONST) return true;
+    double t0 = 0, t1 = r.tfar;
+    for (int i = 0; i < 3; i++) {
+        double tn = (v.pmin[i] - r.org[i]) / r.dir[i];
+        double tf = (v.pmax[i] - r.org[i]) / r.dir[i];
+        if (tn > tf) std::swap(tn, tf);
+        t0 = tn > t0 ? tn : t0;
+        t1 = tf < t1 ? tf : t1;
+        if (t0 > t1) return false;
+    }
+    return true;
+}
+// get_majorant / get_sigma_s / get_sigma_a, src/media/*.inl
+static V3 majorant(const MediumS &m, const Ray &r) {
+    if (m.kind == LJ_MEDIUM_HOMOGENEOUS) return m.sigma_a + m.sigma_s;
+    if (vol_intersect(m.density, r)) return m.density.max_data * m.density.scale;
+    return V3{};
+}
+static void sigmas(const MediumS &m, V3 p, V3 &ss, V3 &sa) {
+    if (m.kind == LJ_MEDIUM_HOMOGENEOUS) {
+        ss = m.sigma_s;
+        sa = m.sigma_a;
+        return;
+    }
+    V3 d = vol_lookup(m.density, p), a = vol_lookup(m.albedo, p);
+    ss = d * a;
+    sa = d * (V3{1, 1, 1} - a);
+}
+static V3 vexp(V3 v) { return V3{std::exp(v.x), std::exp(v.y), std::exp(v.z)}; }
+static double chan(V3 v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : v.z); }
+static int update_medium(const Vertex &v, V3 dir, int medium) {
+    if (v.interior_medium_id != v.exterior_medium_id)
+        return dot(dir, v.geometric_normal) > 0 ? v.exterior_medium_id : v.interior_medium_id;
+    return medium;
+}
+static double phase_eval(const MediumS &m, V3 wi, V3 wo) {
+    return m.phase == LJ_PHASE_HG ? hg_eval(m.g, wi, wo) : kInvFourPi;
+}
+
+// Test-only switch for the unbiasedness check of the restatement: 0 = MIS
+// (the algorithm), 1 = light sampling only, 2 = direction sampling only.  All
+// three estimate the same integral.
+static int g_vol_mis_mode = 0;
+static double mis_nee(double pn, double pd) {
+    if (g_vol_mis_mode == 1) return 1.0;
+    if (g_vol_mis_mode == 2) return 0.0;
+    return (pn * pn) / (pn * pn + pd * pd);
+}
+static double mis_dir(double pd, double pn) {
+    if (g_vol_mis_mode == 1) return 0.0;
+    if (g_vol_mis_mode == 2) return 1.0;
+    return (pd * pd) / (pd * pd + pn * pn);
+}
+
+// NEE from p (medium point when mat == nullptr, else a surface vertex vx with
+// material mat), through index-matching surfaces, with ratio tracking.
+static V3 vol_nee(const Scene &sc, V3 p, int medium, const Vertex *vx, const MatP *mat, V3 dir_view,
+                  int bounces, Rng &rng) {
+    double lu0 = rng.next(), lu1 = rng.next(), lw = rng.next(), sw = rng.next();
+    if (sc.lights.empty()) return V3{};
+    int lid = sample_1d(sc.light_dist, lw);
+    const LightS &light = sc.lights[lid];
+    PN pl = sample_point_on_light(sc, light, p, V2{lu0, lu1}, sw);
+    bool env = light.kind == LJ_LIGHT_ENVMAP;
+    V3 dir = env ? -pl.n : normalize(pl.p - p);
+    double eps = shadow_eps(sc);
+    V3 T{1, 1, 1}, p_nee{1, 1, 1}, p_dir{1, 1, 1};
+    // from a surface, the shadow ray starts in the medium on its own side
+    int shadow_medium = vx ? update_medium(*vx, dir, medium) : medium, shadow_bounces = 0;
+    V3 p0 = p;
+    double origin_eps = vx ? eps : 0.0;
+    for (int guard = 0; guard < 1 << 16; guard++) {
+        double dist = env ? INFINITY : distance(pl.p, p0);
+        Ray sr{p0, dir, origin_eps, env ? INFINITY : (1 - eps) * dist};
+        std::optional<Vertex> is = intersect(sc, sr);
+        double next_t = is ? distance(p0, is->position) : dist;
+        if (shadow_medium >= 0) {
+            const MediumS &m = sc.media[shadow_medium];
+            V3 maj = majorant(m, sr);
+            double mmax = max3(maj);
+            int c = std::clamp((int)(rng.next() * 3), 0, 2);
+            double acc = 0;
+            for (int it = 0; it < sc.opt.max_null_collisions; it++) {
+                if (chan(maj, c) <= 0) break;
+                double t = -std::log(1 - rng.next()) / chan(maj, c);
+                double dt = next_t - acc;
+                acc = std::min(acc + t, next_t);
+                if (t < dt) {
+                    V3 ss, sa;
+                    sigmas(m, p0 + dir * acc, ss, sa);
+                    V3 st = ss + sa, sn = maj - st;
+                    V3 e = vexp(maj * -t);
+                    T = T * e * sn / mmax;
+                    p_nee = p_nee * e * maj / mmax;
+                    V3 real = st / maj;
+                    p_dir = p_dir * e * maj * (V3{1, 1, 1} - real) / mmax;
+                    if (max3(T) <= 0) break;
+                } else {
+                    V3 e = vexp(maj * -dt);
+                    T = T * e;
+                    p_nee = p_nee * e;
+                    p_dir = p_dir * e;
+                    break;
+                }
+            }
+        }
+        if (!is) break;
+        if (is->material_id >= 0) return V3{};
+        shadow_bounces++;
+        if (sc.opt.max_depth != -1 && bounces + shadow_bounces + 1 >= sc.opt.max_depth) return V3{};
+        shadow_medium = update_medium(*is, dir, shadow_medium);
+        p0 = p0 + dir * next_t;
+        origin_eps = eps;
+    }
+    if (max3(T) <= 0) return V3{};
+    double G = env ? 1.0 : std::max(-dot(dir, pl.n), 0.0) / distance_squared(pl.p, p);
+    double pdf_nee = sc.light_dist.pmf[lid] * pdf_point_on_light(sc, light, pl, p);
+    if (!(G > 0 && pdf_nee > 0)) return V3{};
+    V3 f;
+    double pdf_dir;
+    if (mat) {
+        f = bsdf_eval(*mat, *vx, dir_view, dir);
+        pdf_dir = bsdf_pdf(*mat, *vx, dir_view, dir);
+    } else {
+        const MediumS &m = sc.media[medium];
+        double ph = phase_eval(m, dir_view, dir);
+        f = V3{ph, ph, ph};
+        pdf_dir = ph;
+    }
+    V3 L = light_emission(sc, light, -dir, 0, pl);
+    double pn_tot = pdf_nee * avg3(p_nee);
+    double pd_tot = pdf_dir * G * avg3(p_dir);
+    double w = mis_nee(pn_tot, pd_tot);
+    return T * f * L * (G * w / pn_tot);
+}
+
+static V3 vol_path_tracing(const Scene &sc, int x, int y, Rng &rng) {
+    int w = sc.cam.w, h = sc.cam.h;
+    double r1 = rng.next(), r2 = rng.next();
+    Ray ray = sample_primary(sc.cam, V2{(x + r1) / w, (y + r2) / h});
+    double eps = shadow_eps(sc);
+    int medium = sc.camera_medium;
+    V3 beta{1, 1, 1}, radiance{};
+    int bounces = 0;
+    double dir_pdf = 0, eta_scale = 1;
+    V3 nee_p{}, multi_dir{1, 1, 1}, multi_nee{1, 1, 1};
+    bool never_scatter = true;
+    RayDiff rd{0, 0.25 / std::max(w, h)};
+    for (int guard = 0; guard < LJ_MAX_BOUNCES + 2; guard++) {
+        std::optional<Vertex> is = intersect(sc, ray, guard == 0 ? rd : RayDiff{});
+        double t_hit = is ? distance(ray.org, is->position) : INFINITY;
+        bool scatter = false;
+        V3 p_scatter;
+        if (medium >= 0) {
+            const MediumS &m = sc.media[medium];
+            V3 maj = majorant(m, ray);
+            double mmax = max3(maj);
+            int c = std::clamp((int)(rng.next() * 3), 0, 2);
+            double acc = 0;
+            V3 T{1, 1, 1}, pd{1, 1, 1}, pn{1, 1, 1};
+            for (int it = 0; it < sc.opt.max_null_collisions; it++) {
+                if (chan(maj, c) <= 0) break;
+                double t = -std::log(1 - rng.next()) / chan(maj, c);
+                double dt = t_hit - acc;
+                acc = std::min(acc + t, t_hit);
+                if (t < dt) {
+                    V3 ss, sa;
+                    V3 pp = ray.org + ray.dir * acc;
+                    sigmas(m, pp, ss, sa);
+                    V3 st = ss + sa;
+                    V3 real = st / maj;
+                    V3 e = vexp(maj * -t);
+                    if (rng.next() < chan(real, c)) {
+                        scatter = true;
+                        T = T * e / mmax;
+                        pd = pd * e * maj * real / mmax;
+                        p_scatter = pp;
+                        break;
+                    }
+                    T = T * e * (maj - st) / mmax;
+                    pd = pd * e * maj * (V3{1, 1, 1} - real) / mmax;
+                    pn = pn * e * maj / mmax;
+                } else {
+                    V3 e = vexp(maj * -dt);
+                    T = T * e;
+                    pd = pd * e;
+                    pn = pn * e;
+                    break;
+                }
+            }
+            beta = beta * T / avg3(pd);
+            multi_dir = multi_dir * pd;
+            multi_nee = multi_nee * pn;
+        }
+        if (scatter) {
+            const MediumS &m = sc.media[medium];
+            V3 ss, sa;
+            sigmas(m, p_scatter, ss, sa);
+            V3 wv = -ray.dir;
+            radiance += beta * ss * vol_nee(sc, p_scatter, medium, nullptr, nullptr, wv, bounces, rng);
+            V2 u{rng.next(), rng.next()};
+            V3 nd = m.phase == LJ_PHASE_HG ? hg_sample(m.g, wv, u) : iso_sample(u);
+            // phase sampling is exact (eval == pdf), so the weight is sigma_s
+            beta = beta * ss;
+            dir_pdf = phase_eval(m, wv, nd);
+            nee_p = p_scatter;
+            multi_dir = V3{1, 1, 1};
+            multi_nee = V3{1, 1, 1};
+            never_scatter = false;
+            ray = Ray{p_scatter, nd, 0, INFINITY};
+        } else {
+            if (!is) {
+                if (sc.envmap >= 0) {
+                    V3 Le = light_emission(sc, sc.lights[sc.envmap], -ray.dir, 0, PN{});
+                    if (never_scatter) {
+                        radiance += beta * Le;
+                    } else {
+                        PN lp{V3{}, -ray.dir};
+                        double pn_tot = sc.light_dist.pmf[sc.envmap] *
+                                        pdf_point_on_light(sc, sc.lights[sc.envmap], lp, nee_p) * avg3(multi_nee);
+                        double pd_tot = dir_pdf * avg3(multi_dir);
+                        radiance += beta * Le * mis_dir(pd_tot, pn_tot);
+                    }
+                }
+                break;
+            }
+            const Vertex &vx = *is;
+            if (sc.shapes[vx.shape_id].area_light_id >= 0) {
+                V3 Le = vertex_emission(sc, vx, -ray.dir);
+                if (never_scatter) {
+                    radiance += beta * Le;
+                } else {
+                    int l2 = sc.shapes[vx.shape_id].area_light_id;
+                    PN lp{vx.position, vx.geometric_normal};
+                    double G = std::fabs(dot(ray.dir, vx.geometric_normal)) / distance_squared(vx.position, nee_p);
+                    double pn_tot = sc.light_dist.pmf[l2] * pdf_point_on_light(sc, sc.lights[l2], lp, nee_p) *
+                                    avg3(multi_nee);
+                    double pd_tot = dir_pdf * G * avg3(multi_dir);
+                    radiance += beta * Le * mis_dir(pd_tot, pn_tot);
+                }
+            }
+            if (sc.opt.max_depth != -1 && bounces == sc.opt.max_depth - 1) break;
+            if (vx.material_id < 0) {
+                medium = update_medium(vx, ray.dir, medium);
+                ray = Ray{vx.position, ray.dir, eps, INFINITY};
+                bounces++;
+                continue;
+            }
+            MatP mat = resolve_mat(sc, vx.material_id, vx);
+            V3 wv = -ray.dir;
+            radiance += beta * vol_nee(sc, vx.position, medium, &vx, &mat, wv, bounces, rng);
+            V2 bu{rng.next(), rng.next()};
+            double bw = rng.next();
+            std::optional<BsdfSample> bs = bsdf_sample(mat, vx, wv, bu, bw);
+            if (!bs) break;
+            V3 f = bsdf_eval(mat, vx, wv, bs->dir_out);
+            double pdf = bsdf_pdf(mat, vx, wv, bs->dir_out);
+            if (pdf <= 0) break;
+            if (bs->eta != 0) eta_scale /= bs->eta * bs->eta;
+            beta = beta * f / pdf;
+            dir_pdf = pdf;
+            nee_p = vx.position;
+            multi_dir = V3{1, 1, 1};
+            multi_nee = V3{1, 1, 1};
+            never_scatter = false;
+            medium = update_medium(vx, bs->dir_out, medium);
+            ray = Ray{vx.position, bs->dir_out, eps, INFINITY};
+        }
+        if (bounces >= sc.opt.rr_depth) {
+            double rr = std::min(max3(beta) / eta_scale, 0.95);
+            if (rng.next() > rr) break;
+            beta = beta / rr;
+        }
+        bounces++;
+    }
+    return radiance;
+}
+
 }  // namespace ljo
 
 using namespace ljo;
@@ -1581,8 +1956,13 @@ int ljo_render(void *s, int mode, uint64_t seed, int spp, int sample_offset, int
                     V3 acc{};
                     for (int k = 0; k < spp; k++) {
                         if (mode == 1) rng = Rng{pcg_keyed(seed, (uint64_t)y * w + x, (uint64_t)(sample_offset + k)), true};
-                        V3 L = path_tracing(*sc, x, y, rng, mode == 0 && yx_order);
-                        acc += L;
+                        if (sc->opt.integrator == LJ_INTEGRATOR_VOLPATH) {
+                            // src/render.cpp:138-143: drop samples with no finite channel
+                            V3 L = vol_path_tracing(*sc, x, y, rng);
+                            if (isfinite_any(L)) acc += L;
+                        } else {
+                            acc += path_tracing(*sc, x, y, rng, mode == 0 && yx_order);
+                        }
                     }
                     acc = acc / (double)spp;
                     double *o = out + ((size_t)y * w + x) * 3;
@@ -1612,7 +1992,8 @@ int ljo_render_samples(void *s, uint64_t seed, const int32_t *pixels, int64_t n,
             int x = p % w, y = p / w;
             for (int k = 0; k < spp; k++) {
                 Rng rng{pcg_keyed(seed, (uint64_t)p, (uint64_t)(sample_offset + k)), true};
-                V3 L = path_tracing(*sc, x, y, rng, false);
+                V3 L = sc->opt.integrator == LJ_INTEGRATOR_VOLPATH ? vol_path_tracing(*sc, x, y, rng)
+                                                                   : path_tracing(*sc, x, y, rng, false);
                 double *o = out + ((size_t)i * spp + k) * 3;
                 o[0] = L.x; o[1] = L.y; o[2] = L.z;
             }
@@ -1854,6 +2235,9 @@ void ljo_pcg(uint64_t stream, uint64_t seed, int k, uint32_t *out) {
     Pcg p = pcg_init(stream, seed);
     for (int i = 0; i < k; i++) out[i] = pcg_next(p);
 }
+// Test-only: select the volumetric estimator (0 MIS, 1 light only, 2 direction only).
+void ljo_set_vol_mis_mode(int mode) { g_vol_mis_mode = mode; }
+
 void ljo_pcg_keyed(uint64_t job_seed, uint64_t pixel, uint64_t sample, int k, uint32_t *out) {
     Pcg p = pcg_keyed(job_seed, pixel, sample);
     for (int i = 0; i < k; i++) out[i] = pcg_next(p);

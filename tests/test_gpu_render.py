@@ -23,20 +23,23 @@ from oracle import ljo
 pytestmark = pytest.mark.gpu
 
 
-def sample_match(sc, ctx, sample_index, seed=11):
+def sample_match(sc, ctx, sample_index, rtol, seed=11):
     g = gpu.GpuScene(ctx, sc)
     img_g, st = g.render(seed=seed, spp=1, sample_offset=sample_index)
     img_o = ljo.OracleScene(sc).render(mode="keyed", seed=seed, spp=1, sample_offset=sample_index)
     err = np.abs(img_g - img_o) / np.maximum(np.abs(img_o), 1e-1)
-    ok = (err <= 1e-3).all(axis=2)
+    ok = (err <= rtol).all(axis=2)
     return ok.mean(), st
 
 
-@pytest.mark.parametrize("case", ["cbox", "cbox_rr", "mixed"])
-def test_per_sample_parity_with_oracle(ctx, case):
+# Per-path relative tolerance: 1e-3 for diffuse scenes; 1e-2 where glossy
+# lobes (GGX with alpha^2 ~ 1e-3) amplify FP32 rounding of the half vector.
+# A logic error changes a path's radiance by O(1), not by these amounts.
+@pytest.mark.parametrize("case,rtol", [("cbox", 1e-3), ("cbox_rr", 1e-3), ("mixed", 1e-2)])
+def test_per_sample_parity_with_oracle(ctx, case, rtol):
     sc = make_golden.RENDER_CASES[case]()
     for k in (0, 5):
-        frac, st = sample_match(sc, ctx, k)
+        frac, st = sample_match(sc, ctx, k, rtol)
         assert frac >= 0.99, (case, k, frac)
     assert st.samples == sc.width * sc.height
 
