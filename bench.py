@@ -1,35 +1,52 @@
-"""Benchmark: lajolla's path-tracing hot path on one GB300.
+"""Benchmark: lajolla's rendering hot path on one GB300, served.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Workload (a "step" = one full render of the scene):
-  cbox     seeded Cornell box, 36 FP32 triangles, quad light (17,12,4),
-           Lambertian U[0.1,0.8]^3, 256x256, 64 spp, max depth 6, box filter
-           -- the reference's CPU-runnable path-tracing configuration.
+Workload (a "step" = serving one batch of render jobs):
+  serving  32 jobs with Poisson arrivals (mean 200/s, seeded).  Each job
+           renders one of 6 resident scenes -- seeded Cornell boxes with
+           tessellated walls and seeded terrain + icosphere + HDR-envmap
+           scenes (Disney BSDFs), 10k-2M triangles, log-uniform -- at a square
+           resolution in {128, 256, 512, 1024}, spp in {4, 16, 64, 256}, max
+           depth uniform in 6..64 (Russian roulette from depth 5).
+           ~1e9 camera samples per step.
 
-Our arm (--impl ours): scene resident on the GPU; K timed renders through
-lj_gpu_render_device on torch's current stream, each bracketed by CUDA
-events, with a 512 MiB write between steps to flush L2 (the wavefront state,
-~0.8 GB, is larger than L2 as well).  value = Msamples/s (all ranks).
-e2e: the same metric through the C ABI with host buffers -- each step uploads
-the scene description from host memory (lj_gpu_scene_create, BVH build
-included) and renders into a host buffer (lj_gpu_render, device->host copy
-of the image included).
-roofline: the dominant kernel class of a profiled render (LJ_RENDER_PROFILE),
-algorithmic bytes per launch (include/lj_bytes_model.h) / its average launch
-time, against the measured HBM copy bandwidth (MEASURED_PEAKS.json).
-cpu_baseline: the oracle's C++ restatement of the reference path
-(oracle/lj_oracle.cpp, same algorithm, FP64, all host threads) on a bounded
-sample of the same scene.
+Our arm (--impl ours):
+  value     Msamples/s of the continuous-batching server (lj_gpu_server_*):
+            jobs submitted at their arrival times, the paths of all live jobs
+            in one pool of wavefront queues replayed as CUDA graphs, pool and
+            block size from the autotuner; each job's image returned to host
+            memory.  Step time = host clock from the first arrival to the last
+            completion, the device synchronized on both sides.
+  plain     the same jobs through the single-scene wavefront renderer, one at
+            a time in arrival order (lj_gpu_render_job_device + image to
+            host).  Both arms trace the same keyed samples, so their images
+            (and errors) match: rel_mse reports both against a 4096-spp
+            render for a few jobs.
+  latency   p50 / p99 of (completion - arrival) per job, both arms.
+  e2e       one step through the C ABI from host memory: the scene pool is
+            uploaded (lj_gpu_scene_create: descriptors from host, device BVH
+            build) inside the timed region, then the jobs are served.
+  roofline  the dominant kernel class of a profiled server step
+            (LJ_SERVER_PROFILE: CUDA events around every kernel on the
+            server's stream), compulsory algorithmic bytes per launch
+            (include/lj_bytes_model.h) / average launch time, against the
+            measured HBM copy bandwidth (MEASURED_PEAKS.json).
+  cpu_baseline  the oracle's C++ restatement of the reference path tracer
+            (oracle/lj_oracle.cpp, FP64, all host threads) on a bounded
+            sample of the same scenes.
+The working set (path pool ~1 GB, scenes up to 2M triangles, accumulators)
+is larger than L2.
 
-Reference arm (--impl reference): the reference's CPU path on the host
-cores -- the reference renderer cannot be built on this machine (its sources
-are not present here), so its C++ restatement in oracle/ runs instead,
-pinned sample-for-sample to the reference's own renders (tests/golden).
+Reference arm (--impl reference): the reference's CPU path tracer on the
+host cores -- the reference renderer cannot be built on the benchmark machine
+(its sources are not present there), so its C++ restatement in oracle/ runs
+instead, pinned sample-for-sample to the reference's own renders
+(tests/golden), on a bounded sample of the serving scenes per step.
 
-Multi-GPU: replicas only (each rank renders its own copy of the job; no
-collective on the data path); value sums all ranks' samples over the slowest
-rank's time.
+Multi-GPU: replicas only (each rank serves its own copy of the job stream;
+no collective on the data path); value sums all ranks' samples over the
+slowest rank's time.
 """
 import argparse
 import json
@@ -47,24 +64,43 @@ sys.path.insert(0, ROOT)
 
 from lajolla_public_gb300 import abi, scenes  # noqa: E402
 
-WORKLOAD = dict(name="cbox", seed=0, width=256, height=256, spp=64, max_depth=6)
-METRIC = "Msamples/s (path-traced camera samples per second)"
+WORKLOAD = dict(name="serving", scene_seed=0, n_scenes=6, n_jobs=32, rate=200.0)
+METRIC = "Msamples/s (served render jobs, batched; plain GPU and p50/p99 job latency beside it)"
+TUNE_CACHE = os.path.join(ROOT, "lajolla_public_gb300", "_lib", "autotune.json")
 
 
-def make_scene():
+def make_scenes():
+    return scenes.serving_scenes(WORKLOAD["scene_seed"], WORKLOAD["n_scenes"])
+
+
+def make_jobs(step_seed):
+    return scenes.serving_jobs(seed=step_seed, n_jobs=WORKLOAD["n_jobs"], n_scenes=WORKLOAD["n_scenes"],
+                               rate=WORKLOAD["rate"])
+
+
+def job_samples(jobs):
+    return sum(j["width"] * j["height"] * j["spp"] for j in jobs)
+
+
+def config_dict(pool, opts=None):
     w = WORKLOAD
-    return scenes.cornell_box(seed=w["seed"], width=w["width"], height=w["height"], spp=w["spp"],
-                              max_depth=w["max_depth"])
-
-
-def config_dict(sc):
-    w = WORKLOAD
-    return {"workload": "cbox: seeded Cornell box %dx%d, %d spp, max depth %d, %d triangles, 1 quad light"
-                        % (w["width"], w["height"], w["spp"], w["max_depth"], sc.num_triangles),
-            "width": w["width"], "height": w["height"], "spp": w["spp"], "max_depth": w["max_depth"],
-            "triangles": sc.num_triangles, "integrator": "path (NEE + MIS, RR from depth 5)",
-            "l2": "wavefront state (~0.8 GB) larger than L2; 512 MiB L2 flush between timed steps",
-            "parallelism": "replicas"}
+    cfg = {"workload": "serving: %d jobs per step, Poisson arrivals %.0f/s; %d resident scenes "
+                       "(tessellated Cornell boxes and terrain+icospheres+envmap, %d-%d triangles); "
+                       "resolution {128,256,512,1024}^2, spp {4,16,64,256}, max depth 6-64"
+                       % (w["n_jobs"], w["rate"], w["n_scenes"], min(s.num_triangles for s in pool),
+                          max(s.num_triangles for s in pool)),
+           "jobs_per_step": w["n_jobs"], "arrival_rate_per_s": w["rate"],
+           "scene_triangles": [s.num_triangles for s in pool],
+           "integrator": "path (NEE + MIS, RR from depth 5)",
+           "l2": "working set (path pool ~1 GB, scenes, accumulators) larger than L2",
+           "timing": "host clock per step, device synchronized on both sides",
+           "parallelism": "replicas"}
+    if opts is not None:
+        cfg["server"] = {"path_pool": int(opts.path_pool), "block_size": int(opts.block_size),
+                         "policy": "SRPT" if opts.policy == abi.LJ_SCHED_SRPT else "FIFO",
+                         "cuda_graphs": bool(opts.use_graphs), "waves_per_poll": int(opts.waves_per_poll),
+                         "tuned_by": "lj_gpu_server_autotune (cache %s)" % os.path.relpath(TUNE_CACHE, ROOT)}
+    return cfg
 
 
 # ---------------------------------------------------------------- clocks
@@ -129,50 +165,27 @@ def measured_peaks():
 # same constants as include/lj_bytes_model.h).
 BYTES_RAY = 32          # lj_ray: org + tnear + dir + tfar
 BYTES_HIT = 16          # t, prim, u, v
-BYTES_NODE = 80         # compressed 8-wide node
-BYTES_PRIM = 48         # leaf triangle record (v0, e1, e2)
 BYTES_PATH_STATE = 64   # pixel 4 + rng 8 + beta 16 + L 16 + prev 16 + nv 4
 BYTES_SHADE_GEOM = 52   # 3 vertex indices + 3 positions + prim->shape
 BYTES_SHADE_MAT = 160   # material record: type, eta, textured flags, 12 x RGB slot values
 BYTES_SHADOW_ENTRY = 52  # shadow ray 32 + path 4 + contribution 16
 
 
-def kernel_bytes(cls, st, bvh_per_closest, bvh_per_shadow):
-    """Algorithmic bytes moved by all launches of one kernel class."""
+def kernel_bytes(cls, samples, rays_closest, rays_shadow, segments):
+    """Compulsory algorithmic bytes moved by all launches of one kernel class
+    (queues, hits, path state, shading records; BVH bytes excluded)."""
     if cls == abi.LJ_KERNEL_TRACE:
-        return st.rays_closest * (BYTES_RAY + BYTES_HIT + bvh_per_closest)
+        return rays_closest * (BYTES_RAY + BYTES_HIT)
     if cls == abi.LJ_KERNEL_SHADOW:
-        # shadow entry read + radiance read-modify-write + traversal
-        return st.rays_shadow * (BYTES_SHADOW_ENTRY + 32 + bvh_per_shadow)
+        # shadow entry read + radiance read-modify-write
+        return rays_shadow * (BYTES_SHADOW_ENTRY + 32)
     if cls == abi.LJ_KERNEL_SHADE:
-        seg = st.path_segments
         reads = BYTES_RAY + BYTES_HIT + 4 + BYTES_PATH_STATE + BYTES_SHADE_GEOM + BYTES_SHADE_MAT
         writes = BYTES_PATH_STATE + BYTES_RAY + 4
-        return seg * (reads + writes) + st.rays_shadow * BYTES_SHADOW_ENTRY
+        return segments * (reads + writes) + rays_shadow * BYTES_SHADOW_ENTRY
     if cls == abi.LJ_KERNEL_CAMERA:
-        return st.samples * (BYTES_RAY + 4 + BYTES_PATH_STATE)
+        return samples * (BYTES_RAY + 4 + BYTES_PATH_STATE)
     return 0
-
-
-# ------------------------------------------------------------ CPU baseline
-def cpu_baseline(sc, target_s=10.0):
-    """The oracle restatement on all host cores, bounded to ~target_s seconds."""
-    from oracle import ljo
-    ljo.build()
-    o = ljo.OracleScene(sc)
-    cores = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    o.render(mode="keyed", seed=1, spp=1, nthreads=cores)
-    t1 = time.perf_counter() - t0
-    spp = int(max(1, min(sc.spp, target_s / max(t1, 1e-3))))
-    t0 = time.perf_counter()
-    o.render(mode="keyed", seed=2, spp=spp, nthreads=cores)
-    dt = time.perf_counter() - t0
-    samples = sc.width * sc.height * spp
-    return {"value": samples / dt / 1e6, "unit": "Msamples/s", "cores": cores, "kind": "port",
-            "sample": "%dx%d at %d spp (%d samples, %.1f s) of the same scene; C++ restatement of "
-                      "src/path_tracing.h pinned to the reference's renders" % (sc.width, sc.height, spp,
-                                                                               samples, dt)}
 
 
 # ------------------------------------------------------------ arms
@@ -202,6 +215,70 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
+def pct(xs, q):
+    return float(np.percentile(np.asarray(xs, np.float64), q)) if xs else None
+
+
+def job_desc(j):
+    from lajolla_public_gb300 import gpu
+    return gpu.job_desc(seed=j["seed"], spp=j["spp"], width=j["width"], height=j["height"],
+                        max_depth=j["max_depth"], rr_depth=j["rr_depth"])
+
+
+def serve_step(srv, gscenes, jobs, keep=()):
+    """Submits `jobs` at their arrival times and waits for all of them.
+    Returns (seconds, latencies_ms, {index: image} for `keep`)."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ids = []
+    for j in jobs:
+        dt = j["arrival_s"] - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        ids.append(srv.submit(gscenes[j["scene"]], job_desc(j)))
+    lat, imgs, fin = [], {}, []
+    for k, jid in enumerate(ids):
+        img, st = srv.wait(jid, timeout=600)
+        lat.append(st.finish_ms - st.submit_ms)
+        fin.append(st.finish_ms)
+        if k in keep:
+            imgs[k] = img
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, lat, imgs
+
+
+def plain_step(gscenes, jobs, out, stream, keep=()):
+    """The same jobs one at a time through the single-scene renderer."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat, imgs = [], {}
+    for k, j in enumerate(jobs):
+        dt = j["arrival_s"] - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        n = j["width"] * j["height"] * 3
+        gscenes[j["scene"]].render_job_device(out[:n], job_desc(j), stream=stream)
+        img = out[:n].cpu()   # synchronizes
+        lat.append((time.perf_counter() - t0 - j["arrival_s"]) * 1e3)
+        if k in keep:
+            imgs[k] = img.numpy().reshape(j["height"], j["width"], 3)
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, lat, imgs
+
+
+def tuned_options(ctx, gscenes):
+    """Server options from the autotuner (cached per device and workload)."""
+    from lajolla_public_gb300 import gpu
+    tune = scenes.serving_jobs(seed=999, n_jobs=8, n_scenes=WORKLOAD["n_scenes"], resolutions=(128, 256),
+                               spps=(4, 16))
+    jd = [job_desc(j) for j in tune]
+    os.makedirs(os.path.dirname(TUNE_CACHE), exist_ok=True)
+    opt = gpu.server_options(policy=abi.LJ_SCHED_SRPT)
+    return gpu.autotune(ctx, gscenes, jd, [j["scene"] for j in tune], cache_path=TUNE_CACHE, options=opt)
+
+
 def run_ours(args):
     import torch
     from lajolla_public_gb300 import gpu
@@ -209,134 +286,143 @@ def run_ours(args):
     rank, world, local = dist_setup(args.gpus)
     torch.cuda.set_device(local)
     ctx = gpu.Context(local)
-    sc = make_scene()
-    g = gpu.GpuScene(ctx, sc)
-    n_px = sc.width * sc.height
-    out = torch.empty(n_px * 3, dtype=torch.float32, device="cuda")
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    pool = make_scenes()
+    gscenes = [gpu.GpuScene(ctx, s) for s in pool]
     stream = torch.cuda.current_stream().cuda_stream
+    max_px = 1024 * 1024
+    out = torch.empty(max_px * 3, dtype=torch.float32, device="cuda")
 
+    opts = tuned_options(ctx, gscenes)
+    srv = gpu.Server(ctx, opts)
+
+    # warm-up steps (both arms)
     for i in range(args.warmup):
-        g.render_device(out, seed=100 + i, stream=stream, stats=False)
-    torch.cuda.synchronize()
+        jobs = make_jobs(100 + i)
+        serve_step(srv, gscenes, jobs)
+        if i == 0:
+            plain_step(gscenes, jobs, out, stream)
 
-    # profiled render (not timed): per-kernel-class times + counts
-    st_prof = g.render_device(out, seed=7, stream=stream, stats=True, profile=True)
-    rays = scenes.random_rays(9, 65536)
-    # BVH bytes per ray from the instrumented traversal on camera-like rays
-    cam_rays = torch.from_numpy(_camera_rays(sc, 65536)).cuda()
-    nn_c, np_c = g.trace_counters(cam_rays, any_hit=False)
-    nn_s, np_s = g.trace_counters(cam_rays, any_hit=True)
-    bvh_closest = (nn_c * BYTES_NODE + np_c * BYTES_PRIM) / len(cam_rays)
-    bvh_shadow = (nn_s * BYTES_NODE + np_s * BYTES_PRIM) / len(cam_rays)
-    del rays
-
-    # timed region
+    # timed steps
     clocks = ClockSampler(local)
     clocks.start()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    st0 = srv.stats()
     barrier(world)
-    torch.cuda.synchronize()
-    launches = 0
-    st = None
+    b_secs, b_lat, p_secs, p_lat = [], [], [], []
+    samples = 0
+    keep_imgs = None
     for i in range(args.steps):
-        flush.fill_(i & 0xff)
-        starts[i].record()
-        st = g.render_device(out, seed=1000 + i, stream=stream, stats=False)
-        ends[i].record()
-    torch.cuda.synchronize()
+        jobs = make_jobs(1000 + i)
+        samples += job_samples(jobs)
+        keep = tuple(sorted(range(len(jobs)), key=lambda k: jobs[k]["width"] * jobs[k]["spp"])[:3]) if i == 0 else ()
+        sec, lat, bimgs = serve_step(srv, gscenes, jobs, keep)
+        b_secs.append(sec)
+        b_lat += lat
+        sec, lat, pimgs = plain_step(gscenes, jobs, out, stream, keep)
+        p_secs.append(sec)
+        p_lat += lat
+        if i == 0:
+            keep_imgs = (jobs, keep, bimgs, pimgs)
     barrier(world)
     ck = clocks.stop()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = max_over_ranks(sum(step_ms), world)
-    launches = st_prof.kernel_launches * args.steps
-    samples_per_step = n_px * sc.spp
-    value = samples_per_step * args.steps * world / (total_ms / 1e3) / 1e6
+    st1 = srv.stats()
+    b_total = max_over_ranks(sum(b_secs), world)
+    p_total = max_over_ranks(sum(p_secs), world)
+    value = samples * world / b_total / 1e6
+    plain_value = samples * world / p_total / 1e6
+    launches = st1.kernel_launches - st0.kernel_launches
 
-    # e2e through the C ABI with host buffers
-    e2e_ms = []
-    desc_bytes = scene_host_bytes(sc)
-    img_bytes = n_px * 3 * 4
-    for i in range(max(1, min(args.steps, 3))):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        g2 = gpu.GpuScene(ctx, sc)
-        g2.render(seed=2000 + i)
-        g2.close()
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_value = samples_per_step * world / (max_over_ranks(statistics.mean(e2e_ms), world) / 1e3) / 1e6
+    # matched error: a few jobs of the first step against 4096-spp renders
+    jobs0, keep, bimgs, pimgs = keep_imgs
+    rel_mse = []
+    for k in keep:
+        j = dict(jobs0[k])
+        ref_job = dict(j, spp=4096, seed=j["seed"] ^ 0x5bd1e995)
+        n = j["width"] * j["height"] * 3
+        gscenes[j["scene"]].render_job_device(out[:n], job_desc(ref_job), stream=stream)
+        ref = out[:n].cpu().numpy().reshape(j["height"], j["width"], 3).astype(np.float64)
+        den = float(np.mean(ref ** 2)) + 1e-30
+        rel_mse.append({"job": "%dx%d %d spp depth %d" % (j["width"], j["height"], j["spp"], j["max_depth"]),
+                        "batched": float(np.mean((bimgs[k] - ref) ** 2) / den),
+                        "plain": float(np.mean((pimgs[k] - ref) ** 2) / den),
+                        "batched_vs_plain_max_abs": float(np.abs(bimgs[k] - pimgs[k]).max())})
 
-    # roofline of the dominant kernel class
+    # e2e: upload the scene pool from host memory inside the timed region
+    srv_e2e = gpu.Server(ctx, opts)
+    jobs = make_jobs(5000)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g2 = [gpu.GpuScene(ctx, s) for s in pool]
+    sec, _, _ = serve_step(srv_e2e, g2, jobs)
+    e2e_s = time.perf_counter() - t0
+    srv_e2e.stop()
+    for g in g2:
+        g.close()
+    e2e_value = job_samples(jobs) * world / max_over_ranks(e2e_s, world) / 1e6
+    h2d = sum(scene_host_bytes(s) for s in pool) + len(jobs) * 40
+    d2h = sum(j["width"] * j["height"] * 12 for j in jobs)
+
+    # roofline: a profiled server step (events around every kernel)
+    prof = gpu.Server(ctx, gpu.server_options(path_pool=opts.path_pool, block_size=opts.block_size,
+                                              policy=opts.policy, use_graphs=False, profile=True))
+    jobs = make_jobs(1000)
+    serve_step(prof, gscenes, jobs)
+    ps = prof.stats()
+    prof.stop()
     peak, peak_kind = measured_peaks()
-    cls_ms = list(st_prof.class_ms)
+    cls_ms = list(ps.class_ms)
     dom = int(np.argmax(cls_ms[:abi.LJ_KERNEL_OTHER]))
-    # compulsory bytes (queues, hits, path state): what must cross HBM; the
-    # BVH bytes of a small scene are served by L1/L2 and reported separately
-    nb = kernel_bytes(dom, st_prof, 0.0, 0.0)
-    nb_bvh = kernel_bytes(dom, st_prof, bvh_closest, bvh_shadow)
-    launches_dom = max(1, st_prof.class_launches[dom])
+    nb = kernel_bytes(dom, job_samples(jobs), ps.rays_closest, ps.rays_shadow, ps.path_segments)
+    launches_dom = max(1, ps.class_launches[dom])
     avg_launch_s = cls_ms[dom] / 1e3 / launches_dom
     achieved = nb / launches_dom / avg_launch_s / 1e9
-    achieved_bvh = nb_bvh / launches_dom / avg_launch_s / 1e9
-    traffic = load_traffic(abi.KERNEL_CLASS_NAMES[dom])
+    traffic = load_traffic("srv_" + abi.KERNEL_CLASS_NAMES[dom])
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(b_total * 1e3 / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded scene generator)", "config": config_dict(sc),
+        "data": "synthetic (seeded scene and job generators)", "config": config_dict(pool, opts),
+        "latency_ms": {"p50": round(pct(b_lat, 50), 2), "p99": round(pct(b_lat, 99), 2), "jobs": len(b_lat)},
+        "plain": {"value": round(plain_value, 3), "unit": "Msamples/s",
+                  "ms_per_step": round(p_total * 1e3 / args.steps, 3),
+                  "latency_ms": {"p50": round(pct(p_lat, 50), 2), "p99": round(pct(p_lat, 99), 2)},
+                  "what": "same jobs, one at a time, lj_gpu_render_job_device + image to host"},
+        "batched_over_plain": round(value / plain_value, 3),
+        "rel_mse_vs_4096spp": rel_mse,
         "clocks": ck,
-        "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": desc_bytes,
-                "d2h_bytes_per_step": img_bytes,
-                "what": "lj_gpu_scene_create (upload + device BVH build) + lj_gpu_render (image to host)"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "what": "scene pool uploaded from host (lj_gpu_scene_create, BVH build) + one step served, "
+                        "images to host"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": abi.KERNEL_CLASS_NAMES[dom], "achieved": round(achieved, 1),
+        "roofline": {"bound": "hbm", "kernel": "k_srv_" + abi.KERNEL_CLASS_NAMES[dom], "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6800 GB/s", "traffic": traffic,
                      "bytes_per_launch": round(nb / launches_dom), "avg_launch_us": round(avg_launch_s * 1e6, 2),
-                     "with_bvh": {"achieved": round(achieved_bvh, 1), "bytes_per_launch": round(nb_bvh / launches_dom),
-                                  "note": "incl. BVH node/leaf bytes (lj_gpu_trace_counters); for a small scene "
-                                          "they are L1/L2 hits, not HBM traffic"}},
+                     "bytes": "compulsory (queues, hits, path state, shading records); BVH excluded"},
         "kernel_ms_per_step": {abi.KERNEL_CLASS_NAMES[c]: round(cls_ms[c], 3) for c in range(abi.LJ_KERNEL_CLASSES)},
-        "rays_per_step": {"closest": st_prof.rays_closest, "shadow": st_prof.rays_shadow,
-                          "segments": st_prof.path_segments},
-        "mrays_per_s": round((st_prof.rays_closest + st_prof.rays_shadow) / (st_prof.device_ms / 1e3) / 1e6, 1),
-        "bvh_bytes_per_ray": {"closest": round(bvh_closest, 1), "shadow": round(bvh_shadow, 1)},
+        "rays_per_step": {"closest": ps.rays_closest, "shadow": ps.rays_shadow, "segments": ps.path_segments},
+        "mrays_per_s": round((st1.rays_closest - st0.rays_closest + st1.rays_shadow - st0.rays_shadow)
+                             / b_total / 1e6, 1),
     }
+    srv.stop()
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(sc, target_s=args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(pool, target_s=args.cpu_seconds)
         print(json.dumps(line), flush=True)
-    g.close()
+    for g in gscenes:
+        g.close()
     ctx.close()
 
 
-def _camera_rays(sc, n):
-    """Primary-like rays from the camera toward random screen points (host)."""
-    rng = np.random.default_rng(3)
-    m = sc.cam_to_world
-    aspect = sc.width / sc.height
-    t = np.tan(np.radians(sc.fov / 2))
-    sx, sy = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
-    d_cam = np.stack([-sx * t, -sy * t / aspect, np.ones(n)], axis=1)
-    d = d_cam @ m[:3, :3].T
-    d /= np.linalg.norm(d, axis=1, keepdims=True)
-    r = np.zeros((n, 8), np.float32)
-    r[:, 0:3] = m[:3, 3]
-    r[:, 4:7] = d
-    r[:, 7] = np.inf
-    return r
-
-
 def scene_host_bytes(sc):
+    import ctypes as C
     b = 0
     for s in sc.shapes:
         if s["kind"] == abi.LJ_SHAPE_MESH:
             b += s["positions"].nbytes + s["indices"].nbytes
             b += 0 if s["normals"] is None else s["normals"].nbytes
             b += 0 if s["uvs"] is None else s["uvs"].nbytes
-    import ctypes as C
     b += C.sizeof(abi.lj_shape_desc) * len(sc.shapes) + C.sizeof(abi.lj_material_desc) * len(sc.materials)
     b += C.sizeof(abi.lj_light_desc) * len(sc.lights) + C.sizeof(abi.lj_scene_desc)
     for im in sc.images:
@@ -346,7 +432,7 @@ def scene_host_bytes(sc):
 
 def load_traffic(kernel_name):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/*.json), or None."""
+    summary (profiles/traffic.json), or None."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         d = json.load(open(p))
@@ -356,42 +442,65 @@ def load_traffic(kernel_name):
     return None
 
 
+# ------------------------------------------------------------ CPU side
+def cpu_sample(pool, target_s):
+    """The oracle restatement on all host cores over random pixels of every
+    scene of the pool (1 spp each, the scenes' own resolution and depth),
+    sized to about target_s seconds.  Returns (Msamples/s, cores, text)."""
+    from oracle import ljo
+    ljo.build()
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(7)
+    oss = [ljo.OracleScene(s) for s in pool]
+
+    def run(n_px, seed):
+        t0 = time.perf_counter()
+        for s, o in zip(pool, oss):
+            px = rng.integers(0, s.width * s.height, n_px).astype(np.int32)
+            o.render_samples(px, 1, seed=seed, nthreads=cores)
+        return time.perf_counter() - t0
+
+    t1 = run(256, 1)
+    n_px = int(max(256, min(1 << 20, 256 * target_s / max(t1, 1e-3))))
+    dt = run(n_px, 2)
+    n = n_px * len(pool)
+    text = ("%d random pixels x 1 spp of each of the %d serving scenes (%d samples, %.1f s); C++ restatement "
+            "of src/path_tracing.h pinned to the reference's renders, %d threads" % (n_px, len(pool), n, dt, cores))
+    return n / dt / 1e6, cores, text
+
+
+def cpu_baseline(pool, target_s=10.0):
+    v, cores, text = cpu_sample(pool, target_s)
+    return {"value": round(v, 4), "unit": "Msamples/s", "cores": cores, "kind": "port", "sample": text}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from oracle import ljo
-    ljo.build()
-    sc = make_scene()
-    o = ljo.OracleScene(sc)
-    cores = os.cpu_count() or 1
-    # bounded sample per step: the full image at `spp_step` samples per pixel
-    t0 = time.perf_counter()
-    o.render(mode="keyed", seed=1, spp=1, nthreads=cores)
-    t1 = time.perf_counter() - t0
-    spp_step = int(max(1, min(sc.spp, 8.0 / max(t1, 1e-3))))
+    pool = make_scenes()
     for i in range(args.warmup):
-        o.render(mode="keyed", seed=10 + i, spp=1, nthreads=cores)
-    times = []
+        cpu_sample(pool, 0.5)
+    vals, texts, secs = [], [], []
     for i in range(args.steps):
         t0 = time.perf_counter()
-        o.render(mode="keyed", seed=100 + i, spp=spp_step, nthreads=cores)
-        times.append(time.perf_counter() - t0)
-    samples = sc.width * sc.height * spp_step
-    value = samples * args.steps / sum(times) / 1e6
-    sample = ("%dx%d at %d spp per step (%d samples) of the %d-spp job; lajolla's path tracer "
-              "(C++ restatement, FP64, %d threads)" % (sc.width, sc.height, spp_step, samples, sc.spp, cores))
+        v, cores, text = cpu_sample(pool, 6.0)
+        secs.append(time.perf_counter() - t0)
+        vals.append(v)
+        texts.append(text)
+    value = statistics.mean(vals)
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Msamples/s",
             "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(1e3 * sum(times) / args.steps, 3), "higher_is_better": True,
+            "ms_per_step": round(1e3 * sum(secs) / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene generator)",
-            "config": config_dict(sc),
+            "config": config_dict(pool),
             "cpu_baseline": {"value": round(value, 4), "unit": "Msamples/s", "cores": cores, "kind": "port",
-                             "sample": sample},
+                             "sample": "per step: " + texts[-1]},
             "e2e": {"value": round(value, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "the reference renderer itself cannot be compiled on this machine (its sources are not "
-                    "shipped here); its C++ restatement in oracle/ runs instead"}
+            "note": "the reference renderer cannot be built on the benchmark machine (its sources are not "
+                    "there); its C++ restatement in oracle/ runs instead, on a bounded sample of the "
+                    "serving scenes (the reference has no server: it renders one scene per process)"}
     print(json.dumps(line), flush=True)
 
 

@@ -310,7 +310,9 @@ typedef struct lj_ray {
 
 /* Hit layout: 16 bytes.  prim = global primitive index (triangles of all
  * meshes in shape order, then spheres), -1 on miss. u, v = barycentrics
- * (Embree convention: p = (1-u-v) p0 + u p1 + v p2). */
+ * (Embree convention: p = (1-u-v) p0 + u p1 + v p2).  Primitives at exactly
+ * the same distance resolve to the lower index, whatever the traversal
+ * order. */
 typedef struct lj_hit {
     float t;
     int32_t prim;
@@ -406,6 +408,107 @@ int lj_gpu_phase_batch(lj_ctx *ctx, int32_t phase_kind, float g,
                        const float *d_dir_in, const float *d_dir_out,
                        const float *d_rnd, float *d_out_value, float *d_out_pdf,
                        float *d_out_dir, int64_t n, void *stream);
+
+/* ---- serving: continuous batching of render jobs ------------------------ */
+/* No counterpart in the reference, whose main.cpp renders one scene per
+ * process.  A server keeps scenes, BVHs and per-job accumulators resident and
+ * runs the paths of every live job in one pool of wavefront queues: when a
+ * path ends, its slot is refilled with a sample of the next job in the
+ * scheduling order, so jobs that arrive while others run are admitted as
+ * slots and memory free up and their work overlaps on the device.  Each
+ * wave (ray generation, closest hit, shade, shadow rays, retire) is replayed
+ * from a captured CUDA graph.  Samples are keyed on (job seed, pixel,
+ * sample) as in lj_gpu_render and summed in 64-bit fixed point (2^-32
+ * units), so a job's image is bit-identical whatever else runs beside it.
+ * Path-integrator scenes only (other integrators: LJ_ERR_UNSUPPORTED).
+ * The server runs a host thread of its own; its functions may be called
+ * from any one client thread at a time.  A scene submitted to a server stays
+ * registered with it until lj_gpu_server_stop; lj_gpu_scene_destroy leaves
+ * such a scene alive (and sets the context's error message). */
+enum { LJ_SCHED_FIFO = 0, LJ_SCHED_SRPT = 1 };  /* SRPT: fewest remaining samples first */
+typedef struct lj_server_options {
+    int64_t hbm_budget_bytes;    /* scenes + live jobs + path pool; 0 = 120 GiB            */
+    int64_t path_pool;           /* paths in flight over all jobs; 0 = 1 << 22             */
+    int32_t block_size;          /* 64, 128 or 256; 0 = 128                                */
+    int32_t max_live_jobs;       /* job table size, <= 4096; 0 = 256                       */
+    int32_t max_queued_jobs;     /* submissions waiting for admission; 0 = 65536           */
+    int32_t waves_per_poll;      /* waves between host completion checks; 0 = 8            */
+    int32_t policy;              /* LJ_SCHED_*                                             */
+    int32_t use_graphs;          /* 1 = replay captured CUDA graphs, 0 = plain launches    */
+    int32_t flags;               /* LJ_SERVER_PROFILE: time each kernel class with CUDA
+                                    events (plain launches, a host sync per poll)          */
+    int32_t pad;
+} lj_server_options;
+#define LJ_SERVER_PROFILE 1
+
+typedef struct lj_job_desc {
+    uint64_t seed;               /* RNG key, as lj_render_params.seed                      */
+    int32_t spp;                 /* 0 = scene options.samples_per_pixel                    */
+    int32_t sample_offset;
+    int32_t width, height;       /* 0 = the scene camera's resolution (same fov)           */
+    int32_t override_depth;      /* 1 = use max_depth / rr_depth below                     */
+    int32_t max_depth, rr_depth;
+    int32_t pad;
+} lj_job_desc;
+
+enum { LJ_JOB_QUEUED = 0, LJ_JOB_RUNNING = 1, LJ_JOB_DONE = 2, LJ_JOB_FAILED = 3, LJ_JOB_CANCELLED = 4 };
+typedef struct lj_job_status {
+    int32_t state;               /* LJ_JOB_*                                               */
+    int32_t error;               /* LJ_ERR_* when FAILED                                   */
+    int32_t width, height;
+    int64_t samples_total;
+    int64_t samples_done;        /* as of the server's last completion check              */
+    int64_t samples_dropped;     /* non-finite samples left out of the sum                 */
+    double submit_ms, admit_ms, finish_ms;   /* server clock (ms since start)              */
+} lj_job_status;
+
+typedef struct lj_server_stats {
+    int64_t jobs_submitted, jobs_done, jobs_failed, jobs_cancelled;
+    int64_t waves;               /* wavefront passes launched                              */
+    int64_t graph_launches;
+    int64_t samples_done;
+    int64_t bytes_resident;      /* scenes + live jobs + path pool                         */
+    double busy_ms;              /* host time with paths in flight                         */
+    int64_t rays_closest, rays_shadow, path_segments;   /* device counters, last poll     */
+    int64_t kernel_launches;
+    double class_ms[LJ_KERNEL_CLASSES];        /* LJ_SERVER_PROFILE only (regen = CAMERA,
+                                                  plan + retire = OTHER)                   */
+    int64_t class_launches[LJ_KERNEL_CLASSES];
+} lj_server_stats;
+
+int lj_gpu_server_start(lj_ctx *ctx, const lj_server_options *options, lj_server **out);
+/* Queues a render of `scene` (LJ_ERR_QUEUE_FULL when max_queued_jobs are
+ * waiting; LJ_ERR_OUT_OF_MEMORY when the job cannot fit the budget even
+ * alone).  *job_id identifies it in the calls below. */
+int lj_gpu_server_submit(lj_server *server, lj_scene *scene, const lj_job_desc *job, int64_t *job_id);
+int lj_gpu_server_poll(lj_server *server, int64_t job_id, lj_job_status *status);
+/* Waits until the job is no longer queued or running (timeout_s < 0: no
+ * limit; LJ_ERR_TIMEOUT otherwise).  When it is DONE and out_rgb is not
+ * NULL, copies its W*H*3 FP32 image (mean over spp) there and forgets the
+ * job.  Returns LJ_ERR_CANCELLED / the job's error for those states. */
+int lj_gpu_server_wait(lj_server *server, int64_t job_id, double timeout_s, float *out_rgb,
+                       lj_job_status *status);
+/* Stops issuing the job's samples; paths already in flight finish. */
+int lj_gpu_server_cancel(lj_server *server, int64_t job_id);
+int lj_gpu_server_stats(lj_server *server, lj_server_stats *stats);
+const char *lj_gpu_server_last_error(lj_server *server);
+/* Cancels what is left, waits for the device, frees everything. */
+int lj_gpu_server_stop(lj_server *server);
+
+/* One job through the single-scene wavefront renderer (no batching): the
+ * same samples a server job of this description traces, into device memory
+ * `d_out_rgb` (W*H*3 floats at the job's resolution) on `stream`.  Stats as
+ * lj_gpu_render_device.  No counterpart in the reference. */
+int lj_gpu_render_job_device(lj_scene *scene, const lj_job_desc *job, float *d_out_rgb, void *stream,
+                             lj_stats *stats);
+
+/* Autotuner: runs the given job mix (job i renders scenes[job_scene[i]])
+ * once per candidate (path pool x block size) and writes the fastest into
+ * *options (other fields are kept).  With cache_path, results are read from
+ * and stored in that JSON file, keyed by device and workload size. */
+int lj_gpu_server_autotune(lj_ctx *ctx, lj_scene *const *scenes, const lj_job_desc *jobs,
+                           const int32_t *job_scene, int32_t n_jobs, const char *cache_path,
+                           lj_server_options *options);
 
 #ifdef __cplusplus
 }

@@ -166,6 +166,39 @@ class lj_bsdf_batch(C.Structure):
                 ("d_out_roughness", C.c_void_p), ("d_out_valid", C.c_void_p)]
 
 
+LJ_SCHED_FIFO, LJ_SCHED_SRPT = 0, 1
+LJ_SERVER_PROFILE = 1
+LJ_JOB_QUEUED, LJ_JOB_RUNNING, LJ_JOB_DONE, LJ_JOB_FAILED, LJ_JOB_CANCELLED = range(5)
+
+
+class lj_server_options(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("path_pool", C.c_int64),
+                ("block_size", C.c_int32), ("max_live_jobs", C.c_int32),
+                ("max_queued_jobs", C.c_int32), ("waves_per_poll", C.c_int32),
+                ("policy", C.c_int32), ("use_graphs", C.c_int32), ("flags", C.c_int32), ("pad", C.c_int32)]
+
+
+class lj_job_desc(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("spp", C.c_int32), ("sample_offset", C.c_int32),
+                ("width", C.c_int32), ("height", C.c_int32), ("override_depth", C.c_int32),
+                ("max_depth", C.c_int32), ("rr_depth", C.c_int32), ("pad", C.c_int32)]
+
+
+class lj_job_status(C.Structure):
+    _fields_ = [("state", C.c_int32), ("error", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+                ("samples_total", C.c_int64), ("samples_done", C.c_int64), ("samples_dropped", C.c_int64),
+                ("submit_ms", C.c_double), ("admit_ms", C.c_double), ("finish_ms", C.c_double)]
+
+
+class lj_server_stats(C.Structure):
+    _fields_ = [("jobs_submitted", C.c_int64), ("jobs_done", C.c_int64), ("jobs_failed", C.c_int64),
+                ("jobs_cancelled", C.c_int64), ("waves", C.c_int64), ("graph_launches", C.c_int64),
+                ("samples_done", C.c_int64), ("bytes_resident", C.c_int64), ("busy_ms", C.c_double),
+                ("rays_closest", C.c_int64), ("rays_shadow", C.c_int64), ("path_segments", C.c_int64),
+                ("kernel_launches", C.c_int64),
+                ("class_ms", C.c_double * LJ_KERNEL_CLASSES), ("class_launches", C.c_int64 * LJ_KERNEL_CLASSES)]
+
+
 STRUCT_SIZES = {
     "lj_texture_desc": C.sizeof(lj_texture_desc),
     "lj_material_desc": C.sizeof(lj_material_desc),
@@ -179,6 +212,10 @@ STRUCT_SIZES = {
     "lj_scene_desc": C.sizeof(lj_scene_desc),
     "lj_scene_info": C.sizeof(lj_scene_info),
     "lj_render_params": C.sizeof(lj_render_params),
+    "lj_server_options": C.sizeof(lj_server_options),
+    "lj_job_desc": C.sizeof(lj_job_desc),
+    "lj_job_status": C.sizeof(lj_job_status),
+    "lj_server_stats": C.sizeof(lj_server_stats),
     "lj_stats": C.sizeof(lj_stats),
     "lj_ray": C.sizeof(lj_ray),
     "lj_hit": C.sizeof(lj_hit),

@@ -208,10 +208,40 @@ int check_desc(const lj_scene_desc *d, std::string &msg) {
         }
     }
     if (d->envmap_light_id >= d->num_lights) { msg = "envmap light id out of range"; return -1; }
+    if (d->camera.medium_id >= d->num_media || d->camera.medium_id < -1) { msg = "camera medium id out of range"; return -1; }
+    for (int i = 0; i < d->num_media; i++) {
+        const lj_medium_desc &m = d->media[i];
+        if (m.kind != LJ_MEDIUM_HOMOGENEOUS && m.kind != LJ_MEDIUM_HETEROGENEOUS) { msg = "medium: unknown kind"; return -1; }
+        if (m.phase_kind != LJ_PHASE_ISOTROPIC && m.phase_kind != LJ_PHASE_HG) { msg = "medium: unknown phase"; return -1; }
+    }
     return 0;
 }
 
 }  // namespace
+
+namespace lj {
+// Camera (src/camera.cpp:7-21) at resolution width x height.
+void make_cam_rec(const lj_camera_desc &c, int width, int height, CamRec &cam) {
+    double aspect = (double)width / (double)height;
+    M4d sc_m{}, tr{}, persp{};
+    sc_m.m[0] = -0.5; sc_m.m[5] = -0.5 * aspect; sc_m.m[10] = 1.0; sc_m.m[15] = 1;
+    tr.m[0] = 1; tr.m[5] = 1; tr.m[10] = 1; tr.m[15] = 1; tr.m[3] = -1.0; tr.m[7] = -1.0 / aspect;
+    double cot = 1.0 / std::tan((M_PI / 180.0) * (c.fov / 2.0));
+    persp.m[0] = cot; persp.m[5] = cot; persp.m[10] = 1; persp.m[11] = -1; persp.m[14] = 1;
+    M4d s2c = m4_inverse(m4_mul(m4_mul(sc_m, tr), persp));
+    for (int k = 0; k < 16; k++) {
+        cam.sample_to_cam[k] = (float)s2c.m[k];
+        cam.cam_to_world[k] = (float)c.cam_to_world[k];
+    }
+    // xform_point(cam_to_world, 0) with the homogeneous divide
+    double w = c.cam_to_world[15];
+    for (int k = 0; k < 3; k++) cam.org[k] = (float)(c.cam_to_world[k * 4 + 3] / w);
+    cam.w = width;
+    cam.h = height;
+    cam.filter_kind = c.filter_kind;
+    cam.filter_param = c.filter_param;
+}
+}  // namespace lj
 
 extern "C" {
 
@@ -244,6 +274,7 @@ void lj_gpu_shutdown(lj_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    while (!ctx->servers.empty()) lj_gpu_server_stop(ctx->servers.back());
     while (!ctx->scenes.empty()) lj_gpu_scene_destroy(ctx->scenes.back());
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->d_status) cudaFree(ctx->d_status);
@@ -514,31 +545,61 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
         return fail(LJ_ERR_CUDA);
     ds.num_lights = d->num_lights;
 
-    // ---- camera (src/camera.cpp:7-21) ----
-    {
-        const lj_camera_desc &c = d->camera;
-        double aspect = (double)c.width / (double)c.height;
-        M4d sc_m{}, tr{}, persp{};
-        sc_m.m[0] = -0.5; sc_m.m[5] = -0.5 * aspect; sc_m.m[10] = 1.0; sc_m.m[15] = 1;
-        tr.m[0] = 1; tr.m[5] = 1; tr.m[10] = 1; tr.m[15] = 1; tr.m[3] = -1.0; tr.m[7] = -1.0 / aspect;
-        double cot = 1.0 / std::tan((M_PI / 180.0) * (c.fov / 2.0));
-        persp.m[0] = cot; persp.m[5] = cot; persp.m[10] = 1; persp.m[11] = -1; persp.m[14] = 1;
-        M4d s2c = m4_inverse(m4_mul(m4_mul(sc_m, tr), persp));
-        for (int k = 0; k < 16; k++) {
-            ds.cam.sample_to_cam[k] = (float)s2c.m[k];
-            ds.cam.cam_to_world[k] = (float)c.cam_to_world[k];
-        }
-        // xform_point(cam_to_world, 0) with the homogeneous divide
-        double w = c.cam_to_world[15];
-        for (int k = 0; k < 3; k++) ds.cam.org[k] = (float)(c.cam_to_world[k * 4 + 3] / w);
-        ds.cam.w = c.width;
-        ds.cam.h = c.height;
-        ds.cam.filter_kind = c.filter_kind;
-        ds.cam.filter_param = c.filter_param;
-    }
+    sc->camera = d->camera;
+    make_cam_rec(d->camera, d->camera.width, d->camera.height, ds.cam);
     ds.max_depth = d->options.max_depth;
     ds.rr_depth = d->options.rr_depth;
     sc->has_media = d->num_media > 0;
+
+    // ---- media (src/medium.h, src/volume.h; .vol data as load_volume gives it) ----
+    {
+        std::vector<MediumRec> media(d->num_media);
+        for (int i = 0; i < d->num_media; i++) {
+            const lj_medium_desc &m = d->media[i];
+            MediumRec &r = media[i];
+            memset(&r, 0, sizeof(r));
+            r.kind = m.kind;
+            r.phase_kind = m.phase_kind;
+            r.g = m.g;
+            for (int c = 0; c < 3; c++) { r.sigma_a[c] = m.sigma_a[c]; r.sigma_s[c] = m.sigma_s[c]; }
+            const lj_volume_desc *src[2] = {&m.albedo, &m.density};
+            VolRec *dst[2] = {&r.albedo, &r.density};
+            for (int k = 0; k < 2 && m.kind == LJ_MEDIUM_HETEROGENEOUS; k++) {
+                const lj_volume_desc &v = *src[k];
+                VolRec &o = *dst[k];
+                o.kind = v.kind;
+                o.scale = v.scale;
+                if (v.kind == LJ_VOL_CONST) {
+                    for (int c = 0; c < 3; c++) o.value[c] = o.max_value[c] = v.value[c];
+                    continue;
+                }
+                size_t n = (size_t)v.res[0] * v.res[1] * v.res[2];
+                if (n == 0 || !v.data || (v.channels != 1 && v.channels != 3)) {
+                    err = "medium " + std::to_string(i) + ": bad grid volume";
+                    return fail(LJ_ERR_INVALID_ARG);
+                }
+                std::vector<float> rgb(n * 3);
+                float mx[3] = {0, 0, 0};
+                for (size_t p = 0; p < n; p++)
+                    for (int c = 0; c < 3; c++) {
+                        float x = v.channels == 3 ? v.data[p * 3 + c] : v.data[p];
+                        rgb[p * 3 + c] = x;
+                        mx[c] = std::max(mx[c], x);
+                    }
+                for (int c = 0; c < 3; c++) {
+                    o.res[c] = v.res[c];
+                    o.pmin[c] = v.p_min[c];
+                    o.pmax[c] = v.p_max[c];
+                    o.max_value[c] = v.scale * mx[c];
+                }
+                if (upload(sc, rgb, &o.data, &err)) return fail(LJ_ERR_CUDA);
+            }
+        }
+        if (upload(sc, media, &ds.media, &err)) return fail(LJ_ERR_CUDA);
+        ds.num_media = d->num_media;
+        ds.camera_medium = d->camera.medium_id;
+        ds.max_null_collisions = d->options.max_null_collisions;
+    }
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
         err = "scene upload: stream synchronize failed";
         return fail(LJ_ERR_CUDA);
@@ -550,6 +611,10 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
 
 void lj_gpu_scene_destroy(lj_scene *sc) {
     if (!sc) return;
+    if (sc->server_refs.load() > 0) {
+        set_error(sc->ctx, LJ_ERR_INVALID_ARG, "scene_destroy: the scene is registered with a running server");
+        return;
+    }
     auto &live = sc->ctx->scenes;
     live.erase(std::remove(live.begin(), live.end(), sc), live.end());
     cudaSetDevice(sc->ctx->device);

@@ -118,7 +118,9 @@ LJ_D float xdot(V3 a, V3 b) {
 LJ_D V3 xsub(V3 a, V3 b) { return V3{__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)}; }
 
 // Moller-Trumbore on precomputed (v0, e1 = v1 - v0, e2 = v2 - v0); accepts
-// tnear < t < tfar.  Same operation sequence as ljo::tri_intersect.
+// tnear < t <= tfar (callers reject t == tfar unless it breaks a tie
+// with the current closest hit).  Same operation sequence as
+// ljo::tri_intersect.
 LJ_D bool tri_intersect(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float tnear, float tfar, float &t_out,
                         float &u_out, float &v_out) {
     V3 pvec = xcross(d, e2);
@@ -132,7 +134,7 @@ LJ_D bool tri_intersect(V3 v0, V3 e1, V3 e2, V3 o, V3 d, float tnear, float tfar
     float v = __fmul_rn(xdot(d, qvec), inv_det);
     if (!(v >= 0.0f && __fadd_rn(u, v) <= 1.0f)) return false;
     float t = __fmul_rn(xdot(e2, qvec), inv_det);
-    if (!(t > tnear && t < tfar)) return false;
+    if (!(t > tnear && t <= tfar)) return false;
     t_out = t;
     u_out = u;
     v_out = v;

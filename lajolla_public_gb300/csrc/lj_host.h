@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -17,8 +18,10 @@ struct lj_ctx {
     // grow-only scratch for the Morton / radix-sort entry point
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
-    // live scenes of this context: lj_gpu_shutdown destroys what is left
+    // live scenes and servers of this context: lj_gpu_shutdown stops and
+    // destroys what is left
     std::vector<struct lj_scene *> scenes;
+    std::vector<struct lj_server *> servers;
 };
 
 // Wavefront buffers owned by a scene, grown on demand (lj_path.cu).
@@ -40,11 +43,21 @@ struct lj_scene {
     std::vector<int> prim_shape_host;   // global prim -> shape
     PathBuffers path;
     bool has_media = false;
+    lj_camera_desc camera{};
+    std::atomic<int> server_refs{0};   // servers this scene is registered with
 };
 
 namespace lj {
 int set_error(lj_ctx *ctx, int code, const std::string &msg);
+// lj_capi.cu: camera record (src/camera.cpp:7-21) at a given resolution
+void make_cam_rec(const lj_camera_desc &c, int width, int height, CamRec &cam);
 // lj_path.cu
 int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, cudaStream_t s,
-                lj_stats *stats, bool sync_stats);
+                lj_stats *stats, bool sync_stats, const lj_job_desc *job);
+// lj_volpath.cu
+int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out, cudaStream_t s,
+                   lj_stats *stats);
+// lj_aux.cu
+int render_aux(lj_scene *scene, const lj_render_params *params, float *d_out, cudaStream_t s,
+               lj_stats *stats);
 }  // namespace lj

@@ -21,84 +21,12 @@
 #include <vector>
 
 #include "lj_host.h"
-#include "lj_shade.cuh"
 #include "lj_trace.cuh"
+#include "lj_wavefront.cuh"
 
 namespace lj {
 
 namespace {
-
-struct PathSoA {
-    int *pixel;
-    uint64_t *rng;
-    float4 *beta;    // xyz: throughput after the pending BSDF sample (beta f / p), w: rr_prob
-    float4 *L;       // xyz: radiance, w: eta_scale
-    float4 *prev;    // xyz: vertex that sampled the pending ray, w: its BSDF pdf (solid angle)
-    int *nv;         // num_vertices of the next loop iteration (2 = primary ray pending)
-};
-
-struct Queues {
-    float4 *ray[2];
-    int *path[2];
-    float4 *hit;
-    float4 *sray;
-    int *spath;
-    float4 *scontrib;
-    int *counts;                  // [0], [1]: ray queues, [2]: shadow queue, [3]: pad
-    unsigned long long *stats;    // [0] closest rays, [1] shadow rays, [2] shade segments
-};
-
-LJ_D uint32_t lane_id() { return threadIdx.x & 31u; }
-
-// Append one entry per calling thread; one atomicAdd per group of
-// converged threads.
-LJ_D int queue_slot(int *counter) {
-    unsigned active = __activemask();
-    int leader = __ffs(active) - 1;
-    int base = 0;
-    if ((int)lane_id() == leader) base = atomicAdd(counter, __popc(active));
-    base = __shfl_sync(active, base, leader);
-    return base + __popc(active & ((1u << lane_id()) - 1u));
-}
-
-LJ_D Pcg load_rng(const PathSoA &ps, int p) {
-    Pcg r;
-    r.state = ps.rng[p];
-    r.inc = ((uint64_t)ps.pixel[p] << 1u) | 1u;
-    return r;
-}
-
-// sample_primary, src/camera.cpp:23-47
-LJ_D void camera_ray(const CamRec &c, float sx, float sy, V3 &o, V3 &d) {
-    float px = sx * c.w, py = sy * c.h;
-    float dx = px - floorf(px), dy = py - floorf(py);
-    float ox, oy;
-    if (c.filter_kind == 0) {
-        ox = (2.0f * dx - 1.0f) * (c.filter_param * 0.5f);
-        oy = (2.0f * dy - 1.0f) * (c.filter_param * 0.5f);
-    } else if (c.filter_kind == 1) {
-        float h = c.filter_param * 0.5f;
-        ox = dx < 0.5f ? h * (sqrtf(2.0f * dx) - 1.0f) : h * (1.0f - sqrtf(1.0f - 2.0f * (dx - 0.5f)));
-        oy = dy < 0.5f ? h * (sqrtf(2.0f * dy) - 1.0f) : h * (1.0f - sqrtf(1.0f - 2.0f * (dy - 0.5f)));
-    } else {
-        float r = c.filter_param * sqrtf(-2.0f * logf(fmaxf(dx, 1e-8f)));
-        float sp, cp;
-        sincosf(kTwoPi * dy, &sp, &cp);
-        ox = r * cp;
-        oy = r * sp;
-    }
-    float rx = (floorf(px) + 0.5f + ox) / c.w, ry = (floorf(py) + 0.5f + oy) / c.h;
-    const float *m = c.sample_to_cam;
-    float t0 = m[0] * rx + m[1] * ry + m[3];
-    float t1 = m[4] * rx + m[5] * ry + m[7];
-    float t2 = m[8] * rx + m[9] * ry + m[11];
-    float t3 = m[12] * rx + m[13] * ry + m[15];
-    V3 pt = normalize(V3{t0 / t3, t1 / t3, t2 / t3});
-    const float *w = c.cam_to_world;
-    d = normalize(V3{w[0] * pt.x + w[1] * pt.y + w[2] * pt.z, w[4] * pt.x + w[5] * pt.y + w[6] * pt.z,
-                     w[8] * pt.x + w[9] * pt.y + w[10] * pt.z});
-    o = V3{c.org[0], c.org[1], c.org[2]};
-}
 
 __global__ void k_camera(DevScene sc, PathSoA ps, Queues q, int P, int num_pixels, int sample_base,
                          uint64_t seed) {
@@ -161,143 +89,10 @@ __global__ void __launch_bounds__(128) k_trace_shadow(DevBvh bvh, const float4 *
 __global__ void __launch_bounds__(128) k_shade(DevScene sc, PathSoA ps, Queues q, int cur,
                                                float spread0, int *status) {
     const int n = q.counts[cur];
-    const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(q.stats + 2, (unsigned long long)n);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int p = q.path[cur][i];
-        float4 r0 = q.ray[cur][2 * i], r1 = q.ray[cur][2 * i + 1];
-        V3 ro{r0.x, r0.y, r0.z}, rd{r1.x, r1.y, r1.z};
-        float4 hit = q.hit[i];
-        int prim = __float_as_int(hit.y);
-        int nv = ps.nv[p];
-        float4 Lw = ps.L[p];
-        V3 L{Lw.x, Lw.y, Lw.z};
-        float eta_scale = Lw.w;
-        float4 bw = ps.beta[p];
-        V3 beta{bw.x, bw.y, bw.z};
-        const bool primary = nv == 2;
-        Pcg rng = load_rng(ps, p);
-        bool alive = true;
-
-        if (prim < 0) {
-            // miss: environment map (path_tracing.h:17-28, :284-302)
-            if (sc.env.light_id >= 0) {
-                V3 Le = env_emission(sc, -rd);
-                if (primary) {
-                    L += Le;
-                } else {
-                    float4 pv = ps.prev[p];
-                    float p2 = pv.w;   // G = 1 for directions at infinity
-                    float p1 = __ldg(sc.light_pmf + sc.env.light_id) * env_pdf(sc, rd);
-                    float w2 = (p2 * p2) / (p1 * p1 + p2 * p2);
-                    L += beta * Le * w2;
-                }
-            }
-            alive = false;
-        } else {
-            Vertex vx = make_vertex(sc, ro, rd, hit.x, prim, hit.z, hit.w, primary ? spread0 : 0.0f);
-            if (primary) {
-                if (vx.light >= 0) L += light_emission(sc, vx.light, -rd, PN{vx.p, vx.ng});
-                beta = V3{1.0f, 1.0f, 1.0f};
-                nv = 3;
-            } else {
-                float4 pv = ps.prev[p];
-                V3 prev_p{pv.x, pv.y, pv.z};
-                if (vx.light >= 0) {
-                    // BSDF-sampled hit on an area light (path_tracing.h:268-283)
-                    V3 Le = light_emission(sc, vx.light, -rd, PN{vx.p, vx.ng});
-                    V3 dv = vx.p - prev_p;
-                    float G = fabsf(dot(rd, vx.ng)) / dot(dv, dv);
-                    float p2 = pv.w * G;
-                    float p1 = __ldg(sc.light_pmf + vx.light) *
-                               pdf_point_on_light(sc, vx.light, PN{vx.p, vx.ng}, prev_p);
-                    float w2 = (p2 * p2) / (p1 * p1 + p2 * p2);
-                    L += beta * Le * w2;
-                }
-                // Russian roulette of the iteration that sampled this ray
-                // (path_tracing.h:311-318): that iteration's num_vertices is nv - 1
-                float rr = 1.0f;
-                if (nv - 2 >= sc.rr_depth) {
-                    rr = bw.w;
-                    if (pcg_uniform(rng) > rr) alive = false;
-                }
-                beta = beta * (1.0f / rr);
-            }
-            if (alive && sc.max_depth != -1 && nv > sc.max_depth + 1) alive = false;
-            if (alive && nv > LJ_MAX_BOUNCES + 2) {
-                atomicOr(status, kStatusBounceCap);
-                alive = false;
-            }
-            if (alive) {
-                MatParams mat = resolve_material(sc, vx.material, vx.u, vx.v, vx.uv_screen_size);
-                BsdfVertex bv{vx.ng, vx.frame};
-                V3 wv = -rd;
-                // ---- next event estimation (path_tracing.h:98-207) ----
-                float lu0 = pcg_uniform(rng), lu1 = pcg_uniform(rng);
-                float lw = pcg_uniform(rng), sw = pcg_uniform(rng);
-                // (a scene without lights has no NEE; the reference asserts there)
-                int lid = sc.num_lights > 0 ? sample_light(sc, lw) : -1;
-                PN pl{V3{0, 0, 0}, V3{0, 0, 0}};
-                if (lid >= 0) pl = sample_point_on_light(sc, lid, vx.p, lu0, lu1, sw);
-                V3 dl{0, 0, 1};
-                float G = 0.0f, tmax = 0.0f, p1 = 0.0f;
-                if (lid < 0) {
-                    // no light: G stays 0
-                } else if (sc.lights[lid].kind == 0) {
-                    V3 dd = pl.p - vx.p;
-                    float dist2 = dot(dd, dd);
-                    float dist = sqrtf(dist2);
-                    dl = dd / dist;
-                    G = fmaxf(-dot(dl, pl.n), 0.0f) / dist2;
-                    tmax = (1.0f - sc.eps) * dist;
-                } else {
-                    dl = -pl.n;
-                    G = 1.0f;
-                    tmax = __int_as_float(0x7f800000);
-                }
-                if (lid >= 0) p1 = __ldg(sc.light_pmf + lid) * pdf_point_on_light(sc, lid, pl, vx.p);
-                if (G > 0.0f && p1 > 0.0f) {
-                    V3 f = bsdf_eval(mat, bv, wv, dl);
-                    V3 Le = light_emission(sc, lid, -dl, pl);
-                    float p2 = bsdf_pdf(mat, bv, wv, dl) * G;
-                    float w1 = (p1 * p1) / (p1 * p1 + p2 * p2);
-                    V3 c = beta * f * Le * (G * w1 / p1);
-                    if (c.x > 0.0f || c.y > 0.0f || c.z > 0.0f) {
-                        int s = queue_slot(q.counts + 2);
-                        q.sray[2 * s] = make_float4(vx.p.x, vx.p.y, vx.p.z, sc.eps);
-                        q.sray[2 * s + 1] = make_float4(dl.x, dl.y, dl.z, tmax);
-                        q.spath[s] = p;
-                        q.scontrib[s] = make_float4(c.x, c.y, c.z, 0.0f);
-                    }
-                }
-                // ---- BSDF sampling (path_tracing.h:210-256) ----
-                float bu0 = pcg_uniform(rng), bu1 = pcg_uniform(rng), bwr = pcg_uniform(rng);
-                BsdfSample bs = bsdf_sample(mat, bv, wv, bu0, bu1, bwr);
-                if (!bs.valid) {
-                    alive = false;
-                } else {
-                    V3 f = bsdf_eval(mat, bv, wv, bs.dir);
-                    float pdf = bsdf_pdf(mat, bv, wv, bs.dir);
-                    if (!(pdf > 0.0f)) {
-                        alive = false;
-                    } else {
-                        if (bs.eta != 0.0f) eta_scale /= (bs.eta * bs.eta);
-                        float rr_prob = fminf(max3(beta) / eta_scale, 0.95f);
-                        V3 bn = beta * f / pdf;
-                        ps.beta[p] = make_float4(bn.x, bn.y, bn.z, rr_prob);
-                        ps.prev[p] = make_float4(vx.p.x, vx.p.y, vx.p.z, pdf);
-                        ps.nv[p] = nv + 1;
-                        int s = queue_slot(q.counts + nxt);
-                        q.ray[nxt][2 * s] = make_float4(vx.p.x, vx.p.y, vx.p.z, sc.eps);
-                        q.ray[nxt][2 * s + 1] = make_float4(bs.dir.x, bs.dir.y, bs.dir.z, __int_as_float(0x7f800000));
-                        q.path[nxt][s] = p;
-                    }
-                }
-            }
-        }
-        ps.L[p] = make_float4(L.x, L.y, L.z, eta_scale);
-        ps.rng[p] = rng.state;
-    }
+    const ShadeCfg cfg{sc.max_depth, sc.rr_depth, spread0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        shade_segment(sc, ps, q, cur, i, cfg, status);
 }
 
 // Per pixel: sum the batch's samples in sample order (deterministic).
@@ -359,12 +154,23 @@ int grid_persistent(const void *kernel, int threads) {
 }  // namespace
 
 int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, cudaStream_t s,
-                lj_stats *stats, bool sync_stats) {
+                lj_stats *stats, bool sync_stats, const lj_job_desc *job) {
     lj_ctx *ctx = scene->ctx;
-    const DevScene &sc = scene->dev;
+    DevScene sc = scene->dev;   // job overrides: resolution (camera) and depth options
+    int W = scene->width, H = scene->height;
+    int max_depth = scene->options.max_depth;
+    if (job && job->width > 0 && job->height > 0) {
+        W = job->width;
+        H = job->height;
+        make_cam_rec(scene->camera, W, H, sc.cam);
+    }
+    if (job && job->override_depth) {
+        if (job->max_depth < -1) return set_error(ctx, LJ_ERR_INVALID_ARG, "render: max_depth must be >= -1");
+        sc.max_depth = max_depth = job->max_depth;
+        sc.rr_depth = job->rr_depth;
+    }
     std::string e;
     std::string *err = &e;
-    const int W = scene->width, H = scene->height;
     const int num_pixels = W * H;
     const int spp = params->spp > 0 ? params->spp : scene->options.samples_per_pixel;
     if (spp <= 0) return set_error(ctx, LJ_ERR_INVALID_ARG, "render: samples per pixel must be positive");
@@ -384,6 +190,7 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
     }
     char *cur = (char *)scene->path.block;
     PathSoA ps;
+    ps.job = nullptr;
     ps.pixel = carve<int>(cur, P);
     ps.rng = carve<uint64_t>(cur, P);
     ps.beta = carve<float4>(cur, P);
@@ -391,6 +198,7 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
     ps.prev = carve<float4>(cur, P);
     ps.nv = carve<int>(cur, P);
     Queues q;
+    q.retire = nullptr;
     q.ray[0] = carve<float4>(cur, 2 * P);
     q.ray[1] = carve<float4>(cur, 2 * P);
     q.path[0] = carve<int>(cur, P);
@@ -407,8 +215,7 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
     const int g_trace = grid_persistent((const void *)k_trace_queue, 128);
     const int g_shadow = grid_persistent((const void *)k_trace_shadow, 128);
     const int g_shade = grid_persistent((const void *)k_shade, 128);
-    const int passes = scene->options.max_depth == -1 ? LJ_MAX_BOUNCES + 1
-                                                      : std::max(1, scene->options.max_depth);
+    const int passes = max_depth == -1 ? LJ_MAX_BOUNCES + 1 : std::max(1, max_depth);
     const float spread0 = 0.25f / (float)std::max(W, H);
     cudaEvent_t e0, e1;
     bool timed = stats != nullptr;
@@ -464,7 +271,7 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
             class_launches[LJ_KERNEL_SHADE]++;
             class_launches[LJ_KERNEL_SHADOW]++;
             curq ^= 1;
-            if (scene->options.max_depth == -1 && (pass & 7) == 7) {
+            if (max_depth == -1 && (pass & 7) == 7) {
                 int c = 0;
                 LJ_CUDA_TRY(cudaMemcpyAsync(&c, q.counts + curq, sizeof(int), cudaMemcpyDeviceToHost, s));
                 LJ_CUDA_TRY(cudaStreamSynchronize(s));
@@ -533,11 +340,36 @@ int lj_gpu_render_device(lj_scene *scene, const lj_render_params *params, float 
                          lj_stats *stats) {
     if (!scene || !params || !d_out_rgb) return LJ_ERR_INVALID_ARG;
     cudaSetDevice(scene->ctx->device);
-    if (scene->options.integrator != LJ_INTEGRATOR_PATH)
-        return set_error(scene->ctx, LJ_ERR_UNSUPPORTED, "render: integrator not available in this build");
     cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
     if (stats) memset(stats, 0, sizeof(*stats));
-    return render_path(scene, params, d_out_rgb, s, stats, stats != nullptr);
+    // integrator dispatch, src/render.cpp:155-170
+    if (scene->options.integrator == LJ_INTEGRATOR_PATH)
+        return render_path(scene, params, d_out_rgb, s, stats, stats != nullptr, nullptr);
+    if (scene->options.integrator == LJ_INTEGRATOR_VOLPATH) {
+        // versions 1-5 are simplifications of 6 for homework; 0 and 6 select the full one
+        if (scene->options.vol_path_version != 0 && scene->options.vol_path_version != 6)
+            return set_error(scene->ctx, LJ_ERR_UNSUPPORTED, "render: only vol_path_version 0 / 6 is built");
+        return render_volpath(scene, params, d_out_rgb, s, stats);
+    }
+    if (scene->options.integrator >= LJ_INTEGRATOR_DEPTH && scene->options.integrator <= LJ_INTEGRATOR_MIPMAP_LEVEL)
+        return render_aux(scene, params, d_out_rgb, s, stats);
+    return set_error(scene->ctx, LJ_ERR_UNSUPPORTED, "render: unknown integrator");
+}
+
+int lj_gpu_render_job_device(lj_scene *scene, const lj_job_desc *job, float *d_out_rgb, void *stream,
+                             lj_stats *stats) {
+    if (!scene || !job || !d_out_rgb) return LJ_ERR_INVALID_ARG;
+    if (scene->options.integrator != LJ_INTEGRATOR_PATH)
+        return set_error(scene->ctx, LJ_ERR_UNSUPPORTED, "render_job: path-integrator scenes only");
+    if ((job->width > 0) != (job->height > 0))
+        return set_error(scene->ctx, LJ_ERR_INVALID_ARG, "render_job: give both width and height, or neither");
+    cudaSetDevice(scene->ctx->device);
+    if (stats) memset(stats, 0, sizeof(*stats));
+    lj_render_params p{};
+    p.seed = job->seed;
+    p.spp = job->spp;
+    p.sample_offset = job->sample_offset;
+    return render_path(scene, &p, d_out_rgb, (cudaStream_t)stream, stats, stats != nullptr, job);
 }
 
 int lj_gpu_render(lj_scene *scene, const lj_render_params *params, float *out_rgb, lj_stats *stats) {

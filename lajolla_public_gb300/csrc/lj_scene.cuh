@@ -94,6 +94,27 @@ struct EnvRec {
     const float *pdf_marg;   // th
 };
 
+// Volume<Spectrum> (src/volume.h:12-30): constant value or an FP32 grid,
+// (z, y, x, rgb) with x fastest, trilinear lookup, scale applied on lookup.
+struct VolRec {
+    int kind;              // LJ_VOL_CONST / LJ_VOL_GRID
+    int res[3];
+    float value[3];
+    float pmin[3], pmax[3];
+    float scale;
+    float max_value[3];    // scale * max over the grid (or the constant)
+    const float *data;     // 3 floats per voxel
+};
+
+// Medium (src/medium.h) + phase function.
+struct MediumRec {
+    int kind;              // LJ_MEDIUM_HOMOGENEOUS / LJ_MEDIUM_HETEROGENEOUS
+    int phase_kind;        // LJ_PHASE_ISOTROPIC / LJ_PHASE_HG
+    float g;
+    float sigma_a[3], sigma_s[3];
+    VolRec albedo, density;
+};
+
 struct CamRec {
     float sample_to_cam[16];  // row-major
     float cam_to_world[16];
@@ -126,6 +147,11 @@ struct DevScene {
     // images (textures other than the envmap)
     const MipLevel *image_levels; // image i, level l -> image_levels[i * 8 + l]
     const int *image_num_levels;
+    // participating media
+    const MediumRec *media;
+    int num_media;
+    int camera_medium;
+    int max_null_collisions;
     // camera + options
     CamRec cam;
     float eps;                    // min(radius * 1e-5, 0.01): src/scene.h:99-105

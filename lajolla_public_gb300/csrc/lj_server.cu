@@ -1,0 +1,1208 @@
+// Render server: continuous batching of path-tracing jobs over one pool of
+// wavefront queues.  No counterpart in the reference (main.cpp renders one
+// scene per process); the per-path work is path_tracing
+// (src/path_tracing.h:7-325) through shade_segment, exactly as in the
+// single-scene renderer.
+//
+// Device side, one wave (all kernels read their sizes from device memory,
+// so a fixed launch sequence can be captured once and replayed):
+//   plan     one warp: split the free path slots among the jobs that still
+//            have samples to issue, in the host's scheduling order
+//            (prefix sums over remaining samples), and advance their
+//            issued-sample counters
+//   regen    free slot <- (job, pixel, sample): keyed PCG stream, camera
+//            ray appended to the current ray queue
+//   trace    closest hit; each ray uses the BVH of its job's scene
+//   shade    shade_segment with the job's scene and depth options
+//   shadow   any-hit for the queued NEE rays
+//   retire   finished paths: 64-bit fixed-point sums into the job's
+//            accumulator, done counter, slot back on the free stack
+// Two waves (ray queues 0 -> 1 -> 0) form one CUDA graph.
+//
+// Host side, a worker thread admits jobs under the HBM budget, keeps the
+// order list current, replays the graph, and every few waves reads the jobs'
+// counters back (pinned memory, one event per read) to finish jobs: convert
+// the accumulator to the mean image and copy it to pinned host memory.
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "lj_host.h"
+#include "lj_trace.cuh"
+#include "lj_wavefront.cuh"
+
+namespace lj {
+namespace {
+
+constexpr int kMaxScenes = 256;
+constexpr int kPollsInFlight = 2;
+
+struct SrvJob {
+    CamRec cam;
+    unsigned long long seed;
+    long long total;             // npix * spp
+    unsigned long long *accum;   // npix * 3 sums in units of 2^-32
+    int scene, npix, spp, sample_offset;
+    int max_depth, rr_depth;
+    float spread0;
+    float clamp;                 // |sample| bound that keeps the sums inside int64
+};
+
+struct SrvCtr {
+    unsigned long long issued, done, dropped, pad;
+};
+
+struct SrvDev {
+    const DevScene *scenes;
+    const SrvJob *jobs;
+    SrvCtr *ctr;
+    const int *cancel;
+    const int *order;            // [0] = entries, [1..] job slots
+    int *plan_off;               // per entry: first regen index; [n] = total taken
+    long long *plan_start;       // per entry: first linear sample index
+    int *free_ids;
+    PathSoA ps;
+    Queues q;                    // counts: [0],[1] rays, [2] shadow, [3] retire, [4] free, [5] regen
+    int *status;
+};
+
+__global__ void k_srv_plan(SrvDev d, int cur) {
+    const int lane = threadIdx.x;
+    int *counts = d.q.counts;
+    const int n_order = d.order[0];
+    const long long freec = counts[4];
+    long long carry = 0;
+    for (int base = 0; base < n_order; base += 32) {
+        const int k = base + lane;
+        long long rem = 0, start = 0;
+        int j = -1;
+        if (k < n_order) {
+            j = d.order[1 + k];
+            start = (long long)d.ctr[j].issued;
+            if (!d.cancel[j]) rem = max(0LL, d.jobs[j].total - start);
+        }
+        long long incl = rem;
+        for (int o = 1; o < 32; o <<= 1) {
+            long long y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const long long off = min(carry + incl - rem, freec);
+        const long long n = min(rem, freec - off);
+        if (k < n_order) {
+            d.plan_off[k] = (int)off;
+            d.plan_start[k] = start;
+            if (n > 0) d.ctr[j].issued += (unsigned long long)n;
+        }
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) {
+        const long long take = min(carry, freec);
+        d.plan_off[n_order] = (int)take;
+        counts[5] = (int)take;
+        counts[4] = (int)(freec - take);
+        counts[cur ^ 1] = 0;
+        counts[2] = 0;
+        counts[3] = 0;
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(B) k_srv_regen(SrvDev d, int cur) {
+    const int n = d.q.counts[5];
+    const int base = d.q.counts[4];   // slots popped by the plan: free_ids[base, base + n)
+    const int n_order = d.order[0];
+    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
+        int lo = 0, hi = n_order - 1;   // last entry whose first index is <= i
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (d.plan_off[mid] <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        const int j = d.order[1 + lo];
+        const SrvJob &jb = d.jobs[j];
+        const long long lin = d.plan_start[lo] + (i - d.plan_off[lo]);
+        const int pixel = (int)(lin % jb.npix);
+        const int sample = jb.sample_offset + (int)(lin / jb.npix);
+        const int p = d.free_ids[base + i];
+        Pcg rng = pcg_keyed(jb.seed, (uint64_t)pixel, (uint64_t)sample);
+        const int x = pixel % jb.cam.w, y = pixel / jb.cam.w;
+        float r1 = pcg_uniform(rng), r2 = pcg_uniform(rng);
+        V3 o, dir;
+        camera_ray(jb.cam, (x + r1) / jb.cam.w, (y + r2) / jb.cam.h, o, dir);
+        d.ps.job[p] = j;
+        d.ps.pixel[p] = pixel;
+        d.ps.rng[p] = rng.state;
+        d.ps.beta[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+        d.ps.L[p] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        d.ps.prev[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        d.ps.nv[p] = 2;
+        const int s = queue_slot(d.q.counts + cur);
+        d.q.ray[cur][2 * s] = make_float4(o.x, o.y, o.z, 0.0f);
+        d.q.ray[cur][2 * s + 1] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0x7f800000));
+        d.q.path[cur][s] = p;
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(B) k_srv_trace(SrvDev d, int cur) {
+    const int n = d.q.counts[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.q.stats + 0, (unsigned long long)n);
+    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
+        const int p = d.q.path[cur][i];
+        const DevBvh &bvh = d.scenes[d.jobs[d.ps.job[p]].scene].bvh;
+        float4 r0 = d.q.ray[cur][2 * i], r1 = d.q.ray[cur][2 * i + 1];
+        TraceHit h{0.0f, -1, 0.0f, 0.0f};
+        int ovf = 0;
+        bool f = trace_bvh<false>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
+        d.q.hit[i] = f ? make_float4(h.t, __int_as_float(h.prim), h.u, h.v)
+                       : make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f);
+        if (ovf) atomicOr(d.status, kStatusStackOverflow);
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(B) k_srv_shade(SrvDev d, int cur) {
+    const int n = d.q.counts[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.q.stats + 2, (unsigned long long)n);
+    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
+        const SrvJob &jb = d.jobs[d.ps.job[d.q.path[cur][i]]];
+        const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
+        shade_segment(d.scenes[jb.scene], d.ps, d.q, cur, i, cfg, d.status);
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(B) k_srv_shadow(SrvDev d) {
+    const int n = d.q.counts[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.q.stats + 1, (unsigned long long)n);
+    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
+        const int p = d.q.spath[i];
+        const DevBvh &bvh = d.scenes[d.jobs[d.ps.job[p]].scene].bvh;
+        float4 r0 = d.q.sray[2 * i], r1 = d.q.sray[2 * i + 1];
+        TraceHit h{0.0f, -1, 0.0f, 0.0f};
+        int ovf = 0;
+        bool occ = trace_bvh<true>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
+        if (ovf) atomicOr(d.status, kStatusStackOverflow);
+        if (!occ) {
+            float4 c = d.q.scontrib[i];
+            float4 l = d.ps.L[p];
+            d.ps.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
+        }
+    }
+}
+
+LJ_D unsigned long long to_fixed(float v, float clamp) {
+    v = fminf(fmaxf(v, -clamp), clamp);
+    return (unsigned long long)__float2ll_rn(v * 4294967296.0f);   // exact scaling by 2^32
+}
+
+template <int B>
+__global__ void __launch_bounds__(B) k_srv_retire(SrvDev d) {
+    const int n = d.q.counts[3];
+    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
+        const int p = d.q.retire[i];
+        const int j = d.ps.job[p];
+        const SrvJob &jb = d.jobs[j];
+        const float4 L = d.ps.L[p];
+        if (isfinite(L.x) && isfinite(L.y) && isfinite(L.z)) {
+            unsigned long long *a = jb.accum + 3 * (size_t)d.ps.pixel[p];
+            atomicAdd(a, to_fixed(L.x, jb.clamp));
+            atomicAdd(a + 1, to_fixed(L.y, jb.clamp));
+            atomicAdd(a + 2, to_fixed(L.z, jb.clamp));
+        } else {
+            atomicAdd(&d.ctr[j].dropped, 1ULL);
+        }
+        const unsigned active = __activemask();
+        const unsigned same = __match_any_sync(active, j);
+        if ((int)(threadIdx.x & 31u) == __ffs(same) - 1) atomicAdd(&d.ctr[j].done, (unsigned long long)__popc(same));
+        d.free_ids[queue_slot(d.q.counts + 4)] = p;
+    }
+}
+
+__global__ void k_srv_finalize(const unsigned long long *acc, float *img, long long n, double scale) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) img[i] = (float)((double)(long long)acc[i] * scale);
+}
+
+__global__ void k_srv_init_free(int *free_ids, int *counts, int P) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < P) free_ids[i] = i;
+    if (i == 0) {
+        for (int k = 0; k < 8; k++) counts[k] = 0;
+        counts[4] = P;
+    }
+}
+
+struct KernelSet {
+    void (*regen)(SrvDev, int);
+    void (*trace)(SrvDev, int);
+    void (*shade)(SrvDev, int);
+    void (*shadow)(SrvDev);
+    void (*retire)(SrvDev);
+};
+template <int B>
+KernelSet kernel_set() {
+    return KernelSet{k_srv_regen<B>, k_srv_trace<B>, k_srv_shade<B>, k_srv_shadow<B>, k_srv_retire<B>};
+}
+
+int occupancy_grid(const void *fn, int block, int sms) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, 0);
+    return std::max(1, sms * std::max(1, per_sm));
+}
+
+double now_ms(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+size_t pool_bytes(size_t P) {
+    size_t b = 0;
+    // path state: job, pixel, rng, beta, L, prev, nv
+    b += align256(P * 4) * 2 + align256(P * 8) + align256(P * 16) * 3 + align256(P * 4);
+    // queues: ray x2, path x2, hit, shadow ray, shadow path, contrib, retire, free ids
+    b += align256(P * 32) * 2 + align256(P * 4) * 2 + align256(P * 16) + align256(P * 32) + align256(P * 4) +
+         align256(P * 16) + align256(P * 4) + align256(P * 4);
+    b += 256 * 2;   // counts, stats
+    return b;
+}
+
+template <typename T>
+T *carve(char *&p, size_t n) {
+    T *r = (T *)p;
+    p += align256(n * sizeof(T));
+    return r;
+}
+
+}  // namespace
+}  // namespace lj
+
+using namespace lj;
+
+struct HostJob {
+    int64_t id = 0;
+    lj_scene *scene = nullptr;
+    int scene_slot = -1;
+    int w = 0, h = 0, spp = 0, sample_offset = 0, max_depth = 0, rr_depth = 0;
+    uint64_t seed = 0;
+    int64_t total = 0;
+    int64_t bytes = 0;
+    int slot = -1;
+    int state = LJ_JOB_QUEUED;
+    int error = 0;
+    bool cancel_req = false, cancel_sent = false, finishing = false;
+    // counter read-backs enqueued before these sequence numbers predate the
+    // job's admission (stale counters of the slot) or its cancel flag
+    int64_t admit_seq = 0, cancel_seq = 0;
+    unsigned long long *d_accum = nullptr;
+    float *d_img = nullptr;
+    float *h_img = nullptr;
+    cudaEvent_t done_ev = nullptr;
+    int64_t samples_done = 0, dropped = 0;
+    double t_submit = 0, t_admit = 0, t_finish = 0;
+};
+
+struct lj_server {
+    lj_ctx *ctx = nullptr;
+    int device = 0;
+    lj_server_options opt{};
+    int block = 128;
+    int64_t P = 0;
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t mempool = nullptr;
+    std::chrono::steady_clock::time_point t0;
+
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    bool stopping = false;
+    std::chrono::steady_clock::time_point stop_time;
+    bool dead = false;          // the worker hit a CUDA error
+    std::string last_error;
+
+    std::vector<lj_scene *> scenes;            // scene slot -> scene
+    std::unordered_map<int64_t, std::unique_ptr<HostJob>> jobs;
+    std::deque<HostJob *> pending;
+    std::vector<HostJob *> live;               // job slot -> job
+    std::vector<int> free_slots;
+    std::vector<int> order;                    // job slots in scheduling order (worker only)
+    int64_t next_id = 1;
+    int64_t bytes_pool = 0, bytes_scenes = 0, bytes_jobs = 0;
+
+    // device
+    void *d_pool = nullptr;
+    DevScene *d_scenes = nullptr;
+    SrvJob *d_jobs = nullptr;
+    SrvCtr *d_ctr = nullptr;
+    int *d_cancel = nullptr;
+    int *d_order = nullptr;
+    int *d_plan_off = nullptr;
+    long long *d_plan_start = nullptr;
+    SrvDev dev{};
+    KernelSet ks{};
+    int grid[5] = {1, 1, 1, 1, 1};
+    cudaGraphExec_t graph = nullptr;
+
+    // pinned host staging
+    SrvJob *h_jobs = nullptr;                  // one staging entry per job slot
+    int *h_order[2] = {nullptr, nullptr};
+    cudaEvent_t order_ev[2] = {nullptr, nullptr};
+    int order_buf = 0;
+    int *h_one = nullptr;                      // constant 1 (cancel flag source)
+    SrvCtr *h_ctr[kPollsInFlight] = {nullptr, nullptr};
+    cudaEvent_t poll_ev[kPollsInFlight] = {nullptr, nullptr};
+    bool poll_pending[kPollsInFlight] = {false, false};
+    int64_t poll_seq[kPollsInFlight] = {0, 0};
+    int64_t next_poll_seq = 1;
+    int poll_next = 0;
+
+    unsigned long long *h_qstats[kPollsInFlight] = {nullptr, nullptr};   // device ray counters
+
+    // LJ_SERVER_PROFILE: an event pair around every kernel of a batch
+    bool profile = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    size_t n_marks = 0;
+
+    // stats
+    int64_t n_submitted = 0, n_done = 0, n_failed = 0, n_cancelled = 0;
+    int64_t waves = 0, graph_launches = 0, samples_done = 0, kernel_launches = 0;
+    int64_t rays_closest = 0, rays_shadow = 0, path_segments = 0;
+    double class_ms[LJ_KERNEL_CLASSES] = {0, 0, 0, 0, 0};
+    int64_t class_launches[LJ_KERNEL_CLASSES] = {0, 0, 0, 0, 0};
+    double busy_ms = 0;
+};
+
+namespace {
+
+int srv_error(lj_server *s, int code, const std::string &msg) {
+    s->last_error = msg;
+    return code;
+}
+
+#define SRV_CUDA(expr)                                                                      \
+    do {                                                                                    \
+        cudaError_t _e = (expr);                                                            \
+        if (_e != cudaSuccess) return std::string(#expr) + ": " + cudaGetErrorString(_e);   \
+    } while (0)
+
+void mark(lj_server *s, int cls, bool begin) {
+    if (!s->profile) return;
+    if (begin) {
+        if (s->n_marks == s->marks.size()) {
+            cudaEvent_t a, b;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            s->marks.push_back({cls, {a, b}});
+        }
+        s->marks[s->n_marks].first = cls;
+        cudaEventRecord(s->marks[s->n_marks].second.first, s->stream);
+    } else {
+        cudaEventRecord(s->marks[s->n_marks].second.second, s->stream);
+        s->class_launches[cls]++;
+        s->n_marks++;
+    }
+}
+
+// Launch one wave (cur -> cur ^ 1) on the server stream.
+void launch_wave(lj_server *s, int cur) {
+    const int B = s->block;
+    mark(s, LJ_KERNEL_OTHER, true);
+    k_srv_plan<<<1, 32, 0, s->stream>>>(s->dev, cur);
+    mark(s, LJ_KERNEL_OTHER, false);
+    mark(s, LJ_KERNEL_CAMERA, true);
+    s->ks.regen<<<s->grid[0], B, 0, s->stream>>>(s->dev, cur);
+    mark(s, LJ_KERNEL_CAMERA, false);
+    mark(s, LJ_KERNEL_TRACE, true);
+    s->ks.trace<<<s->grid[1], B, 0, s->stream>>>(s->dev, cur);
+    mark(s, LJ_KERNEL_TRACE, false);
+    mark(s, LJ_KERNEL_SHADE, true);
+    s->ks.shade<<<s->grid[2], B, 0, s->stream>>>(s->dev, cur);
+    mark(s, LJ_KERNEL_SHADE, false);
+    mark(s, LJ_KERNEL_SHADOW, true);
+    s->ks.shadow<<<s->grid[3], B, 0, s->stream>>>(s->dev);
+    mark(s, LJ_KERNEL_SHADOW, false);
+    mark(s, LJ_KERNEL_OTHER, true);
+    s->ks.retire<<<s->grid[4], B, 0, s->stream>>>(s->dev);
+    mark(s, LJ_KERNEL_OTHER, false);
+}
+
+// LJ_SERVER_PROFILE: wait for the batch and add up its kernel times.
+cudaError_t collect_marks(lj_server *s) {
+    if (!s->profile || s->n_marks == 0) return cudaSuccess;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    for (size_t k = 0; k < s->n_marks && e == cudaSuccess; k++) {
+        float ms = 0;
+        e = cudaEventElapsedTime(&ms, s->marks[k].second.first, s->marks[k].second.second);
+        s->class_ms[s->marks[k].first] += ms;
+    }
+    s->n_marks = 0;
+    return e;
+}
+
+std::string build_device(lj_server *s) {
+    SRV_CUDA(cudaSetDevice(s->device));
+    SRV_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = s->device;
+    SRV_CUDA(cudaMemPoolCreate(&s->mempool, &props));
+    uint64_t keep = UINT64_MAX;
+    SRV_CUDA(cudaMemPoolSetAttribute(s->mempool, cudaMemPoolAttrReleaseThreshold, &keep));
+
+    const int64_t P = s->P;
+    const int J = s->opt.max_live_jobs;
+    size_t pb = pool_bytes((size_t)P);
+    SRV_CUDA(cudaMalloc(&s->d_pool, pb));
+    s->bytes_pool = (int64_t)pb;
+    SRV_CUDA(cudaMalloc(&s->d_scenes, sizeof(DevScene) * kMaxScenes));
+    SRV_CUDA(cudaMalloc(&s->d_jobs, sizeof(SrvJob) * J));
+    SRV_CUDA(cudaMalloc(&s->d_ctr, sizeof(SrvCtr) * J));
+    SRV_CUDA(cudaMalloc(&s->d_cancel, sizeof(int) * J));
+    SRV_CUDA(cudaMalloc(&s->d_order, sizeof(int) * (J + 1)));
+    SRV_CUDA(cudaMalloc(&s->d_plan_off, sizeof(int) * (J + 1)));
+    SRV_CUDA(cudaMalloc(&s->d_plan_start, sizeof(long long) * (J + 1)));
+    SRV_CUDA(cudaMemsetAsync(s->d_ctr, 0, sizeof(SrvCtr) * J, s->stream));
+    SRV_CUDA(cudaMemsetAsync(s->d_cancel, 0, sizeof(int) * J, s->stream));
+    SRV_CUDA(cudaMemsetAsync(s->d_order, 0, sizeof(int) * (J + 1), s->stream));
+    s->bytes_pool += (int64_t)(sizeof(DevScene) * kMaxScenes + (sizeof(SrvJob) + sizeof(SrvCtr) + 16) * J);
+
+    SRV_CUDA(cudaMallocHost(&s->h_jobs, sizeof(SrvJob) * J));
+    for (int b = 0; b < 2; b++) {
+        SRV_CUDA(cudaMallocHost(&s->h_order[b], sizeof(int) * (J + 1)));
+        SRV_CUDA(cudaEventCreateWithFlags(&s->order_ev[b], cudaEventDisableTiming));
+    }
+    SRV_CUDA(cudaMallocHost(&s->h_one, sizeof(int)));
+    *s->h_one = 1;
+    for (int b = 0; b < kPollsInFlight; b++) {
+        SRV_CUDA(cudaMallocHost(&s->h_ctr[b], sizeof(SrvCtr) * J));
+        SRV_CUDA(cudaMallocHost(&s->h_qstats[b], sizeof(unsigned long long) * 4));
+        memset(s->h_qstats[b], 0, sizeof(unsigned long long) * 4);
+        SRV_CUDA(cudaEventCreateWithFlags(&s->poll_ev[b], cudaEventDisableTiming));
+    }
+
+    char *cur = (char *)s->d_pool;
+    SrvDev &d = s->dev;
+    d.scenes = s->d_scenes;
+    d.jobs = s->d_jobs;
+    d.ctr = s->d_ctr;
+    d.cancel = s->d_cancel;
+    d.order = s->d_order;
+    d.plan_off = s->d_plan_off;
+    d.plan_start = s->d_plan_start;
+    d.ps.job = carve<int>(cur, P);
+    d.ps.pixel = carve<int>(cur, P);
+    d.ps.rng = carve<uint64_t>(cur, P);
+    d.ps.beta = carve<float4>(cur, P);
+    d.ps.L = carve<float4>(cur, P);
+    d.ps.prev = carve<float4>(cur, P);
+    d.ps.nv = carve<int>(cur, P);
+    d.q.ray[0] = carve<float4>(cur, 2 * P);
+    d.q.ray[1] = carve<float4>(cur, 2 * P);
+    d.q.path[0] = carve<int>(cur, P);
+    d.q.path[1] = carve<int>(cur, P);
+    d.q.hit = carve<float4>(cur, P);
+    d.q.sray = carve<float4>(cur, 2 * P);
+    d.q.spath = carve<int>(cur, P);
+    d.q.scontrib = carve<float4>(cur, P);
+    d.q.retire = carve<int>(cur, P);
+    d.free_ids = carve<int>(cur, P);
+    d.q.counts = carve<int>(cur, 64);
+    d.q.stats = carve<unsigned long long>(cur, 32);
+    d.status = s->ctx->d_status;
+    SRV_CUDA(cudaMemsetAsync(d.q.stats, 0, 8 * sizeof(unsigned long long), s->stream));
+    k_srv_init_free<<<(int)((P + 255) / 256), 256, 0, s->stream>>>(d.free_ids, d.q.counts, (int)P);
+    SRV_CUDA(cudaGetLastError());
+
+    switch (s->block) {
+    case 64: s->ks = kernel_set<64>(); break;
+    case 256: s->ks = kernel_set<256>(); break;
+    default: s->ks = kernel_set<128>(); break;
+    }
+    int sms = 0;
+    SRV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+    s->grid[0] = occupancy_grid((const void *)s->ks.regen, s->block, sms);
+    s->grid[1] = occupancy_grid((const void *)s->ks.trace, s->block, sms);
+    s->grid[2] = occupancy_grid((const void *)s->ks.shade, s->block, sms);
+    s->grid[3] = occupancy_grid((const void *)s->ks.shadow, s->block, sms);
+    s->grid[4] = occupancy_grid((const void *)s->ks.retire, s->block, sms);
+
+    s->profile = (s->opt.flags & LJ_SERVER_PROFILE) != 0;
+    if (s->opt.use_graphs && !s->profile) {
+        cudaGraph_t g = nullptr;
+        SRV_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        launch_wave(s, 0);
+        launch_wave(s, 1);
+        SRV_CUDA(cudaStreamEndCapture(s->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
+        cudaGraphDestroy(g);
+        SRV_CUDA(e);
+    }
+    SRV_CUDA(cudaStreamSynchronize(s->stream));
+    return "";
+}
+
+// ---- worker-thread helpers (called with s->mu held unless noted) ----------
+
+std::string push_order(lj_server *s) {
+    int b = s->order_buf;
+    s->order_buf ^= 1;
+    SRV_CUDA(cudaEventSynchronize(s->order_ev[b]));   // the copy from two updates ago
+    int *h = s->h_order[b];
+    h[0] = (int)s->order.size();
+    for (size_t k = 0; k < s->order.size(); k++) h[1 + k] = s->order[k];
+    SRV_CUDA(cudaMemcpyAsync(s->d_order, h, sizeof(int) * (s->order.size() + 1), cudaMemcpyHostToDevice,
+                             s->stream));
+    SRV_CUDA(cudaEventRecord(s->order_ev[b], s->stream));
+    return "";
+}
+
+void sort_order(lj_server *s) {
+    if (s->opt.policy != LJ_SCHED_SRPT) return;   // FIFO: admission order
+    std::stable_sort(s->order.begin(), s->order.end(), [&](int a, int b) {
+        const HostJob *ja = s->live[a], *jb = s->live[b];
+        return ja->total - ja->samples_done < jb->total - jb->samples_done;
+    });
+}
+
+std::string admit(lj_server *s, HostJob *j) {
+    int slot = s->free_slots.back();
+    s->free_slots.pop_back();
+    j->slot = slot;
+    s->live[slot] = j;
+    const size_t npix = (size_t)j->w * j->h;
+    SRV_CUDA(cudaMallocFromPoolAsync((void **)&j->d_accum, npix * 3 * 8, s->mempool, s->stream));
+    SRV_CUDA(cudaMallocFromPoolAsync((void **)&j->d_img, npix * 3 * 4, s->mempool, s->stream));
+    SRV_CUDA(cudaMemsetAsync(j->d_accum, 0, npix * 3 * 8, s->stream));
+    SrvJob &h = s->h_jobs[slot];
+    memset(&h, 0, sizeof(h));
+    make_cam_rec(j->scene->camera, j->w, j->h, h.cam);
+    h.seed = j->seed;
+    h.total = j->total;
+    h.accum = j->d_accum;
+    h.scene = j->scene_slot;
+    h.npix = (int)npix;
+    h.spp = j->spp;
+    h.sample_offset = j->sample_offset;
+    h.max_depth = j->max_depth;
+    h.rr_depth = j->rr_depth;
+    h.spread0 = 0.25f / (float)std::max(j->w, j->h);
+    h.clamp = (float)std::ldexp(1.0, 30) / (float)j->spp;
+    SRV_CUDA(cudaMemcpyAsync(s->d_jobs + slot, &h, sizeof(SrvJob), cudaMemcpyHostToDevice, s->stream));
+    SRV_CUDA(cudaMemsetAsync(s->d_ctr + slot, 0, sizeof(SrvCtr), s->stream));
+    SRV_CUDA(cudaMemsetAsync(s->d_cancel + slot, 0, sizeof(int), s->stream));
+    j->state = LJ_JOB_RUNNING;
+    j->t_admit = now_ms(s->t0);
+    j->admit_seq = s->next_poll_seq;
+    s->bytes_jobs += j->bytes;
+    s->order.push_back(slot);
+    return "";
+}
+
+// Start finishing a job whose paths have all retired.
+std::string finish(lj_server *s, HostJob *j) {
+    const long long n = (long long)j->w * j->h * 3;
+    const bool cancelled = j->cancel_req;
+    if (!cancelled) {
+        k_srv_finalize<<<(int)((n + 255) / 256), 256, 0, s->stream>>>(j->d_accum, j->d_img, n,
+                                                                       std::ldexp(1.0, -32) / j->spp);
+        SRV_CUDA(cudaGetLastError());
+        s->kernel_launches++;
+        SRV_CUDA(cudaMallocHost(&j->h_img, sizeof(float) * n));
+        SRV_CUDA(cudaMemcpyAsync(j->h_img, j->d_img, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream));
+    }
+    SRV_CUDA(cudaFreeAsync(j->d_accum, s->stream));
+    SRV_CUDA(cudaFreeAsync(j->d_img, s->stream));
+    j->d_accum = nullptr;
+    j->d_img = nullptr;
+    SRV_CUDA(cudaEventCreateWithFlags(&j->done_ev, cudaEventDisableTiming));
+    SRV_CUDA(cudaEventRecord(j->done_ev, s->stream));
+    j->finishing = true;
+    s->order.erase(std::remove(s->order.begin(), s->order.end(), j->slot), s->order.end());
+    return "";
+}
+
+bool fits(lj_server *s, const HostJob *j) {
+    return s->bytes_pool + s->bytes_scenes + s->bytes_jobs + j->bytes <= s->opt.hbm_budget_bytes;
+}
+
+void fail_all(lj_server *s, const std::string &msg) {
+    s->dead = true;
+    s->last_error = msg;
+    for (auto &kv : s->jobs) {
+        HostJob *j = kv.second.get();
+        if (j->state == LJ_JOB_QUEUED || j->state == LJ_JOB_RUNNING) {
+            j->state = LJ_JOB_FAILED;
+            j->error = LJ_ERR_CUDA;
+            s->n_failed++;
+        }
+    }
+    s->pending.clear();
+    s->cv_done.notify_all();
+}
+
+// Process one counter read-back (sequence number seq): update progress,
+// start finishing jobs whose paths have all retired.
+std::string on_snapshot(lj_server *s, const SrvCtr *snap, int64_t seq) {
+    bool changed = false;
+    for (int slot = 0; slot < (int)s->live.size(); slot++) {
+        HostJob *j = s->live[slot];
+        if (!j || j->finishing || seq < j->admit_seq) continue;
+        const SrvCtr &c = snap[slot];
+        j->samples_done = (int64_t)c.done;
+        j->dropped = (int64_t)c.dropped;
+        const bool complete = j->cancel_sent ? (seq >= j->cancel_seq && c.done == c.issued)
+                                             : (int64_t)c.done == j->total;
+        if (complete) {
+            std::string e = finish(s, j);
+            if (!e.empty()) return e;
+            changed = true;
+        } else if ((int64_t)c.issued >= j->total) {
+            // nothing left to issue: keep it out of the plan's order list
+            auto it = std::find(s->order.begin(), s->order.end(), slot);
+            if (it != s->order.end()) {
+                s->order.erase(it);
+                changed = true;
+            }
+        }
+    }
+    if (s->opt.policy == LJ_SCHED_SRPT && s->order.size() > 1) {
+        sort_order(s);
+        changed = true;
+    }
+    if (changed) return push_order(s);
+    return "";
+}
+
+void reap_finished(lj_server *s) {
+    for (int slot = 0; slot < (int)s->live.size(); slot++) {
+        HostJob *j = s->live[slot];
+        if (!j || !j->finishing) continue;
+        if (cudaEventQuery(j->done_ev) != cudaSuccess) continue;
+        cudaEventDestroy(j->done_ev);
+        j->done_ev = nullptr;
+        j->finishing = false;
+        j->t_finish = now_ms(s->t0);
+        if (j->cancel_req) {
+            j->state = LJ_JOB_CANCELLED;
+            s->n_cancelled++;
+        } else {
+            j->state = LJ_JOB_DONE;
+            j->samples_done = j->total;
+            s->n_done++;
+        }
+        s->samples_done += j->samples_done;
+        s->bytes_jobs -= j->bytes;
+        s->live[slot] = nullptr;
+        s->free_slots.push_back(slot);
+        j->slot = -1;
+    }
+    s->cv_done.notify_all();
+}
+
+bool any_live(lj_server *s) {
+    for (HostJob *j : s->live)
+        if (j) return true;
+    return false;
+}
+
+void worker_main(lj_server *s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto t_busy = std::chrono::steady_clock::now();
+    bool busy = false;
+    while (true) {
+        std::string err;
+        // admissions (FIFO over the pending queue, under the budget)
+        bool order_changed = false;
+        while (!s->pending.empty() && !s->free_slots.empty()) {
+            HostJob *j = s->pending.front();
+            if (j->cancel_req) {
+                s->pending.pop_front();
+                j->state = LJ_JOB_CANCELLED;
+                j->t_finish = now_ms(s->t0);
+                s->n_cancelled++;
+                s->cv_done.notify_all();
+                continue;
+            }
+            if (!fits(s, j)) break;
+            s->pending.pop_front();
+            err = admit(s, j);
+            if (!err.empty()) break;
+            order_changed = true;
+        }
+        // cancellations of running jobs
+        for (HostJob *j : s->live) {
+            if (!err.empty()) break;
+            if (j && j->cancel_req && !j->cancel_sent) {
+                cudaError_t e = cudaMemcpyAsync(s->d_cancel + j->slot, s->h_one, sizeof(int),
+                                                cudaMemcpyHostToDevice, s->stream);
+                if (e != cudaSuccess) err = std::string("cancel: ") + cudaGetErrorString(e);
+                j->cancel_sent = true;
+                j->cancel_seq = s->next_poll_seq;
+            }
+        }
+        if (err.empty() && order_changed) {
+            sort_order(s);
+            err = push_order(s);
+        }
+        if (!err.empty()) {
+            fail_all(s, err);
+            break;
+        }
+        const bool live = any_live(s);
+        if (live && s->stopping &&
+            std::chrono::steady_clock::now() - s->stop_time > std::chrono::seconds(60)) {
+            fail_all(s, "stop: cancelled jobs did not drain within 60 s");
+            break;
+        }
+        if (!live) {
+            if (busy) {
+                s->busy_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_busy).count();
+                busy = false;
+            }
+            if (s->stopping) break;
+            s->cv_work.wait_for(lk, std::chrono::milliseconds(50));
+            continue;
+        }
+        if (!busy) {
+            busy = true;
+            t_busy = std::chrono::steady_clock::now();
+        }
+        // launch a batch of waves, then a counter read-back
+        const int pairs = std::max(1, s->opt.waves_per_poll / 2);
+        lk.unlock();
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < pairs && e == cudaSuccess; k++) {
+            if (s->graph) {
+                e = cudaGraphLaunch(s->graph, s->stream);
+            } else {
+                launch_wave(s, 0);
+                launch_wave(s, 1);
+                e = cudaGetLastError();
+            }
+        }
+        if (e == cudaSuccess) e = collect_marks(s);
+        lk.lock();
+        s->waves += 2 * pairs;
+        s->kernel_launches += 12 * pairs;
+        if (s->graph) s->graph_launches += pairs;
+        const int b = s->poll_next;
+        s->poll_next = (b + 1) % kPollsInFlight;
+        if (e == cudaSuccess && s->poll_pending[b]) {
+            // the read-back issued kPollsInFlight batches ago
+            lk.unlock();
+            e = cudaEventSynchronize(s->poll_ev[b]);
+            lk.lock();
+            if (e == cudaSuccess) {
+                s->poll_pending[b] = false;
+                s->rays_closest = (int64_t)s->h_qstats[b][0];
+                s->rays_shadow = (int64_t)s->h_qstats[b][1];
+                s->path_segments = (int64_t)s->h_qstats[b][2];
+                err = on_snapshot(s, s->h_ctr[b], s->poll_seq[b]);
+            }
+        }
+        if (e == cudaSuccess && err.empty()) {
+            e = cudaMemcpyAsync(s->h_ctr[b], s->d_ctr, sizeof(SrvCtr) * s->live.size(), cudaMemcpyDeviceToHost,
+                                s->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(s->h_qstats[b], s->dev.q.stats, sizeof(unsigned long long) * 4,
+                                    cudaMemcpyDeviceToHost, s->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(s->poll_ev[b], s->stream);
+            if (e == cudaSuccess) {
+                s->poll_pending[b] = true;
+                s->poll_seq[b] = s->next_poll_seq++;
+            }
+        }
+        if (e == cudaSuccess && err.empty()) reap_finished(s);
+        if (e != cudaSuccess) err = std::string("server: ") + cudaGetErrorString(e);
+        if (!err.empty()) {
+            fail_all(s, err);
+            break;
+        }
+    }
+    // drain: nothing of ours may still run when buffers are freed
+    lk.unlock();
+    cudaStreamSynchronize(s->stream);
+    unsigned long long q[4] = {0, 0, 0, 0};
+    bool got = !s->dead && cudaMemcpy(q, s->dev.q.stats, sizeof(q), cudaMemcpyDeviceToHost) == cudaSuccess;
+    lk.lock();
+    if (got) {
+        s->rays_closest = (int64_t)q[0];
+        s->rays_shadow = (int64_t)q[1];
+        s->path_segments = (int64_t)q[2];
+    }
+    reap_finished(s);
+    s->cv_done.notify_all();
+}
+
+HostJob *find_job(lj_server *s, int64_t id) {
+    auto it = s->jobs.find(id);
+    return it == s->jobs.end() ? nullptr : it->second.get();
+}
+
+void fill_status(const HostJob *j, lj_job_status *st) {
+    if (!st) return;
+    st->state = j->state;
+    st->error = j->error;
+    st->width = j->w;
+    st->height = j->h;
+    st->samples_total = j->total;
+    st->samples_done = j->samples_done;
+    st->samples_dropped = j->dropped;
+    st->submit_ms = j->t_submit;
+    st->admit_ms = j->t_admit;
+    st->finish_ms = j->t_finish;
+}
+
+void release_device(lj_server *s) {
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (auto &kv : s->jobs) {
+        HostJob *j = kv.second.get();
+        if (j->d_accum) cudaFree(j->d_accum);
+        if (j->d_img) cudaFree(j->d_img);
+        if (j->h_img) cudaFreeHost(j->h_img);
+        if (j->done_ev) cudaEventDestroy(j->done_ev);
+        j->d_accum = nullptr;
+        j->d_img = nullptr;
+        j->h_img = nullptr;
+    }
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    void *dev_ptrs[] = {s->d_pool, s->d_scenes, s->d_jobs, s->d_ctr, s->d_cancel, s->d_order, s->d_plan_off,
+                        s->d_plan_start};
+    for (void *p : dev_ptrs)
+        if (p) cudaFree(p);
+    if (s->h_jobs) cudaFreeHost(s->h_jobs);
+    for (int b = 0; b < 2; b++) {
+        if (s->h_order[b]) cudaFreeHost(s->h_order[b]);
+        if (s->order_ev[b]) cudaEventDestroy(s->order_ev[b]);
+    }
+    if (s->h_one) cudaFreeHost(s->h_one);
+    for (auto &m : s->marks) {
+        cudaEventDestroy(m.second.first);
+        cudaEventDestroy(m.second.second);
+    }
+    s->marks.clear();
+    for (int b = 0; b < kPollsInFlight; b++) {
+        if (s->h_qstats[b]) cudaFreeHost(s->h_qstats[b]);
+        if (s->h_ctr[b]) cudaFreeHost(s->h_ctr[b]);
+        if (s->poll_ev[b]) cudaEventDestroy(s->poll_ev[b]);
+    }
+    if (s->mempool) cudaMemPoolDestroy(s->mempool);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    for (lj_scene *sc : s->scenes) sc->server_refs--;
+    s->scenes.clear();
+}
+
+}  // namespace
+
+extern "C" {
+
+int lj_gpu_server_start(lj_ctx *ctx, const lj_server_options *options, lj_server **out) {
+    if (!ctx || !out) return LJ_ERR_INVALID_ARG;
+    *out = nullptr;
+    lj_server_options o{};
+    if (options) o = *options;
+    if (o.hbm_budget_bytes <= 0) o.hbm_budget_bytes = (int64_t)120 << 30;
+    if (o.path_pool <= 0) o.path_pool = (int64_t)1 << 22;
+    if (o.block_size == 0) o.block_size = 128;
+    if (o.max_live_jobs <= 0) o.max_live_jobs = 256;
+    if (o.max_queued_jobs <= 0) o.max_queued_jobs = 65536;
+    if (o.waves_per_poll <= 0) o.waves_per_poll = 8;
+    if (o.block_size != 64 && o.block_size != 128 && o.block_size != 256)
+        return set_error(ctx, LJ_ERR_INVALID_ARG, "server: block_size must be 64, 128 or 256");
+    if (o.path_pool > ((int64_t)1 << 28) || o.max_live_jobs > 4096)
+        return set_error(ctx, LJ_ERR_INVALID_ARG, "server: path_pool <= 2^28 and max_live_jobs <= 4096");
+    if (o.policy != LJ_SCHED_FIFO && o.policy != LJ_SCHED_SRPT)
+        return set_error(ctx, LJ_ERR_INVALID_ARG, "server: unknown policy");
+    lj_server *s = new (std::nothrow) lj_server();
+    if (!s) return set_error(ctx, LJ_ERR_OUT_OF_MEMORY, "server: host allocation failed");
+    s->ctx = ctx;
+    s->device = ctx->device;
+    s->opt = o;
+    s->block = o.block_size;
+    s->P = o.path_pool;
+    s->t0 = std::chrono::steady_clock::now();
+    s->live.assign(o.max_live_jobs, nullptr);
+    for (int k = o.max_live_jobs - 1; k >= 0; k--) s->free_slots.push_back(k);
+    if ((int64_t)pool_bytes((size_t)s->P) > o.hbm_budget_bytes) {
+        delete s;
+        return set_error(ctx, LJ_ERR_OUT_OF_MEMORY, "server: the path pool alone exceeds the HBM budget");
+    }
+    std::string e = build_device(s);
+    if (!e.empty()) {
+        cudaGetLastError();
+        release_device(s);
+        delete s;
+        return set_error(ctx, e.find("memory") != std::string::npos ? LJ_ERR_OUT_OF_MEMORY : LJ_ERR_CUDA,
+                         "server: " + e);
+    }
+    s->worker = std::thread(worker_main, s);
+    ctx->servers.push_back(s);
+    *out = s;
+    return LJ_OK;
+}
+
+int lj_gpu_server_submit(lj_server *s, lj_scene *scene, const lj_job_desc *job, int64_t *job_id) {
+    if (!s || !scene || !job || !job_id) return LJ_ERR_INVALID_ARG;
+    if (scene->ctx != s->ctx) return srv_error(s, LJ_ERR_INVALID_ARG, "submit: scene of another context");
+    if (scene->options.integrator != LJ_INTEGRATOR_PATH)
+        return srv_error(s, LJ_ERR_UNSUPPORTED, "submit: the server renders path-integrator scenes only");
+    if (job->spp < 0 || job->width < 0 || job->height < 0 || (job->width > 0) != (job->height > 0))
+        return srv_error(s, LJ_ERR_INVALID_ARG, "submit: negative spp / size, or only one of width and height");
+    auto j = std::make_unique<HostJob>();
+    j->scene = scene;
+    j->w = job->width > 0 ? job->width : scene->width;
+    j->h = job->height > 0 ? job->height : scene->height;
+    j->spp = job->spp > 0 ? job->spp : scene->options.samples_per_pixel;
+    j->sample_offset = job->sample_offset;
+    j->seed = job->seed;
+    j->max_depth = job->override_depth ? job->max_depth : scene->options.max_depth;
+    j->rr_depth = job->override_depth ? job->rr_depth : scene->options.rr_depth;
+    if (j->spp <= 0 || j->spp > (1 << 20) || j->w <= 0 || j->h <= 0 || (int64_t)j->w * j->h > (1 << 26) ||
+        j->max_depth < -1 || job->sample_offset < 0)
+        return srv_error(s, LJ_ERR_INVALID_ARG, "submit: bad resolution, spp, sample offset or depth");
+    j->total = (int64_t)j->w * j->h * j->spp;
+    j->bytes = (int64_t)j->w * j->h * (24 + 12);
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->dead) return srv_error(s, LJ_ERR_CUDA, "submit: server stopped after an error: " + s->last_error);
+    if (s->stopping) return srv_error(s, LJ_ERR_INVALID_ARG, "submit: server is stopping");
+    if ((int64_t)s->pending.size() >= s->opt.max_queued_jobs)
+        return srv_error(s, LJ_ERR_QUEUE_FULL, "submit: admission queue is full");
+    // register the scene (kept until the server stops)
+    int slot = -1;
+    for (size_t k = 0; k < s->scenes.size(); k++)
+        if (s->scenes[k] == scene) slot = (int)k;
+    int64_t scene_bytes = slot < 0 ? scene->info.device_bytes : 0;
+    if (s->bytes_pool + s->bytes_scenes + scene_bytes + j->bytes > s->opt.hbm_budget_bytes)
+        return srv_error(s, LJ_ERR_OUT_OF_MEMORY, "submit: the job does not fit the HBM budget");
+    if (slot < 0) {
+        if ((int)s->scenes.size() >= kMaxScenes)
+            return srv_error(s, LJ_ERR_SIZE_LIMIT, "submit: too many distinct scenes for one server");
+        slot = (int)s->scenes.size();
+        // the table entry is written before any job that uses it is admitted
+        cudaSetDevice(s->device);
+        cudaError_t e = cudaMemcpy(s->d_scenes + slot, &scene->dev, sizeof(DevScene), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return srv_error(s, LJ_ERR_CUDA, std::string("submit: ") + cudaGetErrorString(e));
+        s->scenes.push_back(scene);
+        scene->server_refs++;
+        s->bytes_scenes += scene_bytes;
+    }
+    j->scene_slot = slot;
+    j->id = s->next_id++;
+    j->t_submit = now_ms(s->t0);
+    HostJob *raw = j.get();
+    s->jobs[raw->id] = std::move(j);
+    s->pending.push_back(raw);
+    s->n_submitted++;
+    *job_id = raw->id;
+    s->cv_work.notify_one();
+    return LJ_OK;
+}
+
+int lj_gpu_server_poll(lj_server *s, int64_t id, lj_job_status *st) {
+    if (!s) return LJ_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    HostJob *j = find_job(s, id);
+    if (!j) return srv_error(s, LJ_ERR_NOT_FOUND, "poll: unknown job id");
+    fill_status(j, st);
+    return LJ_OK;
+}
+
+int lj_gpu_server_wait(lj_server *s, int64_t id, double timeout_s, float *out_rgb, lj_job_status *st) {
+    if (!s) return LJ_ERR_INVALID_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    HostJob *j = find_job(s, id);
+    if (!j) return srv_error(s, LJ_ERR_NOT_FOUND, "wait: unknown job id");
+    auto pred = [&] { return j->state != LJ_JOB_QUEUED && j->state != LJ_JOB_RUNNING; };
+    if (timeout_s < 0) {
+        s->cv_done.wait(lk, pred);
+    } else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) {
+        fill_status(j, st);
+        return srv_error(s, LJ_ERR_TIMEOUT, "wait: timed out");
+    }
+    fill_status(j, st);
+    if (j->state == LJ_JOB_CANCELLED) return LJ_ERR_CANCELLED;
+    if (j->state == LJ_JOB_FAILED) return j->error ? j->error : LJ_ERR_CUDA;
+    if (out_rgb) {
+        memcpy(out_rgb, j->h_img, sizeof(float) * 3 * (size_t)j->w * j->h);
+        cudaFreeHost(j->h_img);
+        s->jobs.erase(id);
+    }
+    return LJ_OK;
+}
+
+int lj_gpu_server_cancel(lj_server *s, int64_t id) {
+    if (!s) return LJ_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    HostJob *j = find_job(s, id);
+    if (!j) return srv_error(s, LJ_ERR_NOT_FOUND, "cancel: unknown job id");
+    if (j->state == LJ_JOB_QUEUED || j->state == LJ_JOB_RUNNING) j->cancel_req = true;
+    s->cv_work.notify_one();
+    return LJ_OK;
+}
+
+int lj_gpu_server_stats(lj_server *s, lj_server_stats *st) {
+    if (!s || !st) return LJ_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!any_live(s) && s->pending.empty() && !s->dead) {
+        // idle: every path has retired, so the ray counters are final
+        unsigned long long q[4];
+        cudaSetDevice(s->device);
+        if (cudaMemcpy(q, s->dev.q.stats, sizeof(q), cudaMemcpyDeviceToHost) == cudaSuccess) {
+            s->rays_closest = (int64_t)q[0];
+            s->rays_shadow = (int64_t)q[1];
+            s->path_segments = (int64_t)q[2];
+        }
+    }
+    st->jobs_submitted = s->n_submitted;
+    st->jobs_done = s->n_done;
+    st->jobs_failed = s->n_failed;
+    st->jobs_cancelled = s->n_cancelled;
+    st->waves = s->waves;
+    st->graph_launches = s->graph_launches;
+    st->samples_done = s->samples_done;
+    st->bytes_resident = s->bytes_pool + s->bytes_scenes + s->bytes_jobs;
+    st->busy_ms = s->busy_ms;
+    st->rays_closest = s->rays_closest;
+    st->rays_shadow = s->rays_shadow;
+    st->path_segments = s->path_segments;
+    st->kernel_launches = s->kernel_launches;
+    for (int c = 0; c < LJ_KERNEL_CLASSES; c++) {
+        st->class_ms[c] = s->class_ms[c];
+        st->class_launches[c] = s->class_launches[c];
+    }
+    return LJ_OK;
+}
+
+const char *lj_gpu_server_last_error(lj_server *s) { return s ? s->last_error.c_str() : ""; }
+
+int lj_gpu_server_stop(lj_server *s) {
+    if (!s) return LJ_ERR_INVALID_ARG;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+        s->stop_time = std::chrono::steady_clock::now();
+        for (HostJob *j : s->pending) {
+            j->state = LJ_JOB_CANCELLED;
+            s->n_cancelled++;
+        }
+        s->pending.clear();
+        for (HostJob *j : s->live)
+            if (j) j->cancel_req = true;
+        s->cv_work.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    int rc = s->dead ? LJ_ERR_CUDA : LJ_OK;
+    auto &v = s->ctx->servers;
+    v.erase(std::remove(v.begin(), v.end(), s), v.end());
+    release_device(s);
+    delete s;
+    return rc;
+}
+
+int lj_gpu_server_autotune(lj_ctx *ctx, lj_scene *const *scenes, const lj_job_desc *jobs,
+                           const int32_t *job_scene, int32_t n_jobs, const char *cache_path,
+                           lj_server_options *options) {
+    if (!ctx || !scenes || !jobs || !job_scene || n_jobs <= 0 || !options) return LJ_ERR_INVALID_ARG;
+    // workload key: device, SM count, total samples and largest scene (log2 buckets)
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, ctx->device) != cudaSuccess)
+        return set_error(ctx, LJ_ERR_CUDA, "autotune: cannot query the device");
+    double total = 0, max_prims = 1;
+    for (int i = 0; i < n_jobs; i++) {
+        const lj_scene *sc = scenes[job_scene[i]];
+        double w = jobs[i].width > 0 ? jobs[i].width : sc->width;
+        double h = jobs[i].height > 0 ? jobs[i].height : sc->height;
+        double spp = jobs[i].spp > 0 ? jobs[i].spp : sc->options.samples_per_pixel;
+        total += w * h * spp;
+        max_prims = std::max(max_prims, (double)sc->info.num_prims);
+    }
+    std::ostringstream key;
+    key << prop.name << "|sm" << prop.multiProcessorCount << "|samples2^" << (int)std::lround(std::log2(total + 1))
+        << "|prims2^" << (int)std::lround(std::log2(max_prims));
+    std::map<std::string, std::string> cache;
+    if (cache_path) {
+        std::ifstream f(cache_path);
+        std::string line;
+        while (std::getline(f, line)) {
+            size_t a = line.find('"'), b = a == std::string::npos ? a : line.find('"', a + 1);
+            size_t c = b == std::string::npos ? b : line.find('{', b);
+            size_t d = c == std::string::npos ? c : line.find('}', c);
+            if (d == std::string::npos) continue;
+            cache[line.substr(a + 1, b - a - 1)] = line.substr(c, d - c + 1);
+        }
+        auto it = cache.find(key.str());
+        if (it != cache.end()) {
+            const std::string &v = it->second;
+            size_t pp = v.find("\"path_pool\":"), bb = v.find("\"block_size\":");
+            if (pp != std::string::npos && bb != std::string::npos) {
+                options->path_pool = std::strtoll(v.c_str() + pp + 12, nullptr, 10);
+                options->block_size = (int32_t)std::strtol(v.c_str() + bb + 13, nullptr, 10);
+                return LJ_OK;
+            }
+        }
+    }
+    const int64_t pools[] = {(int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22, (int64_t)1 << 23};
+    const int32_t blocks[] = {64, 128, 256};
+    double best = -1;
+    int64_t best_pool = 0;
+    int32_t best_block = 0;
+    for (int64_t pool : pools) {
+        for (int32_t blk : blocks) {
+            lj_server_options o = *options;
+            o.path_pool = pool;
+            o.block_size = blk;
+            lj_server *srv = nullptr;
+            if (lj_gpu_server_start(ctx, &o, &srv) != LJ_OK) continue;   // e.g. pool above the budget
+            auto t0 = std::chrono::steady_clock::now();
+            std::vector<int64_t> ids(n_jobs, 0);
+            bool ok = true;
+            for (int i = 0; i < n_jobs && ok; i++)
+                ok = lj_gpu_server_submit(srv, scenes[job_scene[i]], &jobs[i], &ids[i]) == LJ_OK;
+            for (int i = 0; i < n_jobs && ok; i++) ok = lj_gpu_server_wait(srv, ids[i], 600.0, nullptr, nullptr) == LJ_OK;
+            double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            std::string srv_err = lj_gpu_server_last_error(srv);
+            if (lj_gpu_server_stop(srv) != LJ_OK) ok = false;
+            if (!ok) return set_error(ctx, LJ_ERR_CUDA, "autotune: candidate run failed: " + srv_err);
+            double rate = total / sec * 1e-6;
+            if (rate > best) {
+                best = rate;
+                best_pool = pool;
+                best_block = blk;
+            }
+        }
+    }
+    if (best < 0) return set_error(ctx, LJ_ERR_OUT_OF_MEMORY, "autotune: no candidate fits the HBM budget");
+    options->path_pool = best_pool;
+    options->block_size = best_block;
+    if (cache_path) {
+        std::ostringstream v;
+        v << "{\"path_pool\": " << best_pool << ", \"block_size\": " << best_block << ", \"msamples_s\": " << best << "}";
+        cache[key.str()] = v.str();
+        std::ofstream f(cache_path);
+        f << "{\n";
+        size_t k = 0;
+        for (auto &kv : cache) f << "  \"" << kv.first << "\": " << kv.second << (++k < cache.size() ? "," : "") << "\n";
+        f << "}\n";
+        if (!f) return set_error(ctx, LJ_ERR_INVALID_ARG, "autotune: cannot write the cache file");
+    }
+    return LJ_OK;
+}
+
+}  // extern "C"

@@ -138,6 +138,39 @@ LJ_D Vertex make_vertex(const DevScene &sc, V3 o, V3 d, float t, int prim, float
     return vx;
 }
 
+// ---- camera: sample_primary (src/camera.cpp:23-47) with the pixel filter
+// importance sampled inside the pixel (src/filters/*.inl) ----
+LJ_D void camera_ray(const CamRec &c, float sx, float sy, V3 &o, V3 &d) {
+    float px = sx * c.w, py = sy * c.h;
+    float dx = px - floorf(px), dy = py - floorf(py);
+    float ox, oy;
+    if (c.filter_kind == 0) {
+        ox = (2.0f * dx - 1.0f) * (c.filter_param * 0.5f);
+        oy = (2.0f * dy - 1.0f) * (c.filter_param * 0.5f);
+    } else if (c.filter_kind == 1) {
+        float h = c.filter_param * 0.5f;
+        ox = dx < 0.5f ? h * (sqrtf(2.0f * dx) - 1.0f) : h * (1.0f - sqrtf(1.0f - 2.0f * (dx - 0.5f)));
+        oy = dy < 0.5f ? h * (sqrtf(2.0f * dy) - 1.0f) : h * (1.0f - sqrtf(1.0f - 2.0f * (dy - 0.5f)));
+    } else {
+        float r = c.filter_param * sqrtf(-2.0f * logf(fmaxf(dx, 1e-8f)));
+        float sp, cp;
+        sincosf(kTwoPi * dy, &sp, &cp);
+        ox = r * cp;
+        oy = r * sp;
+    }
+    float rx = (floorf(px) + 0.5f + ox) / c.w, ry = (floorf(py) + 0.5f + oy) / c.h;
+    const float *m = c.sample_to_cam;
+    float t0 = m[0] * rx + m[1] * ry + m[3];
+    float t1 = m[4] * rx + m[5] * ry + m[7];
+    float t2 = m[8] * rx + m[9] * ry + m[11];
+    float t3 = m[12] * rx + m[13] * ry + m[15];
+    V3 pt = normalize(V3{t0 / t3, t1 / t3, t2 / t3});
+    const float *w = c.cam_to_world;
+    d = normalize(V3{w[0] * pt.x + w[1] * pt.y + w[2] * pt.z, w[4] * pt.x + w[5] * pt.y + w[6] * pt.z,
+                     w[8] * pt.x + w[9] * pt.y + w[10] * pt.z});
+    o = V3{c.org[0], c.org[1], c.org[2]};
+}
+
 // ---- textures ----
 LJ_D float modf1(float a) {
     float r = fmodf(a, 1.0f);

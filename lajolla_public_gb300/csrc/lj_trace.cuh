@@ -163,15 +163,19 @@ LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, Trac
             if (f1.w == 0.0f) {
                 float4 f2 = __ldg(pp + 2);
                 float t, u, v;
+                const int prim = __float_as_int(f0.w);
+                // equal distances go to the lower primitive index, so the
+                // result does not depend on the traversal order
                 if (tri_intersect(V3{f0.x, f0.y, f0.z}, V3{f1.x, f1.y, f1.z}, V3{f2.x, f2.y, f2.z}, o,
-                                  d, tnear, tfar, t, u, v)) {
+                                  d, tnear, tfar, t, u, v) &&
+                    (t < tfar || (!kAny && found && prim < hit.prim))) {
                     found = true;
                     if (kAny) return true;
                     tfar = t;
                     hit.t = t;
                     hit.u = u;
                     hit.v = v;
-                    hit.prim = __float_as_int(f0.w);
+                    hit.prim = prim;
                 }
             } else {
                 float t = sphere_hit(V3{f0.x, f0.y, f0.z}, f1.x, o, d, tnear, tfar);

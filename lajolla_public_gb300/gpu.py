@@ -26,9 +26,10 @@ _lib = None
 
 
 class LjError(RuntimeError):
-    def __init__(self, code, msg):
+    def __init__(self, code, msg, status=None):
         super().__init__("lj_gpu error %d: %s" % (code, msg))
         self.code = code
+        self.status = status
 
 
 def lib():
@@ -60,6 +61,18 @@ def lib():
         L.lj_gpu_bsdf_batch.argtypes = [vp, C.POINTER(abi.lj_bsdf_batch), i64, vp]
         L.lj_gpu_light_sample_batch.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp]
         L.lj_gpu_phase_batch.argtypes = [vp, i32, C.c_float, vp, vp, vp, vp, vp, vp, i64, vp]
+        L.lj_gpu_server_start.argtypes = [vp, C.POINTER(abi.lj_server_options), C.POINTER(vp)]
+        L.lj_gpu_server_submit.argtypes = [vp, vp, C.POINTER(abi.lj_job_desc), C.POINTER(i64)]
+        L.lj_gpu_server_poll.argtypes = [vp, i64, C.POINTER(abi.lj_job_status)]
+        L.lj_gpu_server_wait.argtypes = [vp, i64, C.c_double, vp, C.POINTER(abi.lj_job_status)]
+        L.lj_gpu_server_cancel.argtypes = [vp, i64]
+        L.lj_gpu_server_stats.argtypes = [vp, C.POINTER(abi.lj_server_stats)]
+        L.lj_gpu_server_last_error.argtypes = [vp]
+        L.lj_gpu_server_last_error.restype = C.c_char_p
+        L.lj_gpu_server_stop.argtypes = [vp]
+        L.lj_gpu_render_job_device.argtypes = [vp, C.POINTER(abi.lj_job_desc), vp, vp, C.POINTER(abi.lj_stats)]
+        L.lj_gpu_server_autotune.argtypes = [vp, C.POINTER(vp), C.POINTER(abi.lj_job_desc), C.POINTER(i32), i32,
+                                             C.c_char_p, C.POINTER(abi.lj_server_options)]
         _lib = L
     return _lib
 
@@ -77,6 +90,7 @@ class Context:
             raise LjError(rc, "lj_gpu_init failed (no CUDA device of compute capability >= 10.0?)")
         self.device = device
         self._scenes = weakref.WeakSet()
+        self._servers = weakref.WeakSet()
 
     def check(self, rc):
         if rc != abi.LJ_OK:
@@ -85,6 +99,8 @@ class Context:
     def close(self):
         """Destroys the context and every scene still open on it."""
         if self.h:
+            for s in list(self._servers):
+                s.stop()
             for s in list(self._scenes):
                 s.close()
             lib().lj_gpu_shutdown(self.h)
@@ -199,6 +215,14 @@ class GpuScene:
                                                   C.byref(st) if st is not None else None))
         return st
 
+    def render_job_device(self, out, job, stream=None, stats=False):
+        """One job (lj_job_desc) through the single-scene renderer into the
+        device tensor `out` (H*W*3 float32 at the job's resolution)."""
+        st = abi.lj_stats() if stats else None
+        self.ctx.check(lib().lj_gpu_render_job_device(self.h, C.byref(job), _ptr(out), stream,
+                                                      C.byref(st) if st is not None else None))
+        return st
+
     def trace_closest(self, rays, stream=None):
         """rays: (n, 8) float32 CUDA tensor -> (n, 4) hits (t, prim bits, u, v)."""
         import torch
@@ -237,3 +261,104 @@ class GpuScene:
         s, l = C.c_int32(), C.c_int32()
         self.ctx.check(lib().lj_gpu_prim_to_shape(self.h, int(prim), C.byref(s), C.byref(l)))
         return s.value, l.value
+
+
+def job_desc(seed=0, spp=0, sample_offset=0, width=0, height=0, max_depth=None, rr_depth=None):
+    j = abi.lj_job_desc(seed=seed, spp=spp, sample_offset=sample_offset, width=width, height=height)
+    if max_depth is not None:
+        j.override_depth = 1
+        j.max_depth = max_depth
+        j.rr_depth = rr_depth if rr_depth is not None else 5
+    return j
+
+
+def server_options(hbm_budget_bytes=0, path_pool=0, block_size=0, max_live_jobs=0, max_queued_jobs=0,
+                   waves_per_poll=0, policy=abi.LJ_SCHED_FIFO, use_graphs=True, profile=False):
+    return abi.lj_server_options(hbm_budget_bytes=hbm_budget_bytes, path_pool=path_pool, block_size=block_size,
+                                 max_live_jobs=max_live_jobs, max_queued_jobs=max_queued_jobs,
+                                 waves_per_poll=waves_per_poll, policy=policy, use_graphs=1 if use_graphs else 0,
+                                 flags=abi.LJ_SERVER_PROFILE if profile else 0)
+
+
+class Server:
+    """Continuous-batching render server (lj_gpu_server_*): jobs over
+    resident scenes share one pool of wavefront queues."""
+
+    def __init__(self, ctx, options=None):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        opt = options if options is not None else server_options()
+        ctx.check(lib().lj_gpu_server_start(ctx.h, C.byref(opt), C.byref(self.h)))
+        self._sizes = {}
+        ctx._servers.add(self)
+
+    def check(self, rc):
+        if rc != abi.LJ_OK:
+            raise LjError(rc, lib().lj_gpu_server_last_error(self.h).decode())
+
+    def submit(self, gscene, job=None, **kw):
+        """Queues a render of GpuScene `gscene`; returns the job id."""
+        j = job if job is not None else job_desc(**kw)
+        jid = C.c_int64()
+        self.check(lib().lj_gpu_server_submit(self.h, gscene.h, C.byref(j), C.byref(jid)))
+        w = j.width or gscene.scene.width
+        h = j.height or gscene.scene.height
+        self._sizes[jid.value] = (h, w)
+        return jid.value
+
+    def poll(self, jid):
+        st = abi.lj_job_status()
+        self.check(lib().lj_gpu_server_poll(self.h, jid, C.byref(st)))
+        return st
+
+    def wait(self, jid, timeout=-1.0):
+        """Blocks until the job ends; returns (image HxWx3 float32, status)."""
+        h, w = self._sizes[jid]
+        out = np.zeros((h, w, 3), np.float32)
+        st = abi.lj_job_status()
+        rc = lib().lj_gpu_server_wait(self.h, jid, float(timeout), out.ctypes.data_as(C.c_void_p), C.byref(st))
+        if rc != abi.LJ_OK:
+            raise LjError(rc, lib().lj_gpu_server_last_error(self.h).decode(), status=st)
+        del self._sizes[jid]
+        return out, st
+
+    def cancel(self, jid):
+        self.check(lib().lj_gpu_server_cancel(self.h, jid))
+
+    def stats(self):
+        st = abi.lj_server_stats()
+        self.check(lib().lj_gpu_server_stats(self.h, C.byref(st)))
+        return st
+
+    def stop(self):
+        # a closed context has already stopped its servers
+        if self.h and self.ctx.h:
+            rc = lib().lj_gpu_server_stop(self.h)
+            self.h = C.c_void_p()
+            if rc != abi.LJ_OK:
+                raise LjError(rc, "server stopped after a device error")
+        self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.stop()
+
+
+def autotune(ctx, gscenes, jobs, job_scene, cache_path=None, options=None):
+    """Runs the job mix once per (path pool, block size) candidate and
+    returns the options of the fastest (cached in `cache_path`)."""
+    opt = options if options is not None else server_options()
+    arr = (C.c_void_p * len(gscenes))(*[g.h.value for g in gscenes])
+    jd = (abi.lj_job_desc * len(jobs))(*jobs)
+    js = (C.c_int32 * len(jobs))(*job_scene)
+    ctx.check(lib().lj_gpu_server_autotune(ctx.h, arr, jd, js, len(jobs),
+                                           cache_path.encode() if cache_path else None, C.byref(opt)))
+    return opt

@@ -58,6 +58,41 @@ def checker_tex(c0, c1, uscale=1.0, vscale=1.0):
                 value1=[f32(x) for x in c1], uscale=f32(uscale), vscale=f32(vscale))
 
 
+def image_tex(image_id, uscale=1.0, vscale=1.0, uoffset=0.0, voffset=0.0):
+    return dict(kind=abi.LJ_TEX_IMAGE, image_id=int(image_id), uscale=f32(uscale), vscale=f32(vscale),
+                uoffset=f32(uoffset), voffset=f32(voffset))
+
+
+def rgbe_image(rng, h, w, exponent=128):
+    """Random RGB image whose values survive a Radiance RGBE round trip
+    exactly: each channel is k * 2^(exponent - 136) with k in [16, 255]
+    (the decoder multiplies the byte by 2^(e - 136)).  k >= 16 also keeps
+    every scanline from starting with the run-length marker bytes (2, 2)."""
+    k = rng.integers(16, 256, size=(h, w, 3))
+    return (k * 2.0 ** (exponent - 136)).astype(np.float32)
+
+
+def write_hdr(path, img):
+    """Flat (not run-length encoded) Radiance RGBE file of an image made by
+    rgbe_image; row 0 of `img` is the first scanline."""
+    img = np.asarray(img, np.float64)
+    h, w, _ = img.shape
+    m = img.max(axis=2)
+    e = np.zeros((h, w), np.int64)
+    nz = m > 0
+    e[nz] = np.frexp(m[nz])[1] - 8 + 136   # largest channel's byte in [128, 256)
+    # the file stores one exponent per pixel: use the image's own one
+    ex = int(e[nz].max()) if nz.any() else 128
+    k = np.rint(img / 2.0 ** (ex - 136)).astype(np.int64)
+    if not np.array_equal(k * 2.0 ** (ex - 136), img) or k.max() > 255:
+        raise ValueError("write_hdr: image is not exactly representable with one shared exponent")
+    rgbe = np.concatenate([k, np.full((h, w, 1), ex, np.int64)], axis=2).astype(np.uint8)
+    with open(path, "wb") as f:
+        f.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
+        f.write(f"-Y {h} +X {w}\n".encode())
+        f.write(rgbe.tobytes())
+
+
 def lambertian(rgb):
     return dict(type=abi.LJ_MAT_LAMBERTIAN, eta=1.0, tex=[const_tex(rgb)])
 
@@ -259,8 +294,30 @@ class Scene:
         def vec(v):
             return ", ".join(r(float(x)) for x in v)
 
+        for i, im in enumerate(self.images):
+            write_hdr(os.path.join(directory, f"{name}_img{i}.hdr"), im)
+
+        def tex(t, pname):
+            kind = t.get("kind", abi.LJ_TEX_CONST)
+            if kind == abi.LJ_TEX_CONST:
+                return [f'    <rgb name="{pname}" value="{vec(t["value0"])}"/>']
+            uv = [f'      <float name="{k}" value="{r(float(t.get(k, d)))}"/>'
+                  for k, d in (("uscale", 1.0), ("vscale", 1.0), ("uoffset", 0.0), ("voffset", 0.0))]
+            if kind == abi.LJ_TEX_CHECKER:
+                return ([f'    <texture type="checkerboard" name="{pname}">',
+                         f'      <rgb name="color0" value="{vec(t["value0"])}"/>',
+                         f'      <rgb name="color1" value="{vec(t["value1"])}"/>'] + uv + ['    </texture>'])
+            fn = os.path.join(directory, f'{name}_img{t["image_id"]}.hdr')
+            return ([f'    <texture type="bitmap" name="{pname}">',
+                     f'      <string name="filename" value="{fn}"/>'] + uv + ['    </texture>'])
+
+        itype = {abi.LJ_INTEGRATOR_PATH: "path", abi.LJ_INTEGRATOR_DEPTH: "depth",
+                 abi.LJ_INTEGRATOR_SHADING_NORMAL: "shadingNormal",
+                 abi.LJ_INTEGRATOR_MEAN_CURVATURE: "meanCurvature",
+                 abi.LJ_INTEGRATOR_RAY_DIFFERENTIAL: "rayDifferential",
+                 abi.LJ_INTEGRATOR_MIPMAP_LEVEL: "mipmapLevel"}[self.integrator]
         out = ['<?xml version="1.0" encoding="utf-8"?>', '<scene version="0.4.0">',
-               '  <integrator type="path">',
+               f'  <integrator type="{itype}">',
                f'    <integer name="maxDepth" value="{self.max_depth}"/>',
                f'    <integer name="rrDepth" value="{self.rr_depth}"/>', '  </integrator>',
                '  <sensor type="perspective">',
@@ -282,21 +339,22 @@ class Scene:
         for i, m in enumerate(self.materials):
             tx = m["tex"]
             if m["type"] == abi.LJ_MAT_LAMBERTIAN:
-                out.append(f'  <bsdf type="diffuse" id="mat{i}"><rgb name="reflectance" value="{vec(tx[0]["value0"])}"/></bsdf>')
+                out += [f'  <bsdf type="diffuse" id="mat{i}">'] + tex(tx[0], "reflectance") + ['  </bsdf>']
             elif m["type"] == abi.LJ_MAT_ROUGHPLASTIC:
-                out += [f'  <bsdf type="roughplastic" id="mat{i}">',
-                        f'    <rgb name="diffuseReflectance" value="{vec(tx[0]["value0"])}"/>',
-                        f'    <rgb name="specularReflectance" value="{vec(tx[1]["value0"])}"/>',
+                out += ([f'  <bsdf type="roughplastic" id="mat{i}">'] + tex(tx[0], "diffuseReflectance") +
+                        tex(tx[1], "specularReflectance")) + [
                         f'    <float name="roughness" value="{r(tx[2]["value0"][0])}"/>',
                         f'    <float name="intIOR" value="{r(m["eta"])}"/>',
                         '    <float name="extIOR" value="1"/>', '  </bsdf>']
             elif m["type"] == abi.LJ_MAT_ROUGHDIELECTRIC:
-                out += [f'  <bsdf type="roughdielectric" id="mat{i}">',
-                        f'    <rgb name="specularReflectance" value="{vec(tx[0]["value0"])}"/>',
-                        f'    <rgb name="specularTransmittance" value="{vec(tx[1]["value0"])}"/>',
+                out += ([f'  <bsdf type="roughdielectric" id="mat{i}">'] + tex(tx[0], "specularReflectance") +
+                        tex(tx[1], "specularTransmittance")) + [
                         f'    <float name="roughness" value="{r(tx[2]["value0"][0])}"/>',
                         f'    <float name="intIOR" value="{r(m["eta"])}"/>',
                         '    <float name="extIOR" value="1"/>', '  </bsdf>']
+            elif m["type"] == abi.LJ_MAT_DISNEY_CLEARCOAT:
+                out += [f'  <bsdf type="disneyclearcoat" id="mat{i}">',
+                        f'    <float name="clearcoatGloss" value="{r(tx[0]["value0"][0])}"/>', '  </bsdf>']
             else:
                 raise ValueError("write_mitsuba: material type %d not supported" % m["type"])
         for i, s in enumerate(self.shapes):
@@ -308,12 +366,19 @@ class Scene:
                     if s["normals"] is not None:
                         for n in s["normals"]:
                             f.write("vn %r %r %r\n" % tuple(float(x) for x in n))
+                    if s["uvs"] is not None:
+                        # the parser stores (s, 1 - t) (src/parsers/parse_obj.cpp:117-120)
+                        for u, v in s["uvs"]:
+                            f.write("vt %r %r\n" % (float(u), 1.0 - float(v)))
+                    vt = "" if s["uvs"] is None else "%d"
+                    vn = "" if s["normals"] is None else "%d"
                     for t in s["indices"]:
-                        a, b, c = (int(x) + 1 for x in t)
-                        if s["normals"] is not None:
-                            f.write(f"f {a}//{a} {b}//{b} {c}//{c}\n")
+                        ids = [int(x) + 1 for x in t]
+                        if vt or vn:
+                            f.write("f " + " ".join(f"{a}/{vt % a if vt else ''}/{vn % a if vn else ''}"
+                                                    for a in ids) + "\n")
                         else:
-                            f.write(f"f {a} {b} {c}\n")
+                            f.write("f %d %d %d\n" % tuple(ids))
                 out.append('  <shape type="obj">')
                 out.append(f'    <string name="filename" value="{fn}"/>')
                 if s["normals"] is None:
@@ -397,12 +462,60 @@ def cornell_box(seed=0, width=256, height=256, spp=64, max_depth=6, rr_depth=5):
     return sc
 
 
+def textured_scene(seed=0, width=64, height=64, spp=16, max_depth=6, integrator=abi.LJ_INTEGRATOR_PATH,
+                   clearcoat=True):
+    """Cornell box with textures and curved surfaces: an image-textured floor
+    (dyadic UVs, so the OBJ round trip is exact), a checkerboard back wall,
+    a smooth-shaded icosphere mesh (vertex normals: non-zero mean
+    curvature), an image-textured analytic sphere and, with `clearcoat`, a
+    DisneyClearcoat box (a material without a spectrum texture)."""
+    rng = np.random.default_rng(seed)
+    sc = cornell_box(seed=seed, width=width, height=height, spp=spp, max_depth=max_depth)
+    sc.integrator = integrator
+    sc.images.append(rgbe_image(rng, 32, 64))
+    sc.images.append(rgbe_image(rng, 16, 16))
+    floor, back, box2 = sc.shapes[0], sc.shapes[2], sc.shapes[6]
+    floor["uvs"] = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32)
+    sc.materials[floor["material_id"]] = dict(type=abi.LJ_MAT_LAMBERTIAN, eta=1.0,
+                                             tex=[image_tex(0, uscale=2.0, vscale=3.0, uoffset=0.25)])
+    back["uvs"] = np.array([[0, 0], [0.5, 0], [0.5, 0.75], [0, 0.75]], np.float32)
+    sc.materials[back["material_id"]] = dict(type=abi.LJ_MAT_LAMBERTIAN, eta=1.0,
+                                            tex=[checker_tex([0.7, 0.2, 0.2], [0.2, 0.2, 0.7], 4.0, 4.0)])
+    if clearcoat:
+        sc.materials[box2["material_id"]] = dict(type=abi.LJ_MAT_DISNEY_CLEARCOAT, eta=1.5, tex=[const_tex(0.7)])
+    v, f = icosphere(2)
+    r = 0.3
+    sc.add_mesh(v * r + np.array([0.45, 0.9, 0.3]), f, sc.add_material(lambertian([0.6, 0.6, 0.3])),
+                normals=v)
+    sc.add_sphere([-0.35, 1.45, -0.3], 0.22, sc.add_material(dict(type=abi.LJ_MAT_LAMBERTIAN, eta=1.0,
+                                                                  tex=[image_tex(1, 3.0, 2.0)])))
+    return sc
+
+
 def triangle_soup(seed, n_tris, offset_sigma=0.01):
     """n triangles: centroids U[0,1]^3, each vertex = centroid + N(0, sigma)."""
     rng = np.random.default_rng(seed)
     cent = rng.uniform(0, 1, (n_tris, 1, 3))
     v = (cent + rng.normal(0, offset_sigma, (n_tris, 3, 3))).astype(np.float32)
     return v.reshape(-1, 3), np.arange(n_tris * 3, dtype=np.int32).reshape(-1, 3)
+
+
+def tied_soup_scene(seed, n_tris):
+    """Every soup triangle twice (the copies far apart in index order) plus
+    coplanar quads facing both ways: many rays see two or more primitives at
+    exactly the same distance."""
+    sc = Scene(8, 8, 1, 1, np.eye(4), 45.0)
+    rng = np.random.default_rng(seed)
+    v, _ = triangle_soup(seed, n_tris)
+    tri = v.reshape(n_tris, 3, 3)
+    pos = np.concatenate([tri, tri[rng.permutation(n_tris)]]).reshape(-1, 3)
+    m = sc.add_material(lambertian([0.5, 0.5, 0.5]))
+    sc.add_mesh(pos, np.arange(len(pos), dtype=np.int32).reshape(-1, 3), m)
+    for z in (0.25, 0.5, 0.75):
+        q = np.array([[0, 0, z], [1, 0, z], [1, 1, z], [0, 1, z]], np.float32)
+        sc.add_mesh(q, np.array([[0, 1, 2], [0, 2, 3]], np.int32), m)
+        sc.add_mesh(q[::-1].copy(), np.array([[0, 1, 2], [0, 2, 3]], np.int32), m)
+    return sc
 
 
 def soup_scene(seed, n_tris):
@@ -630,3 +743,74 @@ def random_rays(seed, n, tnear=0.0, tfar=np.inf):
     r[:, 4:7] = d
     r[:, 7] = tfar
     return r
+
+
+# ---- serving workload (Poisson-arriving render jobs over resident scenes) ----
+def _subdivide_quad(p0, p1, p2, p3, k):
+    """k x k grid over the quad (p0, p1, p2, p3); same winding as _quad."""
+    p0, p1, p2, p3 = (np.asarray(p, np.float64) for p in (p0, p1, p2, p3))
+    t = np.linspace(0.0, 1.0, k + 1)
+    a = p0[None, :] * (1 - t)[:, None] + p1[None, :] * t[:, None]     # p0 -> p1
+    b = p3[None, :] * (1 - t)[:, None] + p2[None, :] * t[:, None]     # p3 -> p2
+    pos = a[None, :, :] * (1 - t)[:, None, None] + b[None, :, :] * t[:, None, None]   # [row j][col i]
+    idx = []
+    for j in range(k):
+        for i in range(k):
+            v00, v01 = j * (k + 1) + i, j * (k + 1) + i + 1
+            v10, v11 = (j + 1) * (k + 1) + i, (j + 1) * (k + 1) + i + 1
+            idx += [[v00, v01, v11], [v00, v11, v10]]
+    return pos.reshape(-1, 3).astype(np.float32), np.array(idx, np.int32)
+
+
+def tessellated_cornell_box(seed=0, n_tris=10000, width=256, height=256, spp=64, max_depth=6):
+    """The seeded Cornell box with each wall quad split into a k x k grid so
+    that the scene holds about n_tris triangles (same surfaces)."""
+    sc = cornell_box(seed=seed, width=width, height=height, spp=spp, max_depth=max_depth)
+    k = max(1, int(round(math.sqrt(max(1, n_tris - 26) / 10.0))))
+    for w in range(5):
+        pos = sc.shapes[w]["positions"]
+        p, i = _subdivide_quad(pos[0], pos[1], pos[2], pos[3], k)
+        sc.shapes[w]["positions"], sc.shapes[w]["indices"] = p, i
+    return sc
+
+
+def resized_terrain_scene(seed=0, n_tris=500000, width=256, height=256, spp=64, max_depth=8,
+                          env_size=(256, 128)):
+    """terrain_scene with its grid and sphere count scaled to about n_tris
+    triangles (16 subdivision-3 icospheres, the rest terrain)."""
+    n_spheres, subdiv = 16, 3
+    rest = max(2000, n_tris - n_spheres * 20 * 4 ** subdiv)
+    nz = max(8, int(round(math.sqrt(rest / 4.0))))
+    return terrain_scene(seed=seed, width=width, height=height, spp=spp, max_depth=max_depth,
+                         grid=(2 * nz, nz), n_spheres=n_spheres, sphere_subdiv=subdiv, env_size=env_size)
+
+
+def serving_scenes(seed=0, n_scenes=6, min_tris=10000, max_tris=2000000):
+    """Scene pool of the serving workload: Cornell-box and terrain scenes
+    (alternating) with triangle counts log-uniform in [min_tris, max_tris]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_scenes):
+        t = int(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris))))
+        if k % 2 == 0:
+            out.append(tessellated_cornell_box(seed=seed * 100 + k, n_tris=t))
+        else:
+            out.append(resized_terrain_scene(seed=seed * 100 + k, n_tris=t))
+    return out
+
+
+def serving_jobs(seed=0, n_jobs=32, n_scenes=6, rate=200.0, resolutions=(128, 256, 512, 1024),
+                 spps=(4, 16, 64, 256), depth=(6, 64)):
+    """Poisson arrivals (mean `rate` per second), scene uniform over the pool,
+    square resolution, spp and max depth (RR from depth 5) uniform over the
+    given choices.  Returns a list of dicts sorted by arrival time."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n_jobs))
+    t -= t[0]
+    jobs = []
+    for k in range(n_jobs):
+        r = int(rng.choice(resolutions))
+        jobs.append(dict(arrival_s=float(t[k]), scene=int(rng.integers(n_scenes)), width=r, height=r,
+                         spp=int(rng.choice(spps)), max_depth=int(rng.integers(depth[0], depth[1] + 1)),
+                         rr_depth=5, seed=int(rng.integers(1 << 40))))
+    return jobs

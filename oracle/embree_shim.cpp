@@ -199,12 +199,16 @@ void rtcIntersect1(RTCScene s, struct RTCRayHit *rh, struct RTCIntersectArgument
     f3 o{r.org_x, r.org_y, r.org_z}, d{r.dir_x, r.dir_y, r.dir_z};
     RTCRayQueryContext ctx;
     rtcInitRayQueryContext(&ctx);
+    int32_t best = -1;   // global index of the closest primitive so far
     traverse<false>(s, o, d, r.tnear, &r.tfar, [&](int32_t pi) {
         const Prim &p = s->prims[pi];
         RTCGeometryTy *g = s->geoms[p.geom];
         if (g->type == RTC_GEOMETRY_TYPE_TRIANGLE) {
             float t, u, v;
-            if (ljo::tri_intersect(s->tri_pre[pi], o, d, r.tnear, r.tfar, t, u, v)) {
+            // equal distances go to the lower primitive index (the GPU's rule)
+            if (ljo::tri_intersect(s->tri_pre[pi], o, d, r.tnear, r.tfar, t, u, v) &&
+                (t < r.tfar || (best >= 0 && pi < best))) {
+                best = pi;
                 const ljo::TriPre &tp = s->tri_pre[pi];
                 f3 ng = ljo::f3_cross(tp.e1, tp.e2);
                 r.tfar = t;
@@ -224,7 +228,9 @@ void rtcIntersect1(RTCScene s, struct RTCRayHit *rh, struct RTCIntersectArgument
             args.rayhit = (RTCRayHitN *)rh;
             args.N = 1;
             args.geomID = p.geom;
+            float before = r.tfar;
             g->intersect_fn(&args);
+            if (r.tfar != before) best = pi;
         }
         return false;
     });
@@ -240,7 +246,7 @@ void rtcOccluded1(RTCScene s, struct RTCRay *r, struct RTCOccludedArguments *) {
         RTCGeometryTy *g = s->geoms[p.geom];
         if (g->type == RTC_GEOMETRY_TYPE_TRIANGLE) {
             float t, u, v;
-            if (ljo::tri_intersect(s->tri_pre[pi], o, d, r->tnear, r->tfar, t, u, v)) {
+            if (ljo::tri_intersect(s->tri_pre[pi], o, d, r->tnear, r->tfar, t, u, v) && t < r->tfar) {
                 r->tfar = -INFINITY;
                 return true;
             }

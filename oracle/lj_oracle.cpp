@@ -1221,7 +1221,8 @@ static bool cast_closest(const Scene &sc, f3 o, f3 d, float tnear, float tfar, R
             const ShapeS &sh = sc.shapes[pr.shape];
             if (sh.kind == LJ_SHAPE_MESH) {
                 float t, u, v;
-                if (tri_intersect(sc.tri_pre[pi], o, d, tnear, tfar, t, u, v)) {
+                if (tri_intersect(sc.tri_pre[pi], o, d, tnear, tfar, t, u, v) &&
+                    (t < tfar || (found && pi < hit.prim))) {
                     f3 ng = f3_cross(sc.tri_pre[pi].e1, sc.tri_pre[pi].e2);
                     tfar = t;
                     hit.t = t; hit.u = u; hit.v = v;
@@ -1271,7 +1272,7 @@ static bool cast_any(const Scene &sc, f3 o, f3 d, float tnear, float tfar) {
             const ShapeS &sh = sc.shapes[sc.prims[pi].shape];
             if (sh.kind == LJ_SHAPE_MESH) {
                 float t, u, v;
-                if (tri_intersect(sc.tri_pre[pi], o, d, tnear, tfar, t, u, v)) return true;
+                if (tri_intersect(sc.tri_pre[pi], o, d, tnear, tfar, t, u, v) && t < tfar) return true;
             } else if (sphere_hit(sc.spheres[sh.sphere], o, d, tnear, tfar) >= 0) {
                 return true;
             }
@@ -1833,23 +1834,7 @@ static V3 vol_path_tracing(const Scene &sc, int x, int y, Rng &rng) {
             multi_dir = multi_dir * pd;
             multi_nee = multi_nee * pn;
         }
-        if (scatter) {
-            const MediumS &m = sc.media[medium];
-            V3 ss, sa;
-            sigmas(m, p_scatter, ss, sa);
-            V3 wv = -ray.dir;
-            radiance += beta * ss * vol_nee(sc, p_scatter, medium, nullptr, nullptr, wv, bounces, rng);
-            V2 u{rng.next(), rng.next()};
-            V3 nd = m.phase == LJ_PHASE_HG ? hg_sample(m.g, wv, u) : iso_sample(u);
-            // phase sampling is exact (eval == pdf), so the weight is sigma_s
-            beta = beta * ss;
-            dir_pdf = phase_eval(m, wv, nd);
-            nee_p = p_scatter;
-            multi_dir = V3{1, 1, 1};
-            multi_nee = V3{1, 1, 1};
-            never_scatter = false;
-            ray = Ray{p_scatter, nd, 0, INFINITY};
-        } else {
+        if (!scatter) {
             if (!is) {
                 if (sc.envmap >= 0) {
                     V3 Le = light_emission(sc, sc.lights[sc.envmap], -ray.dir, 0, PN{});
@@ -1880,7 +1865,27 @@ static V3 vol_path_tracing(const Scene &sc, int x, int y, Rng &rng) {
                     radiance += beta * Le * mis_dir(pd_tot, pn_tot);
                 }
             }
-            if (sc.opt.max_depth != -1 && bounces == sc.opt.max_depth - 1) break;
+        }
+        // homework2.tex v3 loop: the depth limit applies to every event
+        if (sc.opt.max_depth != -1 && bounces == sc.opt.max_depth - 1) break;
+        if (scatter) {
+            const MediumS &m = sc.media[medium];
+            V3 ss, sa;
+            sigmas(m, p_scatter, ss, sa);
+            V3 wv = -ray.dir;
+            radiance += beta * ss * vol_nee(sc, p_scatter, medium, nullptr, nullptr, wv, bounces, rng);
+            V2 u{rng.next(), rng.next()};
+            V3 nd = m.phase == LJ_PHASE_HG ? hg_sample(m.g, wv, u) : iso_sample(u);
+            // phase sampling is exact (eval == pdf), so the weight is sigma_s
+            beta = beta * ss;
+            dir_pdf = phase_eval(m, wv, nd);
+            nee_p = p_scatter;
+            multi_dir = V3{1, 1, 1};
+            multi_nee = V3{1, 1, 1};
+            never_scatter = false;
+            ray = Ray{p_scatter, nd, 0, INFINITY};
+        } else {
+            const Vertex &vx = *is;
             if (vx.material_id < 0) {
                 medium = update_medium(vx, ray.dir, medium);
                 ray = Ray{vx.position, ray.dir, eps, INFINITY};
@@ -1933,6 +1938,36 @@ void ljo_scene_bounds(void *s, double *out /* radius, cx, cy, cz */) {
     out[1] = sc->bcenter.x; out[2] = sc->bcenter.y; out[3] = sc->bcenter.z;
 }
 
+// aux_render's per-pixel colour, src/render.cpp:12-69: one ray through the
+// pixel centre, no random numbers; black where nothing is hit.
+static V3 aux_color(const Scene &sc, int x, int y) {
+    int w = sc.cam.w, h = sc.cam.h;
+    Ray ray = sample_primary(sc.cam, V2{(x + 0.5) / w, (y + 0.5) / h});
+    RayDiff rd{0, 0.25 / std::max(w, h)};   // init_ray_differential, src/ray.h:35-37
+    std::optional<Vertex> v = intersect(sc, ray, rd);
+    if (!v) return V3{0, 0, 0};
+    switch (sc.opt.integrator) {
+    case LJ_INTEGRATOR_DEPTH: {
+        double dist = distance(v->position, ray.org);
+        return V3{dist, dist, dist};
+    }
+    case LJ_INTEGRATOR_SHADING_NORMAL: return v->frame.n;
+    case LJ_INTEGRATOR_MEAN_CURVATURE: return V3{v->mean_curvature, v->mean_curvature, v->mean_curvature};
+    case LJ_INTEGRATOR_RAY_DIFFERENTIAL: return V3{rd.radius, rd.spread, 0};
+    case LJ_INTEGRATOR_MIPMAP_LEVEL: {
+        // get_texture: the first texture of every material, a constant zero
+        // for DisneyClearcoat (src/materials/*.inl get_texture_op)
+        const MatS &m = sc.mats[v->material_id];
+        if (m.type == LJ_MAT_DISNEY_CLEARCOAT || m.tex[0].kind != LJ_TEX_IMAGE) return V3{0, 0, 0};
+        const Img3 &l0 = sc.images[m.tex[0].image].levels[0];
+        double scaled = std::max(l0.w, l0.h) * std::max(m.tex[0].us, m.tex[0].vs) * v->uv_screen_size;
+        double level = std::log2(std::max(scaled, (double)1e-8f));
+        return V3{level, level, level};
+    }
+    default: return V3{0, 0, 0};
+    }
+}
+
 // Render the whole image.  mode 0: the reference's per-tile PCG streams
 // (src/render.cpp:71-101), consumed exactly as the reference does.  mode 1:
 // the GPU's per-(pixel, sample) keyed streams.  out: W*H*3 doubles.
@@ -1953,6 +1988,12 @@ int ljo_render(void *s, int mode, uint64_t seed, int spp, int sample_offset, int
             Rng rng{pcg_init((uint64_t)(ty * ntx + tx)), false};
             for (int y = ty * ts; y < std::min(ty * ts + ts, h); y++)
                 for (int x = tx * ts; x < std::min(tx * ts + ts, w); x++) {
+                    if (sc->opt.integrator < LJ_INTEGRATOR_PATH) {
+                        V3 c = aux_color(*sc, x, y);
+                        double *o = out + ((size_t)y * w + x) * 3;
+                        o[0] = c.x; o[1] = c.y; o[2] = c.z;
+                        continue;
+                    }
                     V3 acc{};
                     for (int k = 0; k < spp; k++) {
                         if (mode == 1) rng = Rng{pcg_keyed(seed, (uint64_t)y * w + x, (uint64_t)(sample_offset + k)), true};
@@ -2032,7 +2073,7 @@ int ljo_trace_closest(void *s, const lj_ray *rays, lj_hit *hits, int64_t n, int 
                         float t = 0, u = 0, v = 0;
                         bool hit = false;
                         if (sh.kind == LJ_SHAPE_MESH) {
-                            hit = tri_intersect(sc->tri_pre[p], o, d, r.tnear, r.tfar, t, u, v);
+                            hit = tri_intersect(sc->tri_pre[p], o, d, r.tnear, r.tfar, t, u, v) && t < r.tfar;
                         } else {
                             double td = sphere_hit(sc->spheres[sh.sphere], o, d, r.tnear, r.tfar);
                             hit = td >= 0;
@@ -2078,7 +2119,7 @@ int ljo_trace_any(void *s, const lj_ray *rays, uint8_t *occ, int64_t n, int brut
                         const ShapeS &sh = sc->shapes[sc->prims[p].shape];
                         float t, u, v;
                         if (sh.kind == LJ_SHAPE_MESH)
-                            hit = tri_intersect(sc->tri_pre[p], o, d, r.tnear, r.tfar, t, u, v);
+                            hit = tri_intersect(sc->tri_pre[p], o, d, r.tnear, r.tfar, t, u, v) && t < r.tfar;
                         else
                             hit = sphere_hit(sc->spheres[sh.sphere], o, d, r.tnear, r.tfar) >= 0;
                     }

@@ -46,7 +46,10 @@ inline TriPre tri_pre(f3 p0, f3 p1, f3 p2) {
     return TriPre{p0, f3_sub(p1, p0), f3_sub(p2, p0)};
 }
 
-// Returns true and fills t,u,v if the ray hits the triangle in (tnear, tfar).
+// Returns true and fills t,u,v if the ray hits the triangle in (tnear, tfar].
+// Callers reject t == tfar unless it breaks a tie with the current closest
+// hit in favour of the lower primitive index (the GPU traversal's rule), so
+// equal distances resolve the same way whatever the traversal order.
 inline bool tri_intersect(const TriPre &tri, f3 o, f3 d, float tnear, float tfar,
                           float &t_out, float &u_out, float &v_out) {
     f3 pvec = f3_cross(d, tri.e2);
@@ -60,7 +63,7 @@ inline bool tri_intersect(const TriPre &tri, f3 o, f3 d, float tnear, float tfar
     float v = f3_dot(d, qvec) * inv_det;
     if (!(v >= 0.0f && u + v <= 1.0f)) return false;
     float t = f3_dot(tri.e2, qvec) * inv_det;
-    if (!(t > tnear && t < tfar)) return false;
+    if (!(t > tnear && t <= tfar)) return false;
     t_out = t; u_out = u; v_out = v;
     return true;
 }

@@ -185,6 +185,10 @@ def mixed_scene(seed, w, h, spp, max_depth):
     sc = scenes.cornell_box(seed=seed, width=w, height=h, spp=spp, max_depth=max_depth)
     sc.materials[5] = scenes.roughplastic([0.6, 0.3, 0.2], [0.8, 0.8, 0.8], 0.2, 1.5)
     sc.materials[6] = scenes.roughdielectric([0.9, 0.9, 0.9], [0.95, 0.9, 0.85], 0.15, 1.45)
+    # lift the glass box off the floor: a bottom face coplanar with the floor
+    # would make which of the two a refracted ray hits depend on the last
+    # bits of its direction (FP32 on the GPU, FP64 in the oracle)
+    sc.shapes[6]["positions"] = sc.shapes[6]["positions"] + np.float32([0, 1e-3, 0])
     m = sc.add_material(scenes.lambertian([0.2, 0.7, 0.3]))
     sc.add_sphere([0.55, 1.45, -0.45], 0.12, m, emission=[6, 8, 10])
     return sc
@@ -194,12 +198,24 @@ RENDER_CASES = {
     "cbox": lambda: scenes.cornell_box(seed=1, width=40, height=32, spp=16, max_depth=6),
     "cbox_rr": lambda: scenes.cornell_box(seed=2, width=24, height=24, spp=8, max_depth=-1),
     "mixed": lambda: mixed_scene(3, 32, 32, 16, 8),
+    # image and checkerboard textures, vertex normals, UVs; the reference's
+    # Disney materials are stubs, so this path case has none
+    "textured": lambda: scenes.textured_scene(4, 40, 32, 16, 6, clearcoat=False),
+}
+
+# aux_render (src/render.cpp:12-69), one case per auxiliary integrator
+AUX_CASES = {
+    name: (lambda integ=integ: scenes.textured_scene(5, 48, 40, 1, 6, integrator=integ))
+    for name, integ in (("depth", abi.LJ_INTEGRATOR_DEPTH), ("shading_normal", abi.LJ_INTEGRATOR_SHADING_NORMAL),
+                        ("mean_curvature", abi.LJ_INTEGRATOR_MEAN_CURVATURE),
+                        ("ray_differential", abi.LJ_INTEGRATOR_RAY_DIFFERENTIAL),
+                        ("mipmap_level", abi.LJ_INTEGRATOR_MIPMAP_LEVEL))
 }
 
 
-def make_renders():
+def make_renders(cases=RENDER_CASES):
     out = {}
-    for name, mk in RENDER_CASES.items():
+    for name, mk in cases.items():
         sc = mk()
         with tempfile.TemporaryDirectory() as d:
             xml = sc.write_mitsuba(d, name)
@@ -218,6 +234,7 @@ def main():
     np.savez_compressed(os.path.join(OUT, "light.npz"), **make_light(rng))
     np.savez_compressed(os.path.join(OUT, "camera.npz"), **make_camera(rng))
     np.savez_compressed(os.path.join(OUT, "renders.npz"), **make_renders())
+    np.savez_compressed(os.path.join(OUT, "aux.npz"), **make_renders(AUX_CASES))
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))
