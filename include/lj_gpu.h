@@ -293,8 +293,10 @@ int lj_gpu_render(lj_scene *scene, const lj_render_params *params,
                   float *out_rgb, lj_stats *stats);
 
 /* Same as lj_gpu_render but leaves the image in device memory `d_out_rgb`
- * (W*H*3 floats) and runs asynchronously on `stream`; stats->device_ms is 0
- * unless `stats` is non-NULL, in which case the call synchronizes. */
+ * (W*H*3 floats) and runs on `stream`; stats->device_ms is 0 unless `stats`
+ * is non-NULL, in which case the call synchronizes.  With max_depth -1 or
+ * above 8 the call also reads the live-path count back every 4 bounces (a
+ * stream synchronization) to stop once every path has ended. */
 int lj_gpu_render_device(lj_scene *scene, const lj_render_params *params,
                          float *d_out_rgb, void *stream, lj_stats *stats);
 
@@ -448,7 +450,7 @@ typedef struct lj_job_desc {
     int32_t width, height;       /* 0 = the scene camera's resolution (same fov)           */
     int32_t override_depth;      /* 1 = use max_depth / rr_depth below                     */
     int32_t max_depth, rr_depth;
-    int32_t pad;
+    int32_t flags;               /* lj_gpu_render_job_device: LJ_RENDER_* bits             */
 } lj_job_desc;
 
 enum { LJ_JOB_QUEUED = 0, LJ_JOB_RUNNING = 1, LJ_JOB_DONE = 2, LJ_JOB_FAILED = 3, LJ_JOB_CANCELLED = 4 };

@@ -181,7 +181,7 @@ class lj_server_options(C.Structure):
 class lj_job_desc(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("spp", C.c_int32), ("sample_offset", C.c_int32),
                 ("width", C.c_int32), ("height", C.c_int32), ("override_depth", C.c_int32),
-                ("max_depth", C.c_int32), ("rr_depth", C.c_int32), ("pad", C.c_int32)]
+                ("max_depth", C.c_int32), ("rr_depth", C.c_int32), ("flags", C.c_int32)]
 
 
 class lj_job_status(C.Structure):

@@ -425,72 +425,130 @@ LJ_HD BsdfSample disney_sample(const DisneyP &p, const BsdfVertex &v, V3 wi, flo
 }
 
 // ---- dispatch (src/material.cpp:90-119) ----
+// kMats: bit t set = material type t can occur.  A kernel compiled for the
+// material set of its scenes drops the other cases (smaller code, fewer
+// registers); the default handles every type.
+constexpr uint32_t kAllMats = (1u << 9) - 1u;
+template <uint32_t kMats>
+LJ_HD constexpr bool has_mat(int t) { return (kMats >> t) & 1u; }
+// texture slots a material type reads (the slot table in lj_gpu.h)
+LJ_HD constexpr int mat_slot_count(int t) { return t == 8 ? 12 : (t == 0 || t == 6) ? 1 : (t == 7 ? 2 : 3); }
+template <uint32_t kMats>
+LJ_HD constexpr int max_mat_slots() {
+    int n = 0;
+    for (int t = 0; t < 9; t++)
+        if (has_mat<kMats>(t) && mat_slot_count(t) > n) n = mat_slot_count(t);
+    return n;
+}
+
+template <uint32_t kMats = kAllMats>
 LJ_HD V3 bsdf_eval(const MatParams &m, const BsdfVertex &v, V3 wi, V3 wo, bool to_view = false) {
+    float ax, ay;
     switch (m.type) {
-    case 0: return lambert_eval(m.s[0], v, wi, wo);
-    case 1: return plastic_eval(m, v, wi, wo);
-    case 2: return diel_eval(DielParams{m.s[0], m.s[1], m.eta, true, m.s[2].x, 0, 0}, v, wi, wo, to_view);
-    case 3: return ddiffuse_eval(m.s[0], m.s[1].x, m.s[2].x, v, wi, wo);
-    case 4: {
-        float ax, ay;
+    case 0:
+        if (has_mat<kMats>(0)) return lambert_eval(m.s[0], v, wi, wo);
+        break;
+    case 1:
+        if (has_mat<kMats>(1)) return plastic_eval(m, v, wi, wo);
+        break;
+    case 2:
+        if (has_mat<kMats>(2))
+            return diel_eval(DielParams{m.s[0], m.s[1], m.eta, true, m.s[2].x, 0, 0}, v, wi, wo, to_view);
+        break;
+    case 3:
+        if (has_mat<kMats>(3)) return ddiffuse_eval(m.s[0], m.s[1].x, m.s[2].x, v, wi, wo);
+        break;
+    case 4:
+        if (!has_mat<kMats>(4)) break;
         disney_alphas(m.s[1].x, m.s[2].x, ax, ay);
         return dmetal_eval(m.s[0], ax, ay, v, wi, wo);
-    }
-    case 5: {
-        float ax, ay;
+    case 5:
+        if (!has_mat<kMats>(5)) break;
         disney_alphas(m.s[1].x, m.s[2].x, ax, ay);
         return diel_eval(DielParams{m.s[0], sqrt3(m.s[0]), m.eta, false, 0, ax, ay}, v, wi, wo, to_view);
-    }
-    case 6: {
-        float c = dclearcoat_eval(m.s[0].x, v, wi, wo);
-        return V3{c, c, c};
-    }
-    case 7: return dsheen_eval(m.s[0], m.s[1].x, v, wi, wo);
-    case 8: return disney_eval(disney_params(m), v, wi, wo, to_view);
+    case 6:
+        if (!has_mat<kMats>(6)) break;
+        ax = dclearcoat_eval(m.s[0].x, v, wi, wo);
+        return V3{ax, ax, ax};
+    case 7:
+        if (has_mat<kMats>(7)) return dsheen_eval(m.s[0], m.s[1].x, v, wi, wo);
+        break;
+    case 8:
+        if (has_mat<kMats>(8)) return disney_eval(disney_params(m), v, wi, wo, to_view);
+        break;
     }
     return V3{0, 0, 0};
 }
+template <uint32_t kMats = kAllMats>
 LJ_HD float bsdf_pdf(const MatParams &m, const BsdfVertex &v, V3 wi, V3 wo) {
+    float ax, ay;
     switch (m.type) {
-    case 0: return lambert_pdf(v, wi, wo);
-    case 1: return plastic_pdf(m, v, wi, wo);
-    case 2: return diel_pdf(DielParams{m.s[0], m.s[1], m.eta, true, m.s[2].x, 0, 0}, v, wi, wo);
-    case 3: return lambert_pdf(v, wi, wo);
-    case 4: {
-        float ax, ay;
+    case 0:
+        if (has_mat<kMats>(0)) return lambert_pdf(v, wi, wo);
+        break;
+    case 1:
+        if (has_mat<kMats>(1)) return plastic_pdf(m, v, wi, wo);
+        break;
+    case 2:
+        if (has_mat<kMats>(2)) return diel_pdf(DielParams{m.s[0], m.s[1], m.eta, true, m.s[2].x, 0, 0}, v, wi, wo);
+        break;
+    case 3:
+        if (has_mat<kMats>(3)) return lambert_pdf(v, wi, wo);
+        break;
+    case 4:
+        if (!has_mat<kMats>(4)) break;
         disney_alphas(m.s[1].x, m.s[2].x, ax, ay);
         return dmetal_pdf(ax, ay, v, wi, wo);
-    }
-    case 5: {
-        float ax, ay;
+    case 5:
+        if (!has_mat<kMats>(5)) break;
         disney_alphas(m.s[1].x, m.s[2].x, ax, ay);
         return diel_pdf(DielParams{m.s[0], sqrt3(m.s[0]), m.eta, false, 0, ax, ay}, v, wi, wo);
-    }
-    case 6: return dclearcoat_pdf(m.s[0].x, v, wi, wo);
-    case 7: return lambert_pdf(v, wi, wo);
-    case 8: return disney_pdf(disney_params(m), v, wi, wo);
+    case 6:
+        if (has_mat<kMats>(6)) return dclearcoat_pdf(m.s[0].x, v, wi, wo);
+        break;
+    case 7:
+        if (has_mat<kMats>(7)) return lambert_pdf(v, wi, wo);
+        break;
+    case 8:
+        if (has_mat<kMats>(8)) return disney_pdf(disney_params(m), v, wi, wo);
+        break;
     }
     return 0.0f;
 }
+template <uint32_t kMats = kAllMats>
 LJ_HD BsdfSample bsdf_sample(const MatParams &m, const BsdfVertex &v, V3 wi, float u0, float u1, float w) {
+    float ax, ay;
     switch (m.type) {
-    case 0: return lambert_sample(v, wi, u0, u1, 1.0f);
-    case 1: return plastic_sample(m, v, wi, u0, u1, w);
-    case 2: return diel_sample(DielParams{m.s[0], m.s[1], m.eta, true, m.s[2].x, 0, 0}, v, wi, u0, u1, w, 0.0f);
-    case 3: return lambert_sample(v, wi, u0, u1, m.s[1].x);
-    case 4: {
-        float ax, ay;
+    case 0:
+        if (has_mat<kMats>(0)) return lambert_sample(v, wi, u0, u1, 1.0f);
+        break;
+    case 1:
+        if (has_mat<kMats>(1)) return plastic_sample(m, v, wi, u0, u1, w);
+        break;
+    case 2:
+        if (has_mat<kMats>(2))
+            return diel_sample(DielParams{m.s[0], m.s[1], m.eta, true, m.s[2].x, 0, 0}, v, wi, u0, u1, w, 0.0f);
+        break;
+    case 3:
+        if (has_mat<kMats>(3)) return lambert_sample(v, wi, u0, u1, m.s[1].x);
+        break;
+    case 4:
+        if (!has_mat<kMats>(4)) break;
         disney_alphas(m.s[1].x, m.s[2].x, ax, ay);
         return dmetal_sample(ax, ay, m.s[1].x, v, wi, u0, u1);
-    }
-    case 5: {
-        float ax, ay;
+    case 5:
+        if (!has_mat<kMats>(5)) break;
         disney_alphas(m.s[1].x, m.s[2].x, ax, ay);
         return diel_sample(DielParams{m.s[0], sqrt3(m.s[0]), m.eta, false, 0, ax, ay}, v, wi, u0, u1, w, m.s[1].x);
-    }
-    case 6: return dclearcoat_sample(m.s[0].x, v, wi, u0, u1);
-    case 7: return lambert_sample(v, wi, u0, u1, 1.0f);
-    case 8: return disney_sample(disney_params(m), v, wi, u0, u1, w);
+    case 6:
+        if (has_mat<kMats>(6)) return dclearcoat_sample(m.s[0].x, v, wi, u0, u1);
+        break;
+    case 7:
+        if (has_mat<kMats>(7)) return lambert_sample(v, wi, u0, u1, 1.0f);
+        break;
+    case 8:
+        if (has_mat<kMats>(8)) return disney_sample(disney_params(m), v, wi, u0, u1, w);
+        break;
     }
     return no_sample();
 }

@@ -421,6 +421,7 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
 
     // ---- materials ----
     std::vector<MatRec> mats(d->num_materials);
+    for (int i = 0; i < d->num_materials; i++) sc->mat_mask |= 1u << d->materials[i].type;
     for (int i = 0; i < d->num_materials; i++) {
         const lj_material_desc &m = d->materials[i];
         MatRec &r = mats[i];

@@ -44,6 +44,7 @@ struct lj_scene {
     PathBuffers path;
     bool has_media = false;
     lj_camera_desc camera{};
+    uint32_t mat_mask = 0;             // bit t: a material of type t exists
     std::atomic<int> server_refs{0};   // servers this scene is registered with
 };
 

@@ -21,7 +21,7 @@
 #include <vector>
 
 #include "lj_host.h"
-#include "lj_trace.cuh"
+#include "lj_trace_queue.cuh"
 #include "lj_wavefront.cuh"
 
 namespace lj {
@@ -50,49 +50,48 @@ __global__ void k_camera(DevScene sc, PathSoA ps, Queues q, int P, int num_pixel
     ps.nv[p] = 2;
 }
 
-__global__ void __launch_bounds__(128) k_trace_queue(DevBvh bvh, const float4 *rays, float4 *hits,
-                                                     const int *count, unsigned long long *stat,
+// Persistent warps with dynamic ray fetch (lj_trace_queue.cuh); *fetch is
+// zeroed before each launch.
+__global__ void __launch_bounds__(128, 8) k_trace_queue(DevBvh bvh, const float4 *rays, float4 *hits,
+                                                     const int *count, int *fetch, unsigned long long *stat,
                                                      int *status) {
-    int n = *count;
+    const int n = *count;
     if (blockIdx.x == 0 && threadIdx.x == 0 && stat) atomicAdd(stat, (unsigned long long)n);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
-        TraceHit h{0.0f, -1, 0.0f, 0.0f};
-        int ovf = 0;
-        bool f = trace_bvh<false>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
-        hits[i] = f ? make_float4(h.t, __int_as_float(h.prim), h.u, h.v)
-                    : make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f);
-        if (ovf) atomicOr(status, kStatusStackOverflow);
-    }
+    ClosestQueueIO io{bvh, rays, hits};
+    trace_queue<false>(io, n, fetch, status);
 }
 
-__global__ void __launch_bounds__(128) k_trace_shadow(DevBvh bvh, const float4 *rays, const int *paths,
-                                                      const float4 *contrib, const int *count, float4 *L,
-                                                      unsigned long long *stat, int *status) {
-    int n = *count;
+__global__ void __launch_bounds__(128, 8) k_trace_shadow(DevBvh bvh, const float4 *rays, const int *paths,
+                                                      const float4 *contrib, const int *count, int *fetch,
+                                                      float4 *L, unsigned long long *stat, int *status) {
+    const int n = *count;
     if (blockIdx.x == 0 && threadIdx.x == 0 && stat) atomicAdd(stat, (unsigned long long)n);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
-        TraceHit h{0.0f, -1, 0.0f, 0.0f};
-        int ovf = 0;
-        bool occ = trace_bvh<true>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
-        if (ovf) atomicOr(status, kStatusStackOverflow);
-        if (!occ) {
-            int p = paths[i];
-            float4 c = contrib[i];
-            float4 l = L[p];
-            L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
-        }
-    }
+    ShadowQueueIO io{bvh, rays, paths, contrib, L};
+    trace_queue<true>(io, n, fetch, status);
 }
 
-__global__ void __launch_bounds__(128) k_shade(DevScene sc, PathSoA ps, Queues q, int cur,
-                                               float spread0, int *status) {
+// One instance per material set (kMats): a scene of Lambertian surfaces only
+// runs a much smaller kernel than one that may meet every Disney lobe.
+template <uint32_t kMats>
+// (the instance for every material type needs more registers: 4 blocks per SM
+// without spills, the others 5)
+__global__ void __launch_bounds__(128, kMats == kAllMats ? 4 : 5) k_shade(DevScene sc, PathSoA ps, Queues q, int cur, float spread0,
+                                                  int *status) {
     const int n = q.counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(q.stats + 2, (unsigned long long)n);
     const ShadeCfg cfg{sc.max_depth, sc.rr_depth, spread0};
+    const SlotPaths paths{ps, q, cur};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        shade_segment(sc, ps, q, cur, i, cfg, status);
+        shade_segment<kMats>(sc, paths, i, cfg, status);
+}
+using ShadeKernel = void (*)(DevScene, PathSoA, Queues, int, float, int *);
+// the smallest instance whose material set covers the scene's
+ShadeKernel shade_kernel_for(uint32_t mat_mask) {
+    constexpr uint32_t kLambert = 1u << LJ_MAT_LAMBERTIAN;
+    constexpr uint32_t kClassic = kLambert | (1u << LJ_MAT_ROUGHPLASTIC) | (1u << LJ_MAT_ROUGHDIELECTRIC);
+    if ((mat_mask & ~kLambert) == 0) return k_shade<kLambert>;
+    if ((mat_mask & ~kClassic) == 0) return k_shade<kClassic>;
+    return k_shade<kAllMats>;
 }
 
 // Per pixel: sum the batch's samples in sample order (deterministic).
@@ -116,14 +115,20 @@ __global__ void k_scale(float *img, int64_t n, float s) {
     if (i < n) img[i] *= s;
 }
 
+// counts: [0], [1] ray queues, [2] shadow queue, [8], [9] ray fetch
+// counters of the closest / shadow traversal kernels
 __global__ void k_set_counts(int *counts, int c0) {
     counts[0] = c0;
     counts[1] = 0;
     counts[2] = 0;
+    counts[8] = 0;
+    counts[9] = 0;
 }
 __global__ void k_zero2(int *counts, int a, int b) {
     counts[a] = 0;
     counts[b] = 0;
+    counts[8] = 0;
+    counts[9] = 0;
 }
 
 template <typename T>
@@ -190,7 +195,6 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
     }
     char *cur = (char *)scene->path.block;
     PathSoA ps;
-    ps.job = nullptr;
     ps.pixel = carve<int>(cur, P);
     ps.rng = carve<uint64_t>(cur, P);
     ps.beta = carve<float4>(cur, P);
@@ -198,7 +202,6 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
     ps.prev = carve<float4>(cur, P);
     ps.nv = carve<int>(cur, P);
     Queues q;
-    q.retire = nullptr;
     q.ray[0] = carve<float4>(cur, 2 * P);
     q.ray[1] = carve<float4>(cur, 2 * P);
     q.path[0] = carve<int>(cur, P);
@@ -214,7 +217,8 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
     LJ_CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(float) * 3 * (size_t)num_pixels, s));
     const int g_trace = grid_persistent((const void *)k_trace_queue, 128);
     const int g_shadow = grid_persistent((const void *)k_trace_shadow, 128);
-    const int g_shade = grid_persistent((const void *)k_shade, 128);
+    const ShadeKernel shade = shade_kernel_for(scene->mat_mask);
+    const int g_shade = grid_persistent((const void *)shade, 128);
     const int passes = max_depth == -1 ? LJ_MAX_BOUNCES + 1 : std::max(1, max_depth);
     const float spread0 = 0.25f / (float)std::max(W, H);
     cudaEvent_t e0, e1;
@@ -255,15 +259,15 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
         for (int pass = 0; pass < passes; pass++) {
             k_zero2<<<1, 1, 0, s>>>(q.counts, curq ^ 1, 2);
             mark_begin(LJ_KERNEL_TRACE);
-            k_trace_queue<<<g_trace, 128, 0, s>>>(sc.bvh, q.ray[curq], q.hit, q.counts + curq, q.stats + 0,
-                                                  ctx->d_status);
+            k_trace_queue<<<g_trace, 128, 0, s>>>(sc.bvh, q.ray[curq], q.hit, q.counts + curq, q.counts + 8,
+                                                  q.stats + 0, ctx->d_status);
             mark_end();
             mark_begin(LJ_KERNEL_SHADE);
-            k_shade<<<g_shade, 128, 0, s>>>(sc, ps, q, curq, spread0, ctx->d_status);
+            shade<<<g_shade, 128, 0, s>>>(sc, ps, q, curq, spread0, ctx->d_status);
             mark_end();
             mark_begin(LJ_KERNEL_SHADOW);
-            k_trace_shadow<<<g_shadow, 128, 0, s>>>(sc.bvh, q.sray, q.spath, q.scontrib, q.counts + 2, ps.L,
-                                                    q.stats + 1, ctx->d_status);
+            k_trace_shadow<<<g_shadow, 128, 0, s>>>(sc.bvh, q.sray, q.spath, q.scontrib, q.counts + 2,
+                                                    q.counts + 9, ps.L, q.stats + 1, ctx->d_status);
             mark_end();
             launches += 4;
             class_launches[LJ_KERNEL_OTHER]++;
@@ -271,7 +275,9 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
             class_launches[LJ_KERNEL_SHADE]++;
             class_launches[LJ_KERNEL_SHADOW]++;
             curq ^= 1;
-            if (max_depth == -1 && (pass & 7) == 7) {
+            // stop early once every path of the batch has ended (paths end
+            // well before a large max_depth through escapes and roulette)
+            if ((max_depth == -1 || max_depth > 8) && (pass & 3) == 3 && pass + 1 < passes) {
                 int c = 0;
                 LJ_CUDA_TRY(cudaMemcpyAsync(&c, q.counts + curq, sizeof(int), cudaMemcpyDeviceToHost, s));
                 LJ_CUDA_TRY(cudaStreamSynchronize(s));
@@ -369,6 +375,7 @@ int lj_gpu_render_job_device(lj_scene *scene, const lj_job_desc *job, float *d_o
     p.seed = job->seed;
     p.spp = job->spp;
     p.sample_offset = job->sample_offset;
+    p.flags = job->flags;
     return render_path(scene, &p, d_out_rgb, (cudaStream_t)stream, stats, stats != nullptr, job);
 }
 

@@ -41,7 +41,7 @@
 #include <vector>
 
 #include "lj_host.h"
-#include "lj_trace.cuh"
+#include "lj_trace_queue.cuh"
 #include "lj_wavefront.cuh"
 
 namespace lj {
@@ -65,6 +65,18 @@ struct SrvCtr {
     unsigned long long issued, done, dropped, pad;
 };
 
+// Path state and ray of every queue entry, in queue order (two buffers:
+// the queue a wave reads and the one it fills).  Keeping state in queue
+// order makes every state access of regen, shade and retire coalesced; a
+// fixed slot per path would scatter them over the whole pool once paths of
+// many jobs and depths interleave.
+struct StateSoA {
+    int *job, *pixel, *nv;
+    uint64_t *rng;
+    float4 *beta, *L, *prev;
+    float4 *ray;             // 2 per entry: org | tnear, dir | tfar
+};
+
 struct SrvDev {
     const DevScene *scenes;
     const SrvJob *jobs;
@@ -73,17 +85,28 @@ struct SrvDev {
     const int *order;            // [0] = entries, [1..] job slots
     int *plan_off;               // per entry: first regen index; [n] = total taken
     long long *plan_start;       // per entry: first linear sample index
-    int *free_ids;
-    PathSoA ps;
-    Queues q;                    // counts: [0],[1] rays, [2] shadow, [3] retire, [4] free, [5] regen
+    StateSoA buf[2];
+    float4 *hit;
+    float4 *sray;                // shadow rays (2 per entry)
+    int *starget;                // entry of the path in the next queue, or retire index | 2^31
+    float4 *scontrib;
+    int *rjob, *rpixel;          // finished paths
+    float4 *rL;
+    int *counts;                 // [0],[1] queues, [2] shadow, [3] retire, [5] regen count,
+                                 // [6] regen base, [8],[9] ray fetch counters
+    unsigned long long *stats;   // [0] closest rays, [1] shadow rays, [2] shade segments
+    int P;                       // queue capacity
     int *status;
 };
 
+constexpr int kRetireBit = (int)0x80000000u;
+
 __global__ void k_srv_plan(SrvDev d, int cur) {
     const int lane = threadIdx.x;
-    int *counts = d.q.counts;
+    int *counts = d.counts;
     const int n_order = d.order[0];
-    const long long freec = counts[4];
+    const int c = counts[cur];                   // paths that continue into this wave
+    const long long freec = (long long)d.P - c;   // room for new paths
     long long carry = 0;
     for (int base = 0; base < n_order; base += 32) {
         const int k = base + lane;
@@ -112,18 +135,22 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
         const long long take = min(carry, freec);
         d.plan_off[n_order] = (int)take;
         counts[5] = (int)take;
-        counts[4] = (int)(freec - take);
+        counts[6] = c;
+        counts[cur] = c + (int)take;
         counts[cur ^ 1] = 0;
         counts[2] = 0;
         counts[3] = 0;
+        counts[8] = 0;
+        counts[9] = 0;
     }
 }
 
 template <int B>
 __global__ void __launch_bounds__(B) k_srv_regen(SrvDev d, int cur) {
-    const int n = d.q.counts[5];
-    const int base = d.q.counts[4];   // slots popped by the plan: free_ids[base, base + n)
+    const int n = d.counts[5];
+    const int base = d.counts[6];   // new paths go after the continuing ones
     const int n_order = d.order[0];
+    const StateSoA &q = d.buf[cur];
     for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
         int lo = 0, hi = n_order - 1;   // last entry whose first index is <= i
         while (lo < hi) {
@@ -134,74 +161,144 @@ __global__ void __launch_bounds__(B) k_srv_regen(SrvDev d, int cur) {
         const int j = d.order[1 + lo];
         const SrvJob &jb = d.jobs[j];
         const long long lin = d.plan_start[lo] + (i - d.plan_off[lo]);
-        const int pixel = (int)(lin % jb.npix);
-        const int sample = jb.sample_offset + (int)(lin / jb.npix);
-        const int p = d.free_ids[base + i];
+        int pixel, sample;
+        if (lin <= 0x7fffffffLL) {   // 32-bit division where it suffices (it is much cheaper)
+            const unsigned l = (unsigned)lin, np = (unsigned)jb.npix;
+            pixel = (int)(l % np);
+            sample = jb.sample_offset + (int)(l / np);
+        } else {
+            pixel = (int)(lin % jb.npix);
+            sample = jb.sample_offset + (int)(lin / jb.npix);
+        }
         Pcg rng = pcg_keyed(jb.seed, (uint64_t)pixel, (uint64_t)sample);
         const int x = pixel % jb.cam.w, y = pixel / jb.cam.w;
         float r1 = pcg_uniform(rng), r2 = pcg_uniform(rng);
         V3 o, dir;
         camera_ray(jb.cam, (x + r1) / jb.cam.w, (y + r2) / jb.cam.h, o, dir);
-        d.ps.job[p] = j;
-        d.ps.pixel[p] = pixel;
-        d.ps.rng[p] = rng.state;
-        d.ps.beta[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-        d.ps.L[p] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
-        d.ps.prev[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        d.ps.nv[p] = 2;
-        const int s = queue_slot(d.q.counts + cur);
-        d.q.ray[cur][2 * s] = make_float4(o.x, o.y, o.z, 0.0f);
-        d.q.ray[cur][2 * s + 1] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0x7f800000));
-        d.q.path[cur][s] = p;
+        const int s = base + i;
+        q.job[s] = j;
+        q.pixel[s] = pixel;
+        q.rng[s] = rng.state;
+        q.beta[s] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+        q.L[s] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);
+        q.prev[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        q.nv[s] = 2;
+        q.ray[2 * s] = make_float4(o.x, o.y, o.z, 0.0f);
+        q.ray[2 * s + 1] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0x7f800000));
     }
 }
 
-template <int B>
-__global__ void __launch_bounds__(B) k_srv_trace(SrvDev d, int cur) {
-    const int n = d.q.counts[cur];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.q.stats + 0, (unsigned long long)n);
-    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
-        const int p = d.q.path[cur][i];
-        const DevBvh &bvh = d.scenes[d.jobs[d.ps.job[p]].scene].bvh;
-        float4 r0 = d.q.ray[cur][2 * i], r1 = d.q.ray[cur][2 * i + 1];
-        TraceHit h{0.0f, -1, 0.0f, 0.0f};
-        int ovf = 0;
-        bool f = trace_bvh<false>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
-        d.q.hit[i] = f ? make_float4(h.t, __int_as_float(h.prim), h.u, h.v)
-                       : make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f);
-        if (ovf) atomicOr(d.status, kStatusStackOverflow);
+// Ray queues of the server: each ray uses the BVH of its path's job's scene.
+struct SrvClosestIO {
+    const SrvDev &d;
+    int cur;
+    LJ_D const DevBvh &bvh(int r) const { return d.scenes[d.jobs[d.buf[cur].job[r]].scene].bvh; }
+    LJ_D void load(int r, V3 &o, V3 &dir, float &tn, float &tf) const { load_ray(d.buf[cur].ray, r, o, dir, tn, tf); }
+    LJ_D void store(int r, const Trav &s) const { d.hit[r] = hit_record(s); }
+};
+struct SrvShadowIO {
+    const SrvDev &d;
+    int nxt;
+    LJ_D int job_of(int r) const {
+        const int t = d.starget[r];
+        return t < 0 ? d.rjob[t & 0x7fffffff] : d.buf[nxt].job[t];
     }
-}
-
-template <int B>
-__global__ void __launch_bounds__(B) k_srv_shade(SrvDev d, int cur) {
-    const int n = d.q.counts[cur];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.q.stats + 2, (unsigned long long)n);
-    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
-        const SrvJob &jb = d.jobs[d.ps.job[d.q.path[cur][i]]];
-        const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
-        shade_segment(d.scenes[jb.scene], d.ps, d.q, cur, i, cfg, d.status);
+    LJ_D const DevBvh &bvh(int r) const { return d.scenes[d.jobs[job_of(r)].scene].bvh; }
+    LJ_D void load(int r, V3 &o, V3 &dir, float &tn, float &tf) const { load_ray(d.sray, r, o, dir, tn, tf); }
+    LJ_D void store(int r, const Trav &s) const {
+        if (s.found) return;
+        const int t = d.starget[r];
+        float4 *L = t < 0 ? d.rL + (t & 0x7fffffff) : d.buf[nxt].L + t;
+        const float4 c = d.scontrib[r], l = *L;
+        *L = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
     }
-}
+};
 
-template <int B>
-__global__ void __launch_bounds__(B) k_srv_shadow(SrvDev d) {
-    const int n = d.q.counts[2];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.q.stats + 1, (unsigned long long)n);
-    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
-        const int p = d.q.spath[i];
-        const DevBvh &bvh = d.scenes[d.jobs[d.ps.job[p]].scene].bvh;
-        float4 r0 = d.q.sray[2 * i], r1 = d.q.sray[2 * i + 1];
-        TraceHit h{0.0f, -1, 0.0f, 0.0f};
-        int ovf = 0;
-        bool occ = trace_bvh<true>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
-        if (ovf) atomicOr(d.status, kStatusStackOverflow);
-        if (!occ) {
-            float4 c = d.q.scontrib[i];
-            float4 l = d.ps.L[p];
-            d.ps.L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
+// The server's path store for shade_segment: state read from queue cur at
+// the entry index, continuing paths written to the end of queue cur ^ 1,
+// finished ones to the retire list; a shadow ray records where its path went.
+struct QueuePaths {
+    const SrvDev &d;
+    int cur;
+    LJ_D void load(int i, PathState &st, float4 &r0, float4 &r1, float4 &hit) const {
+        const StateSoA &q = d.buf[cur];
+        st.slot = i;
+        st.job = q.job[i];
+        st.pixel = q.pixel[i];
+        st.rng = q.rng[i];
+        st.beta = q.beta[i];
+        st.L = q.L[i];
+        st.prev = q.prev[i];
+        st.nv = q.nv[i];
+        r0 = q.ray[2 * i];
+        r1 = q.ray[2 * i + 1];
+        hit = d.hit[i];
+    }
+    // the shadow ray's target is filled in by emit, once it is known
+    LJ_D int shadow(const PathState &, float4 r0, float4 r1, float4 contrib) const {
+        const int k = queue_slot(d.counts + 2);
+        d.sray[2 * k] = r0;
+        d.sray[2 * k + 1] = r1;
+        d.scontrib[k] = contrib;
+        return k;
+    }
+    LJ_D void emit(const PathState &st, const ShadeOut &o) const {
+        int target;
+        if (o.cont) {
+            const int nxt = cur ^ 1;
+            const StateSoA &q = d.buf[nxt];
+            const int s = queue_slot(d.counts + nxt);
+            q.job[s] = st.job;
+            q.pixel[s] = st.pixel;
+            q.rng[s] = st.rng;
+            q.beta[s] = st.beta;
+            q.L[s] = st.L;
+            q.prev[s] = st.prev;
+            q.nv[s] = st.nv;
+            q.ray[2 * s] = o.ray0;
+            q.ray[2 * s + 1] = o.ray1;
+            target = s;
+        } else {
+            const int r = queue_slot(d.counts + 3);
+            d.rjob[r] = st.job;
+            d.rpixel[r] = st.pixel;
+            d.rL[r] = st.L;
+            target = r | kRetireBit;
         }
+        if (o.shadow >= 0) d.starget[o.shadow] = target;
     }
+};
+
+// traversal: 64 registers (full-SM occupancy of 50%, no spills)
+template <int B>
+__global__ void __launch_bounds__(B, 1024 / B) k_srv_trace(SrvDev d, int cur) {
+    const int n = d.counts[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 0, (unsigned long long)n);
+    SrvClosestIO io{d, cur};
+    trace_queue<false>(io, n, d.counts + 8, d.status);
+}
+
+// The scene and job tables are read-only here (restrict: the stores of the
+// shade step cannot alias them, so their fields need not be re-read).
+template <int B>
+__global__ void __launch_bounds__(B, 512 / B) k_srv_shade(SrvDev d, const DevScene *__restrict__ scenes,
+                                                          const SrvJob *__restrict__ jobs, int cur) {
+    const int n = d.counts[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 2, (unsigned long long)n);
+    const QueuePaths paths{d, cur};
+    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
+        const SrvJob &jb = jobs[d.buf[cur].job[i]];
+        const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
+        shade_segment<kAllMats>(scenes[jb.scene], paths, i, cfg, d.status);
+    }
+}
+
+template <int B>
+__global__ void __launch_bounds__(B, 1024 / B) k_srv_shadow(SrvDev d, int cur) {
+    const int n = d.counts[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 1, (unsigned long long)n);
+    SrvShadowIO io{d, cur ^ 1};
+    trace_queue<true>(io, n, d.counts + 9, d.status);
 }
 
 LJ_D unsigned long long to_fixed(float v, float clamp) {
@@ -211,14 +308,13 @@ LJ_D unsigned long long to_fixed(float v, float clamp) {
 
 template <int B>
 __global__ void __launch_bounds__(B) k_srv_retire(SrvDev d) {
-    const int n = d.q.counts[3];
+    const int n = d.counts[3];
     for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
-        const int p = d.q.retire[i];
-        const int j = d.ps.job[p];
+        const int j = d.rjob[i];
         const SrvJob &jb = d.jobs[j];
-        const float4 L = d.ps.L[p];
+        const float4 L = d.rL[i];
         if (isfinite(L.x) && isfinite(L.y) && isfinite(L.z)) {
-            unsigned long long *a = jb.accum + 3 * (size_t)d.ps.pixel[p];
+            unsigned long long *a = jb.accum + 3 * (size_t)d.rpixel[i];
             atomicAdd(a, to_fixed(L.x, jb.clamp));
             atomicAdd(a + 1, to_fixed(L.y, jb.clamp));
             atomicAdd(a + 2, to_fixed(L.z, jb.clamp));
@@ -228,7 +324,6 @@ __global__ void __launch_bounds__(B) k_srv_retire(SrvDev d) {
         const unsigned active = __activemask();
         const unsigned same = __match_any_sync(active, j);
         if ((int)(threadIdx.x & 31u) == __ffs(same) - 1) atomicAdd(&d.ctr[j].done, (unsigned long long)__popc(same));
-        d.free_ids[queue_slot(d.q.counts + 4)] = p;
     }
 }
 
@@ -237,20 +332,11 @@ __global__ void k_srv_finalize(const unsigned long long *acc, float *img, long l
     if (i < n) img[i] = (float)((double)(long long)acc[i] * scale);
 }
 
-__global__ void k_srv_init_free(int *free_ids, int *counts, int P) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < P) free_ids[i] = i;
-    if (i == 0) {
-        for (int k = 0; k < 8; k++) counts[k] = 0;
-        counts[4] = P;
-    }
-}
-
 struct KernelSet {
     void (*regen)(SrvDev, int);
     void (*trace)(SrvDev, int);
-    void (*shade)(SrvDev, int);
-    void (*shadow)(SrvDev);
+    void (*shade)(SrvDev, const DevScene *, const SrvJob *, int);
+    void (*shadow)(SrvDev, int);
     void (*retire)(SrvDev);
 };
 template <int B>
@@ -272,11 +358,11 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 size_t pool_bytes(size_t P) {
     size_t b = 0;
-    // path state: job, pixel, rng, beta, L, prev, nv
-    b += align256(P * 4) * 2 + align256(P * 8) + align256(P * 16) * 3 + align256(P * 4);
-    // queues: ray x2, path x2, hit, shadow ray, shadow path, contrib, retire, free ids
-    b += align256(P * 32) * 2 + align256(P * 4) * 2 + align256(P * 16) + align256(P * 32) + align256(P * 4) +
-         align256(P * 16) + align256(P * 4) + align256(P * 4);
+    // two queue buffers: job, pixel, nv, rng, beta, L, prev, ray
+    b += 2 * (align256(P * 4) * 3 + align256(P * 8) + align256(P * 16) * 3 + align256(P * 32));
+    // hits; shadow rays, targets, contributions; retire job, pixel, radiance
+    b += align256(P * 16) + align256(P * 32) + align256(P * 4) + align256(P * 16);
+    b += align256(P * 4) * 2 + align256(P * 16);
     b += 256 * 2;   // counts, stats
     return b;
 }
@@ -430,10 +516,10 @@ void launch_wave(lj_server *s, int cur) {
     s->ks.trace<<<s->grid[1], B, 0, s->stream>>>(s->dev, cur);
     mark(s, LJ_KERNEL_TRACE, false);
     mark(s, LJ_KERNEL_SHADE, true);
-    s->ks.shade<<<s->grid[2], B, 0, s->stream>>>(s->dev, cur);
+    s->ks.shade<<<s->grid[2], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
     mark(s, LJ_KERNEL_SHADE, false);
     mark(s, LJ_KERNEL_SHADOW, true);
-    s->ks.shadow<<<s->grid[3], B, 0, s->stream>>>(s->dev);
+    s->ks.shadow<<<s->grid[3], B, 0, s->stream>>>(s->dev, cur);
     mark(s, LJ_KERNEL_SHADOW, false);
     mark(s, LJ_KERNEL_OTHER, true);
     s->ks.retire<<<s->grid[4], B, 0, s->stream>>>(s->dev);
@@ -504,29 +590,30 @@ std::string build_device(lj_server *s) {
     d.order = s->d_order;
     d.plan_off = s->d_plan_off;
     d.plan_start = s->d_plan_start;
-    d.ps.job = carve<int>(cur, P);
-    d.ps.pixel = carve<int>(cur, P);
-    d.ps.rng = carve<uint64_t>(cur, P);
-    d.ps.beta = carve<float4>(cur, P);
-    d.ps.L = carve<float4>(cur, P);
-    d.ps.prev = carve<float4>(cur, P);
-    d.ps.nv = carve<int>(cur, P);
-    d.q.ray[0] = carve<float4>(cur, 2 * P);
-    d.q.ray[1] = carve<float4>(cur, 2 * P);
-    d.q.path[0] = carve<int>(cur, P);
-    d.q.path[1] = carve<int>(cur, P);
-    d.q.hit = carve<float4>(cur, P);
-    d.q.sray = carve<float4>(cur, 2 * P);
-    d.q.spath = carve<int>(cur, P);
-    d.q.scontrib = carve<float4>(cur, P);
-    d.q.retire = carve<int>(cur, P);
-    d.free_ids = carve<int>(cur, P);
-    d.q.counts = carve<int>(cur, 64);
-    d.q.stats = carve<unsigned long long>(cur, 32);
+    for (int k = 0; k < 2; k++) {
+        StateSoA &q = d.buf[k];
+        q.job = carve<int>(cur, P);
+        q.pixel = carve<int>(cur, P);
+        q.nv = carve<int>(cur, P);
+        q.rng = carve<uint64_t>(cur, P);
+        q.beta = carve<float4>(cur, P);
+        q.L = carve<float4>(cur, P);
+        q.prev = carve<float4>(cur, P);
+        q.ray = carve<float4>(cur, 2 * P);
+    }
+    d.hit = carve<float4>(cur, P);
+    d.sray = carve<float4>(cur, 2 * P);
+    d.starget = carve<int>(cur, P);
+    d.scontrib = carve<float4>(cur, P);
+    d.rjob = carve<int>(cur, P);
+    d.rpixel = carve<int>(cur, P);
+    d.rL = carve<float4>(cur, P);
+    d.counts = carve<int>(cur, 64);
+    d.stats = carve<unsigned long long>(cur, 32);
+    d.P = (int)P;
     d.status = s->ctx->d_status;
-    SRV_CUDA(cudaMemsetAsync(d.q.stats, 0, 8 * sizeof(unsigned long long), s->stream));
-    k_srv_init_free<<<(int)((P + 255) / 256), 256, 0, s->stream>>>(d.free_ids, d.q.counts, (int)P);
-    SRV_CUDA(cudaGetLastError());
+    SRV_CUDA(cudaMemsetAsync(d.stats, 0, 32 * sizeof(unsigned long long), s->stream));
+    SRV_CUDA(cudaMemsetAsync(d.counts, 0, 64 * sizeof(int), s->stream));
 
     switch (s->block) {
     case 64: s->ks = kernel_set<64>(); break;
@@ -820,7 +907,7 @@ void worker_main(lj_server *s) {
             e = cudaMemcpyAsync(s->h_ctr[b], s->d_ctr, sizeof(SrvCtr) * s->live.size(), cudaMemcpyDeviceToHost,
                                 s->stream);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(s->h_qstats[b], s->dev.q.stats, sizeof(unsigned long long) * 4,
+                e = cudaMemcpyAsync(s->h_qstats[b], s->dev.stats, sizeof(unsigned long long) * 4,
                                     cudaMemcpyDeviceToHost, s->stream);
             if (e == cudaSuccess) e = cudaEventRecord(s->poll_ev[b], s->stream);
             if (e == cudaSuccess) {
@@ -839,7 +926,7 @@ void worker_main(lj_server *s) {
     lk.unlock();
     cudaStreamSynchronize(s->stream);
     unsigned long long q[4] = {0, 0, 0, 0};
-    bool got = !s->dead && cudaMemcpy(q, s->dev.q.stats, sizeof(q), cudaMemcpyDeviceToHost) == cudaSuccess;
+    bool got = !s->dead && cudaMemcpy(q, s->dev.stats, sizeof(q), cudaMemcpyDeviceToHost) == cudaSuccess;
     lk.lock();
     if (got) {
         s->rays_closest = (int64_t)q[0];
@@ -1064,7 +1151,7 @@ int lj_gpu_server_stats(lj_server *s, lj_server_stats *st) {
         // idle: every path has retired, so the ray counters are final
         unsigned long long q[4];
         cudaSetDevice(s->device);
-        if (cudaMemcpy(q, s->dev.q.stats, sizeof(q), cudaMemcpyDeviceToHost) == cudaSuccess) {
+        if (cudaMemcpy(q, s->dev.stats, sizeof(q), cudaMemcpyDeviceToHost) == cudaSuccess) {
             s->rays_closest = (int64_t)q[0];
             s->rays_shadow = (int64_t)q[1];
             s->path_segments = (int64_t)q[2];

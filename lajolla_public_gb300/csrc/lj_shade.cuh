@@ -213,15 +213,20 @@ LJ_D V3 eval_texture(const DevScene &sc, const TexRec &t, float u, float v, floa
     }
     return mip_bilinear(lvls[n - 1], lu, lv);
 }
+// Texture values of the slots the material's type reads (other slots: 0;
+// slots no type of kMats reads are left unset).
+template <uint32_t kMats = kAllMats>
 LJ_D MatParams resolve_material(const DevScene &sc, int mid, float u, float v, float footprint) {
     const MatRec &m = sc.mats[mid];
     MatParams p;
     p.type = m.type;
     p.eta = m.eta;
-    int textured = m.textured;
+    const int textured = m.textured;
+    const int n = mat_slot_count(p.type);
 #pragma unroll
-    for (int k = 0; k < kMatSlots; k++) {
-        if (textured & (1 << k)) p.s[k] = eval_texture(sc, m.tex[k], u, v, footprint);
+    for (int k = 0; k < max_mat_slots<kMats>(); k++) {
+        if (k >= n) p.s[k] = V3{0.0f, 0.0f, 0.0f};
+        else if (textured & (1 << k)) p.s[k] = eval_texture(sc, m.tex[k], u, v, footprint);
         else p.s[k] = V3{m.tex[k].v0[0], m.tex[k].v0[1], m.tex[k].v0[2]};
     }
     return p;

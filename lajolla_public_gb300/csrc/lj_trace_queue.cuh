@@ -1,0 +1,240 @@
+// Traversal of a whole ray queue by persistent warps with dynamic ray fetch
+// (the "persistent while-while" scheme of Aila and Laine, "Understanding the
+// Efficiency of Ray Traversal on GPUs", HPG 2009): each lane keeps its ray's
+// traversal state in registers and steps it one node (plus the primitives
+// that node yields) at a time; when fewer than kRefillLanes lanes of a warp
+// still have a ray, the idle lanes take new rays from the queue (one atomic
+// per warp) and the warp goes on.  Incoherent secondary rays differ widely
+// in length, so this keeps far more lanes busy than one ray per lane per
+// loop trip.  Per ray the node order, the tests and the tie rule are those
+// of trace_bvh (lj_trace.cuh): results are identical.
+#pragma once
+
+#include "lj_internal.h"
+#include "lj_trace.cuh"
+
+namespace lj {
+
+constexpr int kRefillLanes = 20;
+
+struct Trav {
+    V3 o, d, inv;
+    float tnear, tfar;
+    uint32_t oct_xor;
+    uint2 ngroup;
+    int sp;
+    int iter;
+    const uint4 *nodes;
+    const float4 *prims;
+    TraceHit hit;
+    bool found;
+};
+
+LJ_D void trav_init(Trav &s, const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar) {
+    const float tiny = 1e-30f;
+    V3 dd = V3{fabsf(d.x) < tiny ? copysignf(tiny, d.x) : d.x, fabsf(d.y) < tiny ? copysignf(tiny, d.y) : d.y,
+               fabsf(d.z) < tiny ? copysignf(tiny, d.z) : d.z};
+    s.o = o;
+    s.d = d;
+    s.inv = V3{1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z};
+    s.tnear = tnear;
+    s.tfar = tfar;
+    const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
+    s.oct_xor = 7u - oct;
+    s.ngroup = bvh.num_nodes > 0 ? make_uint2(0u, (1u << (24u + (0u ^ s.oct_xor))) | 1u) : make_uint2(0u, 0u);
+    s.sp = 0;
+    s.iter = 0;
+    s.nodes = bvh.nodes;
+    s.prims = bvh.prims;
+    s.hit = TraceHit{0.0f, -1, 0.0f, 0.0f};
+    s.found = false;
+}
+
+// One step: visit one node (or take the pending primitive group) and test
+// the primitives it yields.  Returns true when the ray is finished.
+template <bool kAny>
+LJ_D bool trav_step(Trav &s, uint2 *stack, int *status) {
+    if (++s.iter > (1 << 22)) {   // a well-formed tree needs far fewer steps
+        atomicOr(status, kStatusStackOverflow);
+        return true;
+    }
+    uint2 tgroup = make_uint2(0u, 0u);
+    if (s.ngroup.y > 0x00ffffffu) {
+        const uint32_t k = 31u - __clz(s.ngroup.y & 0xff000000u);
+        const uint32_t slot = (k - 24u) ^ s.oct_xor;
+        const uint32_t imask = s.ngroup.y & 0xffu;
+        const uint32_t child = s.ngroup.x + __popc(imask & ((1u << slot) - 1u));
+        s.ngroup.y &= ~(1u << k);
+        if (s.ngroup.y > 0x00ffffffu) {
+            if (s.sp < kTraversalStack) stack[s.sp++] = s.ngroup;
+            else atomicOr(status, kStatusStackOverflow);
+        }
+        const uint4 *np = s.nodes + (size_t)child * kWideNodeU4;
+        const uint4 c0 = __ldg(np + 0), c1 = __ldg(np + 1), c2 = __ldg(np + 2), c3 = __ldg(np + 3),
+                    c4 = __ldg(np + 4);
+        const float px = __uint_as_float(c0.x), py = __uint_as_float(c0.y), pz = __uint_as_float(c0.z);
+        const float sx = __uint_as_float((c0.w & 0xffu) << 23);
+        const float sy = __uint_as_float(((c0.w >> 8) & 0xffu) << 23);
+        const float sz = __uint_as_float(((c0.w >> 16) & 0xffu) << 23);
+        const uint32_t nimask = c0.w >> 24;
+        const float ax = sx * s.inv.x, bx = (px - s.o.x) * s.inv.x;
+        const float ay = sy * s.inv.y, by = (py - s.o.y) * s.inv.y;
+        const float az = sz * s.inv.z, bz = (pz - s.o.z) * s.inv.z;
+        const bool negx = s.inv.x < 0.0f, negy = s.inv.y < 0.0f, negz = s.inv.z < 0.0f;
+        uint32_t node_hits = 0, prim_hits = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const uint32_t meta = extract_byte(i < 4 ? c1.z : c1.w, i & 3);
+            if (meta == 0u) continue;
+            const uint32_t lox = extract_byte(i < 4 ? c2.x : c2.y, i & 3);
+            const uint32_t loy = extract_byte(i < 4 ? c2.z : c2.w, i & 3);
+            const uint32_t loz = extract_byte(i < 4 ? c3.x : c3.y, i & 3);
+            const uint32_t hix = extract_byte(i < 4 ? c3.z : c3.w, i & 3);
+            const uint32_t hiy = extract_byte(i < 4 ? c4.x : c4.y, i & 3);
+            const uint32_t hiz = extract_byte(i < 4 ? c4.z : c4.w, i & 3);
+            const float nx = fmaf((float)(negx ? hix : lox), ax, bx);
+            const float fx = fmaf((float)(negx ? lox : hix), ax, bx);
+            const float ny = fmaf((float)(negy ? hiy : loy), ay, by);
+            const float fy = fmaf((float)(negy ? loy : hiy), ay, by);
+            const float nz = fmaf((float)(negz ? hiz : loz), az, bz);
+            const float fz = fmaf((float)(negz ? loz : hiz), az, bz);
+            // a few ulps of slack keep hits on box faces from being culled
+            const float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, s.tnear)) * (1.0f - 2.0e-7f);
+            const float tmax = fminf(fminf(fx, fy), fminf(fz, s.tfar * (1.0f + 2.0e-7f))) * (1.0f + 2.0e-7f);
+            if (tmin <= tmax) {
+                const uint32_t off = meta & 0x1fu;
+                if (off >= 24u) node_hits |= 1u << (24u + ((uint32_t)i ^ s.oct_xor));
+                else prim_hits |= ((meta >> 5) & 7u) << off;
+            }
+        }
+        s.ngroup = make_uint2(c1.x, node_hits | nimask);
+        tgroup = make_uint2(c1.y, prim_hits);
+    } else {
+        tgroup = s.ngroup;
+        s.ngroup = make_uint2(0u, 0u);
+    }
+    while (tgroup.y != 0u) {
+        const int b = __ffs(tgroup.y) - 1;
+        tgroup.y &= tgroup.y - 1u;
+        const float4 *pp = s.prims + (size_t)(tgroup.x + (uint32_t)b) * kPrimF4;
+        const float4 f0 = __ldg(pp + 0), f1 = __ldg(pp + 1);
+        const int prim = __float_as_int(f0.w);
+        if (f1.w == 0.0f) {
+            const float4 f2 = __ldg(pp + 2);
+            float t, u, v;
+            // equal distances go to the lower primitive index
+            if (tri_intersect(V3{f0.x, f0.y, f0.z}, V3{f1.x, f1.y, f1.z}, V3{f2.x, f2.y, f2.z}, s.o, s.d, s.tnear,
+                              s.tfar, t, u, v) &&
+                (t < s.tfar || (!kAny && s.found && prim < s.hit.prim))) {
+                s.found = true;
+                if (kAny) return true;
+                s.tfar = t;
+                s.hit = TraceHit{t, prim, u, v};
+            }
+        } else {
+            const float t = sphere_hit(V3{f0.x, f0.y, f0.z}, f1.x, s.o, s.d, s.tnear, s.tfar);
+            if (t >= 0.0f) {
+                s.found = true;
+                if (kAny) return true;
+                s.tfar = t;
+                s.hit = TraceHit{t, prim, 0.0f, 0.0f};   // sphere uv is recomputed from the hit point
+            }
+        }
+    }
+    if (s.ngroup.y <= 0x00ffffffu) {
+        if (s.sp == 0) return true;
+        s.ngroup = stack[--s.sp];
+    }
+    return false;
+}
+
+// Traces rays [0, n) of a queue.  IO supplies, per ray index r:
+//   const DevBvh &bvh(int r)                  the BVH to trace against
+//   void load(int r, V3 &o, V3 &d, float &tnear, float &tfar)
+//   void store(int r, const Trav &s)          s.found / s.hit hold the result
+// *fetch must be 0 at launch; every warp of the grid must call this.
+template <bool kAny, class IO>
+LJ_D void trace_queue(IO &io, int n, int *fetch, int *status) {
+    const unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint2 stack[kTraversalStack];
+    Trav s;
+    int ray = -1;
+    bool drained = false;   // warp-uniform: the queue has no rays left
+    for (;;) {
+        if (!drained) {
+            const unsigned want = __ballot_sync(kFull, ray < 0);
+            if (want) {
+                const int leader = __ffs(want) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(fetch, __popc(want));
+                base = __shfl_sync(kFull, base, leader);
+                if (ray < 0) {
+                    const int r = base + __popc(want & ((1u << lane) - 1u));
+                    if (r < n) {
+                        V3 o, d;
+                        float tn, tf;
+                        io.load(r, o, d, tn, tf);
+                        trav_init(s, io.bvh(r), o, d, tn, tf);
+                        ray = r;
+                    }
+                }
+                drained = __any_sync(kFull, base + __popc(want) >= n);
+            }
+        }
+        unsigned act = __ballot_sync(kFull, ray >= 0);
+        if (act == 0) break;
+        do {
+            if (ray >= 0 && trav_step<kAny>(s, stack, status)) {
+                io.store(ray, s);
+                ray = -1;
+            }
+            act = __ballot_sync(kFull, ray >= 0);
+        } while (act != 0 && (drained || __popc(act) >= kRefillLanes));
+    }
+}
+
+// Ray queue layouts of the wavefront: rays as two float4 (org|tnear,
+// dir|tfar), hits as float4 (t, prim bits, u, v).
+LJ_D void load_ray(const float4 *rays, int r, V3 &o, V3 &d, float &tn, float &tf) {
+    const float4 r0 = rays[2 * r], r1 = rays[2 * r + 1];
+    o = V3{r0.x, r0.y, r0.z};
+    d = V3{r1.x, r1.y, r1.z};
+    tn = r0.w;
+    tf = r1.w;
+}
+LJ_D float4 hit_record(const Trav &s) {
+    return s.found ? make_float4(s.hit.t, __int_as_float(s.hit.prim), s.hit.u, s.hit.v)
+                   : make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f);
+}
+
+// One scene: closest hits into a hit buffer.
+struct ClosestQueueIO {
+    DevBvh b;
+    const float4 *rays;
+    float4 *hits;
+    LJ_D const DevBvh &bvh(int) const { return b; }
+    LJ_D void load(int r, V3 &o, V3 &d, float &tn, float &tf) const { load_ray(rays, r, o, d, tn, tf); }
+    LJ_D void store(int r, const Trav &s) const { hits[r] = hit_record(s); }
+};
+
+// One scene: shadow rays; an unoccluded ray adds its NEE contribution to its
+// path's radiance (one shadow ray per path per pass, so no two lanes write
+// the same path).
+struct ShadowQueueIO {
+    DevBvh b;
+    const float4 *rays;
+    const int *paths;
+    const float4 *contrib;
+    float4 *L;
+    LJ_D const DevBvh &bvh(int) const { return b; }
+    LJ_D void load(int r, V3 &o, V3 &d, float &tn, float &tf) const { load_ray(rays, r, o, d, tn, tf); }
+    LJ_D void store(int r, const Trav &s) const {
+        if (s.found) return;
+        const int p = paths[r];
+        const float4 c = contrib[r], l = L[p];
+        L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
+    }
+};
+
+}  // namespace lj

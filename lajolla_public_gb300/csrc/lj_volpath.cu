@@ -266,8 +266,9 @@ __global__ void __launch_bounds__(128) k_vol_shade(DevScene sc, VolSoA ps, VolQu
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(q.stats + 2, (unsigned long long)n);
     const float inf = __int_as_float(0x7f800000);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int p = q.path[cur][i];
-        float4 r0 = q.ray[cur][2 * i], r1 = q.ray[cur][2 * i + 1];
+        const int p = (cur ? q.path[1] : q.path[0])[i];
+        const float4 *rays = cur ? q.ray[1] : q.ray[0];
+        float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
         V3 ro{r0.x, r0.y, r0.z}, rd{r1.x, r1.y, r1.z};
         float4 hit = q.hit[i];
         int prim = __float_as_int(hit.y);
@@ -438,9 +439,10 @@ __global__ void __launch_bounds__(128) k_vol_shade(DevScene sc, VolSoA ps, VolQu
         }
         if (alive) {
             int s = queue_slot(q.counts + nxt);
-            q.ray[nxt][2 * s] = make_float4(next_o.x, next_o.y, next_o.z, next_tnear);
-            q.ray[nxt][2 * s + 1] = make_float4(next_d.x, next_d.y, next_d.z, inf);
-            q.path[nxt][s] = p;
+            float4 *nrays = nxt ? q.ray[1] : q.ray[0];
+            nrays[2 * s] = make_float4(next_o.x, next_o.y, next_o.z, next_tnear);
+            nrays[2 * s + 1] = make_float4(next_d.x, next_d.y, next_d.z, inf);
+            (nxt ? q.path[1] : q.path[0])[s] = p;
         }
         ps.beta[p] = make_float4(beta.x, beta.y, beta.z, eta_scale);
         ps.L[p] = make_float4(L.x, L.y, L.z, dir_pdf);

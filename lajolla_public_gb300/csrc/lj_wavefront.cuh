@@ -2,24 +2,49 @@
 // (src/path_tracing.h:7-325), shared by the single-scene renderer
 // (lj_path.cu) and the multi-job server (lj_server.cu).
 //
-// Path state is SoA indexed by path slot; queues hold (ray, path slot)
-// pairs.  The random-number order per path is the reference's: 2 for the
-// screen position, then per bounce 4 for light sampling (uv, light, shape),
-// 3 for BSDF sampling (uv, w), 1 for Russian roulette when applicable.
+// The shade step reads one path's state and hit, and hands the outcome (the
+// next ray, if any, and the NEE shadow ray with its contribution) to a path
+// store, which decides where state lives:
+//   SlotPaths   (single-scene renderer) state in fixed slots, queues carry
+//               slot ids; a finished path's radiance stays in its slot.
+//   the server's store keeps state in queue order instead (lj_server.cu).
+// The random-number order per path is the reference's: 2 for the screen
+// position, then per bounce 4 for light sampling (uv, light, shape), 3 for
+// BSDF sampling (uv, w), 1 for Russian roulette when applicable.
 #pragma once
 
+#include "../../include/lj_gpu.h"
+#include "lj_internal.h"
 #include "lj_shade.cuh"
 
 namespace lj {
 
+// State of one path between two bounces.
+struct PathState {
+    int slot;        // SlotPaths: the path's slot
+    int job;         // server: job table slot
+    int pixel;
+    uint64_t rng;
+    float4 beta;     // xyz: throughput after the pending BSDF sample (beta f / p), w: rr_prob
+    float4 L;        // xyz: radiance, w: eta_scale
+    float4 prev;     // xyz: vertex that sampled the pending ray, w: its BSDF pdf (solid angle)
+    int nv;          // num_vertices of the next loop iteration (2 = primary ray pending)
+};
+
+// Outcome of one shade step besides the updated state.
+struct ShadeOut {
+    bool cont;               // a next ray was sampled
+    float4 ray0, ray1;       // next ray: org | tnear, dir | tfar
+    int shadow;              // the store's handle of this step's shadow ray, -1 if none
+};
+
 struct PathSoA {
-    int *job;        // server: job table slot of the path (unused by the plain renderer)
     int *pixel;
     uint64_t *rng;
-    float4 *beta;    // xyz: throughput after the pending BSDF sample (beta f / p), w: rr_prob
-    float4 *L;       // xyz: radiance, w: eta_scale
-    float4 *prev;    // xyz: vertex that sampled the pending ray, w: its BSDF pdf (solid angle)
-    int *nv;         // num_vertices of the next loop iteration (2 = primary ray pending)
+    float4 *beta;
+    float4 *L;
+    float4 *prev;
+    int *nv;
 };
 
 struct Queues {
@@ -29,9 +54,12 @@ struct Queues {
     float4 *sray;
     int *spath;
     float4 *scontrib;
-    int *retire;                  // server: paths that ended this pass (nullptr: not collected)
-    int *counts;                  // [0], [1]: ray queues, [2]: shadow queue, [3]: retire queue
+    int *counts;                  // [0], [1]: ray queues, [2]: shadow queue
     unsigned long long *stats;    // [0] closest rays, [1] shadow rays, [2] shade segments
+    // select with a branch, not an index: indexing a kernel parameter's
+    // array with a run-time value would copy the whole struct to local memory
+    LJ_HD float4 *rays(int k) const { return k ? ray[1] : ray[0]; }
+    LJ_HD int *paths(int k) const { return k ? path[1] : path[0]; }
 };
 
 // Per-job path options: max_depth / rr_depth as in RenderOptions
@@ -54,36 +82,76 @@ LJ_D int queue_slot(int *counter) {
     return base + __popc(active & ((1u << lane_id()) - 1u));
 }
 
-LJ_D Pcg load_rng(const PathSoA &ps, int p) {
-    Pcg r;
-    r.state = ps.rng[p];
-    r.inc = ((uint64_t)ps.pixel[p] << 1u) | 1u;
-    return r;
-}
+// The single-scene renderer's store: queue cur holds (ray, slot) pairs.
+struct SlotPaths {
+    PathSoA ps;
+    Queues q;
+    int cur;
+    LJ_D void load(int i, PathState &st, float4 &r0, float4 &r1, float4 &hit) const {
+        const int p = q.paths(cur)[i];
+        st.slot = p;
+        st.job = 0;
+        st.pixel = ps.pixel[p];
+        st.rng = ps.rng[p];
+        st.beta = ps.beta[p];
+        st.L = ps.L[p];
+        st.prev = ps.prev[p];
+        st.nv = ps.nv[p];
+        const float4 *rays = q.rays(cur);
+        r0 = rays[2 * i];
+        r1 = rays[2 * i + 1];
+        hit = q.hit[i];
+    }
+    // NEE shadow ray: an unoccluded one adds contrib to the path's radiance
+    LJ_D int shadow(const PathState &st, float4 r0, float4 r1, float4 contrib) const {
+        const int s = queue_slot(q.counts + 2);
+        q.sray[2 * s] = r0;
+        q.sray[2 * s + 1] = r1;
+        q.spath[s] = st.slot;
+        q.scontrib[s] = contrib;
+        return -1;
+    }
+    LJ_D void emit(const PathState &st, const ShadeOut &o) const {
+        const int p = st.slot;
+        ps.L[p] = st.L;
+        ps.rng[p] = st.rng;
+        if (o.cont) {
+            ps.beta[p] = st.beta;
+            ps.prev[p] = st.prev;
+            ps.nv[p] = st.nv;
+            const int nxt = cur ^ 1;
+            const int s = queue_slot(q.counts + nxt);
+            float4 *rays = q.rays(nxt);
+            rays[2 * s] = o.ray0;
+            rays[2 * s + 1] = o.ray1;
+            q.paths(nxt)[s] = p;
+        }
+    }
+};
 
-
-
-// One queue entry: the hit of path q.path[cur][i] -> emission (with MIS for
-// BSDF-sampled hits), Russian roulette, NEE (shadow ray queued with its
-// contribution), BSDF sample -> next ray in queue cur ^ 1.
-LJ_D void shade_segment(const DevScene &sc, const PathSoA &ps, const Queues &q, int cur, int i,
-                        const ShadeCfg &cfg, int *status) {
-    const int nxt = cur ^ 1;
-    const int p = q.path[cur][i];
-    float4 r0 = q.ray[cur][2 * i], r1 = q.ray[cur][2 * i + 1];
-    V3 ro{r0.x, r0.y, r0.z}, rd{r1.x, r1.y, r1.z};
-    float4 hit = q.hit[i];
-    int prim = __float_as_int(hit.y);
-    int nv = ps.nv[p];
-    float4 Lw = ps.L[p];
-    V3 L{Lw.x, Lw.y, Lw.z};
-    float eta_scale = Lw.w;
-    float4 bw = ps.beta[p];
-    V3 beta{bw.x, bw.y, bw.z};
+// One queue entry: the hit of a path -> emission (with MIS for BSDF-sampled
+// hits), Russian roulette, NEE (a shadow ray with its contribution), BSDF
+// sample -> the next ray.
+// kMats: the material types the scenes can hold (kAllMats: any).
+template <uint32_t kMats, class Paths>
+LJ_D void shade_segment(const DevScene &sc, const Paths &paths, int i, const ShadeCfg &cfg, int *status) {
+    PathState st;
+    float4 r0, r1, hit;
+    paths.load(i, st, r0, r1, hit);
+    ShadeOut out;
+    out.cont = false;
+    out.shadow = -1;
+    const V3 ro{r0.x, r0.y, r0.z}, rd{r1.x, r1.y, r1.z};
+    const int prim = __float_as_int(hit.y);
+    int nv = st.nv;
+    V3 L{st.L.x, st.L.y, st.L.z};
+    float eta_scale = st.L.w;
+    V3 beta{st.beta.x, st.beta.y, st.beta.z};
     const bool primary = nv == 2;
-    Pcg rng = load_rng(ps, p);
+    Pcg rng;
+    rng.state = st.rng;
+    rng.inc = ((uint64_t)st.pixel << 1u) | 1u;
     bool alive = true;
-    bool continued = false;
 
     if (prim < 0) {
         // miss: environment map (path_tracing.h:17-28, :284-302)
@@ -92,8 +160,7 @@ LJ_D void shade_segment(const DevScene &sc, const PathSoA &ps, const Queues &q, 
             if (primary) {
                 L += Le;
             } else {
-                float4 pv = ps.prev[p];
-                float p2 = pv.w;   // G = 1 for directions at infinity
+                float p2 = st.prev.w;   // G = 1 for directions at infinity
                 float p1 = __ldg(sc.light_pmf + sc.env.light_id) * env_pdf(sc, rd);
                 float w2 = (p2 * p2) / (p1 * p1 + p2 * p2);
                 L += beta * Le * w2;
@@ -107,14 +174,13 @@ LJ_D void shade_segment(const DevScene &sc, const PathSoA &ps, const Queues &q, 
             beta = V3{1.0f, 1.0f, 1.0f};
             nv = 3;
         } else {
-            float4 pv = ps.prev[p];
-            V3 prev_p{pv.x, pv.y, pv.z};
+            V3 prev_p{st.prev.x, st.prev.y, st.prev.z};
             if (vx.light >= 0) {
                 // BSDF-sampled hit on an area light (path_tracing.h:268-283)
                 V3 Le = light_emission(sc, vx.light, -rd, PN{vx.p, vx.ng});
                 V3 dv = vx.p - prev_p;
                 float G = fabsf(dot(rd, vx.ng)) / dot(dv, dv);
-                float p2 = pv.w * G;
+                float p2 = st.prev.w * G;
                 float p1 = __ldg(sc.light_pmf + vx.light) *
                            pdf_point_on_light(sc, vx.light, PN{vx.p, vx.ng}, prev_p);
                 float w2 = (p2 * p2) / (p1 * p1 + p2 * p2);
@@ -124,7 +190,7 @@ LJ_D void shade_segment(const DevScene &sc, const PathSoA &ps, const Queues &q, 
             // (path_tracing.h:311-318): that iteration's num_vertices is nv - 1
             float rr = 1.0f;
             if (nv - 2 >= cfg.rr_depth) {
-                rr = bw.w;
+                rr = st.beta.w;
                 if (pcg_uniform(rng) > rr) alive = false;
             }
             beta = beta * (1.0f / rr);
@@ -135,7 +201,7 @@ LJ_D void shade_segment(const DevScene &sc, const PathSoA &ps, const Queues &q, 
             alive = false;
         }
         if (alive) {
-            MatParams mat = resolve_material(sc, vx.material, vx.u, vx.v, vx.uv_screen_size);
+            MatParams mat = resolve_material<kMats>(sc, vx.material, vx.u, vx.v, vx.uv_screen_size);
             BsdfVertex bv{vx.ng, vx.frame};
             V3 wv = -rd;
             // ---- next event estimation (path_tracing.h:98-207) ----
@@ -163,50 +229,38 @@ LJ_D void shade_segment(const DevScene &sc, const PathSoA &ps, const Queues &q, 
             }
             if (lid >= 0) p1 = __ldg(sc.light_pmf + lid) * pdf_point_on_light(sc, lid, pl, vx.p);
             if (G > 0.0f && p1 > 0.0f) {
-                V3 f = bsdf_eval(mat, bv, wv, dl);
+                V3 f = bsdf_eval<kMats>(mat, bv, wv, dl);
                 V3 Le = light_emission(sc, lid, -dl, pl);
-                float p2 = bsdf_pdf(mat, bv, wv, dl) * G;
+                float p2 = bsdf_pdf<kMats>(mat, bv, wv, dl) * G;
                 float w1 = (p1 * p1) / (p1 * p1 + p2 * p2);
                 V3 c = beta * f * Le * (G * w1 / p1);
-                if (c.x > 0.0f || c.y > 0.0f || c.z > 0.0f) {
-                    int s = queue_slot(q.counts + 2);
-                    q.sray[2 * s] = make_float4(vx.p.x, vx.p.y, vx.p.z, sc.eps);
-                    q.sray[2 * s + 1] = make_float4(dl.x, dl.y, dl.z, tmax);
-                    q.spath[s] = p;
-                    q.scontrib[s] = make_float4(c.x, c.y, c.z, 0.0f);
-                }
+                if (c.x > 0.0f || c.y > 0.0f || c.z > 0.0f)
+                    out.shadow = paths.shadow(st, make_float4(vx.p.x, vx.p.y, vx.p.z, sc.eps),
+                                              make_float4(dl.x, dl.y, dl.z, tmax), make_float4(c.x, c.y, c.z, 0.0f));
             }
             // ---- BSDF sampling (path_tracing.h:210-256) ----
             float bu0 = pcg_uniform(rng), bu1 = pcg_uniform(rng), bwr = pcg_uniform(rng);
-            BsdfSample bs = bsdf_sample(mat, bv, wv, bu0, bu1, bwr);
-            if (!bs.valid) {
-                alive = false;
-            } else {
-                V3 f = bsdf_eval(mat, bv, wv, bs.dir);
-                float pdf = bsdf_pdf(mat, bv, wv, bs.dir);
-                if (!(pdf > 0.0f)) {
-                    alive = false;
-                } else {
+            BsdfSample bs = bsdf_sample<kMats>(mat, bv, wv, bu0, bu1, bwr);
+            if (bs.valid) {
+                V3 f = bsdf_eval<kMats>(mat, bv, wv, bs.dir);
+                float pdf = bsdf_pdf<kMats>(mat, bv, wv, bs.dir);
+                if (pdf > 0.0f) {
                     if (bs.eta != 0.0f) eta_scale /= (bs.eta * bs.eta);
                     float rr_prob = fminf(max3(beta) / eta_scale, 0.95f);
                     V3 bn = beta * f / pdf;
-                    ps.beta[p] = make_float4(bn.x, bn.y, bn.z, rr_prob);
-                    ps.prev[p] = make_float4(vx.p.x, vx.p.y, vx.p.z, pdf);
-                    ps.nv[p] = nv + 1;
-                    int s = queue_slot(q.counts + nxt);
-                    q.ray[nxt][2 * s] = make_float4(vx.p.x, vx.p.y, vx.p.z, sc.eps);
-                    q.ray[nxt][2 * s + 1] = make_float4(bs.dir.x, bs.dir.y, bs.dir.z, __int_as_float(0x7f800000));
-                    q.path[nxt][s] = p;
-                    continued = true;
+                    st.beta = make_float4(bn.x, bn.y, bn.z, rr_prob);
+                    st.prev = make_float4(vx.p.x, vx.p.y, vx.p.z, pdf);
+                    st.nv = nv + 1;
+                    out.cont = true;
+                    out.ray0 = make_float4(vx.p.x, vx.p.y, vx.p.z, sc.eps);
+                    out.ray1 = make_float4(bs.dir.x, bs.dir.y, bs.dir.z, __int_as_float(0x7f800000));
                 }
             }
         }
     }
-    ps.L[p] = make_float4(L.x, L.y, L.z, eta_scale);
-    ps.rng[p] = rng.state;
-    // a finished path: the server's retire step accumulates it once its
-    // pending shadow ray (if any) has been traced
-    if (!continued && q.retire) q.retire[queue_slot(q.counts + 3)] = p;
+    st.L = make_float4(L.x, L.y, L.z, eta_scale);
+    st.rng = rng.state;
+    paths.emit(st, out);
 }
 
 }  // namespace lj

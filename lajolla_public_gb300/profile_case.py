@@ -1,0 +1,114 @@
+"""Small, repeatable GPU cases for profiling, and a summary of ncu launch lists.
+
+    python -m lajolla_public_gb300.profile_case run CASE [--warmup W] [--repeat R]
+    python -m lajolla_public_gb300.profile_case summarize LAUNCHES.csv
+
+`run` renders one named case W + R times (plain single-scene renderer unless
+the case says otherwise) and prints the device time of the last render with
+its per-kernel-class split; it is meant to run under `ncu -k ... -s ... -c ...`
+with a capture of a few launches.
+
+Cases:
+  cbox          seeded Cornell box, 256x256, 64 spp, max depth 6
+  terrain       seeded terrain + 16 icospheres + envmap, 1.26M triangles,
+                512x512, 16 spp, max depth 8
+  terrain_srv   the terrain case as one server job (server kernels)
+
+`summarize` reads the CSV that `ncu --metrics gpu__time_duration.sum --csv
+--log-file F` writes and prints launches, total time and share per kernel.
+"""
+import argparse
+import csv
+import sys
+import time
+from collections import OrderedDict
+
+import numpy as np
+
+from . import abi, scenes
+
+
+def make_case(name):
+    if name == "cbox":
+        return scenes.cornell_box(seed=0, width=256, height=256, spp=64, max_depth=6)
+    if name in ("terrain", "terrain_srv"):
+        return scenes.resized_terrain_scene(seed=5, n_tris=1261476, width=512, height=512, spp=16, max_depth=8)
+    raise SystemExit("unknown case %r" % name)
+
+
+def run(args):
+    import torch
+    from . import gpu
+    sc = make_case(args.case)
+    ctx = gpu.Context(0)
+    g = gpu.GpuScene(ctx, sc)
+    n = sc.width * sc.height * 3
+    if args.case.endswith("_srv"):
+        opts = gpu.server_options(path_pool=args.pool, block_size=args.block, use_graphs=not args.profile,
+                                  profile=args.profile)
+        with gpu.Server(ctx, opts) as srv:
+            for i in range(args.warmup + args.repeat):
+                t0 = time.perf_counter()
+                srv.wait(srv.submit(g, seed=i), timeout=600)
+                dt = time.perf_counter() - t0
+            st = srv.stats()
+        cls = {abi.KERNEL_CLASS_NAMES[c]: round(st.class_ms[c] / (args.warmup + args.repeat), 3)
+               for c in range(abi.LJ_KERNEL_CLASSES)}
+        print("%s: %d samples, last job %.2f ms (host clock), pool %d block %d, per-job classes %s"
+              % (args.case, sc.width * sc.height * sc.spp, dt * 1e3, args.pool, args.block, cls))
+    else:
+        out = torch.empty(n, dtype=torch.float32, device="cuda")
+        stream = torch.cuda.current_stream().cuda_stream
+        st = None
+        for i in range(args.warmup + args.repeat):
+            st = g.render_device(out, seed=i, stream=stream, stats=True, profile=True)
+        cls = {abi.KERNEL_CLASS_NAMES[c]: round(st.class_ms[c], 3) for c in range(abi.LJ_KERNEL_CLASSES)}
+        print("%s: %d samples, %.2f ms, %.1f Msamples/s, closest %d shadow %d, classes %s"
+              % (args.case, st.samples, st.device_ms, st.samples / st.device_ms / 1e3, st.rays_closest,
+                 st.rays_shadow, cls))
+    g.close()
+    ctx.close()
+
+
+def summarize(args):
+    tot = OrderedDict()
+    with open(args.csv, newline="") as f:
+        lines = [l for l in f if l.startswith('"')]
+    for row in csv.DictReader(lines):
+        if row.get("Metric Name") != "gpu__time_duration.sum":
+            continue
+        name = row["Kernel Name"].split("(")[0].replace("lj::<unnamed>::", "").replace("lj::", "")
+        v = float(row["Metric Value"].replace(",", ""))
+        unit = row.get("Metric Unit", "ns")
+        us = v / 1e3 if unit == "ns" else (v * 1e3 if unit == "msecond" else v)
+        n, t = tot.get(name, (0, 0.0))
+        tot[name] = (n + 1, t + us)
+    total = sum(t for _, t in tot.values()) or 1.0
+    print("%-44s %9s %13s %7s" % ("kernel", "launches", "total_us", "share"))
+    for name, (n, t) in sorted(tot.items(), key=lambda kv: -kv[1][1]):
+        short = name if len(name) <= 44 else name[:41] + "..."
+        print("%-44s %9d %13.1f %6.1f%%" % (short, n, t, 100.0 * t / total))
+    print("%-44s %9d %13.1f" % ("TOTAL", sum(n for n, _ in tot.values()), total))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    r = sub.add_parser("run")
+    r.add_argument("case")
+    r.add_argument("--warmup", type=int, default=1)
+    r.add_argument("--repeat", type=int, default=1)
+    r.add_argument("--pool", type=int, default=1 << 22, help="server path pool")
+    r.add_argument("--block", type=int, default=128, help="server block size")
+    r.add_argument("--profile", action="store_true", help="server: time each kernel class")
+    s = sub.add_parser("summarize")
+    s.add_argument("csv")
+    args = ap.parse_args(argv)
+    if args.cmd == "run":
+        run(args)
+    else:
+        summarize(args)
+
+
+if __name__ == "__main__":
+    main()
