@@ -331,6 +331,12 @@ int lj_gpu_trace_any(lj_scene *scene, const lj_ray *d_rays, uint8_t *d_occluded,
 /* Maps a global primitive index to (shape id, primitive id within shape). */
 int lj_gpu_prim_to_shape(lj_scene *scene, int32_t prim, int32_t *shape_id,
                          int32_t *local_prim);
+/* Primitive index of every leaf record of the scene's BVH, in leaf order
+ * (host array of capacity entries; *count = number of records; out = NULL
+ * only reports the count).  For structural checks (every primitive exactly
+ * once).  No reference counterpart. */
+int lj_gpu_bvh_leaf_prims(lj_scene *scene, int32_t *out, int64_t capacity, int64_t *count);
+
 /* Instrumented traversal (a separate, slower kernel; for byte accounting):
  * for n rays, the total number of 80-byte wide nodes fetched and 48-byte leaf
  * primitive records tested by closest-hit (any_hit = 0) or any-hit traversal.
@@ -442,6 +448,7 @@ typedef struct lj_server_options {
     int32_t pad;
 } lj_server_options;
 #define LJ_SERVER_PROFILE 1
+#define LJ_SERVER_ONE_SHADE_KERNEL 2   /* every job through the all-materials shade kernel */
 
 typedef struct lj_job_desc {
     uint64_t seed;               /* RNG key, as lj_render_params.seed                      */

@@ -168,6 +168,7 @@ class lj_bsdf_batch(C.Structure):
 
 LJ_SCHED_FIFO, LJ_SCHED_SRPT = 0, 1
 LJ_SERVER_PROFILE = 1
+LJ_SERVER_ONE_SHADE_KERNEL = 2
 LJ_JOB_QUEUED, LJ_JOB_RUNNING, LJ_JOB_DONE, LJ_JOB_FAILED, LJ_JOB_CANCELLED = range(5)
 
 

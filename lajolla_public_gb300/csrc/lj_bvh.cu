@@ -9,9 +9,10 @@
 //   2. 30-bit Morton codes of centroids over the centroid box
 //   3. stable LSD radix sort of (code, primitive) -- 4 passes of 8 bits,
 //      warp-match ranking, no library sort
-//   4. Karras (HPG 2012) binary radix tree: one thread per internal node
-//   5. bottom-up boxes (atomic arrival counters, L2-coherent loads)
-//   6. level-synchronous collapse into the compressed 8-wide layout of
+//   4. binary tree by PLOC clustering over the Morton order (Meister and
+//      Bittner 2018; below), or -- BvhInput::karras -- the Karras (HPG 2012)
+//      radix tree with bottom-up boxes (atomic arrival counters)
+//   5. level-synchronous collapse into the compressed 8-wide layout of
 //      lj_scene.cuh: greedy largest-area child expansion, octant slot
 //      assignment, 8-bit conservative quantization, leaves of <= 3 primitives
 //      stored contiguously in leaf order.
@@ -266,6 +267,189 @@ __global__ void k_bottom_up(int n, const int2 *child, const int *parent_int, con
     }
 }
 
+// ---- PLOC: parallel locally-ordered clustering ------------------------------
+// Meister and Bittner, "Parallel Locally-Ordered Clustering for Bounding
+// Volume Hierarchy Construction" (IEEE TVCG 2018).  Clusters start as the
+// Morton-sorted primitives; each round every cluster finds, among the
+// kPlocRadius clusters on either side in the current (Morton-ordered) array,
+// the one whose union box has the least surface area (ties: lower index);
+// mutual nearest neighbours merge into a new binary node, and the array is
+// compacted in order.  The result is a binary tree of near-SAH quality, in
+// the same child / range / box arrays the Karras tree fills, so the collapse
+// below serves both; range holds (0, primitives - 1) here.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocBlock = 256;
+
+struct PlocClusters {
+    int *id;          // binary node id, or ~sorted position for a primitive
+    float4 *lo, *hi;
+    int *cnt;         // primitives below
+};
+
+__device__ __forceinline__ float union_half_area(float4 l0, float4 h0, float4 l1, float4 h1) {
+    float dx = fmaxf(h0.x, h1.x) - fminf(l0.x, l1.x);
+    float dy = fmaxf(h0.y, h1.y) - fminf(l0.y, l1.y);
+    float dz = fmaxf(h0.z, h1.z) - fminf(l0.z, l1.z);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void k_ploc_init(const uint32_t *sorted, const float4 *plo, const float4 *phi, int n, PlocClusters c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t g = sorted[i];
+    c.id[i] = ~i;
+    c.lo[i] = plo[g];
+    c.hi[i] = phi[g];
+    c.cnt[i] = 1;
+}
+
+__global__ void __launch_bounds__(kPlocBlock) k_ploc_nn(PlocClusters c, int count, int *nn) {
+    __shared__ float4 slo[kPlocBlock + 2 * kPlocRadius], shi[kPlocBlock + 2 * kPlocRadius];
+    const int base = blockIdx.x * kPlocBlock - kPlocRadius;
+    for (int k = threadIdx.x; k < kPlocBlock + 2 * kPlocRadius; k += kPlocBlock) {
+        int g = base + k;
+        if (g >= 0 && g < count) {
+            slo[k] = c.lo[g];
+            shi[k] = c.hi[g];
+        }
+    }
+    __syncthreads();
+    const int i = blockIdx.x * kPlocBlock + threadIdx.x;
+    if (i >= count) return;
+    const float4 l = slo[i - base], h = shi[i - base];
+    float best = __int_as_float(0x7f800000);
+    int bj = -1;
+    const int j0 = max(0, i - kPlocRadius), j1 = min(count - 1, i + kPlocRadius);
+    for (int j = j0; j <= j1; j++) {
+        if (j == i) continue;
+        float cost = union_half_area(l, h, slo[j - base], shi[j - base]);
+        if (cost < best) {   // ascending j: equal costs keep the lower index
+            best = cost;
+            bj = j;
+        }
+    }
+    if (bj < 0) bj = i > 0 ? i - 1 : min(i + 1, count - 1);   // non-finite boxes: still progress
+    nn[i] = bj;
+}
+
+// flags[i] = (keep, merge): i merges with its partner j > i; j disappears.
+__global__ void k_ploc_flags(const int *nn, int count, int2 *flags) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    int j = nn[i];
+    bool mutual = j != i && nn[j] == i;
+    flags[i] = make_int2(mutual && j < i ? 0 : 1, mutual && i < j ? 1 : 0);
+}
+
+// Exclusive scan of int2 (two independent sums), 1024 elements per block.
+constexpr int kScanBlock = 256, kScanItems = 4, kScanTile = kScanBlock * kScanItems;
+__global__ void __launch_bounds__(kScanBlock) k_scan2_tiles(const int2 *in, int2 *out, int n, int2 *tile_sums) {
+    __shared__ int2 warp_sums[kScanBlock / 32];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int2 v[kScanItems];
+    int2 run = make_int2(0, 0);
+    for (int k = 0; k < kScanItems; k++) {
+        int2 x = base + k < n ? in[base + k] : make_int2(0, 0);
+        v[k] = run;
+        run.x += x.x;
+        run.y += x.y;
+    }
+    // warp-inclusive scan of the thread totals
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int2 incl = run;
+    for (int o = 1; o < 32; o <<= 1) {
+        int ax = __shfl_up_sync(0xffffffffu, incl.x, o), ay = __shfl_up_sync(0xffffffffu, incl.y, o);
+        if (lane >= o) {
+            incl.x += ax;
+            incl.y += ay;
+        }
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    int2 woff = make_int2(0, 0);
+    for (int w = 0; w < warp; w++) {
+        woff.x += warp_sums[w].x;
+        woff.y += warp_sums[w].y;
+    }
+    const int2 toff = make_int2(woff.x + incl.x - run.x, woff.y + incl.y - run.y);
+    for (int k = 0; k < kScanItems; k++)
+        if (base + k < n) out[base + k] = make_int2(v[k].x + toff.x, v[k].y + toff.y);
+    if (threadIdx.x == kScanBlock - 1) tile_sums[blockIdx.x] = make_int2(toff.x + run.x, toff.y + run.y);
+}
+// one block of 1024 threads: exclusive scan of the tile sums in place,
+// total in sums[tiles]
+__global__ void __launch_bounds__(1024) k_scan2_sums(int2 *sums, int tiles) {
+    __shared__ int2 wsum[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int2 carry = make_int2(0, 0);
+    for (int base = 0; base < tiles; base += 1024) {
+        const int t = base + threadIdx.x;
+        const int2 x = t < tiles ? sums[t] : make_int2(0, 0);
+        int2 incl = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            int ax = __shfl_up_sync(0xffffffffu, incl.x, o), ay = __shfl_up_sync(0xffffffffu, incl.y, o);
+            if (lane >= o) {
+                incl.x += ax;
+                incl.y += ay;
+            }
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        int2 woff = make_int2(0, 0);
+        for (int w = 0; w < warp; w++) {
+            woff.x += wsum[w].x;
+            woff.y += wsum[w].y;
+        }
+        int2 total = make_int2(0, 0);
+        for (int w = 0; w < 32; w++) {
+            total.x += wsum[w].x;
+            total.y += wsum[w].y;
+        }
+        if (t < tiles) sums[t] = make_int2(carry.x + woff.x + incl.x - x.x, carry.y + woff.y + incl.y - x.y);
+        carry.x += total.x;
+        carry.y += total.y;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) sums[tiles] = carry;
+}
+__global__ void k_scan2_add(int2 *out, int n, const int2 *tile_sums) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int2 o = tile_sums[i / kScanTile], v = out[i];
+    out[i] = make_int2(v.x + o.x, v.y + o.y);
+}
+
+__global__ void k_ploc_compact(PlocClusters in, PlocClusters out, const int *nn, const int2 *flags,
+                               const int2 *prefix, int count, int node_base, int2 *child, int2 *range,
+                               float4 *nlo, float4 *nhi) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int2 f = flags[i];
+    if (!f.x) return;
+    const int dst = prefix[i].x;
+    if (f.y) {
+        const int j = nn[i];
+        const int id = node_base - prefix[i].y;
+        const float4 l0 = in.lo[i], h0 = in.hi[i], l1 = in.lo[j], h1 = in.hi[j];
+        const float4 l = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), 0.0f);
+        const float4 h = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), 0.0f);
+        const int cnt = in.cnt[i] + in.cnt[j];
+        child[id] = make_int2(in.id[i], in.id[j]);
+        range[id] = make_int2(0, cnt - 1);
+        nlo[id] = l;
+        nhi[id] = h;
+        out.id[dst] = id;
+        out.lo[dst] = l;
+        out.hi[dst] = h;
+        out.cnt[dst] = cnt;
+    } else {
+        out.id[dst] = in.id[i];
+        out.lo[dst] = in.lo[i];
+        out.hi[dst] = in.hi[i];
+        out.cnt[dst] = in.cnt[i];
+    }
+}
+
 // ---- collapse to the compressed 8-wide layout ----------------------------
 struct CollapseArgs {
     const int2 *child;      // binary internal nodes
@@ -444,7 +628,21 @@ __global__ void k_collapse(CollapseArgs a) {
         } else {
             uint32_t unary = c.count == 1 ? 1u : (c.count == 2 ? 3u : 7u);
             meta[s] = (unary << 5) | (uint32_t)prim_off;
-            for (int m = 0; m < c.count; m++) write_prim(a, c.first + m, prim_base + prim_off + m);
+            // the subtree's primitives, left to right (a walk of at most 2
+            // internal nodes: Karras subtrees are contiguous, PLOC ones need not be)
+            int todo[4], nt = 0, m = 0;
+            todo[nt++] = c.enc;
+            while (nt > 0 && m < c.count) {
+                const int e = todo[--nt];
+                if (e < 0) {
+                    write_prim(a, ~e, prim_base + prim_off + m);
+                    m++;
+                } else if (nt + 2 <= 4) {
+                    const int2 ce = a.child[e];
+                    todo[nt++] = ce.y;
+                    todo[nt++] = ce.x;
+                }
+            }
             prim_off += c.count;
         }
     }
@@ -607,7 +805,54 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
     LJ_CUDA_TRY(cudaMemsetAsync(parent_int, 0xff, sizeof(int) * ni, s));
     LJ_CUDA_TRY(cudaMemsetAsync(parent_leaf, 0xff, sizeof(int) * n, s));
     LJ_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(uint32_t) * ni, s));
-    if (n > 1) {
+    if (n > 1 && !in.karras) {
+        // PLOC rounds; each round reads its cluster count back (a few dozen rounds)
+        PlocClusters cl[2];
+        int *nn;
+        int2 *pflags, *prefix, *tsums;
+        const int tiles_max = (n + kScanTile - 1) / kScanTile;
+        for (int k = 0; k < 2; k++) {
+            LJ_CUDA_TRY(cudaMallocAsync(&cl[k].id, sizeof(int) * n, s));
+            LJ_CUDA_TRY(cudaMallocAsync(&cl[k].lo, sizeof(float4) * n, s));
+            LJ_CUDA_TRY(cudaMallocAsync(&cl[k].hi, sizeof(float4) * n, s));
+            LJ_CUDA_TRY(cudaMallocAsync(&cl[k].cnt, sizeof(int) * n, s));
+        }
+        LJ_CUDA_TRY(cudaMallocAsync(&nn, sizeof(int) * n, s));
+        LJ_CUDA_TRY(cudaMallocAsync(&pflags, sizeof(int2) * n, s));
+        LJ_CUDA_TRY(cudaMallocAsync(&prefix, sizeof(int2) * n, s));
+        LJ_CUDA_TRY(cudaMallocAsync(&tsums, sizeof(int2) * (tiles_max + 1), s));
+        k_ploc_init<<<grid_for(n, 256), 256, 0, s>>>(idx, plo, phi, n, cl[0]);
+        int count = n, merged = 0, c = 0;
+        for (int round = 0; round < 1 << 16 && count > 1; round++) {
+            const int tiles = (count + kScanTile - 1) / kScanTile;
+            k_ploc_nn<<<grid_for(count, kPlocBlock), kPlocBlock, 0, s>>>(cl[c], count, nn);
+            k_ploc_flags<<<grid_for(count, 256), 256, 0, s>>>(nn, count, pflags);
+            k_scan2_tiles<<<tiles, kScanBlock, 0, s>>>(pflags, prefix, count, tsums);
+            k_scan2_sums<<<1, 1024, 0, s>>>(tsums, tiles);
+            k_scan2_add<<<grid_for(count, 256), 256, 0, s>>>(prefix, count, tsums);
+            k_ploc_compact<<<grid_for(count, 256), 256, 0, s>>>(cl[c], cl[c ^ 1], nn, pflags, prefix, count,
+                                                                 n - 2 - merged, child, range, nlo, nhi);
+            int2 tot;
+            LJ_CUDA_TRY(cudaMemcpyAsync(&tot, tsums + tiles, sizeof(int2), cudaMemcpyDeviceToHost, s));
+            LJ_CUDA_TRY(cudaStreamSynchronize(s));
+            if (tot.y <= 0) {
+                if (err) *err = "BVH build: a clustering round merged nothing";
+                return -5;
+            }
+            merged += tot.y;
+            count = tot.x;
+            c ^= 1;
+        }
+        for (int k = 0; k < 2; k++) {
+            cudaFreeAsync(cl[k].id, s); cudaFreeAsync(cl[k].lo, s); cudaFreeAsync(cl[k].hi, s);
+            cudaFreeAsync(cl[k].cnt, s);
+        }
+        cudaFreeAsync(nn, s); cudaFreeAsync(pflags, s); cudaFreeAsync(prefix, s); cudaFreeAsync(tsums, s);
+        if (merged != n - 1) {
+            if (err) *err = "BVH build: clustering left " + std::to_string(n - merged) + " roots";
+            return -5;
+        }
+    } else if (n > 1) {
         k_karras<<<grid_for(n - 1, 256), 256, 0, s>>>(codes, n, child, range, parent_int, parent_leaf);
         k_bottom_up<<<grid_for(n, 256), 256, 0, s>>>(n, child, parent_int, parent_leaf, idx, plo, phi,
                                                       nlo, nhi, flags);

@@ -640,6 +640,26 @@ int lj_gpu_prim_to_shape(lj_scene *sc, int32_t prim, int32_t *shape_id, int32_t 
     return LJ_OK;
 }
 
+int lj_gpu_bvh_leaf_prims(lj_scene *sc, int32_t *out, int64_t capacity, int64_t *count) {
+    if (!sc || !count) return LJ_ERR_INVALID_ARG;
+    const int64_t n = sc->dev.bvh.num_leaf_prims;
+    *count = n;
+    if (!out) return LJ_OK;
+    if (capacity < n) return set_error(sc->ctx, LJ_ERR_SIZE_LIMIT, "bvh_leaf_prims: capacity below the primitive count");
+    if (n == 0) return LJ_OK;
+    cudaSetDevice(sc->ctx->device);
+    std::vector<float4> rec((size_t)n * kPrimF4);
+    if (cudaMemcpy(rec.data(), sc->dev.bvh.prims, sizeof(float4) * rec.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return set_error(sc->ctx, LJ_ERR_CUDA, "bvh_leaf_prims: copy failed");
+    for (int64_t i = 0; i < n; i++) {
+        float w = rec[(size_t)i * kPrimF4].w;
+        int32_t id;
+        memcpy(&id, &w, sizeof(id));
+        out[i] = id;
+    }
+    return LJ_OK;
+}
+
 static int check_status(lj_ctx *ctx, cudaStream_t s, const char *what) {
     int st = 0;
     if (cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||

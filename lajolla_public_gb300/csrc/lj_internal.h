@@ -48,6 +48,7 @@ struct BvhInput {
     const int *tri_vidx;    // device, 3 per triangle
     const float *spheres;   // device, 4 floats (c, r) per sphere (prims num_tris ..)
     int num_tris, num_spheres;
+    int karras = 0;         // 1: Karras radix tree over the Morton order, 0: PLOC clustering
 };
 struct BvhOutput {
     uint4 *nodes = nullptr;     // device, owned by the scene

@@ -59,7 +59,15 @@ struct SrvJob {
     int max_depth, rr_depth;
     float spread0;
     float clamp;                 // |sample| bound that keeps the sums inside int64
+    int mclass;                  // 0: materials of kClassicMats only, 1: any (shade kernel instance)
+    int pad;
 };
+
+// Material classes of the server's two shade kernel instances.  A queue
+// holds class-0 paths from its front and class-1 paths from its back, so
+// each instance reads a contiguous range.
+constexpr uint32_t kClassicMats =
+    (1u << LJ_MAT_LAMBERTIAN) | (1u << LJ_MAT_ROUGHPLASTIC) | (1u << LJ_MAT_ROUGHDIELECTRIC);
 
 struct SrvCtr {
     unsigned long long issued, done, dropped, pad;
@@ -92,8 +100,13 @@ struct SrvDev {
     float4 *scontrib;
     int *rjob, *rpixel;          // finished paths
     float4 *rL;
-    int *counts;                 // [0],[1] queues, [2] shadow, [3] retire, [5] regen count,
-                                 // [6] regen base, [8],[9] ray fetch counters
+    int *counts;                 // [0],[1] class-0 entries (front) of queue 0 / 1, [2] shadow,
+                                 // [3] retire, [5] regen count, [8],[9] ray fetch counters,
+                                 // [10],[11] class-1 entries (back) of queue 0 / 1
+    // queue position of the k-th entry of class 1 (filled from the back)
+    LJ_D int back(int k) const { return P - 1 - k; }
+    // position of ray r of a queue with n0 class-0 entries
+    LJ_D int entry(int r, int n0) const { return r < n0 ? r : back(r - n0); }
     unsigned long long *stats;   // [0] closest rays, [1] shadow rays, [2] shade segments
     int P;                       // queue capacity
     int *status;
@@ -105,8 +118,8 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
     const int lane = threadIdx.x;
     int *counts = d.counts;
     const int n_order = d.order[0];
-    const int c = counts[cur];                   // paths that continue into this wave
-    const long long freec = (long long)d.P - c;   // room for new paths
+    const int c = counts[cur] + counts[10 + cur];   // paths that continue into this wave
+    const long long freec = (long long)d.P - c;      // room for new paths
     long long carry = 0;
     for (int base = 0; base < n_order; base += 32) {
         const int k = base + lane;
@@ -135,9 +148,8 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
         const long long take = min(carry, freec);
         d.plan_off[n_order] = (int)take;
         counts[5] = (int)take;
-        counts[6] = c;
-        counts[cur] = c + (int)take;
         counts[cur ^ 1] = 0;
+        counts[10 + (cur ^ 1)] = 0;
         counts[2] = 0;
         counts[3] = 0;
         counts[8] = 0;
@@ -148,7 +160,6 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
 template <int B>
 __global__ void __launch_bounds__(B) k_srv_regen(SrvDev d, int cur) {
     const int n = d.counts[5];
-    const int base = d.counts[6];   // new paths go after the continuing ones
     const int n_order = d.order[0];
     const StateSoA &q = d.buf[cur];
     for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
@@ -175,7 +186,8 @@ __global__ void __launch_bounds__(B) k_srv_regen(SrvDev d, int cur) {
         float r1 = pcg_uniform(rng), r2 = pcg_uniform(rng);
         V3 o, dir;
         camera_ray(jb.cam, (x + r1) / jb.cam.w, (y + r2) / jb.cam.h, o, dir);
-        const int s = base + i;
+        // appended after the paths that continue into this wave
+        const int s = jb.mclass == 0 ? queue_slot(d.counts + cur) : d.back(queue_slot(d.counts + 10 + cur));
         q.job[s] = j;
         q.pixel[s] = pixel;
         q.rng[s] = rng.state;
@@ -191,10 +203,12 @@ __global__ void __launch_bounds__(B) k_srv_regen(SrvDev d, int cur) {
 // Ray queues of the server: each ray uses the BVH of its path's job's scene.
 struct SrvClosestIO {
     const SrvDev &d;
-    int cur;
-    LJ_D const DevBvh &bvh(int r) const { return d.scenes[d.jobs[d.buf[cur].job[r]].scene].bvh; }
-    LJ_D void load(int r, V3 &o, V3 &dir, float &tn, float &tf) const { load_ray(d.buf[cur].ray, r, o, dir, tn, tf); }
-    LJ_D void store(int r, const Trav &s) const { d.hit[r] = hit_record(s); }
+    int cur, n0;   // n0: class-0 entries of queue cur
+    LJ_D const DevBvh &bvh(int r) const { return d.scenes[d.jobs[d.buf[cur].job[d.entry(r, n0)]].scene].bvh; }
+    LJ_D void load(int r, V3 &o, V3 &dir, float &tn, float &tf) const {
+        load_ray(d.buf[cur].ray, d.entry(r, n0), o, dir, tn, tf);
+    }
+    LJ_D void store(int r, const Trav &s) const { d.hit[d.entry(r, n0)] = hit_record(s); }
 };
 struct SrvShadowIO {
     const SrvDev &d;
@@ -215,8 +229,10 @@ struct SrvShadowIO {
 };
 
 // The server's path store for shade_segment: state read from queue cur at
-// the entry index, continuing paths written to the end of queue cur ^ 1,
-// finished ones to the retire list; a shadow ray records where its path went.
+// the entry index, continuing paths appended to queue cur ^ 1 (at the front
+// for class 0, the back for class 1), finished ones to the retire list; a
+// shadow ray records where its path went.
+template <int kClass>
 struct QueuePaths {
     const SrvDev &d;
     int cur;
@@ -247,7 +263,7 @@ struct QueuePaths {
         if (o.cont) {
             const int nxt = cur ^ 1;
             const StateSoA &q = d.buf[nxt];
-            const int s = queue_slot(d.counts + nxt);
+            const int s = kClass == 0 ? queue_slot(d.counts + nxt) : d.back(queue_slot(d.counts + 10 + nxt));
             q.job[s] = st.job;
             q.pixel[s] = st.pixel;
             q.rng[s] = st.rng;
@@ -272,24 +288,27 @@ struct QueuePaths {
 // traversal: 64 registers (full-SM occupancy of 50%, no spills)
 template <int B>
 __global__ void __launch_bounds__(B, 1024 / B) k_srv_trace(SrvDev d, int cur) {
-    const int n = d.counts[cur];
+    const int n0 = d.counts[cur], n = n0 + d.counts[10 + cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 0, (unsigned long long)n);
-    SrvClosestIO io{d, cur};
+    SrvClosestIO io{d, cur, n0};
     trace_queue<false>(io, n, d.counts + 8, d.status);
 }
 
 // The scene and job tables are read-only here (restrict: the stores of the
 // shade step cannot alias them, so their fields need not be re-read).
-template <int B>
-__global__ void __launch_bounds__(B, 512 / B) k_srv_shade(SrvDev d, const DevScene *__restrict__ scenes,
-                                                          const SrvJob *__restrict__ jobs, int cur) {
-    const int n = d.counts[cur];
+// One instance per material class: class 0 (the queue's front) runs the
+// smaller kernel compiled for kClassicMats.
+template <int B, int kClass>
+__global__ void __launch_bounds__(B, (kClass == 0 ? 640 : 512) / B)
+    k_srv_shade(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
+    const int n = d.counts[kClass == 0 ? cur : 10 + cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 2, (unsigned long long)n);
-    const QueuePaths paths{d, cur};
+    const QueuePaths<kClass> paths{d, cur};
     for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
-        const SrvJob &jb = jobs[d.buf[cur].job[i]];
+        const int e = kClass == 0 ? i : d.back(i);
+        const SrvJob &jb = jobs[d.buf[cur].job[e]];
         const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
-        shade_segment<kAllMats>(scenes[jb.scene], paths, i, cfg, d.status);
+        shade_segment<kClass == 0 ? kClassicMats : kAllMats>(scenes[jb.scene], paths, e, cfg, d.status);
     }
 }
 
@@ -335,13 +354,15 @@ __global__ void k_srv_finalize(const unsigned long long *acc, float *img, long l
 struct KernelSet {
     void (*regen)(SrvDev, int);
     void (*trace)(SrvDev, int);
-    void (*shade)(SrvDev, const DevScene *, const SrvJob *, int);
+    void (*shade0)(SrvDev, const DevScene *, const SrvJob *, int);
+    void (*shade1)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*shadow)(SrvDev, int);
     void (*retire)(SrvDev);
 };
 template <int B>
 KernelSet kernel_set() {
-    return KernelSet{k_srv_regen<B>, k_srv_trace<B>, k_srv_shade<B>, k_srv_shadow<B>, k_srv_retire<B>};
+    return KernelSet{k_srv_regen<B>,    k_srv_trace<B>,  k_srv_shade<B, 0>,
+                     k_srv_shade<B, 1>, k_srv_shadow<B>, k_srv_retire<B>};
 }
 
 int occupancy_grid(const void *fn, int block, int sms) {
@@ -440,7 +461,7 @@ struct lj_server {
     long long *d_plan_start = nullptr;
     SrvDev dev{};
     KernelSet ks{};
-    int grid[5] = {1, 1, 1, 1, 1};
+    int grid[6] = {1, 1, 1, 1, 1, 1};
     cudaGraphExec_t graph = nullptr;
 
     // pinned host staging
@@ -516,7 +537,10 @@ void launch_wave(lj_server *s, int cur) {
     s->ks.trace<<<s->grid[1], B, 0, s->stream>>>(s->dev, cur);
     mark(s, LJ_KERNEL_TRACE, false);
     mark(s, LJ_KERNEL_SHADE, true);
-    s->ks.shade<<<s->grid[2], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    s->ks.shade0<<<s->grid[2], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    mark(s, LJ_KERNEL_SHADE, false);
+    mark(s, LJ_KERNEL_SHADE, true);
+    s->ks.shade1<<<s->grid[5], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
     mark(s, LJ_KERNEL_SHADE, false);
     mark(s, LJ_KERNEL_SHADOW, true);
     s->ks.shadow<<<s->grid[3], B, 0, s->stream>>>(s->dev, cur);
@@ -624,7 +648,8 @@ std::string build_device(lj_server *s) {
     SRV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
     s->grid[0] = occupancy_grid((const void *)s->ks.regen, s->block, sms);
     s->grid[1] = occupancy_grid((const void *)s->ks.trace, s->block, sms);
-    s->grid[2] = occupancy_grid((const void *)s->ks.shade, s->block, sms);
+    s->grid[2] = occupancy_grid((const void *)s->ks.shade0, s->block, sms);
+    s->grid[5] = occupancy_grid((const void *)s->ks.shade1, s->block, sms);
     s->grid[3] = occupancy_grid((const void *)s->ks.shadow, s->block, sms);
     s->grid[4] = occupancy_grid((const void *)s->ks.retire, s->block, sms);
 
@@ -689,6 +714,7 @@ std::string admit(lj_server *s, HostJob *j) {
     h.rr_depth = j->rr_depth;
     h.spread0 = 0.25f / (float)std::max(j->w, j->h);
     h.clamp = (float)std::ldexp(1.0, 30) / (float)j->spp;
+    h.mclass = (j->scene->mat_mask & ~kClassicMats) == 0 && !(s->opt.flags & LJ_SERVER_ONE_SHADE_KERNEL) ? 0 : 1;
     SRV_CUDA(cudaMemcpyAsync(s->d_jobs + slot, &h, sizeof(SrvJob), cudaMemcpyHostToDevice, s->stream));
     SRV_CUDA(cudaMemsetAsync(s->d_ctr + slot, 0, sizeof(SrvCtr), s->stream));
     SRV_CUDA(cudaMemsetAsync(s->d_cancel + slot, 0, sizeof(int), s->stream));
@@ -886,7 +912,7 @@ void worker_main(lj_server *s) {
         if (e == cudaSuccess) e = collect_marks(s);
         lk.lock();
         s->waves += 2 * pairs;
-        s->kernel_launches += 12 * pairs;
+        s->kernel_launches += 14 * pairs;
         if (s->graph) s->graph_launches += pairs;
         const int b = s->poll_next;
         s->poll_next = (b + 1) % kPollsInFlight;

@@ -139,9 +139,10 @@ LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, Trac
                 float fy = fmaf((float)(negy ? loy : hiy), ay, by);
                 float nz = fmaf((float)(negz ? hiz : loz), az, bz);
                 float fz = fmaf((float)(negz ? loz : hiz), az, bz);
-                // a few ulps of slack keep hits on box faces from being culled
-                float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, tnear)) * (1.0f - 2.0e-7f);
-                float tmax = fminf(fminf(fx, fy), fminf(fz, tfar * (1.0f + 2.0e-7f))) * (1.0f + 2.0e-7f);
+                // slack of ~8 ulps: hits on box faces, and hits at exactly the
+                // current closest distance (ties), are never culled
+                float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, tnear)) * (1.0f - 1.0e-6f);
+                float tmax = fminf(fminf(fx, fy), fminf(fz, tfar * (1.0f + 1.0e-6f))) * (1.0f + 1.0e-6f);
                 if (tmin <= tmax) {
                     uint32_t off = meta & 0x1fu;
                     if (off >= 24u) node_hits |= 1u << (24u + ((uint32_t)i ^ oct_xor));

@@ -98,9 +98,10 @@ LJ_D bool trav_step(Trav &s, uint2 *stack, int *status) {
             const float fy = fmaf((float)(negy ? loy : hiy), ay, by);
             const float nz = fmaf((float)(negz ? hiz : loz), az, bz);
             const float fz = fmaf((float)(negz ? loz : hiz), az, bz);
-            // a few ulps of slack keep hits on box faces from being culled
-            const float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, s.tnear)) * (1.0f - 2.0e-7f);
-            const float tmax = fminf(fminf(fx, fy), fminf(fz, s.tfar * (1.0f + 2.0e-7f))) * (1.0f + 2.0e-7f);
+            // slack of ~8 ulps: hits on box faces, and hits at exactly the
+            // current closest distance (ties), are never culled
+            const float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, s.tnear)) * (1.0f - 1.0e-6f);
+            const float tmax = fminf(fminf(fx, fy), fminf(fz, s.tfar * (1.0f + 1.0e-6f))) * (1.0f + 1.0e-6f);
             if (tmin <= tmax) {
                 const uint32_t off = meta & 0x1fu;
                 if (off >= 24u) node_hits |= 1u << (24u + ((uint32_t)i ^ s.oct_xor));

@@ -70,6 +70,7 @@ def lib():
         L.lj_gpu_server_last_error.argtypes = [vp]
         L.lj_gpu_server_last_error.restype = C.c_char_p
         L.lj_gpu_server_stop.argtypes = [vp]
+        L.lj_gpu_bvh_leaf_prims.argtypes = [vp, vp, i64, C.POINTER(i64)]
         L.lj_gpu_render_job_device.argtypes = [vp, C.POINTER(abi.lj_job_desc), vp, vp, C.POINTER(abi.lj_stats)]
         L.lj_gpu_server_autotune.argtypes = [vp, C.POINTER(vp), C.POINTER(abi.lj_job_desc), C.POINTER(i32), i32,
                                              C.c_char_p, C.POINTER(abi.lj_server_options)]
@@ -215,6 +216,14 @@ class GpuScene:
                                                   C.byref(st) if st is not None else None))
         return st
 
+    def leaf_prims(self):
+        """Primitive index of every BVH leaf record (int32 array, leaf order)."""
+        n = C.c_int64()
+        self.ctx.check(lib().lj_gpu_bvh_leaf_prims(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value, np.int32)
+        self.ctx.check(lib().lj_gpu_bvh_leaf_prims(self.h, out.ctypes.data_as(C.c_void_p), n.value, C.byref(n)))
+        return out
+
     def render_job_device(self, out, job, stream=None, stats=False):
         """One job (lj_job_desc) through the single-scene renderer into the
         device tensor `out` (H*W*3 float32 at the job's resolution)."""
@@ -274,11 +283,13 @@ def job_desc(seed=0, spp=0, sample_offset=0, width=0, height=0, max_depth=None, 
 
 
 def server_options(hbm_budget_bytes=0, path_pool=0, block_size=0, max_live_jobs=0, max_queued_jobs=0,
-                   waves_per_poll=0, policy=abi.LJ_SCHED_FIFO, use_graphs=True, profile=False):
+                   waves_per_poll=0, policy=abi.LJ_SCHED_FIFO, use_graphs=True, profile=False,
+                   one_shade_kernel=False):
     return abi.lj_server_options(hbm_budget_bytes=hbm_budget_bytes, path_pool=path_pool, block_size=block_size,
                                  max_live_jobs=max_live_jobs, max_queued_jobs=max_queued_jobs,
                                  waves_per_poll=waves_per_poll, policy=policy, use_graphs=1 if use_graphs else 0,
-                                 flags=abi.LJ_SERVER_PROFILE if profile else 0)
+                                 flags=(abi.LJ_SERVER_PROFILE if profile else 0) |
+                                 (abi.LJ_SERVER_ONE_SHADE_KERNEL if one_shade_kernel else 0))
 
 
 class Server:

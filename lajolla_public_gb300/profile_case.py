@@ -13,6 +13,7 @@ Cases:
   terrain       seeded terrain + 16 icospheres + envmap, 1.26M triangles,
                 512x512, 16 spp, max depth 8
   terrain_srv   the terrain case as one server job (server kernels)
+  cbox_srv      the cbox case as one server job
 
 `summarize` reads the CSV that `ncu --metrics gpu__time_duration.sum --csv
 --log-file F` writes and prints launches, total time and share per kernel.
@@ -31,6 +32,8 @@ from . import abi, scenes
 def make_case(name):
     if name == "cbox":
         return scenes.cornell_box(seed=0, width=256, height=256, spp=64, max_depth=6)
+    if name == "cbox_srv":
+        return scenes.cornell_box(seed=0, width=256, height=256, spp=64, max_depth=6)
     if name in ("terrain", "terrain_srv"):
         return scenes.resized_terrain_scene(seed=5, n_tris=1261476, width=512, height=512, spp=16, max_depth=8)
     raise SystemExit("unknown case %r" % name)
@@ -45,7 +48,7 @@ def run(args):
     n = sc.width * sc.height * 3
     if args.case.endswith("_srv"):
         opts = gpu.server_options(path_pool=args.pool, block_size=args.block, use_graphs=not args.profile,
-                                  profile=args.profile)
+                                  profile=args.profile, one_shade_kernel=args.one_shade_kernel)
         with gpu.Server(ctx, opts) as srv:
             for i in range(args.warmup + args.repeat):
                 t0 = time.perf_counter()
@@ -101,6 +104,7 @@ def main(argv=None):
     r.add_argument("--pool", type=int, default=1 << 22, help="server path pool")
     r.add_argument("--block", type=int, default=128, help="server block size")
     r.add_argument("--profile", action="store_true", help="server: time each kernel class")
+    r.add_argument("--one-shade-kernel", action="store_true", help="server: all-materials shade kernel only")
     s = sub.add_parser("summarize")
     s.add_argument("csv")
     args = ap.parse_args(argv)

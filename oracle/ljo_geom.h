@@ -180,7 +180,9 @@ struct CpuBvh {
 
 // Slab test in FP32; returns entry distance or +inf on miss.
 inline bool box_hit(const Box &b, f3 o, f3 inv_d, float tnear, float tfar) {
-    float t0 = tnear, t1 = tfar;
+    // slack of ~8 ulps (the GPU traversal's): hits on box faces, and hits at
+    // exactly the current closest distance (ties), are never culled
+    float t0 = tnear, t1 = tfar * 1.000001f;
     const float oo[3] = {o.x, o.y, o.z};
     const float id[3] = {inv_d.x, inv_d.y, inv_d.z};
     for (int a = 0; a < 3; a++) {
@@ -188,9 +190,7 @@ inline bool box_hit(const Box &b, f3 o, f3 inv_d, float tnear, float tfar) {
         float tb = (b.hi[a] - oo[a]) * id[a];
         if (std::isnan(ta)) ta = -INFINITY;   // 0 * inf on a slab boundary
         if (std::isnan(tb)) tb = INFINITY;
-        float tmin = std::min(ta, tb), tmax = std::max(ta, tb);
-        // widen by a few ulps so that boxes of flat triangles are never missed
-        tmax *= 1.0000004f;
+        float tmin = std::min(ta, tb) * 0.999999f, tmax = std::max(ta, tb) * 1.000001f;
         t0 = std::max(t0, tmin);
         t1 = std::min(t1, tmax);
         if (t0 > t1) return false;

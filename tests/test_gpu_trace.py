@@ -52,6 +52,17 @@ def test_closest_and_any_match_brute_force(ctx):
     assert info.num_prims == 20040 and info.num_wide_nodes > 0
 
 
+@pytest.mark.parametrize("make", [lambda: _soup_with_spheres(1, 20000, 40), lambda: scenes.tied_soup_scene(7, 4000),
+                                  lambda: scenes.cornell_box(seed=1)])
+def test_bvh_holds_every_primitive_once(ctx, make):
+    sc = make()
+    g = gpu.GpuScene(ctx, sc)
+    leaves = g.leaf_prims()
+    n = g.info().num_prims
+    assert len(leaves) == n
+    assert np.array_equal(np.sort(leaves), np.arange(n, dtype=np.int32))
+
+
 def test_ties_resolve_to_lowest_index(ctx):
     sc = scenes.tied_soup_scene(7, 4000)
     rays = scenes.random_rays(8, 40000)
