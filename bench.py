@@ -388,7 +388,9 @@ def run_ours(args):
     launches_dom = max(1, ps.class_launches[dom])
     avg_launch_s = cls_ms[dom] / 1e3 / launches_dom
     achieved = nb / launches_dom / avg_launch_s / 1e9
-    traffic = load_traffic("srv_" + abi.KERNEL_CLASS_NAMES[dom])
+    units = {abi.LJ_KERNEL_TRACE: ps.rays_closest, abi.LJ_KERNEL_SHADOW: ps.rays_shadow,
+             abi.LJ_KERNEL_SHADE: ps.path_segments}.get(dom, job_samples(jobs))
+    traffic = load_traffic("k_srv_" + abi.KERNEL_CLASS_NAMES[dom], units / launches_dom)
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
@@ -446,15 +448,17 @@ def scene_host_bytes(sc):
     return int(b)
 
 
-def load_traffic(kernel_name):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/traffic.json), or None."""
+def load_traffic(kernel_name, units_per_launch):
+    """DRAM bytes per launch of the dominant kernel: the per-unit figure of
+    the committed ncu capture (profiles/traffic.json, measured on a smaller
+    case of the same kernel) times the units of an average launch here, or
+    None."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         d = json.load(open(p))
         v = d.get(kernel_name)
-        if isinstance(v, dict):
-            return v.get("dram_bytes_per_launch")
+        if isinstance(v, dict) and v.get("dram_bytes_per_unit"):
+            return round(float(v["dram_bytes_per_unit"]) * units_per_launch)
     return None
 
 

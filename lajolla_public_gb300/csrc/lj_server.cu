@@ -92,6 +92,7 @@ struct SrvDev {
     const int *cancel;
     const int *order;            // [0] = entries, [1..] job slots
     int *plan_off;               // per entry: first regen index; [n] = total taken
+    int *plan_coff;              // per entry: new paths of the same class in earlier entries
     long long *plan_start;       // per entry: first linear sample index
     StateSoA buf[2];
     float4 *hit;
@@ -101,8 +102,9 @@ struct SrvDev {
     int *rjob, *rpixel;          // finished paths
     float4 *rL;
     int *counts;                 // [0],[1] class-0 entries (front) of queue 0 / 1, [2] shadow,
-                                 // [3] retire, [5] regen count, [8],[9] ray fetch counters,
-                                 // [10],[11] class-1 entries (back) of queue 0 / 1
+                                 // [3] retire, [5] regen count, [6],[7] class-0 / class-1
+                                 // entries that continue into the wave, [8],[9] ray fetch
+                                 // counters, [10],[11] class-1 entries (back) of queue 0 / 1
     // queue position of the k-th entry of class 1 (filled from the back)
     LJ_D int back(int k) const { return P - 1 - k; }
     // position of ray r of a queue with n0 class-0 entries
@@ -118,16 +120,17 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
     const int lane = threadIdx.x;
     int *counts = d.counts;
     const int n_order = d.order[0];
-    const int c = counts[cur] + counts[10 + cur];   // paths that continue into this wave
-    const long long freec = (long long)d.P - c;      // room for new paths
-    long long carry = 0;
+    const int c0 = counts[cur], c1 = counts[10 + cur];   // paths that continue into this wave
+    const long long freec = (long long)d.P - c0 - c1;     // room for new paths
+    long long carry = 0, carry0 = 0, carry1 = 0;
     for (int base = 0; base < n_order; base += 32) {
         const int k = base + lane;
         long long rem = 0, start = 0;
-        int j = -1;
+        int j = -1, cls = 0;
         if (k < n_order) {
             j = d.order[1 + k];
             start = (long long)d.ctr[j].issued;
+            cls = d.jobs[j].mclass;
             if (!d.cancel[j]) rem = max(0LL, d.jobs[j].total - start);
         }
         long long incl = rem;
@@ -137,17 +140,34 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
         }
         const long long off = min(carry + incl - rem, freec);
         const long long n = min(rem, freec - off);
+        // prefix of the granted counts within each class
+        long long n0 = cls == 0 ? n : 0, n1 = cls == 0 ? 0 : n;
+        long long i0 = n0, i1 = n1;
+        for (int o = 1; o < 32; o <<= 1) {
+            long long y0 = __shfl_up_sync(0xffffffffu, i0, o), y1 = __shfl_up_sync(0xffffffffu, i1, o);
+            if (lane >= o) {
+                i0 += y0;
+                i1 += y1;
+            }
+        }
         if (k < n_order) {
             d.plan_off[k] = (int)off;
+            d.plan_coff[k] = (int)(cls == 0 ? carry0 + i0 - n0 : carry1 + i1 - n1);
             d.plan_start[k] = start;
             if (n > 0) d.ctr[j].issued += (unsigned long long)n;
         }
         carry += __shfl_sync(0xffffffffu, incl, 31);
+        carry0 += __shfl_sync(0xffffffffu, i0, 31);
+        carry1 += __shfl_sync(0xffffffffu, i1, 31);
     }
     if (lane == 0) {
         const long long take = min(carry, freec);
         d.plan_off[n_order] = (int)take;
         counts[5] = (int)take;
+        counts[6] = c0;
+        counts[7] = c1;
+        counts[cur] = c0 + (int)carry0;   // carry0 + carry1 == take
+        counts[10 + cur] = c1 + (int)carry1;
         counts[cur ^ 1] = 0;
         counts[10 + (cur ^ 1)] = 0;
         counts[2] = 0;
@@ -186,8 +206,11 @@ __global__ void __launch_bounds__(B) k_srv_regen(SrvDev d, int cur) {
         float r1 = pcg_uniform(rng), r2 = pcg_uniform(rng);
         V3 o, dir;
         camera_ray(jb.cam, (x + r1) / jb.cam.w, (y + r2) / jb.cam.h, o, dir);
-        // appended after the paths that continue into this wave
-        const int s = jb.mclass == 0 ? queue_slot(d.counts + cur) : d.back(queue_slot(d.counts + 10 + cur));
+        // after the paths that continue into this wave, in sample order (a
+        // fixed, coherent order: neighbouring threads of later kernels get
+        // neighbouring pixels)
+        const int t = d.plan_coff[lo] + (i - d.plan_off[lo]);
+        const int s = jb.mclass == 0 ? d.counts[6] + t : d.back(d.counts[7] + t);
         q.job[s] = j;
         q.pixel[s] = pixel;
         q.rng[s] = rng.state;
@@ -458,6 +481,7 @@ struct lj_server {
     int *d_cancel = nullptr;
     int *d_order = nullptr;
     int *d_plan_off = nullptr;
+    int *d_plan_coff = nullptr;
     long long *d_plan_start = nullptr;
     SrvDev dev{};
     KernelSet ks{};
@@ -585,6 +609,7 @@ std::string build_device(lj_server *s) {
     SRV_CUDA(cudaMalloc(&s->d_cancel, sizeof(int) * J));
     SRV_CUDA(cudaMalloc(&s->d_order, sizeof(int) * (J + 1)));
     SRV_CUDA(cudaMalloc(&s->d_plan_off, sizeof(int) * (J + 1)));
+    SRV_CUDA(cudaMalloc(&s->d_plan_coff, sizeof(int) * (J + 1)));
     SRV_CUDA(cudaMalloc(&s->d_plan_start, sizeof(long long) * (J + 1)));
     SRV_CUDA(cudaMemsetAsync(s->d_ctr, 0, sizeof(SrvCtr) * J, s->stream));
     SRV_CUDA(cudaMemsetAsync(s->d_cancel, 0, sizeof(int) * J, s->stream));
@@ -613,6 +638,7 @@ std::string build_device(lj_server *s) {
     d.cancel = s->d_cancel;
     d.order = s->d_order;
     d.plan_off = s->d_plan_off;
+    d.plan_coff = s->d_plan_coff;
     d.plan_start = s->d_plan_start;
     for (int k = 0; k < 2; k++) {
         StateSoA &q = d.buf[k];
@@ -997,7 +1023,7 @@ void release_device(lj_server *s) {
     }
     if (s->graph) cudaGraphExecDestroy(s->graph);
     void *dev_ptrs[] = {s->d_pool, s->d_scenes, s->d_jobs, s->d_ctr, s->d_cancel, s->d_order, s->d_plan_off,
-                        s->d_plan_start};
+                        s->d_plan_coff, s->d_plan_start};
     for (void *p : dev_ptrs)
         if (p) cudaFree(p);
     if (s->h_jobs) cudaFreeHost(s->h_jobs);
