@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_queue(DevBvh bvh, const float4
     const int n = *count;
     if (blockIdx.x == 0 && threadIdx.x == 0 && stat) atomicAdd(stat, (unsigned long long)n);
     ClosestQueueIO io{bvh, rays, hits};
-    trace_queue<false>(io, n, fetch, status);
+    trace_queue<false, 128>(io, n, fetch, status);
 }
 
 __global__ void __launch_bounds__(128, 8) k_trace_shadow(DevBvh bvh, const float4 *rays, const int *paths,
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_shadow(DevBvh bvh, const float
     const int n = *count;
     if (blockIdx.x == 0 && threadIdx.x == 0 && stat) atomicAdd(stat, (unsigned long long)n);
     ShadowQueueIO io{bvh, rays, paths, contrib, L};
-    trace_queue<true>(io, n, fetch, status);
+    trace_queue<true, 128>(io, n, fetch, status);
 }
 
 // One instance per material set (kMats): a scene of Lambertian surfaces only

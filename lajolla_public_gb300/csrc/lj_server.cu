@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(B, 1024 / B) k_srv_trace(SrvDev d, int cur) {
     const int n0 = d.counts[cur], n = n0 + d.counts[10 + cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 0, (unsigned long long)n);
     SrvClosestIO io{d, cur, n0};
-    trace_queue<false>(io, n, d.counts + 8, d.status);
+    trace_queue<false, B>(io, n, d.counts + 8, d.status);
 }
 
 // The scene and job tables are read-only here (restrict: the stores of the
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(B, 1024 / B) k_srv_shadow(SrvDev d, int cur) {
     const int n = d.counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 1, (unsigned long long)n);
     SrvShadowIO io{d, cur ^ 1};
-    trace_queue<true>(io, n, d.counts + 9, d.status);
+    trace_queue<true, B>(io, n, d.counts + 9, d.status);
 }
 
 LJ_D unsigned long long to_fixed(float v, float clamp) {

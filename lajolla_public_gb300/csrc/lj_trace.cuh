@@ -65,6 +65,12 @@ LJ_D float sphere_hit(V3 c, float r, V3 o, V3 d, float tnear, float tfar) {
 }
 
 LJ_D uint32_t extract_byte(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
+// Byte i of w as a float, exactly: one byte permute puts it into the
+// mantissa of 2^23 (bits 0x4B000000), one add removes the 2^23.  Cheaper
+// than an integer extract + int-to-float conversion.
+LJ_D float byte_to_float(uint32_t w, int i) {
+    return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)i)) - 8388608.0f;
+}
 
 // Returns true on hit.  kAny: stop at the first hit (occlusion query).
 // `hit` is updated with the closest hit; tfar shrinks as hits are found.
@@ -123,22 +129,23 @@ LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, Trac
             float ay = sy * inv.y, by = (py - o.y) * inv.y;
             float az = sz * inv.z, bz = (pz - o.z) * inv.z;
             uint32_t node_hits = 0, prim_hits = 0;
+            // near / far plane words per axis (see trav_step)
+            const uint32_t nx0 = negx ? c3.z : c2.x, nx1 = negx ? c3.w : c2.y;
+            const uint32_t fx0 = negx ? c2.x : c3.z, fx1 = negx ? c2.y : c3.w;
+            const uint32_t ny0 = negy ? c4.x : c2.z, ny1 = negy ? c4.y : c2.w;
+            const uint32_t fy0 = negy ? c2.z : c4.x, fy1 = negy ? c2.w : c4.y;
+            const uint32_t nz0 = negz ? c4.z : c3.x, nz1 = negz ? c4.w : c3.y;
+            const uint32_t fz0 = negz ? c3.x : c4.z, fz1 = negz ? c3.y : c4.w;
 #pragma unroll
             for (int i = 0; i < 8; i++) {
                 uint32_t meta = extract_byte(i < 4 ? c1.z : c1.w, i & 3);
                 if (meta == 0u) continue;
-                uint32_t lox = extract_byte(i < 4 ? c2.x : c2.y, i & 3);
-                uint32_t loy = extract_byte(i < 4 ? c2.z : c2.w, i & 3);
-                uint32_t loz = extract_byte(i < 4 ? c3.x : c3.y, i & 3);
-                uint32_t hix = extract_byte(i < 4 ? c3.z : c3.w, i & 3);
-                uint32_t hiy = extract_byte(i < 4 ? c4.x : c4.y, i & 3);
-                uint32_t hiz = extract_byte(i < 4 ? c4.z : c4.w, i & 3);
-                float nx = fmaf((float)(negx ? hix : lox), ax, bx);
-                float fx = fmaf((float)(negx ? lox : hix), ax, bx);
-                float ny = fmaf((float)(negy ? hiy : loy), ay, by);
-                float fy = fmaf((float)(negy ? loy : hiy), ay, by);
-                float nz = fmaf((float)(negz ? hiz : loz), az, bz);
-                float fz = fmaf((float)(negz ? loz : hiz), az, bz);
+                float nx = fmaf(byte_to_float(i < 4 ? nx0 : nx1, i & 3), ax, bx);
+                float fx = fmaf(byte_to_float(i < 4 ? fx0 : fx1, i & 3), ax, bx);
+                float ny = fmaf(byte_to_float(i < 4 ? ny0 : ny1, i & 3), ay, by);
+                float fy = fmaf(byte_to_float(i < 4 ? fy0 : fy1, i & 3), ay, by);
+                float nz = fmaf(byte_to_float(i < 4 ? nz0 : nz1, i & 3), az, bz);
+                float fz = fmaf(byte_to_float(i < 4 ? fz0 : fz1, i & 3), az, bz);
                 // slack of ~8 ulps: hits on box faces, and hits at exactly the
                 // current closest distance (ties), are never culled
                 float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, tnear)) * (1.0f - 1.0e-6f);

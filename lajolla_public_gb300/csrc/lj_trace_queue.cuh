@@ -16,6 +16,21 @@
 namespace lj {
 
 constexpr int kRefillLanes = 20;
+constexpr int kSmemStack = 8;   // stack entries per thread kept in shared memory
+
+// Traversal stack of one lane: the top kSmemStack entries in shared memory
+// (entry k of thread t at column t of row k: consecutive lanes, consecutive
+// words, no bank conflicts), deeper entries in local memory.
+struct TravStack {
+    uint2 *col;       // &smem[threadIdx.x]
+    int stride;       // threads per block
+    uint2 deep[kTraversalStack - kSmemStack];
+    LJ_D void put(int k, uint2 v) {
+        if (k < kSmemStack) col[k * stride] = v;
+        else deep[k - kSmemStack] = v;
+    }
+    LJ_D uint2 get(int k) const { return k < kSmemStack ? col[k * stride] : deep[k - kSmemStack]; }
+};
 
 struct Trav {
     V3 o, d, inv;
@@ -53,7 +68,7 @@ LJ_D void trav_init(Trav &s, const DevBvh &bvh, V3 o, V3 d, float tnear, float t
 // One step: visit one node (or take the pending primitive group) and test
 // the primitives it yields.  Returns true when the ray is finished.
 template <bool kAny>
-LJ_D bool trav_step(Trav &s, uint2 *stack, int *status) {
+LJ_D bool trav_step(Trav &s, TravStack &stack, int *status) {
     if (++s.iter > (1 << 22)) {   // a well-formed tree needs far fewer steps
         atomicOr(status, kStatusStackOverflow);
         return true;
@@ -66,7 +81,7 @@ LJ_D bool trav_step(Trav &s, uint2 *stack, int *status) {
         const uint32_t child = s.ngroup.x + __popc(imask & ((1u << slot) - 1u));
         s.ngroup.y &= ~(1u << k);
         if (s.ngroup.y > 0x00ffffffu) {
-            if (s.sp < kTraversalStack) stack[s.sp++] = s.ngroup;
+            if (s.sp < kTraversalStack) stack.put(s.sp++, s.ngroup);
             else atomicOr(status, kStatusStackOverflow);
         }
         const uint4 *np = s.nodes + (size_t)child * kWideNodeU4;
@@ -81,27 +96,30 @@ LJ_D bool trav_step(Trav &s, uint2 *stack, int *status) {
         const float ay = sy * s.inv.y, by = (py - s.o.y) * s.inv.y;
         const float az = sz * s.inv.z, bz = (pz - s.o.z) * s.inv.z;
         const bool negx = s.inv.x < 0.0f, negy = s.inv.y < 0.0f, negz = s.inv.z < 0.0f;
+        // the words holding the near / far plane bytes of the 8 children, per
+        // axis (lo planes are near for a positive direction component)
+        const uint32_t nx0 = negx ? c3.z : c2.x, nx1 = negx ? c3.w : c2.y;
+        const uint32_t fx0 = negx ? c2.x : c3.z, fx1 = negx ? c2.y : c3.w;
+        const uint32_t ny0 = negy ? c4.x : c2.z, ny1 = negy ? c4.y : c2.w;
+        const uint32_t fy0 = negy ? c2.z : c4.x, fy1 = negy ? c2.w : c4.y;
+        const uint32_t nz0 = negz ? c4.z : c3.x, nz1 = negz ? c4.w : c3.y;
+        const uint32_t fz0 = negz ? c3.x : c4.z, fz1 = negz ? c3.y : c4.w;
+        const float tnear = s.tnear, tfar = s.tfar * (1.0f + 1.0e-6f);
         uint32_t node_hits = 0, prim_hits = 0;
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             const uint32_t meta = extract_byte(i < 4 ? c1.z : c1.w, i & 3);
             if (meta == 0u) continue;
-            const uint32_t lox = extract_byte(i < 4 ? c2.x : c2.y, i & 3);
-            const uint32_t loy = extract_byte(i < 4 ? c2.z : c2.w, i & 3);
-            const uint32_t loz = extract_byte(i < 4 ? c3.x : c3.y, i & 3);
-            const uint32_t hix = extract_byte(i < 4 ? c3.z : c3.w, i & 3);
-            const uint32_t hiy = extract_byte(i < 4 ? c4.x : c4.y, i & 3);
-            const uint32_t hiz = extract_byte(i < 4 ? c4.z : c4.w, i & 3);
-            const float nx = fmaf((float)(negx ? hix : lox), ax, bx);
-            const float fx = fmaf((float)(negx ? lox : hix), ax, bx);
-            const float ny = fmaf((float)(negy ? hiy : loy), ay, by);
-            const float fy = fmaf((float)(negy ? loy : hiy), ay, by);
-            const float nz = fmaf((float)(negz ? hiz : loz), az, bz);
-            const float fz = fmaf((float)(negz ? loz : hiz), az, bz);
+            const float nx = fmaf(byte_to_float(i < 4 ? nx0 : nx1, i & 3), ax, bx);
+            const float fx = fmaf(byte_to_float(i < 4 ? fx0 : fx1, i & 3), ax, bx);
+            const float ny = fmaf(byte_to_float(i < 4 ? ny0 : ny1, i & 3), ay, by);
+            const float fy = fmaf(byte_to_float(i < 4 ? fy0 : fy1, i & 3), ay, by);
+            const float nz = fmaf(byte_to_float(i < 4 ? nz0 : nz1, i & 3), az, bz);
+            const float fz = fmaf(byte_to_float(i < 4 ? fz0 : fz1, i & 3), az, bz);
             // slack of ~8 ulps: hits on box faces, and hits at exactly the
             // current closest distance (ties), are never culled
-            const float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, s.tnear)) * (1.0f - 1.0e-6f);
-            const float tmax = fminf(fminf(fx, fy), fminf(fz, s.tfar * (1.0f + 1.0e-6f))) * (1.0f + 1.0e-6f);
+            const float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, tnear)) * (1.0f - 1.0e-6f);
+            const float tmax = fminf(fminf(fx, fy), fminf(fz, tfar)) * (1.0f + 1.0e-6f);
             if (tmin <= tmax) {
                 const uint32_t off = meta & 0x1fu;
                 if (off >= 24u) node_hits |= 1u << (24u + ((uint32_t)i ^ s.oct_xor));
@@ -144,7 +162,7 @@ LJ_D bool trav_step(Trav &s, uint2 *stack, int *status) {
     }
     if (s.ngroup.y <= 0x00ffffffu) {
         if (s.sp == 0) return true;
-        s.ngroup = stack[--s.sp];
+        s.ngroup = stack.get(--s.sp);
     }
     return false;
 }
@@ -153,12 +171,16 @@ LJ_D bool trav_step(Trav &s, uint2 *stack, int *status) {
 //   const DevBvh &bvh(int r)                  the BVH to trace against
 //   void load(int r, V3 &o, V3 &d, float &tnear, float &tfar)
 //   void store(int r, const Trav &s)          s.found / s.hit hold the result
-// *fetch must be 0 at launch; every warp of the grid must call this.
-template <bool kAny, class IO>
+// *fetch must be 0 at launch; every warp of the grid must call this, with
+// blockDim.x == kBlock.
+template <bool kAny, int kBlock, class IO>
 LJ_D void trace_queue(IO &io, int n, int *fetch, int *status) {
     const unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    uint2 stack[kTraversalStack];
+    __shared__ uint2 stack_top[kSmemStack * kBlock];
+    TravStack stack;
+    stack.col = stack_top + threadIdx.x;
+    stack.stride = kBlock;
     Trav s;
     int ray = -1;
     bool drained = false;   // warp-uniform: the queue has no rays left

@@ -57,8 +57,10 @@ def run(args):
             st = srv.stats()
         cls = {abi.KERNEL_CLASS_NAMES[c]: round(st.class_ms[c] / (args.warmup + args.repeat), 3)
                for c in range(abi.LJ_KERNEL_CLASSES)}
-        print("%s: %d samples, last job %.2f ms (host clock), pool %d block %d, per-job classes %s"
-              % (args.case, sc.width * sc.height * sc.spp, dt * 1e3, args.pool, args.block, cls))
+        print("%s: %d samples, last job %.2f ms (host clock), pool %d block %d, per-job classes %s, "
+              "rays over all jobs: closest %d shadow %d, waves %d"
+              % (args.case, sc.width * sc.height * sc.spp, dt * 1e3, args.pool, args.block, cls, st.rays_closest,
+                 st.rays_shadow, st.waves))
     else:
         out = torch.empty(n, dtype=torch.float32, device="cuda")
         stream = torch.cuda.current_stream().cuda_stream
