@@ -22,6 +22,7 @@
 
 #include "lj_internal.h"
 #include "lj_trace.cuh"
+#include "lj_trace_queue.cuh"
 
 namespace lj {
 
@@ -660,27 +661,36 @@ __global__ void k_collapse(CollapseArgs a) {
 
 __global__ void k_set_int(int *p, int v) { *p = v; }
 
-__global__ void k_trace_closest(DevBvh bvh, const float4 *rays, float4 *hits, int64_t n, int *status) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
-    TraceHit h{0.0f, -1, 0.0f, 0.0f};
-    int ovf = 0;
-    bool f = trace_bvh<false>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
-    hits[i] = f ? make_float4(h.t, __int_as_float(h.prim), h.u, h.v)
-                : make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f);
-    if (ovf) atomicOr(status, kStatusStackOverflow);
+// Batch ray casting: lj_ray / lj_hit have the wavefront queues' layout, so
+// the persistent dynamic-fetch traversal of lj_trace_queue.cuh serves them.
+struct AnyBatchIO {
+    DevBvh b;
+    const float4 *rays;
+    uint8_t *occ;
+    LJ_D const DevBvh &bvh(int) const { return b; }
+    LJ_D void load(int r, V3 &o, V3 &d, float &tn, float &tf) const { load_ray(rays, r, o, d, tn, tf); }
+    LJ_D void store(int r, const Trav &s) const { occ[r] = s.found ? 1 : 0; }
+};
+
+__global__ void __launch_bounds__(128, 8) k_trace_closest(DevBvh bvh, const float4 *rays, float4 *hits, int n,
+                                                          int *fetch, int *status) {
+    ClosestQueueIO io{bvh, rays, hits};
+    trace_queue<false, 128>(io, n, fetch, status);
 }
 
-__global__ void k_trace_any(DevBvh bvh, const float4 *rays, uint8_t *occ, int64_t n, int *status) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
-    TraceHit h{0.0f, -1, 0.0f, 0.0f};
-    int ovf = 0;
-    bool f = trace_bvh<true>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
-    occ[i] = f ? 1 : 0;
-    if (ovf) atomicOr(status, kStatusStackOverflow);
+__global__ void __launch_bounds__(128, 8) k_trace_any(DevBvh bvh, const float4 *rays, uint8_t *occ, int n,
+                                                      int *fetch, int *status) {
+    AnyBatchIO io{bvh, rays, occ};
+    trace_queue<true, 128>(io, n, fetch, status);
+}
+
+// persistent grid of a traversal kernel on the current device
+int batch_grid(const void *kernel) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
+    return std::max(1, sms * std::max(1, per_sm));
 }
 
 template <bool kAny>
@@ -909,18 +919,37 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
     return 0;
 }
 
+// Chunks of at most 2^30 rays; each launch gets a zeroed fetch counter of
+// its own (stream-ordered allocation), so calls on different streams do not
+// share one.
+template <bool kAny>
+int launch_trace_batch(const DevBvh &bvh, const void *rays, void *out, int64_t n, int *d_status, cudaStream_t s) {
+    if (n <= 0) return 0;
+    int *fetch = nullptr;
+    if (cudaMallocAsync(&fetch, sizeof(int), s) != cudaSuccess) return -2;
+    const int grid = batch_grid(kAny ? (const void *)k_trace_any : (const void *)k_trace_closest);
+    const int64_t chunk = (int64_t)1 << 30;
+    int rc = 0;
+    for (int64_t off = 0; off < n && rc == 0; off += chunk) {
+        const int m = (int)std::min(chunk, n - off);
+        const float4 *r = (const float4 *)rays + 2 * off;
+        if (cudaMemsetAsync(fetch, 0, sizeof(int), s) != cudaSuccess) rc = -2;
+        if (kAny) k_trace_any<<<grid, 128, 0, s>>>(bvh, r, (uint8_t *)out + off, m, fetch, d_status);
+        else k_trace_closest<<<grid, 128, 0, s>>>(bvh, r, (float4 *)out + off, m, fetch, d_status);
+        if (cudaGetLastError() != cudaSuccess) rc = -2;
+    }
+    cudaFreeAsync(fetch, s);
+    return rc;
+}
+
 int launch_trace_closest(const DevBvh &bvh, const void *rays, void *hits, int64_t n, int *d_status,
                          cudaStream_t s) {
-    if (n <= 0) return 0;
-    k_trace_closest<<<grid_for(n, 128), 128, 0, s>>>(bvh, (const float4 *)rays, (float4 *)hits, n, d_status);
-    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+    return launch_trace_batch<false>(bvh, rays, hits, n, d_status, s);
 }
 
 int launch_trace_any(const DevBvh &bvh, const void *rays, uint8_t *occ, int64_t n, int *d_status,
                      cudaStream_t s) {
-    if (n <= 0) return 0;
-    k_trace_any<<<grid_for(n, 128), 128, 0, s>>>(bvh, (const float4 *)rays, occ, n, d_status);
-    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+    return launch_trace_batch<true>(bvh, rays, occ, n, d_status, s);
 }
 
 }  // namespace lj
