@@ -428,7 +428,9 @@ int lj_gpu_phase_batch(lj_ctx *ctx, int32_t phase_kind, float g,
  * from a captured CUDA graph.  Samples are keyed on (job seed, pixel,
  * sample) as in lj_gpu_render and summed in 64-bit fixed point (2^-32
  * units), so a job's image is bit-identical whatever else runs beside it.
- * Path-integrator scenes only (other integrators: LJ_ERR_UNSUPPORTED).
+ * Path and volumetric path (v6) scenes; each class of job has its own queue
+ * and shade kernel (other integrators: LJ_ERR_UNSUPPORTED).  A sample with a
+ * non-finite channel is dropped and counted in samples_dropped.
  * The server runs a host thread of its own; its functions may be called
  * from any one client thread at a time.  A scene submitted to a server stays
  * registered with it until lj_gpu_server_stop; lj_gpu_scene_destroy leaves

@@ -42,6 +42,7 @@
 
 #include "lj_host.h"
 #include "lj_trace_queue.cuh"
+#include "lj_volwave.cuh"
 #include "lj_wavefront.cuh"
 
 namespace lj {
@@ -59,7 +60,7 @@ struct SrvJob {
     int max_depth, rr_depth;
     float spread0;
     float clamp;                 // |sample| bound that keeps the sums inside int64
-    int mclass;                  // 0: materials of kClassicMats only, 1: any (shade kernel instance)
+    int mclass;                  // shade kernel: 0 path, kClassicMats materials; 1 path, any; 2 volpath
     int pad;
 };
 
@@ -85,6 +86,15 @@ struct StateSoA {
     float4 *ray;             // 2 per entry: org | tnear, dir | tfar
 };
 
+// Volumetric paths: their own queue pair (class 2), same idea.
+struct VolStateSoA {
+    int *job, *pixel;
+    uint64_t *rng;
+    float4 *beta, *L, *neep, *mdir, *mnee;
+    int4 *st;
+    float4 *ray;
+};
+
 struct SrvDev {
     const DevScene *scenes;
     const SrvJob *jobs;
@@ -96,20 +106,24 @@ struct SrvDev {
     long long *plan_start;       // per entry: first linear sample index
     StateSoA buf[2];
     float4 *hit;
+    VolStateSoA vbuf[2];
+    float4 *vhit;
     float4 *sray;                // shadow rays (2 per entry)
     int *starget;                // entry of the path in the next queue, or retire index | 2^31
     float4 *scontrib;
     int *rjob, *rpixel;          // finished paths
     float4 *rL;
     int *counts;                 // [0],[1] class-0 entries (front) of queue 0 / 1, [2] shadow,
-                                 // [3] retire, [5] regen count, [6],[7] class-0 / class-1
+                                 // [3] retire, [5] regen count, [6],[7],[14] class-0 / 1 / 2
                                  // entries that continue into the wave, [8],[9] ray fetch
-                                 // counters, [10],[11] class-1 entries (back) of queue 0 / 1
+                                 // counters, [10],[11] class-1 entries (back) of queue 0 / 1,
+                                 // [12],[13] entries of volpath queue 0 / 1
     // queue position of the k-th entry of class 1 (filled from the back)
     LJ_D int back(int k) const { return P - 1 - k; }
     // position of ray r of a queue with n0 class-0 entries
     LJ_D int entry(int r, int n0) const { return r < n0 ? r : back(r - n0); }
-    unsigned long long *stats;   // [0] closest rays, [1] shadow rays, [2] shade segments
+    unsigned long long *stats;   // [0] closest rays, [1] shadow rays, [2] shade segments,
+                                 // volpath: [5] shadow segments, [7] null, [8] real collisions
     int P;                       // queue capacity
     int *status;
 };
@@ -120,9 +134,10 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
     const int lane = threadIdx.x;
     int *counts = d.counts;
     const int n_order = d.order[0];
-    const int c0 = counts[cur], c1 = counts[10 + cur];   // paths that continue into this wave
-    const long long freec = (long long)d.P - c0 - c1;     // room for new paths
-    long long carry = 0, carry0 = 0, carry1 = 0;
+    // paths that continue into this wave, per class
+    const int c0 = counts[cur], c1 = counts[10 + cur], c2 = counts[12 + cur];
+    const long long freec = (long long)d.P - c0 - c1 - c2;   // room for new paths
+    long long carry = 0, carry0 = 0, carry1 = 0, carry2 = 0;
     for (int base = 0; base < n_order; base += 32) {
         const int k = base + lane;
         long long rem = 0, start = 0;
@@ -141,24 +156,27 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
         const long long off = min(carry + incl - rem, freec);
         const long long n = min(rem, freec - off);
         // prefix of the granted counts within each class
-        long long n0 = cls == 0 ? n : 0, n1 = cls == 0 ? 0 : n;
-        long long i0 = n0, i1 = n1;
+        const long long n0 = cls == 0 ? n : 0, n1 = cls == 1 ? n : 0, n2 = cls == 2 ? n : 0;
+        long long i0 = n0, i1 = n1, i2 = n2;
         for (int o = 1; o < 32; o <<= 1) {
             long long y0 = __shfl_up_sync(0xffffffffu, i0, o), y1 = __shfl_up_sync(0xffffffffu, i1, o);
+            long long y2 = __shfl_up_sync(0xffffffffu, i2, o);
             if (lane >= o) {
                 i0 += y0;
                 i1 += y1;
+                i2 += y2;
             }
         }
         if (k < n_order) {
             d.plan_off[k] = (int)off;
-            d.plan_coff[k] = (int)(cls == 0 ? carry0 + i0 - n0 : carry1 + i1 - n1);
+            d.plan_coff[k] = (int)(cls == 0 ? carry0 + i0 - n0 : (cls == 1 ? carry1 + i1 - n1 : carry2 + i2 - n2));
             d.plan_start[k] = start;
             if (n > 0) d.ctr[j].issued += (unsigned long long)n;
         }
         carry += __shfl_sync(0xffffffffu, incl, 31);
         carry0 += __shfl_sync(0xffffffffu, i0, 31);
         carry1 += __shfl_sync(0xffffffffu, i1, 31);
+        carry2 += __shfl_sync(0xffffffffu, i2, 31);
     }
     if (lane == 0) {
         const long long take = min(carry, freec);
@@ -166,10 +184,13 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
         counts[5] = (int)take;
         counts[6] = c0;
         counts[7] = c1;
-        counts[cur] = c0 + (int)carry0;   // carry0 + carry1 == take
+        counts[14] = c2;
+        counts[cur] = c0 + (int)carry0;   // carry0 + carry1 + carry2 == take
         counts[10 + cur] = c1 + (int)carry1;
+        counts[12 + cur] = c2 + (int)carry2;
         counts[cur ^ 1] = 0;
         counts[10 + (cur ^ 1)] = 0;
+        counts[12 + (cur ^ 1)] = 0;
         counts[2] = 0;
         counts[3] = 0;
         counts[8] = 0;
@@ -210,6 +231,22 @@ __global__ void __launch_bounds__(B) k_srv_regen(SrvDev d, int cur) {
         // fixed, coherent order: neighbouring threads of later kernels get
         // neighbouring pixels)
         const int t = d.plan_coff[lo] + (i - d.plan_off[lo]);
+        if (jb.mclass == 2) {   // volumetric path (initial state of k_vol_camera in lj_volpath.cu)
+            const VolStateSoA &v = d.vbuf[cur];
+            const int s = d.counts[14] + t;
+            v.job[s] = j;
+            v.pixel[s] = pixel;
+            v.rng[s] = rng.state;
+            v.beta[s] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+            v.L[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            v.neep[s] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            v.mdir[s] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+            v.mnee[s] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+            v.st[s] = make_int4(d.scenes[jb.scene].camera_medium, 0, 1, 1);
+            v.ray[2 * s] = make_float4(o.x, o.y, o.z, 0.0f);
+            v.ray[2 * s + 1] = make_float4(dir.x, dir.y, dir.z, __int_as_float(0x7f800000));
+            continue;
+        }
         const int s = jb.mclass == 0 ? d.counts[6] + t : d.back(d.counts[7] + t);
         q.job[s] = j;
         q.pixel[s] = pixel;
@@ -224,14 +261,23 @@ __global__ void __launch_bounds__(B) k_srv_regen(SrvDev d, int cur) {
 }
 
 // Ray queues of the server: each ray uses the BVH of its path's job's scene.
+// Rays r < n01 are path-tracer entries (class 0 front, class 1 back), the
+// rest volumetric ones.
 struct SrvClosestIO {
     const SrvDev &d;
-    int cur, n0;   // n0: class-0 entries of queue cur
-    LJ_D const DevBvh &bvh(int r) const { return d.scenes[d.jobs[d.buf[cur].job[d.entry(r, n0)]].scene].bvh; }
-    LJ_D void load(int r, V3 &o, V3 &dir, float &tn, float &tf) const {
-        load_ray(d.buf[cur].ray, d.entry(r, n0), o, dir, tn, tf);
+    int cur, n0, n01;   // class-0 entries; class-0 + class-1 entries of queue cur
+    LJ_D const DevBvh &bvh(int r) const {
+        const int job = r < n01 ? d.buf[cur].job[d.entry(r, n0)] : d.vbuf[cur].job[r - n01];
+        return d.scenes[d.jobs[job].scene].bvh;
     }
-    LJ_D void store(int r, const Trav &s) const { d.hit[d.entry(r, n0)] = hit_record(s); }
+    LJ_D void load(int r, V3 &o, V3 &dir, float &tn, float &tf) const {
+        if (r < n01) load_ray(d.buf[cur].ray, d.entry(r, n0), o, dir, tn, tf);
+        else load_ray(d.vbuf[cur].ray, r - n01, o, dir, tn, tf);
+    }
+    LJ_D void store(int r, const Trav &s) const {
+        if (r < n01) d.hit[d.entry(r, n0)] = hit_record(s);
+        else d.vhit[r - n01] = hit_record(s);
+    }
 };
 struct SrvShadowIO {
     const SrvDev &d;
@@ -311,9 +357,9 @@ struct QueuePaths {
 // traversal: 64 registers (full-SM occupancy of 50%, no spills)
 template <int B>
 __global__ void __launch_bounds__(B, 1024 / B) k_srv_trace(SrvDev d, int cur) {
-    const int n0 = d.counts[cur], n = n0 + d.counts[10 + cur];
+    const int n0 = d.counts[cur], n01 = n0 + d.counts[10 + cur], n = n01 + d.counts[12 + cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 0, (unsigned long long)n);
-    SrvClosestIO io{d, cur, n0};
+    SrvClosestIO io{d, cur, n0, n01};
     trace_queue<false, B>(io, n, d.counts + 8, d.status);
 }
 
@@ -332,6 +378,65 @@ __global__ void __launch_bounds__(B, (kClass == 0 ? 640 : 512) / B)
         const SrvJob &jb = jobs[d.buf[cur].job[e]];
         const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
         shade_segment<kClass == 0 ? kClassicMats : kAllMats>(scenes[jb.scene], paths, e, cfg, d.status);
+    }
+}
+
+// The volumetric path store: state in queue order in the volpath queues;
+// finished paths go to the retire list (radiance in rL.xyz).
+struct VolQueueStore {
+    const SrvDev &d;
+    int cur;
+    LJ_D void load(int i, VolState &vs, float4 &r0, float4 &r1, float4 &hit) const {
+        const VolStateSoA &v = d.vbuf[cur];
+        vs.slot = i;
+        vs.job = v.job[i];
+        vs.pixel = v.pixel[i];
+        vs.rng = v.rng[i];
+        vs.beta = v.beta[i];
+        vs.L = v.L[i];
+        vs.neep = v.neep[i];
+        vs.mdir = v.mdir[i];
+        vs.mnee = v.mnee[i];
+        vs.st = v.st[i];
+        r0 = v.ray[2 * i];
+        r1 = v.ray[2 * i + 1];
+        hit = d.vhit[i];
+    }
+    LJ_D void emit(const VolState &vs, bool alive, float4 ray0, float4 ray1) const {
+        if (alive) {
+            const int nxt = cur ^ 1;
+            const VolStateSoA &v = d.vbuf[nxt];
+            const int s = queue_slot(d.counts + 12 + nxt);
+            v.job[s] = vs.job;
+            v.pixel[s] = vs.pixel;
+            v.rng[s] = vs.rng;
+            v.beta[s] = vs.beta;
+            v.L[s] = vs.L;
+            v.neep[s] = vs.neep;
+            v.mdir[s] = vs.mdir;
+            v.mnee[s] = vs.mnee;
+            v.st[s] = vs.st;
+            v.ray[2 * s] = ray0;
+            v.ray[2 * s + 1] = ray1;
+        } else {
+            const int r = queue_slot(d.counts + 3);
+            d.rjob[r] = vs.job;
+            d.rpixel[r] = vs.pixel;
+            d.rL[r] = vs.L;
+        }
+    }
+};
+
+template <int B>
+__global__ void __launch_bounds__(B, 384 / B)
+    k_srv_volshade(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
+    const int n = d.counts[12 + cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 2, (unsigned long long)n);
+    const VolQueueStore store{d, cur};
+    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
+        const SrvJob &jb = jobs[d.vbuf[cur].job[i]];
+        const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
+        vol_shade_segment(scenes[jb.scene], store, i, cfg, d.status, d.stats + 4);
     }
 }
 
@@ -379,13 +484,14 @@ struct KernelSet {
     void (*trace)(SrvDev, int);
     void (*shade0)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*shade1)(SrvDev, const DevScene *, const SrvJob *, int);
+    void (*volshade)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*shadow)(SrvDev, int);
     void (*retire)(SrvDev);
 };
 template <int B>
 KernelSet kernel_set() {
-    return KernelSet{k_srv_regen<B>,    k_srv_trace<B>,  k_srv_shade<B, 0>,
-                     k_srv_shade<B, 1>, k_srv_shadow<B>, k_srv_retire<B>};
+    return KernelSet{k_srv_regen<B>,       k_srv_trace<B>,  k_srv_shade<B, 0>, k_srv_shade<B, 1>,
+                     k_srv_volshade<B>,    k_srv_shadow<B>, k_srv_retire<B>};
 }
 
 int occupancy_grid(const void *fn, int block, int sms) {
@@ -407,6 +513,8 @@ size_t pool_bytes(size_t P) {
     // hits; shadow rays, targets, contributions; retire job, pixel, radiance
     b += align256(P * 16) + align256(P * 32) + align256(P * 4) + align256(P * 16);
     b += align256(P * 4) * 2 + align256(P * 16);
+    // two volpath queue buffers: job, pixel, rng, beta, L, neep, mdir, mnee, st, ray; volpath hits
+    b += 2 * (align256(P * 4) * 2 + align256(P * 8) + align256(P * 16) * 6 + align256(P * 32)) + align256(P * 16);
     b += 256 * 2;   // counts, stats
     return b;
 }
@@ -485,7 +593,7 @@ struct lj_server {
     long long *d_plan_start = nullptr;
     SrvDev dev{};
     KernelSet ks{};
-    int grid[6] = {1, 1, 1, 1, 1, 1};
+    int grid[7] = {1, 1, 1, 1, 1, 1, 1};
     cudaGraphExec_t graph = nullptr;
 
     // pinned host staging
@@ -565,6 +673,9 @@ void launch_wave(lj_server *s, int cur) {
     mark(s, LJ_KERNEL_SHADE, false);
     mark(s, LJ_KERNEL_SHADE, true);
     s->ks.shade1<<<s->grid[5], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    mark(s, LJ_KERNEL_SHADE, false);
+    mark(s, LJ_KERNEL_SHADE, true);
+    s->ks.volshade<<<s->grid[6], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
     mark(s, LJ_KERNEL_SHADE, false);
     mark(s, LJ_KERNEL_SHADOW, true);
     s->ks.shadow<<<s->grid[3], B, 0, s->stream>>>(s->dev, cur);
@@ -652,6 +763,20 @@ std::string build_device(lj_server *s) {
         q.ray = carve<float4>(cur, 2 * P);
     }
     d.hit = carve<float4>(cur, P);
+    for (int k = 0; k < 2; k++) {
+        VolStateSoA &v = d.vbuf[k];
+        v.job = carve<int>(cur, P);
+        v.pixel = carve<int>(cur, P);
+        v.rng = carve<uint64_t>(cur, P);
+        v.beta = carve<float4>(cur, P);
+        v.L = carve<float4>(cur, P);
+        v.neep = carve<float4>(cur, P);
+        v.mdir = carve<float4>(cur, P);
+        v.mnee = carve<float4>(cur, P);
+        v.st = carve<int4>(cur, P);
+        v.ray = carve<float4>(cur, 2 * P);
+    }
+    d.vhit = carve<float4>(cur, P);
     d.sray = carve<float4>(cur, 2 * P);
     d.starget = carve<int>(cur, P);
     d.scontrib = carve<float4>(cur, P);
@@ -676,6 +801,7 @@ std::string build_device(lj_server *s) {
     s->grid[1] = occupancy_grid((const void *)s->ks.trace, s->block, sms);
     s->grid[2] = occupancy_grid((const void *)s->ks.shade0, s->block, sms);
     s->grid[5] = occupancy_grid((const void *)s->ks.shade1, s->block, sms);
+    s->grid[6] = occupancy_grid((const void *)s->ks.volshade, s->block, sms);
     s->grid[3] = occupancy_grid((const void *)s->ks.shadow, s->block, sms);
     s->grid[4] = occupancy_grid((const void *)s->ks.retire, s->block, sms);
 
@@ -740,7 +866,8 @@ std::string admit(lj_server *s, HostJob *j) {
     h.rr_depth = j->rr_depth;
     h.spread0 = 0.25f / (float)std::max(j->w, j->h);
     h.clamp = (float)std::ldexp(1.0, 30) / (float)j->spp;
-    h.mclass = (j->scene->mat_mask & ~kClassicMats) == 0 && !(s->opt.flags & LJ_SERVER_ONE_SHADE_KERNEL) ? 0 : 1;
+    if (j->scene->options.integrator == LJ_INTEGRATOR_VOLPATH) h.mclass = 2;
+    else h.mclass = (j->scene->mat_mask & ~kClassicMats) == 0 && !(s->opt.flags & LJ_SERVER_ONE_SHADE_KERNEL) ? 0 : 1;
     SRV_CUDA(cudaMemcpyAsync(s->d_jobs + slot, &h, sizeof(SrvJob), cudaMemcpyHostToDevice, s->stream));
     SRV_CUDA(cudaMemsetAsync(s->d_ctr + slot, 0, sizeof(SrvCtr), s->stream));
     SRV_CUDA(cudaMemsetAsync(s->d_cancel + slot, 0, sizeof(int), s->stream));
@@ -938,7 +1065,7 @@ void worker_main(lj_server *s) {
         if (e == cudaSuccess) e = collect_marks(s);
         lk.lock();
         s->waves += 2 * pairs;
-        s->kernel_launches += 14 * pairs;
+        s->kernel_launches += 16 * pairs;
         if (s->graph) s->graph_launches += pairs;
         const int b = s->poll_next;
         s->poll_next = (b + 1) % kPollsInFlight;
@@ -1100,8 +1227,10 @@ int lj_gpu_server_start(lj_ctx *ctx, const lj_server_options *options, lj_server
 int lj_gpu_server_submit(lj_server *s, lj_scene *scene, const lj_job_desc *job, int64_t *job_id) {
     if (!s || !scene || !job || !job_id) return LJ_ERR_INVALID_ARG;
     if (scene->ctx != s->ctx) return srv_error(s, LJ_ERR_INVALID_ARG, "submit: scene of another context");
-    if (scene->options.integrator != LJ_INTEGRATOR_PATH)
-        return srv_error(s, LJ_ERR_UNSUPPORTED, "submit: the server renders path-integrator scenes only");
+    if (scene->options.integrator != LJ_INTEGRATOR_PATH &&
+        !(scene->options.integrator == LJ_INTEGRATOR_VOLPATH &&
+          (scene->options.vol_path_version == 0 || scene->options.vol_path_version == 6)))
+        return srv_error(s, LJ_ERR_UNSUPPORTED, "submit: the server renders path and volpath (v6) scenes only");
     if (job->spp < 0 || job->width < 0 || job->height < 0 || (job->width > 0) != (job->height > 0))
         return srv_error(s, LJ_ERR_INVALID_ARG, "submit: negative spp / size, or only one of width and height");
     auto j = std::make_unique<HostJob>();

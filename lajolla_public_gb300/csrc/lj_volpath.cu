@@ -19,15 +19,11 @@
 #include <vector>
 
 #include "lj_host.h"
-#include "lj_phase.cuh"
-#include "lj_shade.cuh"
-#include "lj_trace.cuh"
+#include "lj_volwave.cuh"
 
 namespace lj {
 
 namespace {
-
-constexpr int kMaxShadowSegments = 1024;
 
 struct VolSoA {
     int *pixel;
@@ -48,169 +44,6 @@ struct VolQueues {
     unsigned long long *stats;    // [0] closest rays, [1] shadow segments, [2] segments, [3] null, [4] real
 };
 
-LJ_D uint32_t lane() { return threadIdx.x & 31u; }
-LJ_D int queue_slot(int *counter) {
-    unsigned active = __activemask();
-    int leader = __ffs(active) - 1;
-    int base = 0;
-    if ((int)lane() == leader) base = atomicAdd(counter, __popc(active));
-    base = __shfl_sync(active, base, leader);
-    return base + __popc(active & ((1u << lane()) - 1u));
-}
-
-LJ_D float chan(V3 v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : v.z); }
-LJ_D V3 vexp(V3 v) { return V3{expf(v.x), expf(v.y), expf(v.z)}; }
-LJ_D V3 vdiv(V3 a, V3 b) { return V3{a.x / b.x, a.y / b.y, a.z / b.z}; }
-
-// GridVolume lookup (src/volume.h:44-81)
-LJ_D V3 vol_lookup(const VolRec &v, V3 p) {
-    if (v.kind == 0) return V3{v.value[0], v.value[1], v.value[2]};
-    float nx = (p.x - v.pmin[0]) / (v.pmax[0] - v.pmin[0]);
-    float ny = (p.y - v.pmin[1]) / (v.pmax[1] - v.pmin[1]);
-    float nz = (p.z - v.pmin[2]) / (v.pmax[2] - v.pmin[2]);
-    if (nx < 0.f || nx > 1.f || ny < 0.f || ny > 1.f || nz < 0.f || nz > 1.f) return V3{0, 0, 0};
-    nx *= (float)(v.res[0] - 1);
-    ny *= (float)(v.res[1] - 1);
-    nz *= (float)(v.res[2] - 1);
-    int x0 = min(max((int)nx, 0), v.res[0] - 1), y0 = min(max((int)ny, 0), v.res[1] - 1),
-        z0 = min(max((int)nz, 0), v.res[2] - 1);
-    int x1 = min(x0 + 1, v.res[0] - 1), y1 = min(y0 + 1, v.res[1] - 1), z1 = min(z0 + 1, v.res[2] - 1);
-    float dx = nx - x0, dy = ny - y0, dz = nz - z0;
-    auto at = [&](int x, int y, int z) {
-        const float *q = v.data + (((size_t)z * v.res[1] + y) * v.res[0] + x) * 3;
-        return V3{__ldg(q), __ldg(q + 1), __ldg(q + 2)};
-    };
-    V3 r = at(x0, y0, z0) * ((1 - dx) * (1 - dy) * (1 - dz)) + at(x1, y0, z0) * (dx * (1 - dy) * (1 - dz)) +
-           at(x0, y1, z0) * ((1 - dx) * dy * (1 - dz)) + at(x1, y1, z0) * (dx * dy * (1 - dz)) +
-           at(x0, y0, z1) * ((1 - dx) * (1 - dy) * dz) + at(x1, y0, z1) * (dx * (1 - dy) * dz) +
-           at(x0, y1, z1) * ((1 - dx) * dy * dz) + at(x1, y1, z1) * (dx * dy * dz);
-    return r * v.scale;
-}
-// slab test against the density grid box (src/volume.h:124-144); tfar = inf
-LJ_D bool vol_box_hit(const VolRec &v, V3 o, V3 d) {
-    if (v.kind == 0) return true;
-    float t0 = 0.f, t1 = __int_as_float(0x7f800000);
-    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
-    for (int i = 0; i < 3; i++) {
-        float tn = (v.pmin[i] - oo[i]) / dd[i];
-        float tf = (v.pmax[i] - oo[i]) / dd[i];
-        if (tn > tf) { float x = tn; tn = tf; tf = x; }
-        t0 = tn > t0 ? tn : t0;
-        t1 = tf < t1 ? tf : t1;
-        if (t0 > t1) return false;
-    }
-    return true;
-}
-LJ_D V3 majorant(const MediumRec &m, V3 o, V3 d) {
-    if (m.kind == 0) return V3{m.sigma_a[0] + m.sigma_s[0], m.sigma_a[1] + m.sigma_s[1], m.sigma_a[2] + m.sigma_s[2]};
-    if (vol_box_hit(m.density, o, d)) return V3{m.density.max_value[0], m.density.max_value[1], m.density.max_value[2]};
-    return V3{0, 0, 0};
-}
-LJ_D void sigmas(const MediumRec &m, V3 p, V3 &ss, V3 &sa) {
-    if (m.kind == 0) {
-        ss = V3{m.sigma_s[0], m.sigma_s[1], m.sigma_s[2]};
-        sa = V3{m.sigma_a[0], m.sigma_a[1], m.sigma_a[2]};
-        return;
-    }
-    V3 dn = vol_lookup(m.density, p), al = vol_lookup(m.albedo, p);
-    ss = dn * al;
-    sa = dn * (V3{1, 1, 1} - al);
-}
-LJ_D int update_medium(const Vertex &v, V3 dir, int medium) {
-    if (v.interior_medium != v.exterior_medium) return dot(dir, v.ng) > 0.f ? v.exterior_medium : v.interior_medium;
-    return medium;
-}
-
-// NEE from p: a medium point (surface == false) or a surface vertex with a
-// material.  Ratio tracking through media, passing index-matching surfaces.
-LJ_D V3 vol_nee(const DevScene &sc, V3 p, int medium, bool surface, const Vertex &vx, const MatParams &mat,
-                const BsdfVertex &bv, V3 dir_view, int bounces, Pcg &rng, int *status,
-                unsigned long long *seg_stat) {
-    float lu0 = pcg_uniform(rng), lu1 = pcg_uniform(rng), lw = pcg_uniform(rng), sw = pcg_uniform(rng);
-    if (sc.num_lights == 0) return V3{0, 0, 0};
-    int lid = sample_light(sc, lw);
-    PN pl = sample_point_on_light(sc, lid, p, lu0, lu1, sw);
-    bool env = sc.lights[lid].kind != 0;
-    V3 dir = env ? -pl.n : normalize(pl.p - p);
-    V3 T{1, 1, 1}, p_nee{1, 1, 1}, p_dir{1, 1, 1};
-    int smed = surface ? update_medium(vx, dir, medium) : medium;
-    int sbounces = 0;
-    V3 p0 = p;
-    float oeps = surface ? sc.eps : 0.0f;
-    const float inf = __int_as_float(0x7f800000);
-    int segs = 0;
-    for (int seg = 0; seg < kMaxShadowSegments; seg++) {
-        segs++;
-        float dist = env ? inf : length(pl.p - p0);
-        float tmax = env ? inf : (1.0f - sc.eps) * dist;
-        TraceHit h{0.0f, -1, 0.0f, 0.0f};
-        int ovf = 0;
-        bool hit = trace_bvh<false>(sc.bvh, p0, dir, oeps, tmax, h, &ovf);
-        if (ovf) atomicOr(status, kStatusStackOverflow);
-        float next_t = hit ? h.t : dist;
-        if (smed >= 0) {
-            const MediumRec &m = sc.media[smed];
-            V3 maj = majorant(m, p0, dir);
-            float mmax = max3(maj);
-            int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
-            float acc = 0.0f;
-            for (int it = 0; it < sc.max_null_collisions; it++) {
-                if (chan(maj, c) <= 0.0f) break;
-                float t = -logf(1.0f - pcg_uniform(rng)) / chan(maj, c);
-                float dt = next_t - acc;
-                acc = fminf(acc + t, next_t);
-                if (t < dt) {
-                    V3 ss, sa;
-                    sigmas(m, p0 + dir * acc, ss, sa);
-                    V3 st = ss + sa;
-                    V3 e = vexp(maj * -t);
-                    T = T * e * (maj - st) / mmax;
-                    p_nee = p_nee * e * maj / mmax;
-                    p_dir = p_dir * e * maj * (V3{1, 1, 1} - vdiv(st, maj)) / mmax;
-                    if (max3(T) <= 0.0f) break;
-                } else {
-                    V3 e = vexp(maj * -dt);
-                    T = T * e;
-                    p_nee = p_nee * e;
-                    p_dir = p_dir * e;
-                    break;
-                }
-            }
-        }
-        if (!hit) break;
-        int shape = __ldg(sc.prim_shape + h.prim);
-        if (sc.shapes[shape].material_id >= 0) return V3{0, 0, 0};
-        sbounces++;
-        if (sc.max_depth != -1 && bounces + sbounces + 1 >= sc.max_depth) return V3{0, 0, 0};
-        Vertex sv = make_vertex(sc, p0, dir, h.t, h.prim, h.u, h.v, 0.0f);
-        smed = update_medium(sv, dir, smed);
-        p0 = p0 + dir * next_t;
-        oeps = sc.eps;
-        if (seg == kMaxShadowSegments - 1) atomicOr(status, kStatusBounceCap);
-    }
-    if (seg_stat) atomicAdd(seg_stat, (unsigned long long)segs);
-    if (max3(T) <= 0.0f) return V3{0, 0, 0};
-    V3 dp = pl.p - p;
-    float G = env ? 1.0f : fmaxf(-dot(dir, pl.n), 0.0f) / dot(dp, dp);
-    float pdf_nee = __ldg(sc.light_pmf + lid) * pdf_point_on_light(sc, lid, pl, p);
-    if (!(G > 0.0f && pdf_nee > 0.0f)) return V3{0, 0, 0};
-    V3 f;
-    float pdf_dir;
-    if (surface) {
-        f = bsdf_eval(mat, bv, dir_view, dir);
-        pdf_dir = bsdf_pdf(mat, bv, dir_view, dir);
-    } else {
-        const MediumRec &m = sc.media[medium];
-        float ph = phase_eval(m.phase_kind, m.g, dir_view, dir);
-        f = V3{ph, ph, ph};
-        pdf_dir = ph;
-    }
-    V3 Le = light_emission(sc, lid, -dir, pl);
-    float pn = pdf_nee * avg3(p_nee);
-    float pd = pdf_dir * G * avg3(p_dir);
-    float w = (pn * pn) / (pn * pn + pd * pd);
-    return T * f * Le * (G * w / pn);
-}
 
 __global__ void k_vol_camera(DevScene sc, VolSoA ps, VolQueues q, int P, int num_pixels, int sample_base,
                              uint64_t seed);
@@ -259,199 +92,56 @@ __global__ void __launch_bounds__(128) k_vol_trace(DevBvh bvh, const float4 *ray
     }
 }
 
+// The single-scene renderer's store: state in fixed slots, queues carry
+// slot ids.
+struct VolSlotStore {
+    VolSoA ps;
+    VolQueues q;
+    int cur;
+    LJ_D void load(int i, VolState &vs, float4 &r0, float4 &r1, float4 &hit) const {
+        const int p = (cur ? q.path[1] : q.path[0])[i];
+        const float4 *rays = cur ? q.ray[1] : q.ray[0];
+        r0 = rays[2 * i];
+        r1 = rays[2 * i + 1];
+        hit = q.hit[i];
+        vs.slot = p;
+        vs.job = 0;
+        vs.pixel = ps.pixel[p];
+        vs.rng = ps.rng[p];
+        vs.beta = ps.beta[p];
+        vs.L = ps.L[p];
+        vs.neep = ps.neep[p];
+        vs.mdir = ps.mdir[p];
+        vs.mnee = ps.mnee[p];
+        vs.st = ps.st[p];
+    }
+    LJ_D void emit(const VolState &vs, bool alive, float4 ray0, float4 ray1) const {
+        const int p = vs.slot, nxt = cur ^ 1;
+        if (alive) {
+            const int s = queue_slot(q.counts + nxt);
+            float4 *nrays = nxt ? q.ray[1] : q.ray[0];
+            nrays[2 * s] = ray0;
+            nrays[2 * s + 1] = ray1;
+            (nxt ? q.path[1] : q.path[0])[s] = p;
+        }
+        ps.beta[p] = vs.beta;
+        ps.L[p] = vs.L;
+        ps.neep[p] = vs.neep;
+        ps.mdir[p] = vs.mdir;
+        ps.mnee[p] = vs.mnee;
+        ps.st[p] = vs.st;
+        ps.rng[p] = vs.rng;
+    }
+};
+
 __global__ void __launch_bounds__(128) k_vol_shade(DevScene sc, VolSoA ps, VolQueues q, int cur, float spread0,
                                                    int *status) {
     const int n = q.counts[cur];
-    const int nxt = cur ^ 1;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(q.stats + 2, (unsigned long long)n);
-    const float inf = __int_as_float(0x7f800000);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int p = (cur ? q.path[1] : q.path[0])[i];
-        const float4 *rays = cur ? q.ray[1] : q.ray[0];
-        float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
-        V3 ro{r0.x, r0.y, r0.z}, rd{r1.x, r1.y, r1.z};
-        float4 hit = q.hit[i];
-        int prim = __float_as_int(hit.y);
-        float4 bw = ps.beta[p], Lw = ps.L[p], np4 = ps.neep[p], md4 = ps.mdir[p], mn4 = ps.mnee[p];
-        int4 st = ps.st[p];
-        V3 beta{bw.x, bw.y, bw.z}, L{Lw.x, Lw.y, Lw.z}, neep{np4.x, np4.y, np4.z};
-        V3 mdir{md4.x, md4.y, md4.z}, mnee{mn4.x, mn4.y, mn4.z};
-        float eta_scale = bw.w, dir_pdf = Lw.w;
-        int medium = st.x, bounces = st.y;
-        bool never_scatter = st.z != 0, first = st.w != 0;
-        Pcg rng;
-        rng.state = ps.rng[p];
-        rng.inc = ((uint64_t)ps.pixel[p] << 1u) | 1u;
-        bool alive = true, cont = false;
-        V3 next_o{0, 0, 0}, next_d{0, 0, 0};
-        float next_tnear = 0.0f;
-
-        float t_hit = prim >= 0 ? hit.x : inf;
-        bool scatter = false;
-        V3 p_scatter{0, 0, 0};
-        if (medium >= 0) {
-            const MediumRec &m = sc.media[medium];
-            V3 maj = majorant(m, ro, rd);
-            float mmax = max3(maj);
-            int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
-            float acc = 0.0f;
-            V3 T{1, 1, 1}, pd{1, 1, 1}, pn{1, 1, 1};
-            unsigned nulls = 0;
-            for (int it = 0; it < sc.max_null_collisions; it++) {
-                if (chan(maj, c) <= 0.0f) break;
-                float t = -logf(1.0f - pcg_uniform(rng)) / chan(maj, c);
-                float dt = t_hit - acc;
-                acc = fminf(acc + t, t_hit);
-                if (t < dt) {
-                    V3 ss, sa;
-                    V3 pp = ro + rd * acc;
-                    sigmas(m, pp, ss, sa);
-                    V3 stt = ss + sa;
-                    V3 real = vdiv(stt, maj);
-                    V3 e = vexp(maj * -t);
-                    if (pcg_uniform(rng) < chan(real, c)) {
-                        scatter = true;
-                        T = T * e / mmax;
-                        pd = pd * e * maj * real / mmax;
-                        p_scatter = pp;
-                        break;
-                    }
-                    nulls++;
-                    T = T * e * (maj - stt) / mmax;
-                    pd = pd * e * maj * (V3{1, 1, 1} - real) / mmax;
-                    pn = pn * e * maj / mmax;
-                } else {
-                    V3 e = vexp(maj * -dt);
-                    T = T * e;
-                    pd = pd * e;
-                    pn = pn * e;
-                    break;
-                }
-            }
-            if (nulls) atomicAdd(q.stats + 3, (unsigned long long)nulls);
-            if (scatter) atomicAdd(q.stats + 4, 1ull);
-            beta = beta * T / avg3(pd);
-            mdir = mdir * pd;
-            mnee = mnee * pn;
-        }
-        Vertex vx;
-        if (!scatter) {
-            if (prim < 0) {
-                if (sc.env.light_id >= 0) {
-                    V3 Le = env_emission(sc, -rd);
-                    if (never_scatter) {
-                        L += beta * Le;
-                    } else {
-                        float pn = __ldg(sc.light_pmf + sc.env.light_id) * env_pdf(sc, rd) * avg3(mnee);
-                        float pd = dir_pdf * avg3(mdir);
-                        L += beta * Le * ((pd * pd) / (pd * pd + pn * pn));
-                    }
-                }
-                alive = false;
-            } else {
-                vx = make_vertex(sc, ro, rd, hit.x, prim, hit.z, hit.w, first ? spread0 : 0.0f);
-                if (vx.light >= 0) {
-                    V3 Le = light_emission(sc, vx.light, -rd, PN{vx.p, vx.ng});
-                    if (never_scatter) {
-                        L += beta * Le;
-                    } else {
-                        V3 dv = vx.p - neep;
-                        float G = fabsf(dot(rd, vx.ng)) / dot(dv, dv);
-                        float pn = __ldg(sc.light_pmf + vx.light) *
-                                   pdf_point_on_light(sc, vx.light, PN{vx.p, vx.ng}, neep) * avg3(mnee);
-                        float pd = dir_pdf * G * avg3(mdir);
-                        L += beta * Le * ((pd * pd) / (pd * pd + pn * pn));
-                    }
-                }
-            }
-        }
-        if (alive && sc.max_depth != -1 && bounces == sc.max_depth - 1) alive = false;
-        if (alive && bounces > LJ_MAX_BOUNCES) {
-            atomicOr(status, kStatusBounceCap);
-            alive = false;
-        }
-        if (alive && scatter) {
-            const MediumRec &m = sc.media[medium];
-            V3 ss, sa;
-            sigmas(m, p_scatter, ss, sa);
-            V3 wv = -rd;
-            MatParams dummy_mat;
-            dummy_mat.type = 0;
-            BsdfVertex dummy_bv{V3{0, 0, 1}, frame_from_n(V3{0, 0, 1})};
-            L += beta * ss * vol_nee(sc, p_scatter, medium, false, vx, dummy_mat, dummy_bv, wv, bounces, rng,
-                                     status, q.stats + 1);
-            float u0 = pcg_uniform(rng), u1 = pcg_uniform(rng);
-            V3 nd = phase_sample(m.phase_kind, m.g, wv, u0, u1);
-            beta = beta * ss;
-            dir_pdf = phase_eval(m.phase_kind, m.g, wv, nd);
-            neep = p_scatter;
-            mdir = V3{1, 1, 1};
-            mnee = V3{1, 1, 1};
-            never_scatter = false;
-            next_o = p_scatter;
-            next_d = nd;
-            next_tnear = 0.0f;
-        } else if (alive) {
-            if (vx.material < 0) {
-                medium = update_medium(vx, rd, medium);
-                next_o = vx.p;
-                next_d = rd;
-                next_tnear = sc.eps;
-                bounces++;
-                cont = true;
-            } else {
-                MatParams mat = resolve_material(sc, vx.material, vx.u, vx.v, vx.uv_screen_size);
-                BsdfVertex bv{vx.ng, vx.frame};
-                V3 wv = -rd;
-                L += beta * vol_nee(sc, vx.p, medium, true, vx, mat, bv, wv, bounces, rng, status, q.stats + 1);
-                float b0 = pcg_uniform(rng), b1 = pcg_uniform(rng), b2 = pcg_uniform(rng);
-                BsdfSample bs = bsdf_sample(mat, bv, wv, b0, b1, b2);
-                if (!bs.valid) {
-                    alive = false;
-                } else {
-                    V3 f = bsdf_eval(mat, bv, wv, bs.dir);
-                    float pdf = bsdf_pdf(mat, bv, wv, bs.dir);
-                    if (!(pdf > 0.0f)) {
-                        alive = false;
-                    } else {
-                        if (bs.eta != 0.0f) eta_scale /= (bs.eta * bs.eta);
-                        beta = beta * f / pdf;
-                        dir_pdf = pdf;
-                        neep = vx.p;
-                        mdir = V3{1, 1, 1};
-                        mnee = V3{1, 1, 1};
-                        never_scatter = false;
-                        medium = update_medium(vx, bs.dir, medium);
-                        next_o = vx.p;
-                        next_d = bs.dir;
-                        next_tnear = sc.eps;
-                    }
-                }
-            }
-        }
-        if (alive && !cont) {
-            if (bounces >= sc.rr_depth) {
-                float rr = fminf(max3(beta) / eta_scale, 0.95f);
-                if (pcg_uniform(rng) > rr) alive = false;
-                else beta = beta / rr;
-            }
-            bounces++;
-        }
-        if (alive) {
-            int s = queue_slot(q.counts + nxt);
-            float4 *nrays = nxt ? q.ray[1] : q.ray[0];
-            nrays[2 * s] = make_float4(next_o.x, next_o.y, next_o.z, next_tnear);
-            nrays[2 * s + 1] = make_float4(next_d.x, next_d.y, next_d.z, inf);
-            (nxt ? q.path[1] : q.path[0])[s] = p;
-        }
-        ps.beta[p] = make_float4(beta.x, beta.y, beta.z, eta_scale);
-        ps.L[p] = make_float4(L.x, L.y, L.z, dir_pdf);
-        ps.neep[p] = make_float4(neep.x, neep.y, neep.z, 0.0f);
-        ps.mdir[p] = make_float4(mdir.x, mdir.y, mdir.z, 0.0f);
-        ps.mnee[p] = make_float4(mnee.x, mnee.y, mnee.z, 0.0f);
-        ps.st[p] = make_int4(medium, bounces, never_scatter ? 1 : 0, 0);
-        ps.rng[p] = rng.state;
-    }
+    const ShadeCfg cfg{sc.max_depth, sc.rr_depth, spread0};
+    const VolSlotStore store{ps, q, cur};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        vol_shade_segment(sc, store, i, cfg, status, q.stats);
 }
 
 // Per pixel: sum the batch's samples in sample order, skipping samples with

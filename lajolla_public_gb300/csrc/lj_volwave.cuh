@@ -1,0 +1,377 @@
+// The shade step of the volumetric path tracer (v6), shared by the
+// single-scene renderer (lj_volpath.cu) and the server (lj_server.cu): the
+// GPU form of vol_path_tracing (src/vol_path_tracing.h:59-64, a stub in the
+// reference; the algorithm is the one handouts/homework2.tex:303-816
+// specifies, restated in oracle/lj_oracle.cpp with the same random-number
+// order).  One queue entry: free-flight delta tracking over [0, t_hit) with
+// the chromatic majorant (one channel sampled per segment); then, at a real
+// scattering point or a surface: emission with MIS, NEE with ratio tracking
+// through index-matching surfaces (the shadow traversal runs here), phase /
+// BSDF sampling, Russian roulette, the next ray.  A store decides where the
+// state lives (fixed slots or queue order), as for the path tracer.
+#pragma once
+
+#include "../../include/lj_gpu.h"
+#include "lj_internal.h"
+#include "lj_phase.cuh"
+#include "lj_shade.cuh"
+#include "lj_trace.cuh"
+#include "lj_wavefront.cuh"
+
+namespace lj {
+
+constexpr int kMaxShadowSegments = 1024;
+
+// State of one volumetric path between two events.
+struct VolState {
+    int slot, job, pixel;
+    uint64_t rng;
+    float4 beta;   // xyz throughput, w eta_scale
+    float4 L;      // xyz radiance, w dir_pdf (solid angle) of the last scattering
+    float4 neep;   // xyz position of the last vertex that could issue NEE
+    float4 mdir;   // xyz product of free-flight pdfs since that vertex
+    float4 mnee;   // xyz product of ratio-tracking pdfs since that vertex
+    int4 st;       // x medium, y bounces, z never_scatter, w first ray
+};
+
+LJ_D float chan(V3 v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : v.z); }
+LJ_D V3 vexp(V3 v) { return V3{expf(v.x), expf(v.y), expf(v.z)}; }
+LJ_D V3 vdiv(V3 a, V3 b) { return V3{a.x / b.x, a.y / b.y, a.z / b.z}; }
+
+// GridVolume lookup (src/volume.h:44-81)
+LJ_D V3 vol_lookup(const VolRec &v, V3 p) {
+    if (v.kind == 0) return V3{v.value[0], v.value[1], v.value[2]};
+    float nx = (p.x - v.pmin[0]) / (v.pmax[0] - v.pmin[0]);
+    float ny = (p.y - v.pmin[1]) / (v.pmax[1] - v.pmin[1]);
+    float nz = (p.z - v.pmin[2]) / (v.pmax[2] - v.pmin[2]);
+    if (nx < 0.f || nx > 1.f || ny < 0.f || ny > 1.f || nz < 0.f || nz > 1.f) return V3{0, 0, 0};
+    nx *= (float)(v.res[0] - 1);
+    ny *= (float)(v.res[1] - 1);
+    nz *= (float)(v.res[2] - 1);
+    int x0 = min(max((int)nx, 0), v.res[0] - 1), y0 = min(max((int)ny, 0), v.res[1] - 1),
+        z0 = min(max((int)nz, 0), v.res[2] - 1);
+    int x1 = min(x0 + 1, v.res[0] - 1), y1 = min(y0 + 1, v.res[1] - 1), z1 = min(z0 + 1, v.res[2] - 1);
+    float dx = nx - x0, dy = ny - y0, dz = nz - z0;
+    auto at = [&](int x, int y, int z) {
+        const float *q = v.data + (((size_t)z * v.res[1] + y) * v.res[0] + x) * 3;
+        return V3{__ldg(q), __ldg(q + 1), __ldg(q + 2)};
+    };
+    V3 r = at(x0, y0, z0) * ((1 - dx) * (1 - dy) * (1 - dz)) + at(x1, y0, z0) * (dx * (1 - dy) * (1 - dz)) +
+           at(x0, y1, z0) * ((1 - dx) * dy * (1 - dz)) + at(x1, y1, z0) * (dx * dy * (1 - dz)) +
+           at(x0, y0, z1) * ((1 - dx) * (1 - dy) * dz) + at(x1, y0, z1) * (dx * (1 - dy) * dz) +
+           at(x0, y1, z1) * ((1 - dx) * dy * dz) + at(x1, y1, z1) * (dx * dy * dz);
+    return r * v.scale;
+}
+// slab test against the density grid box (src/volume.h:124-144); tfar = inf
+LJ_D bool vol_box_hit(const VolRec &v, V3 o, V3 d) {
+    if (v.kind == 0) return true;
+    float t0 = 0.f, t1 = __int_as_float(0x7f800000);
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    for (int i = 0; i < 3; i++) {
+        float tn = (v.pmin[i] - oo[i]) / dd[i];
+        float tf = (v.pmax[i] - oo[i]) / dd[i];
+        if (tn > tf) { float x = tn; tn = tf; tf = x; }
+        t0 = tn > t0 ? tn : t0;
+        t1 = tf < t1 ? tf : t1;
+        if (t0 > t1) return false;
+    }
+    return true;
+}
+LJ_D V3 majorant(const MediumRec &m, V3 o, V3 d) {
+    if (m.kind == 0) return V3{m.sigma_a[0] + m.sigma_s[0], m.sigma_a[1] + m.sigma_s[1], m.sigma_a[2] + m.sigma_s[2]};
+    if (vol_box_hit(m.density, o, d)) return V3{m.density.max_value[0], m.density.max_value[1], m.density.max_value[2]};
+    return V3{0, 0, 0};
+}
+LJ_D void sigmas(const MediumRec &m, V3 p, V3 &ss, V3 &sa) {
+    if (m.kind == 0) {
+        ss = V3{m.sigma_s[0], m.sigma_s[1], m.sigma_s[2]};
+        sa = V3{m.sigma_a[0], m.sigma_a[1], m.sigma_a[2]};
+        return;
+    }
+    V3 dn = vol_lookup(m.density, p), al = vol_lookup(m.albedo, p);
+    ss = dn * al;
+    sa = dn * (V3{1, 1, 1} - al);
+}
+LJ_D int update_medium(const Vertex &v, V3 dir, int medium) {
+    if (v.interior_medium != v.exterior_medium) return dot(dir, v.ng) > 0.f ? v.exterior_medium : v.interior_medium;
+    return medium;
+}
+
+// NEE from p: a medium point (surface == false) or a surface vertex with a
+// material.  Ratio tracking through media, passing index-matching surfaces.
+LJ_D V3 vol_nee(const DevScene &sc, V3 p, int medium, bool surface, const Vertex &vx, const MatParams &mat,
+                const BsdfVertex &bv, V3 dir_view, int bounces, int max_depth, Pcg &rng, int *status,
+                unsigned long long *seg_stat) {
+    float lu0 = pcg_uniform(rng), lu1 = pcg_uniform(rng), lw = pcg_uniform(rng), sw = pcg_uniform(rng);
+    if (sc.num_lights == 0) return V3{0, 0, 0};
+    int lid = sample_light(sc, lw);
+    PN pl = sample_point_on_light(sc, lid, p, lu0, lu1, sw);
+    bool env = sc.lights[lid].kind != 0;
+    V3 dir = env ? -pl.n : normalize(pl.p - p);
+    V3 T{1, 1, 1}, p_nee{1, 1, 1}, p_dir{1, 1, 1};
+    int smed = surface ? update_medium(vx, dir, medium) : medium;
+    int sbounces = 0;
+    V3 p0 = p;
+    float oeps = surface ? sc.eps : 0.0f;
+    const float inf = __int_as_float(0x7f800000);
+    int segs = 0;
+    for (int seg = 0; seg < kMaxShadowSegments; seg++) {
+        segs++;
+        float dist = env ? inf : length(pl.p - p0);
+        float tmax = env ? inf : (1.0f - sc.eps) * dist;
+        TraceHit h{0.0f, -1, 0.0f, 0.0f};
+        int ovf = 0;
+        bool hit = trace_bvh<false>(sc.bvh, p0, dir, oeps, tmax, h, &ovf);
+        if (ovf) atomicOr(status, kStatusStackOverflow);
+        float next_t = hit ? h.t : dist;
+        if (smed >= 0) {
+            const MediumRec &m = sc.media[smed];
+            V3 maj = majorant(m, p0, dir);
+            float mmax = max3(maj);
+            int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
+            float acc = 0.0f;
+            for (int it = 0; it < sc.max_null_collisions; it++) {
+                if (chan(maj, c) <= 0.0f) break;
+                float t = -logf(1.0f - pcg_uniform(rng)) / chan(maj, c);
+                float dt = next_t - acc;
+                acc = fminf(acc + t, next_t);
+                if (t < dt) {
+                    V3 ss, sa;
+                    sigmas(m, p0 + dir * acc, ss, sa);
+                    V3 st = ss + sa;
+                    V3 e = vexp(maj * -t);
+                    T = T * e * (maj - st) / mmax;
+                    p_nee = p_nee * e * maj / mmax;
+                    p_dir = p_dir * e * maj * (V3{1, 1, 1} - vdiv(st, maj)) / mmax;
+                    if (max3(T) <= 0.0f) break;
+                } else {
+                    V3 e = vexp(maj * -dt);
+                    T = T * e;
+                    p_nee = p_nee * e;
+                    p_dir = p_dir * e;
+                    break;
+                }
+            }
+        }
+        if (!hit) break;
+        int shape = __ldg(sc.prim_shape + h.prim);
+        if (sc.shapes[shape].material_id >= 0) return V3{0, 0, 0};
+        sbounces++;
+        if (max_depth != -1 && bounces + sbounces + 1 >= max_depth) return V3{0, 0, 0};
+        Vertex sv = make_vertex(sc, p0, dir, h.t, h.prim, h.u, h.v, 0.0f);
+        smed = update_medium(sv, dir, smed);
+        p0 = p0 + dir * next_t;
+        oeps = sc.eps;
+        if (seg == kMaxShadowSegments - 1) atomicOr(status, kStatusBounceCap);
+    }
+    if (seg_stat) atomicAdd(seg_stat, (unsigned long long)segs);
+    if (max3(T) <= 0.0f) return V3{0, 0, 0};
+    V3 dp = pl.p - p;
+    float G = env ? 1.0f : fmaxf(-dot(dir, pl.n), 0.0f) / dot(dp, dp);
+    float pdf_nee = __ldg(sc.light_pmf + lid) * pdf_point_on_light(sc, lid, pl, p);
+    if (!(G > 0.0f && pdf_nee > 0.0f)) return V3{0, 0, 0};
+    V3 f;
+    float pdf_dir;
+    if (surface) {
+        f = bsdf_eval(mat, bv, dir_view, dir);
+        pdf_dir = bsdf_pdf(mat, bv, dir_view, dir);
+    } else {
+        const MediumRec &m = sc.media[medium];
+        float ph = phase_eval(m.phase_kind, m.g, dir_view, dir);
+        f = V3{ph, ph, ph};
+        pdf_dir = ph;
+    }
+    V3 Le = light_emission(sc, lid, -dir, pl);
+    float pn = pdf_nee * avg3(p_nee);
+    float pd = pdf_dir * G * avg3(p_dir);
+    float w = (pn * pn) / (pn * pn + pd * pd);
+    return T * f * Le * (G * w / pn);
+}
+
+
+// stats: [1] shadow segments, [3] null collisions, [4] real collisions
+template <class Store>
+LJ_D void vol_shade_segment(const DevScene &sc, const Store &store, int i, const ShadeCfg &cfg, int *status,
+                            unsigned long long *stats) {
+    const float inf = __int_as_float(0x7f800000);
+    VolState vs;
+    float4 r0, r1, hit;
+    store.load(i, vs, r0, r1, hit);
+    V3 ro{r0.x, r0.y, r0.z}, rd{r1.x, r1.y, r1.z};
+    int prim = __float_as_int(hit.y);
+    V3 beta{vs.beta.x, vs.beta.y, vs.beta.z}, L{vs.L.x, vs.L.y, vs.L.z}, neep{vs.neep.x, vs.neep.y, vs.neep.z};
+    V3 mdir{vs.mdir.x, vs.mdir.y, vs.mdir.z}, mnee{vs.mnee.x, vs.mnee.y, vs.mnee.z};
+    float eta_scale = vs.beta.w, dir_pdf = vs.L.w;
+    int medium = vs.st.x, bounces = vs.st.y;
+    bool never_scatter = vs.st.z != 0, first = vs.st.w != 0;
+    Pcg rng;
+    rng.state = vs.rng;
+    rng.inc = ((uint64_t)vs.pixel << 1u) | 1u;
+    bool alive = true, cont = false;
+    V3 next_o{0, 0, 0}, next_d{0, 0, 0};
+    float next_tnear = 0.0f;
+
+    float t_hit = prim >= 0 ? hit.x : inf;
+    bool scatter = false;
+    V3 p_scatter{0, 0, 0};
+    if (medium >= 0) {
+        const MediumRec &m = sc.media[medium];
+        V3 maj = majorant(m, ro, rd);
+        float mmax = max3(maj);
+        int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
+        float acc = 0.0f;
+        V3 T{1, 1, 1}, pd{1, 1, 1}, pn{1, 1, 1};
+        unsigned nulls = 0;
+        for (int it = 0; it < sc.max_null_collisions; it++) {
+            if (chan(maj, c) <= 0.0f) break;
+            float t = -logf(1.0f - pcg_uniform(rng)) / chan(maj, c);
+            float dt = t_hit - acc;
+            acc = fminf(acc + t, t_hit);
+            if (t < dt) {
+                V3 ss, sa;
+                V3 pp = ro + rd * acc;
+                sigmas(m, pp, ss, sa);
+                V3 stt = ss + sa;
+                V3 real = vdiv(stt, maj);
+                V3 e = vexp(maj * -t);
+                if (pcg_uniform(rng) < chan(real, c)) {
+                    scatter = true;
+                    T = T * e / mmax;
+                    pd = pd * e * maj * real / mmax;
+                    p_scatter = pp;
+                    break;
+                }
+                nulls++;
+                T = T * e * (maj - stt) / mmax;
+                pd = pd * e * maj * (V3{1, 1, 1} - real) / mmax;
+                pn = pn * e * maj / mmax;
+            } else {
+                V3 e = vexp(maj * -dt);
+                T = T * e;
+                pd = pd * e;
+                pn = pn * e;
+                break;
+            }
+        }
+        if (nulls) atomicAdd(stats + 3, (unsigned long long)nulls);
+        if (scatter) atomicAdd(stats + 4, 1ull);
+        beta = beta * T / avg3(pd);
+        mdir = mdir * pd;
+        mnee = mnee * pn;
+    }
+    Vertex vx;
+    if (!scatter) {
+        if (prim < 0) {
+            if (sc.env.light_id >= 0) {
+                V3 Le = env_emission(sc, -rd);
+                if (never_scatter) {
+                    L += beta * Le;
+                } else {
+                    float pn = __ldg(sc.light_pmf + sc.env.light_id) * env_pdf(sc, rd) * avg3(mnee);
+                    float pd = dir_pdf * avg3(mdir);
+                    L += beta * Le * ((pd * pd) / (pd * pd + pn * pn));
+                }
+            }
+            alive = false;
+        } else {
+            vx = make_vertex(sc, ro, rd, hit.x, prim, hit.z, hit.w, first ? cfg.spread0 : 0.0f);
+            if (vx.light >= 0) {
+                V3 Le = light_emission(sc, vx.light, -rd, PN{vx.p, vx.ng});
+                if (never_scatter) {
+                    L += beta * Le;
+                } else {
+                    V3 dv = vx.p - neep;
+                    float G = fabsf(dot(rd, vx.ng)) / dot(dv, dv);
+                    float pn = __ldg(sc.light_pmf + vx.light) *
+                               pdf_point_on_light(sc, vx.light, PN{vx.p, vx.ng}, neep) * avg3(mnee);
+                    float pd = dir_pdf * G * avg3(mdir);
+                    L += beta * Le * ((pd * pd) / (pd * pd + pn * pn));
+                }
+            }
+        }
+    }
+    if (alive && cfg.max_depth != -1 && bounces == cfg.max_depth - 1) alive = false;
+    if (alive && bounces > LJ_MAX_BOUNCES) {
+        atomicOr(status, kStatusBounceCap);
+        alive = false;
+    }
+    if (alive && scatter) {
+        const MediumRec &m = sc.media[medium];
+        V3 ss, sa;
+        sigmas(m, p_scatter, ss, sa);
+        V3 wv = -rd;
+        MatParams dummy_mat;
+        dummy_mat.type = 0;
+        BsdfVertex dummy_bv{V3{0, 0, 1}, frame_from_n(V3{0, 0, 1})};
+        L += beta * ss * vol_nee(sc, p_scatter, medium, false, vx, dummy_mat, dummy_bv, wv, bounces, cfg.max_depth, rng,
+                                 status, stats + 1);
+        float u0 = pcg_uniform(rng), u1 = pcg_uniform(rng);
+        V3 nd = phase_sample(m.phase_kind, m.g, wv, u0, u1);
+        beta = beta * ss;
+        dir_pdf = phase_eval(m.phase_kind, m.g, wv, nd);
+        neep = p_scatter;
+        mdir = V3{1, 1, 1};
+        mnee = V3{1, 1, 1};
+        never_scatter = false;
+        next_o = p_scatter;
+        next_d = nd;
+        next_tnear = 0.0f;
+    } else if (alive) {
+        if (vx.material < 0) {
+            medium = update_medium(vx, rd, medium);
+            next_o = vx.p;
+            next_d = rd;
+            next_tnear = sc.eps;
+            bounces++;
+            cont = true;
+        } else {
+            MatParams mat = resolve_material(sc, vx.material, vx.u, vx.v, vx.uv_screen_size);
+            BsdfVertex bv{vx.ng, vx.frame};
+            V3 wv = -rd;
+            L += beta * vol_nee(sc, vx.p, medium, true, vx, mat, bv, wv, bounces, cfg.max_depth, rng, status, stats + 1);
+            float b0 = pcg_uniform(rng), b1 = pcg_uniform(rng), b2 = pcg_uniform(rng);
+            BsdfSample bs = bsdf_sample(mat, bv, wv, b0, b1, b2);
+            if (!bs.valid) {
+                alive = false;
+            } else {
+                V3 f = bsdf_eval(mat, bv, wv, bs.dir);
+                float pdf = bsdf_pdf(mat, bv, wv, bs.dir);
+                if (!(pdf > 0.0f)) {
+                    alive = false;
+                } else {
+                    if (bs.eta != 0.0f) eta_scale /= (bs.eta * bs.eta);
+                    beta = beta * f / pdf;
+                    dir_pdf = pdf;
+                    neep = vx.p;
+                    mdir = V3{1, 1, 1};
+                    mnee = V3{1, 1, 1};
+                    never_scatter = false;
+                    medium = update_medium(vx, bs.dir, medium);
+                    next_o = vx.p;
+                    next_d = bs.dir;
+                    next_tnear = sc.eps;
+                }
+            }
+        }
+    }
+    if (alive && !cont) {
+        if (bounces >= cfg.rr_depth) {
+            float rr = fminf(max3(beta) / eta_scale, 0.95f);
+            if (pcg_uniform(rng) > rr) alive = false;
+            else beta = beta / rr;
+        }
+        bounces++;
+    }
+    vs.beta = make_float4(beta.x, beta.y, beta.z, eta_scale);
+    vs.L = make_float4(L.x, L.y, L.z, dir_pdf);
+    vs.neep = make_float4(neep.x, neep.y, neep.z, 0.0f);
+    vs.mdir = make_float4(mdir.x, mdir.y, mdir.z, 0.0f);
+    vs.mnee = make_float4(mnee.x, mnee.y, mnee.z, 0.0f);
+    vs.st = make_int4(medium, bounces, never_scatter ? 1 : 0, 0);
+    vs.rng = rng.state;
+    store.emit(vs, alive, make_float4(next_o.x, next_o.y, next_o.z, next_tnear),
+               make_float4(next_d.x, next_d.y, next_d.z, inf));
+}
+
+
+}  // namespace lj

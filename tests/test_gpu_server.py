@@ -65,6 +65,19 @@ def test_resolution_and_depth_overrides(ctx):
     assert_matches_plain(img, ref, atol=1e-7)
 
 
+@pytest.mark.parametrize("case", ["homogeneous_dielectric", "heterogeneous_sphere"])
+def test_volpath_job_matches_plain_render(ctx, case):
+    sc = {"homogeneous_dielectric": lambda: scenes.homogeneous_box_scene(width=32, height=24, spp=8,
+                                                                         index_matched=False),
+          "heterogeneous_sphere": lambda: scenes.volume_scene(width=32, height=32, spp=4, grid=32,
+                                                              max_depth=24)}[case]()
+    g = gpu.GpuScene(ctx, sc)
+    ref, _ = g.render(seed=11)
+    img, st = render_alone(ctx, g, seed=11)
+    assert st.state == abi.LJ_JOB_DONE and st.samples_total == sc.width * sc.height * sc.spp
+    assert_matches_plain(img, ref)
+
+
 def _mix(ctx):
     gs = [gpu.GpuScene(ctx, scenes.cornell_box(seed=s, width=w, height=h, spp=4, max_depth=d))
           for s, w, h, d in ((1, 32, 32, 6), (2, 80, 40, 4), (3, 48, 64, 8), (4, 16, 16, -1))]
@@ -72,6 +85,8 @@ def _mix(ctx):
     # Disney materials and an envmap: the other shade kernel instance
     gs.append(gpu.GpuScene(ctx, scenes.resized_terrain_scene(seed=3, n_tris=20000, width=48, height=32, spp=4,
                                                              env_size=(64, 32))))
+    # volumetric path jobs: the third path class
+    gs.append(gpu.GpuScene(ctx, scenes.homogeneous_box_scene(width=24, height=24, spp=4, index_matched=True)))
     rng = np.random.default_rng(0)
     jobs = []
     for k in range(14):
@@ -160,7 +175,9 @@ def test_admission_limits(ctx):
 
 
 def test_bad_requests(ctx):
-    vol = gpu.GpuScene(ctx, scenes.homogeneous_box_scene(width=8, height=8, spp=1))
+    vol_sc = scenes.homogeneous_box_scene(width=8, height=8, spp=1)
+    vol_sc.vol_path_version = 3   # volpath versions 1-5 are not served
+    vol = gpu.GpuScene(ctx, vol_sc)
     cb = gpu.GpuScene(ctx, scenes.cornell_box(seed=1, width=8, height=8, spp=1))
     with gpu.Server(ctx, small_opts()) as srv:
         with pytest.raises(gpu.LjError) as e:
