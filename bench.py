@@ -4,12 +4,15 @@
 
 Workload (a "step" = serving one batch of render jobs):
   serving  32 jobs with Poisson arrivals (mean 200/s, seeded).  Each job
-           renders one of 6 resident scenes -- seeded Cornell boxes with
-           tessellated walls and seeded terrain + icosphere + HDR-envmap
-           scenes (Disney BSDFs), 10k-2M triangles, log-uniform -- at a square
-           resolution in {128, 256, 512, 1024}, spp in {4, 16, 64, 256}, max
-           depth uniform in 6..64 (Russian roulette from depth 5).
-           ~1e9 camera samples per step.
+           renders one of 6 resident scenes -- in turn a seeded Cornell box
+           with tessellated walls, a seeded terrain + icosphere + HDR-envmap
+           scene (Disney BSDFs) and a seeded heterogeneous volume (256^3
+           value-noise density, max 20) in a dielectric sphere over a
+           tessellated floor (volumetric path tracer), 10k-2M triangles,
+           log-uniform -- at a square resolution in {128, 256, 512, 1024},
+           spp in {4, 16, 64, 256}, max depth uniform in 6..64 (Russian
+           roulette from depth 5).  ~0.9e9 camera samples per step, a
+           quarter of them volumetric.
 
 Our arm (--impl ours):
   value     Msamples/s of the continuous-batching server (lj_gpu_server_*):
@@ -85,13 +88,15 @@ def job_samples(jobs):
 def config_dict(pool, opts=None):
     w = WORKLOAD
     cfg = {"workload": "serving: %d jobs per step, Poisson arrivals %.0f/s; %d resident scenes "
-                       "(tessellated Cornell boxes and terrain+icospheres+envmap, %d-%d triangles); "
+                       "(tessellated Cornell boxes, terrain+icospheres+envmap, heterogeneous 256^3 volumes in a "
+                       "dielectric sphere; %d-%d triangles); "
                        "resolution {128,256,512,1024}^2, spp {4,16,64,256}, max depth 6-64"
                        % (w["n_jobs"], w["rate"], w["n_scenes"], min(s.num_triangles for s in pool),
                           max(s.num_triangles for s in pool)),
            "jobs_per_step": w["n_jobs"], "arrival_rate_per_s": w["rate"],
            "scene_triangles": [s.num_triangles for s in pool],
-           "integrator": "path (NEE + MIS, RR from depth 5)",
+           "integrator": "path (NEE + MIS, RR from depth 5); volpath v6 for the volume scenes (delta tracking, "
+                         "ratio-tracking NEE, spectral MIS)",
            "l2": "working set (path pool ~1 GB, scenes, accumulators) larger than L2",
            "timing": "host clock per step, device synchronized on both sides",
            "parallelism": "replicas"}
@@ -169,11 +174,22 @@ BYTES_PATH_STATE = 64   # pixel 4 + rng 8 + beta 16 + L 16 + prev 16 + nv 4
 BYTES_SHADE_GEOM = 52   # 3 vertex indices + 3 positions + prim->shape
 BYTES_SHADE_MAT = 160   # material record: type, eta, textured flags, 12 x RGB slot values
 BYTES_SHADOW_ENTRY = 52  # shadow ray 32 + path 4 + contribution 16
+BYTES_VOL_STATE = 112
+BYTES_NEE_REQUEST = 108
+BYTES_NEE_RESULT = 56
+BYTES_VOL_SEGMENT = (2 * (BYTES_RAY + BYTES_HIT + BYTES_VOL_STATE) + 2 * (BYTES_VOL_STATE + BYTES_RAY)
+                     + 2 * BYTES_NEE_REQUEST + BYTES_NEE_RESULT)
+BYTES_NEE_SHADOW_LOOP = BYTES_NEE_REQUEST + BYTES_NEE_RESULT
 
 
-def kernel_bytes(cls, samples, rays_closest, rays_shadow, segments):
+def kernel_bytes(cls, samples, rays_closest, rays_shadow, segments, vol_segments=0, nee_requests=0):
     """Compulsory algorithmic bytes moved by all launches of one kernel class
-    (queues, hits, path state, shading records; BVH bytes excluded)."""
+    (queues, hits, path state, shading records; BVH bytes and density-grid
+    lookups excluded)."""
+    if cls == abi.LJ_KERNEL_MEDIUM:
+        return vol_segments * BYTES_VOL_SEGMENT
+    if cls == abi.LJ_KERNEL_NEE:
+        return nee_requests * BYTES_NEE_SHADOW_LOOP
     if cls == abi.LJ_KERNEL_TRACE:
         return rays_closest * (BYTES_RAY + BYTES_HIT)
     if cls == abi.LJ_KERNEL_SHADOW:
@@ -383,14 +399,24 @@ def run_ours(args):
         plain_rays[2] += st.path_segments
     peak, peak_kind = measured_peaks()
     cls_ms = list(ps.class_ms)
-    dom = int(np.argmax(cls_ms[:abi.LJ_KERNEL_OTHER]))
-    nb = kernel_bytes(dom, job_samples(jobs), ps.rays_closest, ps.rays_shadow, ps.path_segments)
+    dom = max((c for c in range(abi.LJ_KERNEL_CLASSES) if c != abi.LJ_KERNEL_OTHER), key=lambda c: cls_ms[c])
+    nb = kernel_bytes(dom, job_samples(jobs), ps.rays_closest, ps.rays_shadow, ps.path_segments,
+                      ps.vol_segments, ps.nee_requests)
     launches_dom = max(1, ps.class_launches[dom])
     avg_launch_s = cls_ms[dom] / 1e3 / launches_dom
     achieved = nb / launches_dom / avg_launch_s / 1e9
     units = {abi.LJ_KERNEL_TRACE: ps.rays_closest, abi.LJ_KERNEL_SHADOW: ps.rays_shadow,
-             abi.LJ_KERNEL_SHADE: ps.path_segments}.get(dom, job_samples(jobs))
-    traffic = load_traffic("k_srv_" + abi.KERNEL_CLASS_NAMES[dom], units / launches_dom)
+             abi.LJ_KERNEL_SHADE: ps.path_segments, abi.LJ_KERNEL_MEDIUM: ps.vol_segments,
+             abi.LJ_KERNEL_NEE: ps.nee_requests}.get(dom, job_samples(jobs))
+    kname = {abi.LJ_KERNEL_CAMERA: "k_srv_regen", abi.LJ_KERNEL_MEDIUM: "k_srv_vol_a + k_srv_vol_c",
+             abi.LJ_KERNEL_NEE: "k_srv_vol_b"}.get(dom, "k_srv_" + abi.KERNEL_CLASS_NAMES[dom])
+    traffic = load_traffic(kname, units / launches_dom)
+    if dom in (abi.LJ_KERNEL_MEDIUM, abi.LJ_KERNEL_NEE):
+        note = ("volumetric steps are latency bound, not HBM bound: their dependent density-grid lookups "
+                "(8 x 16 B per tracking step) mostly hit L1/L2 (profiles/ncu_volpath_kernels.md)")
+    else:
+        note = ("traversal is instruction-issue bound, not HBM bound: ncu on a terrain job shows "
+                "79% issue active, 3.1 IPC, 2% of DRAM peak (profiles/ncu_srv_trace_terrain.md)")
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
@@ -410,19 +436,21 @@ def run_ours(args):
                 "what": "scene pool uploaded from host (lj_gpu_scene_create, BVH build) + one step served, "
                         "images to host"},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "k_srv_" + abi.KERNEL_CLASS_NAMES[dom], "achieved": round(achieved, 1),
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                      else "fallback 6800 GB/s", "traffic": traffic,
                      "bytes_per_launch": round(nb / launches_dom), "avg_launch_us": round(avg_launch_s * 1e6, 2),
-                     "bytes": "compulsory (queues, hits, path state, shading records); BVH excluded",
-                     "note": "traversal is instruction-issue bound, not HBM bound: ncu on a terrain job shows "
-                             "79% issue active, 3.1 IPC, 2% of DRAM peak (profiles/ncu_srv_trace_terrain.md)"},
+                     "bytes": "compulsory (queues, hits, path state, shading records); BVH and density-grid "
+                              "bytes excluded",
+                     "note": note},
         "kernel_ms_per_step": {abi.KERNEL_CLASS_NAMES[c]: round(cls_ms[c], 3) for c in range(abi.LJ_KERNEL_CLASSES)},
         "plain_kernel_ms_per_step": {abi.KERNEL_CLASS_NAMES[c]: round(plain_ms[c], 3)
                                      for c in range(abi.LJ_KERNEL_CLASSES)},
         "plain_rays_per_step": {"closest": plain_rays[0], "shadow": plain_rays[1], "segments": plain_rays[2]},
-        "rays_per_step": {"closest": ps.rays_closest, "shadow": ps.rays_shadow, "segments": ps.path_segments},
+        "rays_per_step": {"closest": ps.rays_closest, "shadow": ps.rays_shadow, "segments": ps.path_segments,
+                          "vol_segments": ps.vol_segments, "nee_requests": ps.nee_requests,
+                          "null_collisions": ps.null_collisions, "real_collisions": ps.real_collisions},
         "mrays_per_s": round((st1.rays_closest - st0.rays_closest + st1.rays_shadow - st0.rays_shadow)
                              / b_total / 1e6, 1),
     }
@@ -561,7 +589,8 @@ def cpu_sample(pool, target_s):
     dt = run(n_px, 2)
     n = n_px * len(pool)
     text = ("%d random pixels x 1 spp of each of the %d serving scenes (%d samples, %.1f s); C++ restatement "
-            "of src/path_tracing.h pinned to the reference's renders, %d threads" % (n_px, len(pool), n, dt, cores))
+            "of src/path_tracing.h pinned to the reference's renders (and of the volpath v6 handout "
+            "algorithm for the volume scenes), %d threads" % (n_px, len(pool), n, dt, cores))
     return n / dt / 1e6, cores, text
 
 

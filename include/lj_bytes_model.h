@@ -43,4 +43,24 @@
     (LJ_BYTES_RAY + LJ_BYTES_HIT + 4 + LJ_BYTES_PATH_STATE + LJ_BYTES_SHADE_GEOM + \
      LJ_BYTES_SHADE_MATERIAL + LJ_BYTES_PATH_STATE + LJ_BYTES_RAY + 4)
 
+/* volumetric path state (server layout): job 4 + pixel 4 + rng 8 +
+ * throughput 16 + radiance 16 + NEE vertex 16 + two pdf products 32 +
+ * medium / bounces / flags 16 */
+#define LJ_BYTES_VOL_STATE 112
+/* NEE request: entry 4 + origin, direction, light point, light normal,
+ * sigma_s (5 x 16) + media / bounces / pixel 16 + rng 8 */
+#define LJ_BYTES_NEE_REQUEST 108
+/* NEE result: transmittance, two pdf products (3 x 16) + rng 8 */
+#define LJ_BYTES_NEE_RESULT 56
+/* per volumetric segment (a step): ray + hit + state in, state out (or the
+ * next ray and state), one NEE request written; the c step reads the
+ * request, result, ray, hit and state again and writes state + next ray.
+ * Density-grid lookups are excluded (they hit L1/L2 mostly). */
+#define LJ_BYTES_VOL_SEGMENT                                                                 \
+    (2 * (LJ_BYTES_RAY + LJ_BYTES_HIT + LJ_BYTES_VOL_STATE) + 2 * (LJ_BYTES_VOL_STATE + LJ_BYTES_RAY) + \
+     2 * LJ_BYTES_NEE_REQUEST + LJ_BYTES_NEE_RESULT)
+/* per NEE request (b step): request in, result out (grid lookups and BVH
+ * bytes excluded) */
+#define LJ_BYTES_NEE_SHADOW_LOOP (LJ_BYTES_NEE_REQUEST + LJ_BYTES_NEE_RESULT)
+
 #endif /* LJ_BYTES_MODEL_H */

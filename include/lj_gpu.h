@@ -270,7 +270,11 @@ enum {
     LJ_KERNEL_SHADE = 2,         /* shading / NEE / BSDF sampling       */
     LJ_KERNEL_SHADOW = 3,        /* shadow any-hit traversal            */
     LJ_KERNEL_OTHER = 4,         /* resolve, scale, queue bookkeeping   */
-    LJ_KERNEL_CLASSES = 5
+    LJ_KERNEL_MEDIUM = 5,        /* volpath: delta tracking, emission,
+                                    phase / BSDF sampling              */
+    LJ_KERNEL_NEE = 6,           /* volpath: NEE shadow loop (closest
+                                    hits + ratio tracking)             */
+    LJ_KERNEL_CLASSES = 7
 };
 
 typedef struct lj_stats {
@@ -485,6 +489,8 @@ typedef struct lj_server_stats {
     double class_ms[LJ_KERNEL_CLASSES];        /* LJ_SERVER_PROFILE only (regen = CAMERA,
                                                   plan + retire = OTHER)                   */
     int64_t class_launches[LJ_KERNEL_CLASSES];
+    int64_t vol_segments, nee_requests;        /* volpath device counters, last poll       */
+    int64_t null_collisions, real_collisions;
 } lj_server_stats;
 
 int lj_gpu_server_start(lj_ctx *ctx, const lj_server_options *options, lj_server **out);

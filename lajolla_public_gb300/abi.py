@@ -128,9 +128,10 @@ class lj_scene_info(C.Structure):
 
 
 LJ_RENDER_PROFILE = 1
-(LJ_KERNEL_CAMERA, LJ_KERNEL_TRACE, LJ_KERNEL_SHADE, LJ_KERNEL_SHADOW, LJ_KERNEL_OTHER) = range(5)
-LJ_KERNEL_CLASSES = 5
-KERNEL_CLASS_NAMES = ["camera", "trace", "shade", "shadow", "other"]
+(LJ_KERNEL_CAMERA, LJ_KERNEL_TRACE, LJ_KERNEL_SHADE, LJ_KERNEL_SHADOW, LJ_KERNEL_OTHER, LJ_KERNEL_MEDIUM,
+ LJ_KERNEL_NEE) = range(7)
+LJ_KERNEL_CLASSES = 7
+KERNEL_CLASS_NAMES = ["camera", "trace", "shade", "shadow", "other", "medium", "nee"]
 
 
 class lj_render_params(C.Structure):
@@ -197,7 +198,9 @@ class lj_server_stats(C.Structure):
                 ("samples_done", C.c_int64), ("bytes_resident", C.c_int64), ("busy_ms", C.c_double),
                 ("rays_closest", C.c_int64), ("rays_shadow", C.c_int64), ("path_segments", C.c_int64),
                 ("kernel_launches", C.c_int64),
-                ("class_ms", C.c_double * LJ_KERNEL_CLASSES), ("class_launches", C.c_int64 * LJ_KERNEL_CLASSES)]
+                ("class_ms", C.c_double * LJ_KERNEL_CLASSES), ("class_launches", C.c_int64 * LJ_KERNEL_CLASSES),
+                ("vol_segments", C.c_int64), ("nee_requests", C.c_int64),
+                ("null_collisions", C.c_int64), ("real_collisions", C.c_int64)]
 
 
 STRUCT_SIZES = {

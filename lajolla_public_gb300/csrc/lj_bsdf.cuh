@@ -429,6 +429,9 @@ LJ_HD BsdfSample disney_sample(const DisneyP &p, const BsdfVertex &v, V3 wi, flo
 // material set of its scenes drops the other cases (smaller code, fewer
 // registers); the default handles every type.
 constexpr uint32_t kAllMats = (1u << 9) - 1u;
+constexpr uint32_t kLambertMats = 1u << LJ_MAT_LAMBERTIAN;
+constexpr uint32_t kClassicMats =
+    (1u << LJ_MAT_LAMBERTIAN) | (1u << LJ_MAT_ROUGHPLASTIC) | (1u << LJ_MAT_ROUGHDIELECTRIC);
 template <uint32_t kMats>
 LJ_HD constexpr bool has_mat(int t) { return (kMats >> t) & 1u; }
 // texture slots a material type reads (the slot table in lj_gpu.h)

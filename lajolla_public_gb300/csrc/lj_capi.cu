@@ -579,14 +579,16 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
                     err = "medium " + std::to_string(i) + ": bad grid volume";
                     return fail(LJ_ERR_INVALID_ARG);
                 }
-                std::vector<float> rgb(n * 3);
+                std::vector<float4> rgb(n);
                 float mx[3] = {0, 0, 0};
-                for (size_t p = 0; p < n; p++)
+                for (size_t p = 0; p < n; p++) {
+                    float x[3];
                     for (int c = 0; c < 3; c++) {
-                        float x = v.channels == 3 ? v.data[p * 3 + c] : v.data[p];
-                        rgb[p * 3 + c] = x;
-                        mx[c] = std::max(mx[c], x);
+                        x[c] = v.channels == 3 ? v.data[p * 3 + c] : v.data[p];
+                        mx[c] = std::max(mx[c], x[c]);
                     }
+                    rgb[p] = make_float4(x[0], x[1], x[2], 0.0f);
+                }
                 for (int c = 0; c < 3; c++) {
                     o.res[c] = v.res[c];
                     o.pmin[c] = v.p_min[c];

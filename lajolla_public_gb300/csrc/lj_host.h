@@ -57,7 +57,7 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
                 lj_stats *stats, bool sync_stats, const lj_job_desc *job);
 // lj_volpath.cu
 int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out, cudaStream_t s,
-                   lj_stats *stats);
+                   lj_stats *stats, const lj_job_desc *job);
 // lj_aux.cu
 int render_aux(lj_scene *scene, const lj_render_params *params, float *d_out, cudaStream_t s,
                lj_stats *stats);

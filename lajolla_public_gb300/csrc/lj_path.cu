@@ -87,10 +87,8 @@ __global__ void __launch_bounds__(128, kMats == kAllMats ? 4 : 5) k_shade(DevSce
 using ShadeKernel = void (*)(DevScene, PathSoA, Queues, int, float, int *);
 // the smallest instance whose material set covers the scene's
 ShadeKernel shade_kernel_for(uint32_t mat_mask) {
-    constexpr uint32_t kLambert = 1u << LJ_MAT_LAMBERTIAN;
-    constexpr uint32_t kClassic = kLambert | (1u << LJ_MAT_ROUGHPLASTIC) | (1u << LJ_MAT_ROUGHDIELECTRIC);
-    if ((mat_mask & ~kLambert) == 0) return k_shade<kLambert>;
-    if ((mat_mask & ~kClassic) == 0) return k_shade<kClassic>;
+    if ((mat_mask & ~kLambertMats) == 0) return k_shade<kLambertMats>;
+    if ((mat_mask & ~kClassicMats) == 0) return k_shade<kClassicMats>;
     return k_shade<kAllMats>;
 }
 
@@ -243,7 +241,7 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
     auto mark_end = [&]() {
         if (profile) cudaEventRecord(marks.back().second.second, s);
     };
-    int64_t class_launches[LJ_KERNEL_CLASSES] = {0, 0, 0, 0, 0};
+    int64_t class_launches[LJ_KERNEL_CLASSES] = {};
     for (int sb = 0; sb < spp; sb += nsamp) {
         int ns = std::min(nsamp, spp - sb);
         int Pb = num_pixels * ns;
@@ -321,7 +319,8 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
         }
         if (profile) {
             double other = ms;
-            for (int c = 0; c < LJ_KERNEL_OTHER; c++) other -= stats->class_ms[c];
+            for (int c = 0; c < LJ_KERNEL_CLASSES; c++)
+                if (c != LJ_KERNEL_OTHER) other -= stats->class_ms[c];
             stats->class_ms[LJ_KERNEL_OTHER] = other > 0 ? other : 0;
         }
         int status = 0;
@@ -355,7 +354,7 @@ int lj_gpu_render_device(lj_scene *scene, const lj_render_params *params, float 
         // versions 1-5 are simplifications of 6 for homework; 0 and 6 select the full one
         if (scene->options.vol_path_version != 0 && scene->options.vol_path_version != 6)
             return set_error(scene->ctx, LJ_ERR_UNSUPPORTED, "render: only vol_path_version 0 / 6 is built");
-        return render_volpath(scene, params, d_out_rgb, s, stats);
+        return render_volpath(scene, params, d_out_rgb, s, stats, nullptr);
     }
     if (scene->options.integrator >= LJ_INTEGRATOR_DEPTH && scene->options.integrator <= LJ_INTEGRATOR_MIPMAP_LEVEL)
         return render_aux(scene, params, d_out_rgb, s, stats);
@@ -365,8 +364,10 @@ int lj_gpu_render_device(lj_scene *scene, const lj_render_params *params, float 
 int lj_gpu_render_job_device(lj_scene *scene, const lj_job_desc *job, float *d_out_rgb, void *stream,
                              lj_stats *stats) {
     if (!scene || !job || !d_out_rgb) return LJ_ERR_INVALID_ARG;
-    if (scene->options.integrator != LJ_INTEGRATOR_PATH)
-        return set_error(scene->ctx, LJ_ERR_UNSUPPORTED, "render_job: path-integrator scenes only");
+    const bool vol = scene->options.integrator == LJ_INTEGRATOR_VOLPATH &&
+                     (scene->options.vol_path_version == 0 || scene->options.vol_path_version == 6);
+    if (scene->options.integrator != LJ_INTEGRATOR_PATH && !vol)
+        return set_error(scene->ctx, LJ_ERR_UNSUPPORTED, "render_job: path and volpath (v6) scenes only");
     if ((job->width > 0) != (job->height > 0))
         return set_error(scene->ctx, LJ_ERR_INVALID_ARG, "render_job: give both width and height, or neither");
     cudaSetDevice(scene->ctx->device);
@@ -376,6 +377,7 @@ int lj_gpu_render_job_device(lj_scene *scene, const lj_job_desc *job, float *d_o
     p.spp = job->spp;
     p.sample_offset = job->sample_offset;
     p.flags = job->flags;
+    if (vol) return render_volpath(scene, &p, d_out_rgb, (cudaStream_t)stream, stats, job);
     return render_path(scene, &p, d_out_rgb, (cudaStream_t)stream, stats, stats != nullptr, job);
 }
 

@@ -103,7 +103,7 @@ struct VolRec {
     float pmin[3], pmax[3];
     float scale;
     float max_value[3];    // scale * max over the grid (or the constant)
-    const float *data;     // 3 floats per voxel
+    const float4 *data;    // one float4 per voxel (xyz = the channels, w = 0): one 16-byte load per corner
 };
 
 // Medium (src/medium.h) + phase function.

@@ -50,6 +50,7 @@ namespace {
 
 constexpr int kMaxScenes = 256;
 constexpr int kPollsInFlight = 2;
+constexpr int kStatWords = 9;   // device counters read back (SrvDev::stats)
 
 struct SrvJob {
     CamRec cam;
@@ -61,14 +62,12 @@ struct SrvJob {
     float spread0;
     float clamp;                 // |sample| bound that keeps the sums inside int64
     int mclass;                  // shade kernel: 0 path, kClassicMats materials; 1 path, any; 2 volpath
-    int pad;
+    int all_mats;                // volpath: materials outside kClassicMats occur
 };
 
-// Material classes of the server's two shade kernel instances.  A queue
-// holds class-0 paths from its front and class-1 paths from its back, so
-// each instance reads a contiguous range.
-constexpr uint32_t kClassicMats =
-    (1u << LJ_MAT_LAMBERTIAN) | (1u << LJ_MAT_ROUGHPLASTIC) | (1u << LJ_MAT_ROUGHDIELECTRIC);
+// Material classes of the server's two path shade kernel instances
+// (kClassicMats, kAllMats).  A queue holds class-0 paths from its front and
+// class-1 paths from its back, so each instance reads a contiguous range.
 
 struct SrvCtr {
     unsigned long long issued, done, dropped, pad;
@@ -108,6 +107,7 @@ struct SrvDev {
     float4 *hit;
     VolStateSoA vbuf[2];
     float4 *vhit;
+    NeeQueue nee;                // volpath NEE requests of the wave (count: counts + 16)
     float4 *sray;                // shadow rays (2 per entry)
     int *starget;                // entry of the path in the next queue, or retire index | 2^31
     float4 *scontrib;
@@ -117,13 +117,15 @@ struct SrvDev {
                                  // [3] retire, [5] regen count, [6],[7],[14] class-0 / 1 / 2
                                  // entries that continue into the wave, [8],[9] ray fetch
                                  // counters, [10],[11] class-1 entries (back) of queue 0 / 1,
-                                 // [12],[13] entries of volpath queue 0 / 1
+                                 // [12],[13] entries of volpath queue 0 / 1, [16],[17]
+                                 // volpath NEE requests (front, back)
     // queue position of the k-th entry of class 1 (filled from the back)
     LJ_D int back(int k) const { return P - 1 - k; }
     // position of ray r of a queue with n0 class-0 entries
     LJ_D int entry(int r, int n0) const { return r < n0 ? r : back(r - n0); }
     unsigned long long *stats;   // [0] closest rays, [1] shadow rays, [2] shade segments,
-                                 // volpath: [5] shadow segments, [7] null, [8] real collisions
+                                 // volpath: [3] segments, [4] NEE requests, [5] shadow
+                                 // segments, [7] null, [8] real collisions
     int P;                       // queue capacity
     int *status;
 };
@@ -195,6 +197,8 @@ __global__ void k_srv_plan(SrvDev d, int cur) {
         counts[3] = 0;
         counts[8] = 0;
         counts[9] = 0;
+        counts[16] = 0;
+        counts[17] = 0;
     }
 }
 
@@ -402,6 +406,15 @@ struct VolQueueStore {
         r1 = v.ray[2 * i + 1];
         hit = d.vhit[i];
     }
+    // state of a path that waits for its NEE request: kept in place
+    LJ_D void save(int i, const VolState &vs) const {
+        const VolStateSoA &v = d.vbuf[cur];
+        v.beta[i] = vs.beta;
+        v.L[i] = vs.L;
+        v.mdir[i] = vs.mdir;
+        v.mnee[i] = vs.mnee;
+        v.st[i] = vs.st;
+    }
     LJ_D void emit(const VolState &vs, bool alive, float4 ray0, float4 ray1) const {
         if (alive) {
             const int nxt = cur ^ 1;
@@ -427,16 +440,45 @@ struct VolQueueStore {
     }
 };
 
+// Volumetric paths: the a / b / c steps of lj_volwave.cuh over the volpath
+// queue and the wave's NEE requests.
 template <int B>
-__global__ void __launch_bounds__(B, 384 / B)
-    k_srv_volshade(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
+__global__ void __launch_bounds__(B, 512 / B)
+    k_srv_vol_a(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
     const int n = d.counts[12 + cur];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 2, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 3, (unsigned long long)n);
     const VolQueueStore store{d, cur};
     for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
         const SrvJob &jb = jobs[d.vbuf[cur].job[i]];
         const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
-        vol_shade_segment(scenes[jb.scene], store, i, cfg, d.status, d.stats + 4);
+        vol_segment_a(scenes[jb.scene], store, i, cfg, d.nee, d.status, d.stats + 4);
+    }
+}
+template <int B>
+__global__ void __launch_bounds__(B, 640 / B)
+    k_srv_vol_b(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
+    const int nf = d.counts[16], n = nf + d.counts[17];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 4, (unsigned long long)n);
+    for (int r = blockIdx.x * B + threadIdx.x; r < n; r += gridDim.x * B) {
+        const int k = d.nee.req(r, nf);
+        const SrvJob &jb = jobs[d.vbuf[cur].job[d.nee.entry[k]]];
+        vol_nee_b(scenes[jb.scene], d.nee, k, jb.max_depth, d.status, d.stats + 5);
+    }
+}
+// Three instances: kKind = 0 continues the requests from scattering points
+// (no material code), kKind = 1 / 2 those from surfaces of jobs whose
+// materials are all in kClassicMats (smaller code) / the others.
+template <int B, int kKind>
+__global__ void __launch_bounds__(B, 384 / B)
+    k_srv_vol_c(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
+    const int n = d.counts[kKind == 0 ? 16 : 17];
+    const VolQueueStore store{d, cur};
+    for (int r = blockIdx.x * B + threadIdx.x; r < n; r += gridDim.x * B) {
+        const int k = kKind == 0 ? r : d.nee.cap - 1 - r;
+        const SrvJob &jb = jobs[d.vbuf[cur].job[d.nee.entry[k]]];
+        if (kKind != 0 && jb.all_mats != kKind - 1) continue;
+        const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
+        vol_segment_c<kKind == 1 ? kClassicMats : kAllMats, kKind != 0>(scenes[jb.scene], store, k, cfg, d.nee);
     }
 }
 
@@ -484,14 +526,19 @@ struct KernelSet {
     void (*trace)(SrvDev, int);
     void (*shade0)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*shade1)(SrvDev, const DevScene *, const SrvJob *, int);
-    void (*volshade)(SrvDev, const DevScene *, const SrvJob *, int);
+    void (*vol_a)(SrvDev, const DevScene *, const SrvJob *, int);
+    void (*vol_b)(SrvDev, const DevScene *, const SrvJob *, int);
+    void (*vol_c0)(SrvDev, const DevScene *, const SrvJob *, int);
+    void (*vol_c1)(SrvDev, const DevScene *, const SrvJob *, int);
+    void (*vol_c2)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*shadow)(SrvDev, int);
     void (*retire)(SrvDev);
 };
 template <int B>
 KernelSet kernel_set() {
-    return KernelSet{k_srv_regen<B>,       k_srv_trace<B>,  k_srv_shade<B, 0>, k_srv_shade<B, 1>,
-                     k_srv_volshade<B>,    k_srv_shadow<B>, k_srv_retire<B>};
+    return KernelSet{k_srv_regen<B>,      k_srv_trace<B>,       k_srv_shade<B, 0>,    k_srv_shade<B, 1>,
+                     k_srv_vol_a<B>,      k_srv_vol_b<B>,       k_srv_vol_c<B, 0>,    k_srv_vol_c<B, 1>,
+                     k_srv_vol_c<B, 2>,   k_srv_shadow<B>,      k_srv_retire<B>};
 }
 
 int occupancy_grid(const void *fn, int block, int sms) {
@@ -515,6 +562,8 @@ size_t pool_bytes(size_t P) {
     b += align256(P * 4) * 2 + align256(P * 16);
     // two volpath queue buffers: job, pixel, rng, beta, L, neep, mdir, mnee, st, ray; volpath hits
     b += 2 * (align256(P * 4) * 2 + align256(P * 8) + align256(P * 16) * 6 + align256(P * 32)) + align256(P * 16);
+    // NEE requests: entry; org, dir, lp, ln, ss, T, pn, pd, med; rng
+    b += align256(P * 4) + 9 * align256(P * 16) + align256(P * 8);
     b += 256 * 2;   // counts, stats
     return b;
 }
@@ -593,7 +642,7 @@ struct lj_server {
     long long *d_plan_start = nullptr;
     SrvDev dev{};
     KernelSet ks{};
-    int grid[7] = {1, 1, 1, 1, 1, 1, 1};
+    int grid[11] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
     cudaGraphExec_t graph = nullptr;
 
     // pinned host staging
@@ -609,7 +658,7 @@ struct lj_server {
     int64_t next_poll_seq = 1;
     int poll_next = 0;
 
-    unsigned long long *h_qstats[kPollsInFlight] = {nullptr, nullptr};   // device ray counters
+    unsigned long long *h_qstats[kPollsInFlight] = {nullptr, nullptr};   // device counters (kStatWords)
 
     // LJ_SERVER_PROFILE: an event pair around every kernel of a batch
     bool profile = false;
@@ -619,9 +668,9 @@ struct lj_server {
     // stats
     int64_t n_submitted = 0, n_done = 0, n_failed = 0, n_cancelled = 0;
     int64_t waves = 0, graph_launches = 0, samples_done = 0, kernel_launches = 0;
-    int64_t rays_closest = 0, rays_shadow = 0, path_segments = 0;
-    double class_ms[LJ_KERNEL_CLASSES] = {0, 0, 0, 0, 0};
-    int64_t class_launches[LJ_KERNEL_CLASSES] = {0, 0, 0, 0, 0};
+    unsigned long long counters[kStatWords] = {};   // device counters as of the last read-back
+    double class_ms[LJ_KERNEL_CLASSES] = {};
+    int64_t class_launches[LJ_KERNEL_CLASSES] = {};
     double busy_ms = 0;
 };
 
@@ -674,9 +723,21 @@ void launch_wave(lj_server *s, int cur) {
     mark(s, LJ_KERNEL_SHADE, true);
     s->ks.shade1<<<s->grid[5], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
     mark(s, LJ_KERNEL_SHADE, false);
-    mark(s, LJ_KERNEL_SHADE, true);
-    s->ks.volshade<<<s->grid[6], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
-    mark(s, LJ_KERNEL_SHADE, false);
+    mark(s, LJ_KERNEL_MEDIUM, true);
+    s->ks.vol_a<<<s->grid[6], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    mark(s, LJ_KERNEL_MEDIUM, false);
+    mark(s, LJ_KERNEL_NEE, true);
+    s->ks.vol_b<<<s->grid[7], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    mark(s, LJ_KERNEL_NEE, false);
+    mark(s, LJ_KERNEL_MEDIUM, true);
+    s->ks.vol_c0<<<s->grid[8], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    mark(s, LJ_KERNEL_MEDIUM, false);
+    mark(s, LJ_KERNEL_MEDIUM, true);
+    s->ks.vol_c1<<<s->grid[9], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    mark(s, LJ_KERNEL_MEDIUM, false);
+    mark(s, LJ_KERNEL_MEDIUM, true);
+    s->ks.vol_c2<<<s->grid[10], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    mark(s, LJ_KERNEL_MEDIUM, false);
     mark(s, LJ_KERNEL_SHADOW, true);
     s->ks.shadow<<<s->grid[3], B, 0, s->stream>>>(s->dev, cur);
     mark(s, LJ_KERNEL_SHADOW, false);
@@ -736,8 +797,8 @@ std::string build_device(lj_server *s) {
     *s->h_one = 1;
     for (int b = 0; b < kPollsInFlight; b++) {
         SRV_CUDA(cudaMallocHost(&s->h_ctr[b], sizeof(SrvCtr) * J));
-        SRV_CUDA(cudaMallocHost(&s->h_qstats[b], sizeof(unsigned long long) * 4));
-        memset(s->h_qstats[b], 0, sizeof(unsigned long long) * 4);
+        SRV_CUDA(cudaMallocHost(&s->h_qstats[b], sizeof(unsigned long long) * kStatWords));
+        memset(s->h_qstats[b], 0, sizeof(unsigned long long) * kStatWords);
         SRV_CUDA(cudaEventCreateWithFlags(&s->poll_ev[b], cudaEventDisableTiming));
     }
 
@@ -777,6 +838,18 @@ std::string build_device(lj_server *s) {
         v.ray = carve<float4>(cur, 2 * P);
     }
     d.vhit = carve<float4>(cur, P);
+    d.nee.cap = (int)P;
+    d.nee.entry = carve<int>(cur, P);
+    d.nee.org = carve<float4>(cur, P);
+    d.nee.dir = carve<float4>(cur, P);
+    d.nee.lp = carve<float4>(cur, P);
+    d.nee.ln = carve<float4>(cur, P);
+    d.nee.ss = carve<float4>(cur, P);
+    d.nee.T = carve<float4>(cur, P);
+    d.nee.pn = carve<float4>(cur, P);
+    d.nee.pd = carve<float4>(cur, P);
+    d.nee.med = carve<int4>(cur, P);
+    d.nee.rng = carve<uint64_t>(cur, P);
     d.sray = carve<float4>(cur, 2 * P);
     d.starget = carve<int>(cur, P);
     d.scontrib = carve<float4>(cur, P);
@@ -784,6 +857,7 @@ std::string build_device(lj_server *s) {
     d.rpixel = carve<int>(cur, P);
     d.rL = carve<float4>(cur, P);
     d.counts = carve<int>(cur, 64);
+    d.nee.count = d.counts + 16;
     d.stats = carve<unsigned long long>(cur, 32);
     d.P = (int)P;
     d.status = s->ctx->d_status;
@@ -801,7 +875,11 @@ std::string build_device(lj_server *s) {
     s->grid[1] = occupancy_grid((const void *)s->ks.trace, s->block, sms);
     s->grid[2] = occupancy_grid((const void *)s->ks.shade0, s->block, sms);
     s->grid[5] = occupancy_grid((const void *)s->ks.shade1, s->block, sms);
-    s->grid[6] = occupancy_grid((const void *)s->ks.volshade, s->block, sms);
+    s->grid[6] = occupancy_grid((const void *)s->ks.vol_a, s->block, sms);
+    s->grid[7] = occupancy_grid((const void *)s->ks.vol_b, s->block, sms);
+    s->grid[8] = occupancy_grid((const void *)s->ks.vol_c0, s->block, sms);
+    s->grid[9] = occupancy_grid((const void *)s->ks.vol_c1, s->block, sms);
+    s->grid[10] = occupancy_grid((const void *)s->ks.vol_c2, s->block, sms);
     s->grid[3] = occupancy_grid((const void *)s->ks.shadow, s->block, sms);
     s->grid[4] = occupancy_grid((const void *)s->ks.retire, s->block, sms);
 
@@ -866,8 +944,10 @@ std::string admit(lj_server *s, HostJob *j) {
     h.rr_depth = j->rr_depth;
     h.spread0 = 0.25f / (float)std::max(j->w, j->h);
     h.clamp = (float)std::ldexp(1.0, 30) / (float)j->spp;
+    const bool classic = (j->scene->mat_mask & ~kClassicMats) == 0 && !(s->opt.flags & LJ_SERVER_ONE_SHADE_KERNEL);
     if (j->scene->options.integrator == LJ_INTEGRATOR_VOLPATH) h.mclass = 2;
-    else h.mclass = (j->scene->mat_mask & ~kClassicMats) == 0 && !(s->opt.flags & LJ_SERVER_ONE_SHADE_KERNEL) ? 0 : 1;
+    else h.mclass = classic ? 0 : 1;
+    h.all_mats = classic ? 0 : 1;
     SRV_CUDA(cudaMemcpyAsync(s->d_jobs + slot, &h, sizeof(SrvJob), cudaMemcpyHostToDevice, s->stream));
     SRV_CUDA(cudaMemsetAsync(s->d_ctr + slot, 0, sizeof(SrvCtr), s->stream));
     SRV_CUDA(cudaMemsetAsync(s->d_cancel + slot, 0, sizeof(int), s->stream));
@@ -1065,7 +1145,7 @@ void worker_main(lj_server *s) {
         if (e == cudaSuccess) e = collect_marks(s);
         lk.lock();
         s->waves += 2 * pairs;
-        s->kernel_launches += 16 * pairs;
+        s->kernel_launches += 24 * pairs;
         if (s->graph) s->graph_launches += pairs;
         const int b = s->poll_next;
         s->poll_next = (b + 1) % kPollsInFlight;
@@ -1076,9 +1156,7 @@ void worker_main(lj_server *s) {
             lk.lock();
             if (e == cudaSuccess) {
                 s->poll_pending[b] = false;
-                s->rays_closest = (int64_t)s->h_qstats[b][0];
-                s->rays_shadow = (int64_t)s->h_qstats[b][1];
-                s->path_segments = (int64_t)s->h_qstats[b][2];
+                memcpy(s->counters, s->h_qstats[b], sizeof(s->counters));
                 err = on_snapshot(s, s->h_ctr[b], s->poll_seq[b]);
             }
         }
@@ -1086,7 +1164,7 @@ void worker_main(lj_server *s) {
             e = cudaMemcpyAsync(s->h_ctr[b], s->d_ctr, sizeof(SrvCtr) * s->live.size(), cudaMemcpyDeviceToHost,
                                 s->stream);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(s->h_qstats[b], s->dev.stats, sizeof(unsigned long long) * 4,
+                e = cudaMemcpyAsync(s->h_qstats[b], s->dev.stats, sizeof(unsigned long long) * kStatWords,
                                     cudaMemcpyDeviceToHost, s->stream);
             if (e == cudaSuccess) e = cudaEventRecord(s->poll_ev[b], s->stream);
             if (e == cudaSuccess) {
@@ -1104,14 +1182,10 @@ void worker_main(lj_server *s) {
     // drain: nothing of ours may still run when buffers are freed
     lk.unlock();
     cudaStreamSynchronize(s->stream);
-    unsigned long long q[4] = {0, 0, 0, 0};
+    unsigned long long q[kStatWords] = {};
     bool got = !s->dead && cudaMemcpy(q, s->dev.stats, sizeof(q), cudaMemcpyDeviceToHost) == cudaSuccess;
     lk.lock();
-    if (got) {
-        s->rays_closest = (int64_t)q[0];
-        s->rays_shadow = (int64_t)q[1];
-        s->path_segments = (int64_t)q[2];
-    }
+    if (got) memcpy(s->counters, q, sizeof(q));
     reap_finished(s);
     s->cv_done.notify_all();
 }
@@ -1330,13 +1404,10 @@ int lj_gpu_server_stats(lj_server *s, lj_server_stats *st) {
     std::lock_guard<std::mutex> lk(s->mu);
     if (!any_live(s) && s->pending.empty() && !s->dead) {
         // idle: every path has retired, so the ray counters are final
-        unsigned long long q[4];
+        unsigned long long q[kStatWords];
         cudaSetDevice(s->device);
-        if (cudaMemcpy(q, s->dev.stats, sizeof(q), cudaMemcpyDeviceToHost) == cudaSuccess) {
-            s->rays_closest = (int64_t)q[0];
-            s->rays_shadow = (int64_t)q[1];
-            s->path_segments = (int64_t)q[2];
-        }
+        if (cudaMemcpy(q, s->dev.stats, sizeof(q), cudaMemcpyDeviceToHost) == cudaSuccess)
+            memcpy(s->counters, q, sizeof(q));
     }
     st->jobs_submitted = s->n_submitted;
     st->jobs_done = s->n_done;
@@ -1347,9 +1418,13 @@ int lj_gpu_server_stats(lj_server *s, lj_server_stats *st) {
     st->samples_done = s->samples_done;
     st->bytes_resident = s->bytes_pool + s->bytes_scenes + s->bytes_jobs;
     st->busy_ms = s->busy_ms;
-    st->rays_closest = s->rays_closest;
-    st->rays_shadow = s->rays_shadow;
-    st->path_segments = s->path_segments;
+    st->rays_closest = (int64_t)s->counters[0];
+    st->rays_shadow = (int64_t)s->counters[1];
+    st->path_segments = (int64_t)s->counters[2];
+    st->vol_segments = (int64_t)s->counters[3];
+    st->nee_requests = (int64_t)s->counters[4];
+    st->null_collisions = (int64_t)s->counters[7];
+    st->real_collisions = (int64_t)s->counters[8];
     st->kernel_launches = s->kernel_launches;
     for (int c = 0; c < LJ_KERNEL_CLASSES; c++) {
         st->class_ms[c] = s->class_ms[c];

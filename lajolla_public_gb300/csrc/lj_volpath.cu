@@ -4,14 +4,17 @@
 // oracle/lj_oracle.cpp with the same random-number order).
 //
 // Per pass:
-//   trace_closest   the path queue's rays -> closest hits (shared kernel)
-//   vol_shade       free-flight delta tracking over [0, t_hit) with the
-//                   chromatic majorant (one channel sampled per segment);
-//                   then, at a real scattering point or a surface:
-//                   emission with MIS, NEE with ratio tracking through
-//                   index-matching surfaces (the shadow traversal runs inside
-//                   this kernel), phase / BSDF sampling, Russian roulette,
-//                   next ray appended to the other queue.
+//   vol_trace   the path queue's rays -> closest hits (persistent traversal)
+//   vol_a       free-flight delta tracking over [0, t_hit) with the
+//               chromatic majorant (one channel sampled per segment);
+//               emission with MIS; index-matching surfaces passed; at a
+//               real scattering point or a surface with a material, the
+//               light sample of NEE and a request in the NEE queue
+//   vol_b       per NEE request: the shadow loop (closest hits through
+//               index-matching surfaces, ratio tracking through media)
+//   vol_c       per NEE request: the MIS-weighted contribution, phase /
+//               BSDF sampling, Russian roulette, next ray appended to the
+//               other queue.
 // Null-collision loops are capped by max_null_collisions; shadow-segment and
 // bounce loops by the depth limit and LJ_MAX_BOUNCES.
 #include <algorithm>
@@ -19,6 +22,7 @@
 #include <vector>
 
 #include "lj_host.h"
+#include "lj_trace_queue.cuh"
 #include "lj_volwave.cuh"
 
 namespace lj {
@@ -40,8 +44,10 @@ struct VolQueues {
     float4 *ray[2];
     int *path[2];
     float4 *hit;
-    int *counts;                  // [0], [1] ray queues
+    int *counts;                  // [0], [1] ray queues, [2], [3] NEE requests (front, back), [8] ray fetch
+                                  // counter
     unsigned long long *stats;    // [0] closest rays, [1] shadow segments, [2] segments, [3] null, [4] real
+    NeeQueue nee;
 };
 
 
@@ -77,19 +83,14 @@ __global__ void k_vol_camera(DevScene sc, VolSoA ps, VolQueues q, int P, int num
     ps.st[p] = make_int4(sc.camera_medium, 0, 1, 1);
 }
 
-__global__ void __launch_bounds__(128) k_vol_trace(DevBvh bvh, const float4 *rays, float4 *hits, const int *count,
-                                                   unsigned long long *stat, int *status) {
-    int n = *count;
+// Closest hits of the queue's rays by persistent warps (*fetch = 0 at launch).
+__global__ void __launch_bounds__(128, 8) k_vol_trace(DevBvh bvh, const float4 *rays, float4 *hits,
+                                                      const int *count, int *fetch, unsigned long long *stat,
+                                                      int *status) {
+    const int n = *count;
     if (blockIdx.x == 0 && threadIdx.x == 0 && stat) atomicAdd(stat, (unsigned long long)n);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
-        TraceHit h{0.0f, -1, 0.0f, 0.0f};
-        int ovf = 0;
-        bool f = trace_bvh<false>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf);
-        hits[i] = f ? make_float4(h.t, __int_as_float(h.prim), h.u, h.v)
-                    : make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f);
-        if (ovf) atomicOr(status, kStatusStackOverflow);
-    }
+    ClosestQueueIO io{bvh, rays, hits};
+    trace_queue<false, 128>(io, n, fetch, status);
 }
 
 // The single-scene renderer's store: state in fixed slots, queues carry
@@ -115,6 +116,15 @@ struct VolSlotStore {
         vs.mnee = ps.mnee[p];
         vs.st = ps.st[p];
     }
+    // state of a path that waits for its NEE request
+    LJ_D void save(int, const VolState &vs) const {
+        const int p = vs.slot;
+        ps.beta[p] = vs.beta;
+        ps.L[p] = vs.L;
+        ps.mdir[p] = vs.mdir;
+        ps.mnee[p] = vs.mnee;
+        ps.st[p] = vs.st;
+    }
     LJ_D void emit(const VolState &vs, bool alive, float4 ray0, float4 ray1) const {
         const int p = vs.slot, nxt = cur ^ 1;
         if (alive) {
@@ -134,15 +144,31 @@ struct VolSlotStore {
     }
 };
 
-__global__ void __launch_bounds__(128) k_vol_shade(DevScene sc, VolSoA ps, VolQueues q, int cur, float spread0,
-                                                   int *status) {
+__global__ void __launch_bounds__(128, 4) k_vol_a(DevScene sc, VolSoA ps, VolQueues q, int cur, float spread0,
+                                                  int *status) {
     const int n = q.counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(q.stats + 2, (unsigned long long)n);
     const ShadeCfg cfg{sc.max_depth, sc.rr_depth, spread0};
     const VolSlotStore store{ps, q, cur};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        vol_shade_segment(sc, store, i, cfg, status, q.stats);
+        vol_segment_a(sc, store, i, cfg, q.nee, status, q.stats);
 }
+__global__ void __launch_bounds__(128, 5) k_vol_b(DevScene sc, VolQueues q, int *status) {
+    const int nf = q.counts[2], n = nf + q.counts[3];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+        vol_nee_b(sc, q.nee, q.nee.req(r, nf), sc.max_depth, status, q.stats + 1);
+}
+// kSurface = false: requests from scattering points (front); true: from
+// surfaces (back)
+template <uint32_t kMats, bool kSurface>
+__global__ void __launch_bounds__(128, 3) k_vol_c(DevScene sc, VolSoA ps, VolQueues q, int cur, float spread0) {
+    const int n = q.counts[kSurface ? 3 : 2];
+    const ShadeCfg cfg{sc.max_depth, sc.rr_depth, spread0};
+    const VolSlotStore store{ps, q, cur};
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+        vol_segment_c<kMats, kSurface>(sc, store, kSurface ? q.nee.cap - 1 - r : r, cfg, q.nee);
+}
+using VolCKernel = void (*)(DevScene, VolSoA, VolQueues, int, float);
 
 // Per pixel: sum the batch's samples in sample order, skipping samples with
 // no finite channel (src/render.cpp:138-143, an OR over channels).
@@ -169,8 +195,16 @@ __global__ void k_vol_scale(float *img, int64_t n, float s) {
 __global__ void k_vol_set_counts(int *counts, int c0) {
     counts[0] = c0;
     counts[1] = 0;
+    counts[2] = 0;
+    counts[3] = 0;
+    counts[8] = 0;
 }
-__global__ void k_vol_zero(int *counts, int a) { counts[a] = 0; }
+__global__ void k_vol_zero(int *counts, int a) {
+    counts[a] = 0;
+    counts[2] = 0;
+    counts[3] = 0;
+    counts[8] = 0;
+}
 
 template <typename T>
 T *carve(char *&p, size_t n) {
@@ -183,6 +217,8 @@ size_t vol_bytes(size_t P) {
     auto add = [&](size_t b) { per += ((b + 255) / 256) * 256; };
     add(P * 4); add(P * 8); add(P * 16); add(P * 16); add(P * 16); add(P * 16); add(P * 16); add(P * 16);
     add(P * 32); add(P * 32); add(P * 4); add(P * 4); add(P * 16); add(64); add(64);
+    // NEE queue: entry; org, dir, lp, ln, ss, T, pn, pd, med (16 B each); rng
+    add(P * 4); for (int k = 0; k < 9; k++) add(P * 16); add(P * 8);
     return per;
 }
 int grid_for_kernel(const void *kernel, int threads) {
@@ -196,12 +232,23 @@ int grid_for_kernel(const void *kernel, int threads) {
 }  // namespace
 
 int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out, cudaStream_t s,
-                   lj_stats *stats) {
+                   lj_stats *stats, const lj_job_desc *job) {
     lj_ctx *ctx = scene->ctx;
-    const DevScene &sc = scene->dev;
+    DevScene sc = scene->dev;   // job overrides: resolution (camera) and depth options
+    int W = scene->width, H = scene->height;
+    if (job && job->width > 0 && job->height > 0) {
+        W = job->width;
+        H = job->height;
+        make_cam_rec(scene->camera, W, H, sc.cam);
+    }
+    if (job && job->override_depth) {
+        if (job->max_depth < -1) return set_error(ctx, LJ_ERR_INVALID_ARG, "render: max_depth must be >= -1");
+        sc.max_depth = job->max_depth;
+        sc.rr_depth = job->rr_depth;
+    }
     std::string e;
     std::string *err = &e;
-    const int W = scene->width, H = scene->height, num_pixels = W * H;
+    const int num_pixels = W * H;
     const int spp = params->spp > 0 ? params->spp : scene->options.samples_per_pixel;
     if (spp <= 0) return set_error(ctx, LJ_ERR_INVALID_ARG, "render: samples per pixel must be positive");
     int64_t cap = params->max_paths_in_flight > 0 ? params->max_paths_in_flight : (int64_t)1 << 22;
@@ -236,12 +283,31 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
     q.hit = carve<float4>(cur, P);
     q.counts = carve<int>(cur, 16);
     q.stats = carve<unsigned long long>(cur, 8);
+    q.nee.cap = (int)P;
+    q.nee.count = q.counts + 2;
+    q.nee.entry = carve<int>(cur, P);
+    q.nee.org = carve<float4>(cur, P);
+    q.nee.dir = carve<float4>(cur, P);
+    q.nee.lp = carve<float4>(cur, P);
+    q.nee.ln = carve<float4>(cur, P);
+    q.nee.ss = carve<float4>(cur, P);
+    q.nee.T = carve<float4>(cur, P);
+    q.nee.pn = carve<float4>(cur, P);
+    q.nee.pd = carve<float4>(cur, P);
+    q.nee.med = carve<int4>(cur, P);
+    q.nee.rng = carve<uint64_t>(cur, P);
     LJ_CUDA_TRY(cudaMemsetAsync(q.stats, 0, 8 * sizeof(unsigned long long), s));
     LJ_CUDA_TRY(cudaMemsetAsync(d_out, 0, sizeof(float) * 3 * (size_t)num_pixels, s));
     const int g_trace = grid_for_kernel((const void *)k_vol_trace, 128);
-    const int g_shade = grid_for_kernel((const void *)k_vol_shade, 128);
-    const bool unbounded = scene->options.max_depth == -1;
-    const int passes = unbounded ? LJ_MAX_BOUNCES + 2 : std::max(1, scene->options.max_depth);
+    const VolCKernel k_cs =
+        (scene->mat_mask & ~kClassicMats) == 0 ? k_vol_c<kClassicMats, true> : k_vol_c<kAllMats, true>;
+    const VolCKernel k_cm = k_vol_c<kAllMats, false>;   // no material code
+    const int g_a = grid_for_kernel((const void *)k_vol_a, 128);
+    const int g_b = grid_for_kernel((const void *)k_vol_b, 128);
+    const int g_cm = grid_for_kernel((const void *)k_cm, 128);
+    const int g_cs = grid_for_kernel((const void *)k_cs, 128);
+    const bool unbounded = sc.max_depth == -1;
+    const int passes = unbounded ? LJ_MAX_BOUNCES + 2 : std::max(1, sc.max_depth);
     const float spread0 = 0.25f / (float)std::max(W, H);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (stats) {
@@ -250,22 +316,56 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
         cudaEventRecord(e0, s);
     }
     int64_t launches = 0;
+    // LJ_RENDER_PROFILE: an event pair around every kernel, grouped by class
+    const bool profile = stats && (params->flags & LJ_RENDER_PROFILE);
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    int64_t class_launches[LJ_KERNEL_CLASSES] = {};
+    auto mark_begin = [&](int cls) {
+        class_launches[cls]++;
+        if (!profile) return;
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, s);
+        marks.push_back({cls, {a, b}});
+    };
+    auto mark_end = [&]() {
+        if (profile) cudaEventRecord(marks.back().second.second, s);
+    };
     for (int sb = 0; sb < spp; sb += nsamp) {
         int ns = std::min(nsamp, spp - sb);
         int Pb = num_pixels * ns;
         k_vol_set_counts<<<1, 1, 0, s>>>(q.counts, Pb);
+        class_launches[LJ_KERNEL_OTHER]++;
+        mark_begin(LJ_KERNEL_CAMERA);
         k_vol_camera<<<(Pb + 255) / 256, 256, 0, s>>>(sc, ps, q, Pb, num_pixels, params->sample_offset + sb,
                                                       params->seed);
+        mark_end();
         launches += 2;
         int curq = 0;
         for (int pass = 0; pass < passes; pass++) {
             k_vol_zero<<<1, 1, 0, s>>>(q.counts, curq ^ 1);
-            k_vol_trace<<<g_trace, 128, 0, s>>>(sc.bvh, q.ray[curq], q.hit, q.counts + curq, q.stats + 0,
-                                                ctx->d_status);
-            k_vol_shade<<<g_shade, 128, 0, s>>>(sc, ps, q, curq, spread0, ctx->d_status);
-            launches += 3;
+            class_launches[LJ_KERNEL_OTHER]++;
+            mark_begin(LJ_KERNEL_TRACE);
+            k_vol_trace<<<g_trace, 128, 0, s>>>(sc.bvh, q.ray[curq], q.hit, q.counts + curq, q.counts + 8,
+                                                q.stats + 0, ctx->d_status);
+            mark_end();
+            mark_begin(LJ_KERNEL_MEDIUM);
+            k_vol_a<<<g_a, 128, 0, s>>>(sc, ps, q, curq, spread0, ctx->d_status);
+            mark_end();
+            mark_begin(LJ_KERNEL_NEE);
+            k_vol_b<<<g_b, 128, 0, s>>>(sc, q, ctx->d_status);
+            mark_end();
+            mark_begin(LJ_KERNEL_MEDIUM);
+            k_cm<<<g_cm, 128, 0, s>>>(sc, ps, q, curq, spread0);
+            mark_end();
+            mark_begin(LJ_KERNEL_MEDIUM);
+            k_cs<<<g_cs, 128, 0, s>>>(sc, ps, q, curq, spread0);
+            mark_end();
+            launches += 6;
             curq ^= 1;
-            if ((pass & 7) == 7) {
+            // stop once every path of the batch has ended
+            if ((pass & 3) == 3 && pass + 1 < passes) {
                 int c = 0;
                 LJ_CUDA_TRY(cudaMemcpyAsync(&c, q.counts + curq, sizeof(int), cudaMemcpyDeviceToHost, s));
                 LJ_CUDA_TRY(cudaStreamSynchronize(s));
@@ -274,10 +374,12 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
         }
         k_vol_resolve<<<(num_pixels + 255) / 256, 256, 0, s>>>(ps.L, num_pixels, ns, d_out);
         launches++;
+        class_launches[LJ_KERNEL_OTHER]++;
     }
     int64_t nfl = 3 * (int64_t)num_pixels;
     k_vol_scale<<<(int)((nfl + 255) / 256), 256, 0, s>>>(d_out, nfl, 1.0f / spp);
     launches++;
+    class_launches[LJ_KERNEL_OTHER]++;
     LJ_CUDA_TRY(cudaGetLastError());
     if (stats) {
         cudaEventRecord(e1, s);
@@ -296,6 +398,23 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
         stats->null_collisions = (int64_t)st[3];
         stats->real_collisions = (int64_t)st[4];
         stats->kernel_launches = launches;
+        for (int c = 0; c < LJ_KERNEL_CLASSES; c++) {
+            stats->class_launches[c] = class_launches[c];
+            stats->class_ms[c] = 0.0;
+        }
+        for (auto &m : marks) {
+            float kms = 0;
+            cudaEventElapsedTime(&kms, m.second.first, m.second.second);
+            stats->class_ms[m.first] += kms;
+            cudaEventDestroy(m.second.first);
+            cudaEventDestroy(m.second.second);
+        }
+        if (profile) {
+            double other = ms;
+            for (int c = 0; c < LJ_KERNEL_CLASSES; c++)
+                if (c != LJ_KERNEL_OTHER) other -= stats->class_ms[c];
+            stats->class_ms[LJ_KERNEL_OTHER] = other > 0 ? other : 0;
+        }
         int status = 0;
         LJ_CUDA_TRY(cudaMemcpy(&status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
         if (status) {

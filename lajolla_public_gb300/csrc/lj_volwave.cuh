@@ -53,8 +53,8 @@ LJ_D V3 vol_lookup(const VolRec &v, V3 p) {
     int x1 = min(x0 + 1, v.res[0] - 1), y1 = min(y0 + 1, v.res[1] - 1), z1 = min(z0 + 1, v.res[2] - 1);
     float dx = nx - x0, dy = ny - y0, dz = nz - z0;
     auto at = [&](int x, int y, int z) {
-        const float *q = v.data + (((size_t)z * v.res[1] + y) * v.res[0] + x) * 3;
-        return V3{__ldg(q), __ldg(q + 1), __ldg(q + 2)};
+        const float4 q = __ldg(v.data + ((size_t)z * v.res[1] + y) * v.res[0] + x);
+        return V3{q.x, q.y, q.z};
     };
     V3 r = at(x0, y0, z0) * ((1 - dx) * (1 - dy) * (1 - dz)) + at(x1, y0, z0) * (dx * (1 - dy) * (1 - dz)) +
            at(x0, y1, z0) * ((1 - dx) * dy * (1 - dz)) + at(x1, y1, z0) * (dx * dy * (1 - dz)) +
@@ -97,102 +97,133 @@ LJ_D int update_medium(const Vertex &v, V3 dir, int medium) {
     return medium;
 }
 
-// NEE from p: a medium point (surface == false) or a surface vertex with a
-// material.  Ratio tracking through media, passing index-matching surfaces.
-LJ_D V3 vol_nee(const DevScene &sc, V3 p, int medium, bool surface, const Vertex &vx, const MatParams &mat,
-                const BsdfVertex &bv, V3 dir_view, int bounces, int max_depth, Pcg &rng, int *status,
-                unsigned long long *seg_stat) {
-    float lu0 = pcg_uniform(rng), lu1 = pcg_uniform(rng), lw = pcg_uniform(rng), sw = pcg_uniform(rng);
-    if (sc.num_lights == 0) return V3{0, 0, 0};
-    int lid = sample_light(sc, lw);
-    PN pl = sample_point_on_light(sc, lid, p, lu0, lu1, sw);
-    bool env = sc.lights[lid].kind != 0;
-    V3 dir = env ? -pl.n : normalize(pl.p - p);
+// ---- NEE (next event estimation) in three steps ----
+// A path that reaches a real scattering point or a surface with a material
+// issues one NEE request: vol_segment_a draws the light sample (4 random
+// numbers, as the reference's NEE starts) and appends the request;
+// vol_nee_b runs the shadow loop (closest hits through index-matching
+// surfaces, ratio tracking through media, drawing from the path's stream);
+// vol_segment_c turns its transmittance into the MIS-weighted contribution and
+// continues the path with the stream where the shadow loop left it (phase or
+// BSDF sampling, Russian roulette).  The random-number order per path is that
+// of one sequential NEE call; the shadow loop, which does most of the grid
+// lookups, runs in a small kernel of its own.
+// Requests from scattering points fill the queue from its front, requests
+// from surfaces from its back, so that each instance of the c step reads a
+// contiguous range (and the warps of the b step see one kind mostly).
+constexpr int kNeeSurface = 1, kNeeEnv = 2, kNeeLight = 4, kNeeFirst = 8;
+
+struct NeeQueue {
+    int cap;          // capacity (entries of the path queue)
+    int *count;       // [0] requests from scattering points (front), [1] from surfaces (back)
+    int *entry;       // queue entry of the path
+    float4 *org;      // xyz: NEE origin (scattering point or surface vertex)
+    float4 *dir;      // xyz: direction to the light sample
+    float4 *lp;       // xyz: light sample point, w: light id (int bits)
+    float4 *ln;       // xyz: light sample normal, w: kNee* flags (int bits)
+    float4 *ss;       // xyz: sigma_s at the scattering point
+    int4 *med;        // x: medium the shadow ray starts in, y: path bounces, z: pixel
+    uint64_t *rng;    // PCG state after the light sample (a), after the shadow loop (b)
+    float4 *T;        // b: xyz transmittance, w: 1 = blocked (no contribution)
+    float4 *pn;       // b: xyz product of ratio-tracking pdfs
+    float4 *pd;       // b: xyz product of free-flight pdfs
+    // request r of the b step's range [0, count[0] + count[1])
+    LJ_D int req(int r, int n_front) const { return r < n_front ? r : cap - 1 - (r - n_front); }
+};
+
+// Shadow loop of request k (b step).  max_depth: the job's.
+LJ_D void vol_nee_b(const DevScene &sc, const NeeQueue &nq, int k, int max_depth, int *status,
+                    unsigned long long *seg_stat) {
+    const float4 o4 = nq.org[k], d4 = nq.dir[k], lp4 = nq.lp[k], ln4 = nq.ln[k];
+    const int4 md = nq.med[k];
+    const int flags = __float_as_int(ln4.w);
     V3 T{1, 1, 1}, p_nee{1, 1, 1}, p_dir{1, 1, 1};
-    int smed = surface ? update_medium(vx, dir, medium) : medium;
-    int sbounces = 0;
-    V3 p0 = p;
-    float oeps = surface ? sc.eps : 0.0f;
-    const float inf = __int_as_float(0x7f800000);
-    int segs = 0;
-    for (int seg = 0; seg < kMaxShadowSegments; seg++) {
-        segs++;
-        float dist = env ? inf : length(pl.p - p0);
-        float tmax = env ? inf : (1.0f - sc.eps) * dist;
-        TraceHit h{0.0f, -1, 0.0f, 0.0f};
-        int ovf = 0;
-        bool hit = trace_bvh<false>(sc.bvh, p0, dir, oeps, tmax, h, &ovf);
-        if (ovf) atomicOr(status, kStatusStackOverflow);
-        float next_t = hit ? h.t : dist;
-        if (smed >= 0) {
-            const MediumRec &m = sc.media[smed];
-            V3 maj = majorant(m, p0, dir);
-            float mmax = max3(maj);
-            int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
-            float acc = 0.0f;
-            for (int it = 0; it < sc.max_null_collisions; it++) {
-                if (chan(maj, c) <= 0.0f) break;
-                float t = -logf(1.0f - pcg_uniform(rng)) / chan(maj, c);
-                float dt = next_t - acc;
-                acc = fminf(acc + t, next_t);
-                if (t < dt) {
-                    V3 ss, sa;
-                    sigmas(m, p0 + dir * acc, ss, sa);
-                    V3 st = ss + sa;
-                    V3 e = vexp(maj * -t);
-                    T = T * e * (maj - st) / mmax;
-                    p_nee = p_nee * e * maj / mmax;
-                    p_dir = p_dir * e * maj * (V3{1, 1, 1} - vdiv(st, maj)) / mmax;
-                    if (max3(T) <= 0.0f) break;
-                } else {
-                    V3 e = vexp(maj * -dt);
-                    T = T * e;
-                    p_nee = p_nee * e;
-                    p_dir = p_dir * e;
-                    break;
+    bool blocked = (flags & kNeeLight) == 0;
+    Pcg rng;
+    rng.state = nq.rng[k];
+    rng.inc = ((uint64_t)md.z << 1u) | 1u;
+    if (!blocked) {
+        const bool env = (flags & kNeeEnv) != 0;
+        const V3 dir{d4.x, d4.y, d4.z}, lp{lp4.x, lp4.y, lp4.z};
+        int smed = md.x;
+        const int bounces = md.y;
+        int sbounces = 0;
+        V3 p0{o4.x, o4.y, o4.z};
+        float oeps = (flags & kNeeSurface) ? sc.eps : 0.0f;
+        const float inf = __int_as_float(0x7f800000);
+        int segs = 0;
+        for (int seg = 0; seg < kMaxShadowSegments; seg++) {
+            segs++;
+            float dist = env ? inf : length(lp - p0);
+            float tmax = env ? inf : (1.0f - sc.eps) * dist;
+            TraceHit h{0.0f, -1, 0.0f, 0.0f};
+            int ovf = 0;
+            bool hit = trace_bvh<false>(sc.bvh, p0, dir, oeps, tmax, h, &ovf);
+            if (ovf) atomicOr(status, kStatusStackOverflow);
+            float next_t = hit ? h.t : dist;
+            if (smed >= 0) {
+                const MediumRec &m = sc.media[smed];
+                V3 maj = majorant(m, p0, dir);
+                float mmax = max3(maj);
+                int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
+                float acc = 0.0f;
+                for (int it = 0; it < sc.max_null_collisions; it++) {
+                    if (chan(maj, c) <= 0.0f) break;
+                    float t = -logf(1.0f - pcg_uniform(rng)) / chan(maj, c);
+                    float dt = next_t - acc;
+                    acc = fminf(acc + t, next_t);
+                    if (t < dt) {
+                        V3 ss, sa;
+                        sigmas(m, p0 + dir * acc, ss, sa);
+                        V3 st = ss + sa;
+                        V3 e = vexp(maj * -t);
+                        T = T * e * (maj - st) / mmax;
+                        p_nee = p_nee * e * maj / mmax;
+                        p_dir = p_dir * e * maj * (V3{1, 1, 1} - vdiv(st, maj)) / mmax;
+                        if (max3(T) <= 0.0f) break;
+                    } else {
+                        V3 e = vexp(maj * -dt);
+                        T = T * e;
+                        p_nee = p_nee * e;
+                        p_dir = p_dir * e;
+                        break;
+                    }
                 }
             }
+            if (!hit) break;
+            int shape = __ldg(sc.prim_shape + h.prim);
+            if (sc.shapes[shape].material_id >= 0) {   // an opaque surface blocks the light
+                blocked = true;
+                break;
+            }
+            sbounces++;
+            if (max_depth != -1 && bounces + sbounces + 1 >= max_depth) {
+                blocked = true;
+                break;
+            }
+            Vertex sv = make_vertex(sc, p0, dir, h.t, h.prim, h.u, h.v, 0.0f);
+            smed = update_medium(sv, dir, smed);
+            p0 = p0 + dir * next_t;
+            oeps = sc.eps;
+            if (seg == kMaxShadowSegments - 1) atomicOr(status, kStatusBounceCap);
         }
-        if (!hit) break;
-        int shape = __ldg(sc.prim_shape + h.prim);
-        if (sc.shapes[shape].material_id >= 0) return V3{0, 0, 0};
-        sbounces++;
-        if (max_depth != -1 && bounces + sbounces + 1 >= max_depth) return V3{0, 0, 0};
-        Vertex sv = make_vertex(sc, p0, dir, h.t, h.prim, h.u, h.v, 0.0f);
-        smed = update_medium(sv, dir, smed);
-        p0 = p0 + dir * next_t;
-        oeps = sc.eps;
-        if (seg == kMaxShadowSegments - 1) atomicOr(status, kStatusBounceCap);
+        if (!blocked && seg_stat) atomicAdd(seg_stat, (unsigned long long)segs);
     }
-    if (seg_stat) atomicAdd(seg_stat, (unsigned long long)segs);
-    if (max3(T) <= 0.0f) return V3{0, 0, 0};
-    V3 dp = pl.p - p;
-    float G = env ? 1.0f : fmaxf(-dot(dir, pl.n), 0.0f) / dot(dp, dp);
-    float pdf_nee = __ldg(sc.light_pmf + lid) * pdf_point_on_light(sc, lid, pl, p);
-    if (!(G > 0.0f && pdf_nee > 0.0f)) return V3{0, 0, 0};
-    V3 f;
-    float pdf_dir;
-    if (surface) {
-        f = bsdf_eval(mat, bv, dir_view, dir);
-        pdf_dir = bsdf_pdf(mat, bv, dir_view, dir);
-    } else {
-        const MediumRec &m = sc.media[medium];
-        float ph = phase_eval(m.phase_kind, m.g, dir_view, dir);
-        f = V3{ph, ph, ph};
-        pdf_dir = ph;
-    }
-    V3 Le = light_emission(sc, lid, -dir, pl);
-    float pn = pdf_nee * avg3(p_nee);
-    float pd = pdf_dir * G * avg3(p_dir);
-    float w = (pn * pn) / (pn * pn + pd * pd);
-    return T * f * Le * (G * w / pn);
+    nq.rng[k] = rng.state;
+    nq.T[k] = make_float4(T.x, T.y, T.z, blocked ? 1.0f : 0.0f);
+    nq.pn[k] = make_float4(p_nee.x, p_nee.y, p_nee.z, 0.0f);
+    nq.pd[k] = make_float4(p_dir.x, p_dir.y, p_dir.z, 0.0f);
 }
 
-
-// stats: [1] shadow segments, [3] null collisions, [4] real collisions
+// a step: one queue entry up to its NEE request.  Free-flight delta
+// tracking over [0, t_hit) with the chromatic majorant (one channel sampled
+// per segment); emission with MIS at a light; depth limits; index-matching
+// surfaces are passed here.  Paths that end or pass a surface are emitted;
+// the others are saved in place and get a request in nq.
+// stats: [3] null collisions, [4] real collisions.
 template <class Store>
-LJ_D void vol_shade_segment(const DevScene &sc, const Store &store, int i, const ShadeCfg &cfg, int *status,
-                            unsigned long long *stats) {
+LJ_D void vol_segment_a(const DevScene &sc, const Store &store, int i, const ShadeCfg &cfg, const NeeQueue &nq,
+                        int *status, unsigned long long *stats) {
     const float inf = __int_as_float(0x7f800000);
     VolState vs;
     float4 r0, r1, hit;
@@ -201,19 +232,17 @@ LJ_D void vol_shade_segment(const DevScene &sc, const Store &store, int i, const
     int prim = __float_as_int(hit.y);
     V3 beta{vs.beta.x, vs.beta.y, vs.beta.z}, L{vs.L.x, vs.L.y, vs.L.z}, neep{vs.neep.x, vs.neep.y, vs.neep.z};
     V3 mdir{vs.mdir.x, vs.mdir.y, vs.mdir.z}, mnee{vs.mnee.x, vs.mnee.y, vs.mnee.z};
-    float eta_scale = vs.beta.w, dir_pdf = vs.L.w;
+    float dir_pdf = vs.L.w;
     int medium = vs.st.x, bounces = vs.st.y;
     bool never_scatter = vs.st.z != 0, first = vs.st.w != 0;
     Pcg rng;
     rng.state = vs.rng;
     rng.inc = ((uint64_t)vs.pixel << 1u) | 1u;
-    bool alive = true, cont = false;
-    V3 next_o{0, 0, 0}, next_d{0, 0, 0};
-    float next_tnear = 0.0f;
+    bool alive = true;
 
     float t_hit = prim >= 0 ? hit.x : inf;
     bool scatter = false;
-    V3 p_scatter{0, 0, 0};
+    V3 p_scatter{0, 0, 0}, ss_scatter{0, 0, 0};
     if (medium >= 0) {
         const MediumRec &m = sc.media[medium];
         V3 maj = majorant(m, ro, rd);
@@ -239,6 +268,7 @@ LJ_D void vol_shade_segment(const DevScene &sc, const Store &store, int i, const
                     T = T * e / mmax;
                     pd = pd * e * maj * real / mmax;
                     p_scatter = pp;
+                    ss_scatter = ss;
                     break;
                 }
                 nulls++;
@@ -295,66 +325,164 @@ LJ_D void vol_shade_segment(const DevScene &sc, const Store &store, int i, const
         atomicOr(status, kStatusBounceCap);
         alive = false;
     }
-    if (alive && scatter) {
+    vs.beta = make_float4(beta.x, beta.y, beta.z, vs.beta.w);
+    vs.L = make_float4(L.x, L.y, L.z, dir_pdf);
+    vs.mdir = make_float4(mdir.x, mdir.y, mdir.z, 0.0f);
+    vs.mnee = make_float4(mnee.x, mnee.y, mnee.z, 0.0f);
+    if (alive && !scatter && vx.material < 0) {
+        // index-matching surface: pass through
+        vs.st = make_int4(update_medium(vx, rd, medium), bounces + 1, never_scatter ? 1 : 0, 0);
+        vs.rng = rng.state;
+        store.emit(vs, true, make_float4(vx.p.x, vx.p.y, vx.p.z, sc.eps), make_float4(rd.x, rd.y, rd.z, inf));
+        return;
+    }
+    if (!alive) {
+        vs.st = make_int4(medium, bounces, never_scatter ? 1 : 0, 0);
+        vs.rng = rng.state;
+        store.emit(vs, false, make_float4(0, 0, 0, 0), make_float4(0, 0, 0, inf));
+        return;
+    }
+    // NEE request from the scattering point or the surface vertex; the light
+    // sample's random numbers are drawn here, as the reference's NEE starts
+    const bool surface = !scatter;
+    const V3 p = surface ? vx.p : p_scatter;
+    float lu0 = pcg_uniform(rng), lu1 = pcg_uniform(rng), lw = pcg_uniform(rng), sw = pcg_uniform(rng);
+    int flags = (surface ? kNeeSurface : 0) | (first ? kNeeFirst : 0);
+    int lid = -1, smed = medium;
+    PN pl{V3{0, 0, 0}, V3{0, 0, 0}};
+    V3 dir{0, 0, 1};
+    if (sc.num_lights > 0) {
+        lid = sample_light(sc, lw);
+        pl = sample_point_on_light(sc, lid, p, lu0, lu1, sw);
+        const bool env = sc.lights[lid].kind != 0;
+        dir = env ? -pl.n : normalize(pl.p - p);
+        if (surface) smed = update_medium(vx, dir, medium);
+        flags |= kNeeLight | (env ? kNeeEnv : 0);
+    }
+    vs.st = make_int4(medium, bounces, never_scatter ? 1 : 0, first ? 1 : 0);
+    store.save(i, vs);
+    const int k = surface ? nq.cap - 1 - queue_slot(nq.count + 1) : queue_slot(nq.count);
+    nq.entry[k] = i;
+    nq.org[k] = make_float4(p.x, p.y, p.z, 0.0f);
+    nq.dir[k] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+    nq.lp[k] = make_float4(pl.p.x, pl.p.y, pl.p.z, __int_as_float(lid));
+    nq.ln[k] = make_float4(pl.n.x, pl.n.y, pl.n.z, __int_as_float(flags));
+    nq.ss[k] = make_float4(ss_scatter.x, ss_scatter.y, ss_scatter.z, 0.0f);
+    nq.med[k] = make_int4(smed, bounces, vs.pixel, 0);
+    nq.rng[k] = rng.state;
+}
+
+// c step: request k's contribution (the end of the reference's NEE), then
+// phase (kSurface = false: a request from a scattering point) or BSDF
+// sampling, Russian roulette and the next ray.
+// kMats: the material types the scenes can hold (kAllMats: any).
+template <uint32_t kMats, bool kSurface, class Store>
+LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const ShadeCfg &cfg, const NeeQueue &nq) {
+    const float inf = __int_as_float(0x7f800000);
+    const int i = nq.entry[k];
+    VolState vs;
+    float4 r0, r1, hit;
+    store.load(i, vs, r0, r1, hit);
+    const float4 o4 = nq.org[k], d4 = nq.dir[k], lp4 = nq.lp[k], ln4 = nq.ln[k], T4 = nq.T[k];
+    const int flags = __float_as_int(ln4.w), lid = __float_as_int(lp4.w);
+    constexpr bool surface = kSurface;
+    const V3 ro{r0.x, r0.y, r0.z}, rd{r1.x, r1.y, r1.z};
+    const V3 p{o4.x, o4.y, o4.z}, dir{d4.x, d4.y, d4.z};
+    V3 beta{vs.beta.x, vs.beta.y, vs.beta.z}, L{vs.L.x, vs.L.y, vs.L.z};
+    float eta_scale = vs.beta.w, dir_pdf = vs.L.w;
+    int medium = vs.st.x, bounces = vs.st.y;
+    bool never_scatter = vs.st.z != 0;
+    Pcg rng;
+    rng.state = nq.rng[k];
+    rng.inc = ((uint64_t)vs.pixel << 1u) | 1u;
+    const V3 wv = -rd;
+    Vertex vx;
+    MatParams mat;
+    mat.type = 0;
+    BsdfVertex bv{V3{0, 0, 1}, frame_from_n(V3{0, 0, 1})};
+    if constexpr (surface) {
+        vx = make_vertex(sc, ro, rd, hit.x, __float_as_int(hit.y), hit.z, hit.w,
+                         (flags & kNeeFirst) ? cfg.spread0 : 0.0f);
+        mat = resolve_material<kMats>(sc, vx.material, vx.u, vx.v, vx.uv_screen_size);
+        bv = BsdfVertex{vx.ng, vx.frame};
+    }
+    // the NEE contribution
+    V3 nee{0, 0, 0};
+    const V3 T{T4.x, T4.y, T4.z};
+    if (T4.w == 0.0f && max3(T) > 0.0f) {
+        const bool env = (flags & kNeeEnv) != 0;
+        const PN pl{V3{lp4.x, lp4.y, lp4.z}, V3{ln4.x, ln4.y, ln4.z}};
+        V3 dp = pl.p - p;
+        float G = env ? 1.0f : fmaxf(-dot(dir, pl.n), 0.0f) / dot(dp, dp);
+        float pdf_nee = __ldg(sc.light_pmf + lid) * pdf_point_on_light(sc, lid, pl, p);
+        if (G > 0.0f && pdf_nee > 0.0f) {
+            V3 f;
+            float pdf_dir;
+            if constexpr (surface) {
+                f = bsdf_eval<kMats>(mat, bv, wv, dir);
+                pdf_dir = bsdf_pdf<kMats>(mat, bv, wv, dir);
+            } else {
+                const MediumRec &m = sc.media[medium];
+                float ph = phase_eval(m.phase_kind, m.g, wv, dir);
+                f = V3{ph, ph, ph};
+                pdf_dir = ph;
+            }
+            V3 Le = light_emission(sc, lid, -dir, pl);
+            const float4 pn4 = nq.pn[k], pd4 = nq.pd[k];
+            float pn = pdf_nee * avg3(V3{pn4.x, pn4.y, pn4.z});
+            float pd = pdf_dir * G * avg3(V3{pd4.x, pd4.y, pd4.z});
+            float w = (pn * pn) / (pn * pn + pd * pd);
+            nee = T * f * Le * (G * w / pn);
+        }
+    }
+    bool alive = true;
+    V3 next_o{0, 0, 0}, next_d{0, 0, 0}, neep{vs.neep.x, vs.neep.y, vs.neep.z};
+    V3 mdir{vs.mdir.x, vs.mdir.y, vs.mdir.z}, mnee{vs.mnee.x, vs.mnee.y, vs.mnee.z};
+    float next_tnear = 0.0f;
+    if constexpr (!surface) {
+        // phase sampling at the scattering point
+        const float4 ss4 = nq.ss[k];
+        const V3 ss{ss4.x, ss4.y, ss4.z};
         const MediumRec &m = sc.media[medium];
-        V3 ss, sa;
-        sigmas(m, p_scatter, ss, sa);
-        V3 wv = -rd;
-        MatParams dummy_mat;
-        dummy_mat.type = 0;
-        BsdfVertex dummy_bv{V3{0, 0, 1}, frame_from_n(V3{0, 0, 1})};
-        L += beta * ss * vol_nee(sc, p_scatter, medium, false, vx, dummy_mat, dummy_bv, wv, bounces, cfg.max_depth, rng,
-                                 status, stats + 1);
+        L += beta * ss * nee;
         float u0 = pcg_uniform(rng), u1 = pcg_uniform(rng);
         V3 nd = phase_sample(m.phase_kind, m.g, wv, u0, u1);
         beta = beta * ss;
         dir_pdf = phase_eval(m.phase_kind, m.g, wv, nd);
-        neep = p_scatter;
+        neep = p;
         mdir = V3{1, 1, 1};
         mnee = V3{1, 1, 1};
         never_scatter = false;
-        next_o = p_scatter;
+        next_o = p;
         next_d = nd;
         next_tnear = 0.0f;
-    } else if (alive) {
-        if (vx.material < 0) {
-            medium = update_medium(vx, rd, medium);
-            next_o = vx.p;
-            next_d = rd;
-            next_tnear = sc.eps;
-            bounces++;
-            cont = true;
+    } else {
+        L += beta * nee;
+        float b0 = pcg_uniform(rng), b1 = pcg_uniform(rng), b2 = pcg_uniform(rng);
+        BsdfSample bs = bsdf_sample<kMats>(mat, bv, wv, b0, b1, b2);
+        if (!bs.valid) {
+            alive = false;
         } else {
-            MatParams mat = resolve_material(sc, vx.material, vx.u, vx.v, vx.uv_screen_size);
-            BsdfVertex bv{vx.ng, vx.frame};
-            V3 wv = -rd;
-            L += beta * vol_nee(sc, vx.p, medium, true, vx, mat, bv, wv, bounces, cfg.max_depth, rng, status, stats + 1);
-            float b0 = pcg_uniform(rng), b1 = pcg_uniform(rng), b2 = pcg_uniform(rng);
-            BsdfSample bs = bsdf_sample(mat, bv, wv, b0, b1, b2);
-            if (!bs.valid) {
+            V3 f = bsdf_eval<kMats>(mat, bv, wv, bs.dir);
+            float pdf = bsdf_pdf<kMats>(mat, bv, wv, bs.dir);
+            if (!(pdf > 0.0f)) {
                 alive = false;
             } else {
-                V3 f = bsdf_eval(mat, bv, wv, bs.dir);
-                float pdf = bsdf_pdf(mat, bv, wv, bs.dir);
-                if (!(pdf > 0.0f)) {
-                    alive = false;
-                } else {
-                    if (bs.eta != 0.0f) eta_scale /= (bs.eta * bs.eta);
-                    beta = beta * f / pdf;
-                    dir_pdf = pdf;
-                    neep = vx.p;
-                    mdir = V3{1, 1, 1};
-                    mnee = V3{1, 1, 1};
-                    never_scatter = false;
-                    medium = update_medium(vx, bs.dir, medium);
-                    next_o = vx.p;
-                    next_d = bs.dir;
-                    next_tnear = sc.eps;
-                }
+                if (bs.eta != 0.0f) eta_scale /= (bs.eta * bs.eta);
+                beta = beta * f / pdf;
+                dir_pdf = pdf;
+                neep = vx.p;
+                mdir = V3{1, 1, 1};
+                mnee = V3{1, 1, 1};
+                never_scatter = false;
+                medium = update_medium(vx, bs.dir, medium);
+                next_o = vx.p;
+                next_d = bs.dir;
+                next_tnear = sc.eps;
             }
         }
     }
-    if (alive && !cont) {
+    if (alive) {
         if (bounces >= cfg.rr_depth) {
             float rr = fminf(max3(beta) / eta_scale, 0.95f);
             if (pcg_uniform(rng) > rr) alive = false;
@@ -372,6 +500,5 @@ LJ_D void vol_shade_segment(const DevScene &sc, const Store &store, int i, const
     store.emit(vs, alive, make_float4(next_o.x, next_o.y, next_o.z, next_tnear),
                make_float4(next_d.x, next_d.y, next_d.z, inf));
 }
-
 
 }  // namespace lj

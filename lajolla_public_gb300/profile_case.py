@@ -12,8 +12,12 @@ Cases:
   cbox          seeded Cornell box, 256x256, 64 spp, max depth 6
   terrain       seeded terrain + 16 icospheres + envmap, 1.26M triangles,
                 512x512, 16 spp, max depth 8
-  terrain_srv   the terrain case as one server job (server kernels)
-  cbox_srv      the cbox case as one server job
+  volume        seeded heterogeneous medium (256^3 grid, max density 20) in a
+                dielectric sphere, 512x512, 256 spp, max depth 64 (volpath v6)
+  volume_mid    the volume case at 256x256, 16 spp (one wavefront batch)
+  volume_small  the volume case at 128x128, 64 spp, 64^3 grid
+  terrain_srv, cbox_srv, volume_srv, volume_small_srv
+                the case as one server job (server kernels)
 
 `summarize` reads the CSV that `ncu --metrics gpu__time_duration.sum --csv
 --log-file F` writes and prints launches, total time and share per kernel.
@@ -36,6 +40,12 @@ def make_case(name):
         return scenes.cornell_box(seed=0, width=256, height=256, spp=64, max_depth=6)
     if name in ("terrain", "terrain_srv"):
         return scenes.resized_terrain_scene(seed=5, n_tris=1261476, width=512, height=512, spp=16, max_depth=8)
+    if name in ("volume", "volume_srv"):
+        return scenes.volume_scene(seed=0, width=512, height=512, spp=256, max_depth=64, grid=256)
+    if name in ("volume_mid", "volume_mid_srv"):
+        return scenes.volume_scene(seed=0, width=256, height=256, spp=16, max_depth=64, grid=256)
+    if name in ("volume_small", "volume_small_srv"):
+        return scenes.volume_scene(seed=0, width=128, height=128, spp=64, max_depth=64, grid=64)
     raise SystemExit("unknown case %r" % name)
 
 
@@ -68,9 +78,9 @@ def run(args):
         for i in range(args.warmup + args.repeat):
             st = g.render_device(out, seed=i, stream=stream, stats=True, profile=True)
         cls = {abi.KERNEL_CLASS_NAMES[c]: round(st.class_ms[c], 3) for c in range(abi.LJ_KERNEL_CLASSES)}
-        print("%s: %d samples, %.2f ms, %.1f Msamples/s, closest %d shadow %d, classes %s"
+        print("%s: %d samples, %.2f ms, %.1f Msamples/s, closest %d shadow %d, null %d real %d, classes %s"
               % (args.case, st.samples, st.device_ms, st.samples / st.device_ms / 1e3, st.rays_closest,
-                 st.rays_shadow, cls))
+                 st.rays_shadow, st.null_collisions, st.real_collisions, cls))
     g.close()
     ctx.close()
 

@@ -684,11 +684,12 @@ def value_noise_3d(rng, n, octaves=5, base_cells=4):
 
 def volume_scene(seed=0, width=512, height=512, spp=256, max_depth=64, grid=256, max_density=20.0,
                  sigma_t_scale=(1.05, 0.9, 0.8), albedo=(0.952, 0.889, 0.75), g=0.7,
-                 eta=1.33, roughness=0.1):
+                 eta=1.33, roughness=0.1, floor_grid=1):
     """Seeded volumetric scene: a heterogeneous chromatic medium (5-octave
     value noise scaled to `max_density`, sigma_t = scale * noise as a
     3-channel density, constant albedo, HG g) inside a rough dielectric
-    sphere, over a diffuse plane, lit by one sphere area light."""
+    sphere, over a diffuse plane (split into floor_grid^2 quads), lit by one
+    sphere area light."""
     rng = np.random.default_rng(seed)
     sc = Scene(width, height, spp, max_depth, look_at([0, 1.4, 4.2], [0, 0.9, 0], [0, 1, 0]), 35.0,
                integrator=abi.LJ_INTEGRATOR_VOLPATH, vol_path_version=6)
@@ -704,7 +705,8 @@ def volume_scene(seed=0, width=512, height=512, spp=256, max_depth=64, grid=256,
     diel = sc.add_material(roughdielectric([1, 1, 1], [1, 1, 1], roughness, eta))
     sc.add_sphere(c, r, diel, interior_medium=0, exterior_medium=-1)
     floor_m = sc.add_material(lambertian([0.6, 0.6, 0.6]))
-    fpos, fidx = _quad([-6, 0, 6], [6, 0, 6], [6, 0, -6], [-6, 0, -6])
+    corners = ([-6, 0, 6], [6, 0, 6], [6, 0, -6], [-6, 0, -6])
+    fpos, fidx = _quad(*corners) if floor_grid <= 1 else _subdivide_quad(*corners, floor_grid)
     sc.add_mesh(fpos, fidx, floor_m)
     lm = sc.add_material(lambertian([0.0, 0.0, 0.0]))
     sc.add_sphere([2.0, 3.5, 1.5], 0.5, lm, emission=[30, 28, 25])
@@ -785,17 +787,26 @@ def resized_terrain_scene(seed=0, n_tris=500000, width=256, height=256, spp=64, 
                          grid=(2 * nz, nz), n_spheres=n_spheres, sphere_subdiv=subdiv, env_size=env_size)
 
 
-def serving_scenes(seed=0, n_scenes=6, min_tris=10000, max_tris=2000000):
-    """Scene pool of the serving workload: Cornell-box and terrain scenes
-    (alternating) with triangle counts log-uniform in [min_tris, max_tris]."""
+def resized_volume_scene(seed=0, n_tris=10000, width=256, height=256, spp=64, max_depth=64, grid=256):
+    """volume_scene with its floor split into about n_tris triangles."""
+    return volume_scene(seed=seed, width=width, height=height, spp=spp, max_depth=max_depth, grid=grid,
+                        floor_grid=max(1, int(round(math.sqrt(n_tris / 2.0)))))
+
+
+def serving_scenes(seed=0, n_scenes=6, min_tris=10000, max_tris=2000000, volume_grid=256):
+    """Scene pool of the serving workload: Cornell-box, terrain and
+    volumetric scenes in turn, with triangle counts log-uniform in
+    [min_tris, max_tris]."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(n_scenes):
         t = int(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris))))
-        if k % 2 == 0:
+        if k % 3 == 0:
             out.append(tessellated_cornell_box(seed=seed * 100 + k, n_tris=t))
-        else:
+        elif k % 3 == 1:
             out.append(resized_terrain_scene(seed=seed * 100 + k, n_tris=t))
+        else:
+            out.append(resized_volume_scene(seed=seed * 100 + k, n_tris=t, grid=volume_grid))
     return out
 
 

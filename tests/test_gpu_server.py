@@ -78,6 +78,23 @@ def test_volpath_job_matches_plain_render(ctx, case):
     assert_matches_plain(img, ref)
 
 
+@pytest.mark.parametrize("kind", ["path", "volpath"])
+def test_render_job_device_traces_the_server_jobs_samples(ctx, kind):
+    """lj_gpu_render_job_device with resolution and depth overrides renders
+    the same image as a server job of that description."""
+    import torch
+    sc = (scenes.cornell_box(seed=7, width=48, height=48, spp=4, max_depth=8) if kind == "path" else
+          scenes.homogeneous_box_scene(width=48, height=48, spp=4, index_matched=False))
+    g = gpu.GpuScene(ctx, sc)
+    job = dict(seed=21, spp=8, width=40, height=24, max_depth=5, rr_depth=3)
+    img, _ = render_alone(ctx, g, **job)
+    out = torch.zeros(24 * 40 * 3, dtype=torch.float32, device="cuda")
+    st = g.render_job_device(out, gpu.job_desc(**job), stats=True)
+    torch.cuda.synchronize()
+    assert st.samples == 40 * 24 * 8
+    assert_matches_plain(img, out.cpu().numpy().reshape(24, 40, 3))
+
+
 def _mix(ctx):
     gs = [gpu.GpuScene(ctx, scenes.cornell_box(seed=s, width=w, height=h, spp=4, max_depth=d))
           for s, w, h, d in ((1, 32, 32, 6), (2, 80, 40, 4), (3, 48, 64, 8), (4, 16, 16, -1))]
