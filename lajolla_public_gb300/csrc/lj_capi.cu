@@ -594,6 +594,7 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
                     o.pmin[c] = v.p_min[c];
                     o.pmax[c] = v.p_max[c];
                     o.max_value[c] = v.scale * mx[c];
+                    o.gscale[c] = (float)((double)(v.res[c] - 1) / ((double)v.p_max[c] - (double)v.p_min[c]));
                 }
                 if (upload(sc, rgb, &o.data, &err)) return fail(LJ_ERR_CUDA);
             }

@@ -103,6 +103,7 @@ struct VolRec {
     float pmin[3], pmax[3];
     float scale;
     float max_value[3];    // scale * max over the grid (or the constant)
+    float gscale[3];       // (res - 1) / (pmax - pmin): world offset -> grid coordinate
     const float4 *data;    // one float4 per voxel (xyz = the channels, w = 0): one 16-byte load per corner
 };
 

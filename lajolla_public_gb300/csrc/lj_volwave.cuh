@@ -36,18 +36,18 @@ struct VolState {
 
 LJ_D float chan(V3 v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : v.z); }
 LJ_D V3 vexp(V3 v) { return V3{expf(v.x), expf(v.y), expf(v.z)}; }
-LJ_D V3 vdiv(V3 a, V3 b) { return V3{a.x / b.x, a.y / b.y, a.z / b.z}; }
 
-// GridVolume lookup (src/volume.h:44-81)
+// GridVolume lookup (src/volume.h:44-81): trilinear over the voxel corners,
+// zero outside the box.  The grid coordinate is (p - pmin) * gscale, one
+// multiply per axis (the reference divides by the extent, then scales).
 LJ_D V3 vol_lookup(const VolRec &v, V3 p) {
     if (v.kind == 0) return V3{v.value[0], v.value[1], v.value[2]};
-    float nx = (p.x - v.pmin[0]) / (v.pmax[0] - v.pmin[0]);
-    float ny = (p.y - v.pmin[1]) / (v.pmax[1] - v.pmin[1]);
-    float nz = (p.z - v.pmin[2]) / (v.pmax[2] - v.pmin[2]);
-    if (nx < 0.f || nx > 1.f || ny < 0.f || ny > 1.f || nz < 0.f || nz > 1.f) return V3{0, 0, 0};
-    nx *= (float)(v.res[0] - 1);
-    ny *= (float)(v.res[1] - 1);
-    nz *= (float)(v.res[2] - 1);
+    const float nx = (p.x - v.pmin[0]) * v.gscale[0];
+    const float ny = (p.y - v.pmin[1]) * v.gscale[1];
+    const float nz = (p.z - v.pmin[2]) * v.gscale[2];
+    if (!(nx >= 0.f && nx <= (float)(v.res[0] - 1) && ny >= 0.f && ny <= (float)(v.res[1] - 1) && nz >= 0.f &&
+          nz <= (float)(v.res[2] - 1)))
+        return V3{0, 0, 0};
     int x0 = min(max((int)nx, 0), v.res[0] - 1), y0 = min(max((int)ny, 0), v.res[1] - 1),
         z0 = min(max((int)nz, 0), v.res[2] - 1);
     int x1 = min(x0 + 1, v.res[0] - 1), y1 = min(y0 + 1, v.res[1] - 1), z1 = min(z0 + 1, v.res[2] - 1);
@@ -82,15 +82,17 @@ LJ_D V3 majorant(const MediumRec &m, V3 o, V3 d) {
     if (vol_box_hit(m.density, o, d)) return V3{m.density.max_value[0], m.density.max_value[1], m.density.max_value[2]};
     return V3{0, 0, 0};
 }
-LJ_D void sigmas(const MediumRec &m, V3 p, V3 &ss, V3 &sa) {
-    if (m.kind == 0) {
-        ss = V3{m.sigma_s[0], m.sigma_s[1], m.sigma_s[2]};
-        sa = V3{m.sigma_a[0], m.sigma_a[1], m.sigma_a[2]};
-        return;
-    }
-    V3 dn = vol_lookup(m.density, p), al = vol_lookup(m.albedo, p);
-    ss = dn * al;
-    sa = dn * (V3{1, 1, 1} - al);
+// sigma_t = sigma_s + sigma_a at p: the density itself for a
+// heterogeneous medium (sigma_s = density * albedo, sigma_a = density *
+// (1 - albedo)), so the albedo is looked up only where sigma_s is needed.
+LJ_D V3 sigma_t_at(const MediumRec &m, V3 p) {
+    if (m.kind == 0) return V3{m.sigma_a[0] + m.sigma_s[0], m.sigma_a[1] + m.sigma_s[1], m.sigma_a[2] + m.sigma_s[2]};
+    return vol_lookup(m.density, p);
+}
+// sigma_s at p, given sigma_t there
+LJ_D V3 sigma_s_at(const MediumRec &m, V3 p, V3 st) {
+    if (m.kind == 0) return V3{m.sigma_s[0], m.sigma_s[1], m.sigma_s[2]};
+    return st * vol_lookup(m.albedo, p);
 }
 LJ_D int update_medium(const Vertex &v, V3 dir, int medium) {
     if (v.interior_medium != v.exterior_medium) return dot(dir, v.ng) > 0.f ? v.exterior_medium : v.interior_medium;
@@ -162,32 +164,68 @@ LJ_D void vol_nee_b(const DevScene &sc, const NeeQueue &nq, int k, int max_depth
             if (ovf) atomicOr(status, kStatusStackOverflow);
             float next_t = hit ? h.t : dist;
             if (smed >= 0) {
+                // ratio tracking over [0, next_t).  The sample positions
+                // depend on the random numbers only, so two steps are drawn
+                // ahead and their density lookups issued together; a step
+                // that was drawn but not reached (transmittance zero) gives
+                // its random number back.
                 const MediumRec &m = sc.media[smed];
-                V3 maj = majorant(m, p0, dir);
-                float mmax = max3(maj);
-                int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
+                const V3 maj = majorant(m, p0, dir);
+                const float inv_mmax = 1.0f / max3(maj);
+                const V3 maj_n = maj * inv_mmax;
+                const int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
+                const float majc = chan(maj, c), inv_majc = 1.0f / majc;
+                const int nmax = sc.max_null_collisions;
                 float acc = 0.0f;
-                for (int it = 0; it < sc.max_null_collisions; it++) {
-                    if (chan(maj, c) <= 0.0f) break;
-                    float t = -logf(1.0f - pcg_uniform(rng)) / chan(maj, c);
-                    float dt = next_t - acc;
-                    acc = fminf(acc + t, next_t);
-                    if (t < dt) {
-                        V3 ss, sa;
-                        sigmas(m, p0 + dir * acc, ss, sa);
-                        V3 st = ss + sa;
-                        V3 e = vexp(maj * -t);
-                        T = T * e * (maj - st) / mmax;
-                        p_nee = p_nee * e * maj / mmax;
-                        p_dir = p_dir * e * maj * (V3{1, 1, 1} - vdiv(st, maj)) / mmax;
-                        if (max3(T) <= 0.0f) break;
-                    } else {
-                        V3 e = vexp(maj * -dt);
+                int it = 0;
+                while (majc > 0.0f && it < nmax) {
+                    const float tA = -logf(1.0f - pcg_uniform(rng)) * inv_majc;
+                    const float dtA = next_t - acc;
+                    const float accA = fminf(acc + tA, next_t);
+                    if (!(tA < dtA)) {   // past next_t
+                        const V3 e = vexp(maj * -dtA);
                         T = T * e;
                         p_nee = p_nee * e;
                         p_dir = p_dir * e;
                         break;
                     }
+                    const uint64_t after_a = rng.state;
+                    const bool have_b = it + 1 < nmax;
+                    float tB = 0.0f, dtB = 0.0f, accB = accA;
+                    if (have_b) {
+                        tB = -logf(1.0f - pcg_uniform(rng)) * inv_majc;
+                        dtB = next_t - accA;
+                        accB = fminf(accA + tB, next_t);
+                    }
+                    const bool inside_b = have_b && tB < dtB;
+                    const V3 stA = sigma_t_at(m, p0 + dir * accA);
+                    const V3 stB = sigma_t_at(m, p0 + dir * (inside_b ? accB : accA));
+                    const V3 eA = vexp(maj * -tA);
+                    const V3 fA = eA * (maj - stA) * inv_mmax;
+                    T = T * fA;
+                    p_dir = p_dir * fA;
+                    p_nee = p_nee * eA * maj_n;
+                    it++;
+                    if (max3(T) <= 0.0f) {
+                        rng.state = after_a;
+                        break;
+                    }
+                    if (!have_b) break;
+                    acc = accB;
+                    if (!inside_b) {
+                        const V3 e = vexp(maj * -dtB);
+                        T = T * e;
+                        p_nee = p_nee * e;
+                        p_dir = p_dir * e;
+                        break;
+                    }
+                    const V3 eB = vexp(maj * -tB);
+                    const V3 fB = eB * (maj - stB) * inv_mmax;
+                    T = T * fB;
+                    p_dir = p_dir * fB;
+                    p_nee = p_nee * eB * maj_n;
+                    it++;
+                    if (max3(T) <= 0.0f) break;
                 }
             }
             if (!hit) break;
@@ -244,37 +282,39 @@ LJ_D void vol_segment_a(const DevScene &sc, const Store &store, int i, const Sha
     bool scatter = false;
     V3 p_scatter{0, 0, 0}, ss_scatter{0, 0, 0};
     if (medium >= 0) {
+        // delta tracking with the chromatic majorant: a sampled collision
+        // is real with probability sigma_t / majorant in channel c
         const MediumRec &m = sc.media[medium];
-        V3 maj = majorant(m, ro, rd);
-        float mmax = max3(maj);
-        int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
+        const V3 maj = majorant(m, ro, rd);
+        const float inv_mmax = 1.0f / max3(maj);
+        const V3 maj_n = maj * inv_mmax;
+        const int c = min(max((int)(pcg_uniform(rng) * 3.0f), 0), 2);
+        const float majc = chan(maj, c), inv_majc = 1.0f / majc;
         float acc = 0.0f;
         V3 T{1, 1, 1}, pd{1, 1, 1}, pn{1, 1, 1};
         unsigned nulls = 0;
         for (int it = 0; it < sc.max_null_collisions; it++) {
-            if (chan(maj, c) <= 0.0f) break;
-            float t = -logf(1.0f - pcg_uniform(rng)) / chan(maj, c);
+            if (majc <= 0.0f) break;
+            float t = -logf(1.0f - pcg_uniform(rng)) * inv_majc;
             float dt = t_hit - acc;
             acc = fminf(acc + t, t_hit);
             if (t < dt) {
-                V3 ss, sa;
-                V3 pp = ro + rd * acc;
-                sigmas(m, pp, ss, sa);
-                V3 stt = ss + sa;
-                V3 real = vdiv(stt, maj);
-                V3 e = vexp(maj * -t);
-                if (pcg_uniform(rng) < chan(real, c)) {
+                const V3 pp = ro + rd * acc;
+                const V3 stt = sigma_t_at(m, pp);
+                const V3 e = vexp(maj * -t);
+                if (pcg_uniform(rng) * majc < chan(stt, c)) {
                     scatter = true;
-                    T = T * e / mmax;
-                    pd = pd * e * maj * real / mmax;
+                    T = T * e * inv_mmax;
+                    pd = pd * e * stt * inv_mmax;
                     p_scatter = pp;
-                    ss_scatter = ss;
+                    ss_scatter = sigma_s_at(m, pp, stt);
                     break;
                 }
                 nulls++;
-                T = T * e * (maj - stt) / mmax;
-                pd = pd * e * maj * (V3{1, 1, 1} - real) / mmax;
-                pn = pn * e * maj / mmax;
+                const V3 f = e * (maj - stt) * inv_mmax;
+                T = T * f;
+                pd = pd * f;
+                pn = pn * e * maj_n;
             } else {
                 V3 e = vexp(maj * -dt);
                 T = T * e;
