@@ -455,7 +455,7 @@ __global__ void __launch_bounds__(B, 512 / B)
     }
 }
 template <int B>
-__global__ void __launch_bounds__(B, 640 / B)
+__global__ void __launch_bounds__(B, 512 / B)
     k_srv_vol_b(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
     const int nf = d.counts[16], n = nf + d.counts[17];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 4, (unsigned long long)n);

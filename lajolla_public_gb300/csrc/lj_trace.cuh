@@ -25,16 +25,17 @@ struct TraceHit {
     float u, v;
 };
 
-// Sphere: returns t in [tnear, tfar) of the nearest root, or -1.  Spheres are
-// rare primitives, so this runs in FP64 exactly like the reference's user-
-// geometry callback (src/shapes/sphere.inl:15-106: FP32 ray widened to FP64,
-// the stable quadratic of solve_quadratic), with explicit round-to-nearest
-// intrinsics so no contraction changes a rounding: t is bit-identical to the
-// CPU oracle's.
+// Sphere, exact form: returns t in [tnear, tfar) of the nearest root, or -1,
+// in FP64 exactly like the reference's user-geometry callback
+// (src/shapes/sphere.inl:15-106: FP32 ray widened to FP64, the stable
+// quadratic of solve_quadratic), with explicit round-to-nearest intrinsics
+// so no contraction changes a rounding: t is bit-identical to the CPU
+// oracle's.  FP64 is slow on this GPU; sphere_hit below takes this path only
+// when its FP32 form cannot certify a decision.
 LJ_D double ddot(double ax, double ay, double az, double bx, double by, double bz) {
     return __dadd_rn(__dadd_rn(__dmul_rn(ax, bx), __dmul_rn(ay, by)), __dmul_rn(az, bz));
 }
-LJ_D float sphere_hit(V3 c, float r, V3 o, V3 d, float tnear, float tfar) {
+LJ_D float sphere_hit_fp64(V3 c, float r, V3 o, V3 d, float tnear, float tfar) {
     double vx = __dsub_rn((double)o.x, (double)c.x), vy = __dsub_rn((double)o.y, (double)c.y),
            vz = __dsub_rn((double)o.z, (double)c.z);
     double dx = d.x, dy = d.y, dz = d.z, rr = r;
@@ -62,6 +63,102 @@ LJ_D float sphere_hit(V3 c, float r, V3 o, V3 d, float tnear, float tfar) {
     if (t0 >= tn && t0 < tf) t = t0;
     if (t1 >= tn && t1 < tf && t < 0.0) t = t1;
     return (t >= tn && t < tf) ? (float)t : -1.0f;
+}
+
+// Double-float (hi + lo pair of FP32) arithmetic for sphere_hit: the
+// error-free transformations of Dekker / Knuth (two_sum, two_prod by FMA)
+// with round-to-nearest intrinsics, so no contraction changes them.
+struct F2 {
+    float h, l;
+};
+LJ_D F2 two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return F2{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+LJ_D F2 fast_two_sum(float a, float b) {   // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return F2{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+LJ_D F2 two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return F2{p, __fmaf_rn(a, b, -p)};
+}
+LJ_D F2 df_add(F2 a, F2 b) {   // accurate sum (also under cancellation)
+    F2 s = two_sum(a.h, b.h);
+    const F2 t = two_sum(a.l, b.l);
+    s = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+    return fast_two_sum(s.h, __fadd_rn(s.l, t.l));
+}
+LJ_D F2 df_neg(F2 a) { return F2{-a.h, -a.l}; }
+LJ_D F2 df_mul(F2 a, F2 b) {
+    const F2 p = two_prod(a.h, b.h);
+    return fast_two_sum(p.h, __fadd_rn(p.l, __fadd_rn(__fmul_rn(a.h, b.l), __fmul_rn(a.l, b.h))));
+}
+
+// Sphere, fast form: the same quadratic (halved: t = (-B' +- sqrt(B'^2 -
+// A C)) / A with B' = d.v) with A, B', C and the discriminant in
+// double-float (relative error ~2^-44 of the terms' magnitudes, far below
+// the FP64 callback's own distance to any decision here) and the roots in
+// FP32, each with a forward error bound taken well above the derived one.
+// Hit / miss, the order of the roots and each root's comparison with tnear /
+// tfar are decided here only when the bounds leave no doubt, and a returned
+// t is within 6e-7 relative of the FP64 root; anything closer to a decision
+// boundary (grazing rays, roots near tnear / tfar or each other) goes to
+// sphere_hit_fp64.  So the hit / miss outcome is the FP64 callback's, and t
+// agrees with it to 6e-7 relative (a triangle closer than that to the
+// sphere along the ray may win where the FP64 t would lose).
+LJ_D float sphere_hit(V3 c, float r, V3 o, V3 d, float tnear, float tfar) {
+    constexpr float u = 5.9604645e-8f;         // 2^-24
+    constexpr float kDiscRel = 3.6379788e-12f;  // 2^-38, derived bound ~30 u^2
+    const F2 vx = two_sum(o.x, -c.x), vy = two_sum(o.y, -c.y), vz = two_sum(o.z, -c.z);   // exact
+    const F2 A = df_add(df_add(two_prod(d.x, d.x), two_prod(d.y, d.y)), two_prod(d.z, d.z));
+    const F2 Bh = df_add(df_add(df_add(two_prod(d.x, vx.h), two_prod(d.y, vy.h)), two_prod(d.z, vz.h)),
+                         two_sum(__fmaf_rn(d.x, vx.l, __fmul_rn(d.y, vy.l)), __fmul_rn(d.z, vz.l)));
+    const F2 V = df_add(df_add(df_add(two_prod(vx.h, vx.h), two_prod(vy.h, vy.h)), two_prod(vz.h, vz.h)),
+                        two_sum(2.0f * __fmaf_rn(vx.h, vx.l, __fmaf_rn(vy.h, vy.l, __fmul_rn(vz.h, vz.l))), 0.0f));
+    const F2 r2 = two_prod(r, r);
+    const F2 C = df_add(V, df_neg(r2));
+    const F2 disc = df_add(df_mul(Bh, Bh), df_neg(df_mul(A, C)));
+    const float P = fabsf(d.x * vx.h) + fabsf(d.y * vy.h) + fabsf(d.z * vz.h);
+    const float W = V.h + r2.h;
+    const float M = P * P + A.h * W;
+    const float e_disc = kDiscRel * M + 1e-30f;
+    if (!(A.h > 0.0f) || !(M < 1e30f) || !(fabsf(disc.h) > 4.0f * e_disc) || !(tnear >= 0.0f))
+        return sphere_hit_fp64(c, r, o, d, tnear, tfar);
+    if (disc.h < 0.0f) return -1.0f;
+    const float sq = sqrtf(disc.h);
+    const float q = -(Bh.h + copysignf(sq, Bh.h));
+    const float aq = fabsf(q);
+    // relative error of a root: u (disc to FP32) / 2 + u (sqrt) + u (B' to
+    // FP32, the sum) + u (A or C to FP32) + u (division), plus half the
+    // double-float error of the discriminant; C's absolute double-float
+    // error (~8 u^2 W) adds to the root C / q.  Bounds: 1.25x those.
+    const float rel = 0.5f * (e_disc / disc.h) + 4.5f * u;
+    const float ra = q / A.h, rc = C.h / q;
+    const float ea = 1.25f * fabsf(ra) * rel;
+    const float ec = 1.25f * (fabsf(rc) * rel + 16.0f * u * u * W / aq);
+    float t0 = ra, e0 = ea, t1 = rc, e1 = ec;
+    if (t0 > t1) {
+        t0 = rc;
+        e0 = ec;
+        t1 = ra;
+        e1 = ea;
+    }
+    if (!(t1 - t0 > e0 + e1)) return sphere_hit_fp64(c, r, o, d, tnear, tfar);
+    // 1: in [tnear, tfar), 0: outside, -1: too close to tell
+    auto in_range = [&](float t, float e) {
+        if (t + e < tnear || t - e >= tfar) return 0;
+        if (t - e >= tnear && t + e < tfar) return 1;
+        return -1;
+    };
+    const int s0 = in_range(t0, e0);
+    if (s0 == 1 && e0 <= 6e-7f * fabsf(t0)) return t0;
+    if (s0 != 0) return sphere_hit_fp64(c, r, o, d, tnear, tfar);
+    const int s1 = in_range(t1, e1);
+    if (s1 == 1 && e1 <= 6e-7f * fabsf(t1)) return t1;
+    if (s1 != 0) return sphere_hit_fp64(c, r, o, d, tnear, tfar);
+    return -1.0f;
 }
 
 LJ_D uint32_t extract_byte(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }

@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(128, 4) k_vol_a(DevScene sc, VolSoA ps, VolQue
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         vol_segment_a(sc, store, i, cfg, q.nee, status, q.stats);
 }
-__global__ void __launch_bounds__(128, 5) k_vol_b(DevScene sc, VolQueues q, int *status) {
+__global__ void __launch_bounds__(128, 4) k_vol_b(DevScene sc, VolQueues q, int *status) {
     const int nf = q.counts[2], n = nf + q.counts[3];
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
         vol_nee_b(sc, q.nee, q.nee.req(r, nf), sc.max_depth, status, q.stats + 1);
