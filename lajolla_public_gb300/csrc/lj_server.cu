@@ -597,7 +597,8 @@ struct HostJob {
     int64_t admit_seq = 0, cancel_seq = 0;
     unsigned long long *d_accum = nullptr;
     float *d_img = nullptr;
-    float *h_img = nullptr;
+    float *h_img = nullptr;      // pinned, from the server's pool
+    size_t h_img_cap = 0;        // its size class in bytes
     cudaEvent_t done_ev = nullptr;
     int64_t samples_done = 0, dropped = 0;
     double t_submit = 0, t_admit = 0, t_finish = 0;
@@ -623,6 +624,9 @@ struct lj_server {
 
     std::vector<lj_scene *> scenes;            // scene slot -> scene
     std::unordered_map<int64_t, std::unique_ptr<HostJob>> jobs;
+    // pinned image buffers by size class, reused: freeing pinned memory
+    // synchronizes the device, allocating it is slow
+    std::multimap<size_t, float *> pinned_free;
     std::deque<HostJob *> pending;
     std::vector<HostJob *> live;               // job slot -> job
     std::vector<int> free_slots;
@@ -968,7 +972,16 @@ std::string finish(lj_server *s, HostJob *j) {
                                                                        std::ldexp(1.0, -32) / j->spp);
         SRV_CUDA(cudaGetLastError());
         s->kernel_launches++;
-        SRV_CUDA(cudaMallocHost(&j->h_img, sizeof(float) * n));
+        size_t cap = 1 << 16;
+        while (cap < sizeof(float) * (size_t)n) cap <<= 1;
+        auto it = s->pinned_free.find(cap);
+        if (it != s->pinned_free.end()) {
+            j->h_img = it->second;
+            s->pinned_free.erase(it);
+        } else {
+            SRV_CUDA(cudaMallocHost(&j->h_img, cap));
+        }
+        j->h_img_cap = cap;
         SRV_CUDA(cudaMemcpyAsync(j->h_img, j->d_img, sizeof(float) * n, cudaMemcpyDeviceToHost, s->stream));
     }
     SRV_CUDA(cudaFreeAsync(j->d_accum, s->stream));
@@ -1222,6 +1235,8 @@ void release_device(lj_server *s) {
         j->d_img = nullptr;
         j->h_img = nullptr;
     }
+    for (auto &kv : s->pinned_free) cudaFreeHost(kv.second);
+    s->pinned_free.clear();
     if (s->graph) cudaGraphExecDestroy(s->graph);
     void *dev_ptrs[] = {s->d_pool, s->d_scenes, s->d_jobs, s->d_ctr, s->d_cancel, s->d_order, s->d_plan_off,
                         s->d_plan_coff, s->d_plan_start};
@@ -1382,9 +1397,16 @@ int lj_gpu_server_wait(lj_server *s, int64_t id, double timeout_s, float *out_rg
     if (j->state == LJ_JOB_CANCELLED) return LJ_ERR_CANCELLED;
     if (j->state == LJ_JOB_FAILED) return j->error ? j->error : LJ_ERR_CUDA;
     if (out_rgb) {
-        memcpy(out_rgb, j->h_img, sizeof(float) * 3 * (size_t)j->w * j->h);
-        cudaFreeHost(j->h_img);
+        // copy without the lock (the worker keeps launching), then give the
+        // pinned buffer back to the pool
+        float *buf = j->h_img;
+        const size_t cap = j->h_img_cap, bytes = sizeof(float) * 3 * (size_t)j->w * j->h;
+        j->h_img = nullptr;
         s->jobs.erase(id);
+        lk.unlock();
+        memcpy(out_rgb, buf, bytes);
+        lk.lock();
+        s->pinned_free.emplace(cap, buf);
     }
     return LJ_OK;
 }
