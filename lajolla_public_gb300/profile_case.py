@@ -18,6 +18,9 @@ Cases:
   volume_small  the volume case at 128x128, 64 spp, 64^3 grid
   terrain_srv, cbox_srv, volume_srv, volume_small_srv
                 the case as one server job (server kernels)
+  serving       one step of the serving benchmark on the server: its 6
+                resident scenes and the 32 jobs of its first timed step
+                (job seed 1000), submitted at once
 
 `summarize` reads the CSV that `ncu --metrics gpu__time_duration.sum --csv
 --log-file F` writes and prints launches, total time and share per kernel.
@@ -49,9 +52,40 @@ def make_case(name):
     raise SystemExit("unknown case %r" % name)
 
 
+def run_serving(args):
+    from . import gpu
+    pool = scenes.serving_scenes(0, 6)
+    jobs = scenes.serving_jobs(seed=1000, n_jobs=32, n_scenes=6, rate=200.0)
+    ctx = gpu.Context(0)
+    gs = [gpu.GpuScene(ctx, s) for s in pool]
+    opts = gpu.server_options(path_pool=args.pool, block_size=args.block, use_graphs=not args.profile,
+                              profile=args.profile, policy=abi.LJ_SCHED_SRPT)
+    with gpu.Server(ctx, opts) as srv:
+        for rep in range(args.warmup + args.repeat):
+            t0 = time.perf_counter()
+            ids = [srv.submit(gs[j["scene"]], seed=j["seed"], spp=j["spp"], width=j["width"], height=j["height"],
+                              max_depth=j["max_depth"], rr_depth=j["rr_depth"]) for j in jobs]
+            for i in ids:
+                srv.wait(i, timeout=600)
+            dt = time.perf_counter() - t0
+        st = srv.stats()
+    n = sum(j["width"] * j["height"] * j["spp"] for j in jobs)
+    cls = {abi.KERNEL_CLASS_NAMES[c]: round(st.class_ms[c] / (args.warmup + args.repeat), 3)
+           for c in range(abi.LJ_KERNEL_CLASSES)}
+    print("serving: %d samples, last step %.1f ms (host clock), %.1f Msamples/s, pool %d block %d, per-step "
+          "classes %s, waves %d, launches %d, vol segments %d, NEE requests %d"
+          % (n, dt * 1e3, n / dt / 1e6, args.pool, args.block, cls, st.waves, st.kernel_launches,
+             st.vol_segments, st.nee_requests))
+    for g in gs:
+        g.close()
+    ctx.close()
+
+
 def run(args):
     import torch
     from . import gpu
+    if args.case == "serving":
+        return run_serving(args)
     sc = make_case(args.case)
     ctx = gpu.Context(0)
     g = gpu.GpuScene(ctx, sc)
@@ -68,9 +102,9 @@ def run(args):
         cls = {abi.KERNEL_CLASS_NAMES[c]: round(st.class_ms[c] / (args.warmup + args.repeat), 3)
                for c in range(abi.LJ_KERNEL_CLASSES)}
         print("%s: %d samples, last job %.2f ms (host clock), pool %d block %d, per-job classes %s, "
-              "rays over all jobs: closest %d shadow %d, waves %d"
+              "rays over all jobs: closest %d shadow %d, waves %d, vol segments %d, NEE requests %d"
               % (args.case, sc.width * sc.height * sc.spp, dt * 1e3, args.pool, args.block, cls, st.rays_closest,
-                 st.rays_shadow, st.waves))
+                 st.rays_shadow, st.waves, st.vol_segments, st.nee_requests))
     else:
         out = torch.empty(n, dtype=torch.float32, device="cuda")
         stream = torch.cuda.current_stream().cuda_stream
