@@ -144,24 +144,57 @@ LJ_D void vol_nee_b(const DevScene &sc, const NeeQueue &nq, int k, int max_depth
     Pcg rng;
     rng.state = nq.rng[k];
     rng.inc = ((uint64_t)md.z << 1u) | 1u;
+    const bool env = (flags & kNeeEnv) != 0;
+    const V3 dir{d4.x, d4.y, d4.z}, lp{lp4.x, lp4.y, lp4.z}, org{o4.x, o4.y, o4.z};
+    const float inf = __int_as_float(0x7f800000);
+    const int bounces = md.y;
+    // pass 1: the shadow ray's path through index-matching surfaces, without
+    // random numbers; an opaque surface or the depth limit blocks it, and
+    // then no ratio tracking runs (the contribution is zero either way)
+    TraceHit h0{0.0f, -1, 0.0f, 0.0f};
+    bool hit0 = false;
     if (!blocked) {
-        const bool env = (flags & kNeeEnv) != 0;
-        const V3 dir{d4.x, d4.y, d4.z}, lp{lp4.x, lp4.y, lp4.z};
-        int smed = md.x;
-        const int bounces = md.y;
-        int sbounces = 0;
-        V3 p0{o4.x, o4.y, o4.z};
+        V3 p0 = org;
         float oeps = (flags & kNeeSurface) ? sc.eps : 0.0f;
-        const float inf = __int_as_float(0x7f800000);
+        for (int seg = 0; seg < kMaxShadowSegments; seg++) {
+            const float dist = env ? inf : length(lp - p0);
+            const float tmax = env ? inf : (1.0f - sc.eps) * dist;
+            TraceHit h{0.0f, -1, 0.0f, 0.0f};
+            int ovf = 0;
+            const bool hit = trace_bvh<false>(sc.bvh, p0, dir, oeps, tmax, h, &ovf);
+            if (ovf) atomicOr(status, kStatusStackOverflow);
+            if (seg == 0) {
+                h0 = h;
+                hit0 = hit;
+            }
+            if (!hit) break;
+            if (sc.shapes[__ldg(sc.prim_shape + h.prim)].material_id >= 0 ||
+                (max_depth != -1 && bounces + seg + 2 >= max_depth)) {
+                blocked = true;
+                break;
+            }
+            p0 = p0 + dir * h.t;
+            oeps = sc.eps;
+        }
+    }
+    // pass 2: the same segments again, with ratio tracking through media
+    if (!blocked) {
+        int smed = md.x;
+        int sbounces = 0;
+        V3 p0 = org;
+        float oeps = (flags & kNeeSurface) ? sc.eps : 0.0f;
         int segs = 0;
         for (int seg = 0; seg < kMaxShadowSegments; seg++) {
             segs++;
             float dist = env ? inf : length(lp - p0);
             float tmax = env ? inf : (1.0f - sc.eps) * dist;
-            TraceHit h{0.0f, -1, 0.0f, 0.0f};
-            int ovf = 0;
-            bool hit = trace_bvh<false>(sc.bvh, p0, dir, oeps, tmax, h, &ovf);
-            if (ovf) atomicOr(status, kStatusStackOverflow);
+            TraceHit h = h0;
+            bool hit = hit0;
+            if (seg > 0) {
+                int ovf = 0;
+                hit = trace_bvh<false>(sc.bvh, p0, dir, oeps, tmax, h, &ovf);
+                if (ovf) atomicOr(status, kStatusStackOverflow);
+            }
             float next_t = hit ? h.t : dist;
             if (smed >= 0) {
                 // ratio tracking over [0, next_t).  The sample positions

@@ -1694,6 +1694,15 @@ static double mis_dir(double pd, double pn) {
     return (pd * pd) / (pd * pd + pn * pn);
 }
 
+// Order of the shadow loop's work (test-only switch): 0 = the shadow ray's
+// path through index-matching surfaces is traced first and ratio tracking
+// runs only when it reaches the light (what the GPU does: a blocked shadow
+// ray draws no random numbers); 1 = the handout's order, ratio tracking of
+// each segment before the occlusion test of its end.  Both estimate the
+// same integral (a blocked ray contributes zero either way); they consume
+// the random-number stream differently.
+static int g_vol_nee_order = 0;
+
 // NEE from p (medium point when mat == nullptr, else a surface vertex vx with
 // material mat), through index-matching surfaces, with ratio tracking.
 static V3 vol_nee(const Scene &sc, V3 p, int medium, const Vertex *vx, const MatP *mat, V3 dir_view,
@@ -1707,52 +1716,64 @@ static V3 vol_nee(const Scene &sc, V3 p, int medium, const Vertex *vx, const Mat
     V3 dir = env ? -pl.n : normalize(pl.p - p);
     double eps = shadow_eps(sc);
     V3 T{1, 1, 1}, p_nee{1, 1, 1}, p_dir{1, 1, 1};
-    // from a surface, the shadow ray starts in the medium on its own side
-    int shadow_medium = vx ? update_medium(*vx, dir, medium) : medium, shadow_bounces = 0;
-    V3 p0 = p;
-    double origin_eps = vx ? eps : 0.0;
-    for (int guard = 0; guard < 1 << 16; guard++) {
-        double dist = env ? INFINITY : distance(pl.p, p0);
-        Ray sr{p0, dir, origin_eps, env ? INFINITY : (1 - eps) * dist};
-        std::optional<Vertex> is = intersect(sc, sr);
-        double next_t = is ? distance(p0, is->position) : dist;
-        if (shadow_medium >= 0) {
-            const MediumS &m = sc.media[shadow_medium];
-            V3 maj = majorant(m, sr);
-            double mmax = max3(maj);
-            int c = std::clamp((int)(rng.next() * 3), 0, 2);
-            double acc = 0;
-            for (int it = 0; it < sc.opt.max_null_collisions; it++) {
-                if (chan(maj, c) <= 0) break;
-                double t = -std::log(1 - rng.next()) / chan(maj, c);
-                double dt = next_t - acc;
-                acc = std::min(acc + t, next_t);
-                if (t < dt) {
-                    V3 ss, sa;
-                    sigmas(m, p0 + dir * acc, ss, sa);
-                    V3 st = ss + sa, sn = maj - st;
-                    V3 e = vexp(maj * -t);
-                    T = T * e * sn / mmax;
-                    p_nee = p_nee * e * maj / mmax;
-                    V3 real = st / maj;
-                    p_dir = p_dir * e * maj * (V3{1, 1, 1} - real) / mmax;
-                    if (max3(T) <= 0) break;
-                } else {
-                    V3 e = vexp(maj * -dt);
-                    T = T * e;
-                    p_nee = p_nee * e;
-                    p_dir = p_dir * e;
-                    break;
+    // one walk of the shadow ray through index-matching surfaces, with ratio
+    // tracking of each segment when `track`; false when an opaque surface or
+    // the depth limit blocks it
+    auto walk = [&](bool track) {
+        // from a surface, the shadow ray starts in the medium on its own side
+        int shadow_medium = vx ? update_medium(*vx, dir, medium) : medium, shadow_bounces = 0;
+        V3 p0 = p;
+        double origin_eps = vx ? eps : 0.0;
+        for (int guard = 0; guard < 1 << 16; guard++) {
+            double dist = env ? INFINITY : distance(pl.p, p0);
+            Ray sr{p0, dir, origin_eps, env ? INFINITY : (1 - eps) * dist};
+            std::optional<Vertex> is = intersect(sc, sr);
+            double next_t = is ? distance(p0, is->position) : dist;
+            if (track && shadow_medium >= 0) {
+                const MediumS &m = sc.media[shadow_medium];
+                V3 maj = majorant(m, sr);
+                double mmax = max3(maj);
+                int c = std::clamp((int)(rng.next() * 3), 0, 2);
+                double acc = 0;
+                for (int it = 0; it < sc.opt.max_null_collisions; it++) {
+                    if (chan(maj, c) <= 0) break;
+                    double t = -std::log(1 - rng.next()) / chan(maj, c);
+                    double dt = next_t - acc;
+                    acc = std::min(acc + t, next_t);
+                    if (t < dt) {
+                        V3 ss, sa;
+                        sigmas(m, p0 + dir * acc, ss, sa);
+                        V3 st = ss + sa, sn = maj - st;
+                        V3 e = vexp(maj * -t);
+                        T = T * e * sn / mmax;
+                        p_nee = p_nee * e * maj / mmax;
+                        V3 real = st / maj;
+                        p_dir = p_dir * e * maj * (V3{1, 1, 1} - real) / mmax;
+                        if (max3(T) <= 0) break;
+                    } else {
+                        V3 e = vexp(maj * -dt);
+                        T = T * e;
+                        p_nee = p_nee * e;
+                        p_dir = p_dir * e;
+                        break;
+                    }
                 }
             }
+            if (!is) return true;
+            if (is->material_id >= 0) return false;
+            shadow_bounces++;
+            if (sc.opt.max_depth != -1 && bounces + shadow_bounces + 1 >= sc.opt.max_depth) return false;
+            shadow_medium = update_medium(*is, dir, shadow_medium);
+            p0 = p0 + dir * next_t;
+            origin_eps = eps;
         }
-        if (!is) break;
-        if (is->material_id >= 0) return V3{};
-        shadow_bounces++;
-        if (sc.opt.max_depth != -1 && bounces + shadow_bounces + 1 >= sc.opt.max_depth) return V3{};
-        shadow_medium = update_medium(*is, dir, shadow_medium);
-        p0 = p0 + dir * next_t;
-        origin_eps = eps;
+        return true;
+    };
+    if (g_vol_nee_order == 0) {
+        if (!walk(false)) return V3{};
+        walk(true);
+    } else if (!walk(true)) {
+        return V3{};
     }
     if (max3(T) <= 0) return V3{};
     double G = env ? 1.0 : std::max(-dot(dir, pl.n), 0.0) / distance_squared(pl.p, p);
@@ -2278,6 +2299,7 @@ void ljo_pcg(uint64_t stream, uint64_t seed, int k, uint32_t *out) {
 }
 // Test-only: select the volumetric estimator (0 MIS, 1 light only, 2 direction only).
 void ljo_set_vol_mis_mode(int mode) { g_vol_mis_mode = mode; }
+void ljo_set_vol_nee_order(int order) { g_vol_nee_order = order; }
 
 void ljo_pcg_keyed(uint64_t job_seed, uint64_t pixel, uint64_t sample, int k, uint32_t *out) {
     Pcg p = pcg_keyed(job_seed, pixel, sample);

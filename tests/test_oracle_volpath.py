@@ -6,6 +6,10 @@ parity with reference code is unpinned here) checked for unbiasedness:
     three unbiased estimators of the same integral: their image means agree
     within 4 standard errors on media behind index-matching and rough
     dielectric boundaries, homogeneous and heterogeneous, chromatic;
+  * the shadow loop's two orders -- occlusion through index-matching
+    surfaces first and ratio tracking only for unblocked rays (the GPU's),
+    or the handout's ratio tracking of each segment before its occlusion
+    test -- consume the random numbers differently but agree in the mean;
   * without media, the volumetric integrator equals the path tracer.
 CPU only."""
 import ctypes as C
@@ -17,15 +21,18 @@ from lajolla_public_gb300 import abi, scenes
 from oracle import ljo
 
 
-def _mean_se(sc, mode, spp, seed):
+def _mean_se(sc, mode, spp, seed, order=0):
     L = ljo.lib()
     L.ljo_set_vol_mis_mode.argtypes = [C.c_int]
+    L.ljo_set_vol_nee_order.argtypes = [C.c_int]
     L.ljo_set_vol_mis_mode(mode)
+    L.ljo_set_vol_nee_order(order)
     try:
         o = ljo.OracleScene(sc)
         s = o.render_samples(np.arange(sc.width * sc.height, dtype=np.int32), spp, seed=seed)
     finally:
         L.ljo_set_vol_mis_mode(0)
+        L.ljo_set_vol_nee_order(0)
     flat = s.reshape(-1, 3)
     return flat.mean(axis=0), flat.std(axis=0) / np.sqrt(len(flat))
 
@@ -46,6 +53,15 @@ def test_mis_light_and_direction_estimators_agree(case):
         m, s = _mean_se(sc, mode, 1024, 21 + mode)
         z = np.abs(m - m0) / np.sqrt(s0 ** 2 + s ** 2)
         assert np.all(z < 4.0), (case, mode, m0, m, z)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_shadow_loop_orders_agree(case):
+    sc = CASES[case]()
+    m0, s0 = _mean_se(sc, 0, 1024, 31, order=0)
+    m1, s1 = _mean_se(sc, 0, 1024, 32, order=1)
+    z = np.abs(m1 - m0) / np.sqrt(s0 ** 2 + s1 ** 2)
+    assert np.all(z < 4.0), (case, m0, m1, z)
 
 
 def test_volpath_without_media_equals_path_tracer():
