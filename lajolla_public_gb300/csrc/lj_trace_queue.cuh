@@ -116,10 +116,10 @@ LJ_D bool trav_step(Trav &s, TravStack &stack, int *status) {
             const float fy = fmaf(byte_to_float(i < 4 ? fy0 : fy1, i & 3), ay, by);
             const float nz = fmaf(byte_to_float(i < 4 ? nz0 : nz1, i & 3), az, bz);
             const float fz = fmaf(byte_to_float(i < 4 ? fz0 : fz1, i & 3), az, bz);
-            // slack of ~8 ulps: hits on box faces, and hits at exactly the
-            // current closest distance (ties), are never culled
-            const float tmin = fmaxf(fmaxf(nx, ny), fmaxf(nz, tnear)) * (1.0f - 1.0e-6f);
-            const float tmax = fminf(fminf(fx, fy), fminf(fz, tfar)) * (1.0f + 1.0e-6f);
+            // slack of ~8 ulps (kBoxSlack): hits on box faces, and hits at
+            // exactly the current closest distance (ties), are never culled
+            const float tmin = fmaxf(fmax3(nx, ny, nz), tnear) * kBoxSlack;
+            const float tmax = fmin3(fx, fy, fminf(fz, tfar));
             if (tmin <= tmax) {
                 const uint32_t off = meta & 0x1fu;
                 if (off >= 24u) node_hits |= 1u << (24u + ((uint32_t)i ^ s.oct_xor));

@@ -66,10 +66,10 @@ LJ_D V3 vol_lookup(const VolRec &v, V3 p) {
 LJ_D bool vol_box_hit(const VolRec &v, V3 o, V3 d) {
     if (v.kind == 0) return true;
     float t0 = 0.f, t1 = __int_as_float(0x7f800000);
-    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    const float oo[3] = {o.x, o.y, o.z}, inv[3] = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
     for (int i = 0; i < 3; i++) {
-        float tn = (v.pmin[i] - oo[i]) / dd[i];
-        float tf = (v.pmax[i] - oo[i]) / dd[i];
+        float tn = (v.pmin[i] - oo[i]) * inv[i];
+        float tf = (v.pmax[i] - oo[i]) * inv[i];
         if (tn > tf) { float x = tn; tn = tf; tf = x; }
         t0 = tn > t0 ? tn : t0;
         t1 = tf < t1 ? tf : t1;
@@ -278,7 +278,7 @@ LJ_D void vol_nee_b(const DevScene &sc, const NeeQueue &nq, int k, int max_depth
             oeps = sc.eps;
             if (seg == kMaxShadowSegments - 1) atomicOr(status, kStatusBounceCap);
         }
-        if (!blocked && seg_stat) atomicAdd(seg_stat, (unsigned long long)segs);
+        if (seg_stat) counter_add(seg_stat, blocked ? 0u : (unsigned)segs);
     }
     nq.rng[k] = rng.state;
     nq.T[k] = make_float4(T.x, T.y, T.z, blocked ? 1.0f : 0.0f);
@@ -356,8 +356,8 @@ LJ_D void vol_segment_a(const DevScene &sc, const Store &store, int i, const Sha
                 break;
             }
         }
-        if (nulls) atomicAdd(stats + 3, (unsigned long long)nulls);
-        if (scatter) atomicAdd(stats + 4, 1ull);
+        counter_add(stats + 3, nulls);
+        counter_add(stats + 4, scatter ? 1u : 0u);
         beta = beta * T / avg3(pd);
         mdir = mdir * pd;
         mnee = mnee * pn;

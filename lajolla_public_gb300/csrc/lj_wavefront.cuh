@@ -82,6 +82,14 @@ LJ_D int queue_slot(int *counter) {
     return base + __popc(active & ((1u << lane_id()) - 1u));
 }
 
+// Add v to a counter that many threads update: one atomic per group of
+// converged threads (same-address atomics serialize in L2).
+LJ_D void counter_add(unsigned long long *counter, unsigned v) {
+    const unsigned active = __activemask();
+    const unsigned sum = __reduce_add_sync(active, v);
+    if ((int)lane_id() == __ffs(active) - 1 && sum) atomicAdd(counter, (unsigned long long)sum);
+}
+
 // The single-scene renderer's store: queue cur holds (ray, slot) pairs.
 struct SlotPaths {
     PathSoA ps;
