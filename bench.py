@@ -549,6 +549,12 @@ def scene_host_bytes(sc):
     b += C.sizeof(abi.lj_light_desc) * len(sc.lights) + C.sizeof(abi.lj_scene_desc)
     for im in sc.images:
         b += np.asarray(im, np.float32).nbytes
+    for m in sc.media:
+        b += C.sizeof(abi.lj_medium_desc)
+        for key in ("albedo", "density"):
+            v = m.get(key)
+            if v is not None and v.get("data") is not None:
+                b += np.asarray(v["data"], np.float32).nbytes
     return int(b)
 
 

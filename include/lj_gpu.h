@@ -157,6 +157,12 @@ typedef struct lj_volume_desc {
     float p_min[3], p_max[3];
     float scale;
     const float *data;           /* res.x*res.y*res.z*channels, x fastest */
+    /* Grid value of channel c = data (the one channel, or channel c) *
+     * scale * channel_scale[c]: a scalar grid with a chromatic factor
+     * (density times a colour), stored at one float per voxel.  All zero
+     * means (1, 1, 1), the reference's GridVolume.  No counterpart in the
+     * reference, whose chromatic grids hold three values per voxel. */
+    float channel_scale[3];
 } lj_volume_desc;
 
 /* Medium variant, src/medium.h:10-22; PhaseFunction src/phase_function.h:9-16. */

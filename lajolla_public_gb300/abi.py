@@ -85,7 +85,7 @@ class lj_image_desc(C.Structure):
 class lj_volume_desc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("res", C.c_int32 * 3), ("channels", C.c_int32),
                 ("value", C.c_float * 3), ("p_min", C.c_float * 3), ("p_max", C.c_float * 3),
-                ("scale", C.c_float), ("data", f32p)]
+                ("scale", C.c_float), ("data", f32p), ("channel_scale", C.c_float * 3)]
 
 
 class lj_medium_desc(C.Structure):

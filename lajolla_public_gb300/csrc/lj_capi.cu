@@ -579,24 +579,35 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
                     err = "medium " + std::to_string(i) + ": bad grid volume";
                     return fail(LJ_ERR_INVALID_ARG);
                 }
-                std::vector<float4> rgb(n);
+                const bool cs_set = v.channel_scale[0] != 0.0f || v.channel_scale[1] != 0.0f ||
+                                    v.channel_scale[2] != 0.0f;
                 float mx[3] = {0, 0, 0};
-                for (size_t p = 0; p < n; p++) {
-                    float x[3];
-                    for (int c = 0; c < 3; c++) {
-                        x[c] = v.channels == 3 ? v.data[p * 3 + c] : v.data[p];
-                        mx[c] = std::max(mx[c], x[c]);
+                o.channels = v.channels;
+                if (v.channels == 1) {   // one float per voxel
+                    std::vector<float> one(v.data, v.data + n);
+                    for (size_t p = 0; p < n; p++) mx[0] = std::max(mx[0], one[p]);
+                    mx[1] = mx[2] = mx[0];
+                    if (upload(sc, one, &o.data1, &err)) return fail(LJ_ERR_CUDA);
+                } else {
+                    std::vector<float4> rgb(n);
+                    for (size_t p = 0; p < n; p++) {
+                        float x[3];
+                        for (int c = 0; c < 3; c++) {
+                            x[c] = v.data[p * 3 + c];
+                            mx[c] = std::max(mx[c], x[c]);
+                        }
+                        rgb[p] = make_float4(x[0], x[1], x[2], 0.0f);
                     }
-                    rgb[p] = make_float4(x[0], x[1], x[2], 0.0f);
+                    if (upload(sc, rgb, &o.data, &err)) return fail(LJ_ERR_CUDA);
                 }
                 for (int c = 0; c < 3; c++) {
                     o.res[c] = v.res[c];
                     o.pmin[c] = v.p_min[c];
                     o.pmax[c] = v.p_max[c];
-                    o.max_value[c] = v.scale * mx[c];
+                    o.cscale[c] = cs_set ? v.channel_scale[c] : 1.0f;
+                    o.max_value[c] = v.scale * mx[c] * o.cscale[c];
                     o.gscale[c] = (float)((double)(v.res[c] - 1) / ((double)v.p_max[c] - (double)v.p_min[c]));
                 }
-                if (upload(sc, rgb, &o.data, &err)) return fail(LJ_ERR_CUDA);
             }
         }
         if (upload(sc, media, &ds.media, &err)) return fail(LJ_ERR_CUDA);

@@ -102,9 +102,12 @@ struct VolRec {
     float value[3];
     float pmin[3], pmax[3];
     float scale;
-    float max_value[3];    // scale * max over the grid (or the constant)
+    float max_value[3];    // scale * channel scale * max over the grid (or the constant)
     float gscale[3];       // (res - 1) / (pmax - pmin): world offset -> grid coordinate
+    float cscale[3];       // channel scale (lj_volume_desc.channel_scale; 1 when unset)
+    int channels;          // 1: data1, one float per voxel; 3: data
     const float4 *data;    // one float4 per voxel (xyz = the channels, w = 0): one 16-byte load per corner
+    const float *data1;
 };
 
 // Medium (src/medium.h) + phase function.

@@ -52,15 +52,25 @@ LJ_D V3 vol_lookup(const VolRec &v, V3 p) {
         z0 = min(max((int)nz, 0), v.res[2] - 1);
     int x1 = min(x0 + 1, v.res[0] - 1), y1 = min(y0 + 1, v.res[1] - 1), z1 = min(z0 + 1, v.res[2] - 1);
     float dx = nx - x0, dy = ny - y0, dz = nz - z0;
+    const float w000 = (1 - dx) * (1 - dy) * (1 - dz), w100 = dx * (1 - dy) * (1 - dz);
+    const float w010 = (1 - dx) * dy * (1 - dz), w110 = dx * dy * (1 - dz);
+    const float w001 = (1 - dx) * (1 - dy) * dz, w101 = dx * (1 - dy) * dz;
+    const float w011 = (1 - dx) * dy * dz, w111 = dx * dy * dz;
+    const V3 cs{v.cscale[0], v.cscale[1], v.cscale[2]};
+    if (v.channels == 1) {   // scalar grid times the channel scale: one 4-byte load per corner
+        auto at = [&](int x, int y, int z) { return __ldg(v.data1 + ((size_t)z * v.res[1] + y) * v.res[0] + x); };
+        const float r = at(x0, y0, z0) * w000 + at(x1, y0, z0) * w100 + at(x0, y1, z0) * w010 +
+                        at(x1, y1, z0) * w110 + at(x0, y0, z1) * w001 + at(x1, y0, z1) * w101 +
+                        at(x0, y1, z1) * w011 + at(x1, y1, z1) * w111;
+        return cs * (r * v.scale);
+    }
     auto at = [&](int x, int y, int z) {
         const float4 q = __ldg(v.data + ((size_t)z * v.res[1] + y) * v.res[0] + x);
         return V3{q.x, q.y, q.z};
     };
-    V3 r = at(x0, y0, z0) * ((1 - dx) * (1 - dy) * (1 - dz)) + at(x1, y0, z0) * (dx * (1 - dy) * (1 - dz)) +
-           at(x0, y1, z0) * ((1 - dx) * dy * (1 - dz)) + at(x1, y1, z0) * (dx * dy * (1 - dz)) +
-           at(x0, y0, z1) * ((1 - dx) * (1 - dy) * dz) + at(x1, y0, z1) * (dx * (1 - dy) * dz) +
-           at(x0, y1, z1) * ((1 - dx) * dy * dz) + at(x1, y1, z1) * (dx * dy * dz);
-    return r * v.scale;
+    V3 r = at(x0, y0, z0) * w000 + at(x1, y0, z0) * w100 + at(x0, y1, z0) * w010 + at(x1, y1, z0) * w110 +
+           at(x0, y0, z1) * w001 + at(x1, y0, z1) * w101 + at(x0, y1, z1) * w011 + at(x1, y1, z1) * w111;
+    return (r * v.scale) * cs;
 }
 // slab test against the density grid box (src/volume.h:124-144); tfar = inf
 LJ_D bool vol_box_hit(const VolRec &v, V3 o, V3 d) {

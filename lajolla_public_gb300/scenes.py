@@ -269,6 +269,8 @@ class Scene:
                         vd.p_min[c], vd.p_max[c] = v["p_min"][c], v["p_max"][c]
                     vd.data = ptr(data, C.c_float)
                 vd.scale = v.get("scale", 1.0)
+                for c in range(3):
+                    vd.channel_scale[c] = v.get("channel_scale", (0.0, 0.0, 0.0))[c]
         d.num_shapes, d.num_materials = len(self.shapes), len(self.materials)
         d.num_lights, d.num_media, d.num_images = len(self.lights), len(self.media), len(self.images)
         d.envmap_light_id = self.envmap_light_id
@@ -686,22 +688,23 @@ def volume_scene(seed=0, width=512, height=512, spp=256, max_depth=64, grid=256,
                  sigma_t_scale=(1.05, 0.9, 0.8), albedo=(0.952, 0.889, 0.75), g=0.7,
                  eta=1.33, roughness=0.1, floor_grid=1):
     """Seeded volumetric scene: a heterogeneous chromatic medium (5-octave
-    value noise scaled to `max_density`, sigma_t = scale * noise as a
-    3-channel density, constant albedo, HG g) inside a rough dielectric
-    sphere, over a diffuse plane (split into floor_grid^2 quads), lit by one
-    sphere area light."""
+    value noise scaled to `max_density` as a one-channel FP32 density grid,
+    sigma_t = sigma_t_scale * density through the grid's channel scale,
+    constant albedo, HG g) inside a rough dielectric sphere, over a diffuse
+    plane (split into floor_grid^2 quads), lit by one sphere area light."""
     rng = np.random.default_rng(seed)
     sc = Scene(width, height, spp, max_depth, look_at([0, 1.4, 4.2], [0, 0.9, 0], [0, 1, 0]), 35.0,
                integrator=abi.LJ_INTEGRATOR_VOLPATH, vol_path_version=6)
     noise = value_noise_3d(rng, grid)
     noise = noise - noise.min()
     noise = noise / noise.max() * max_density
-    dens = (noise[..., None] * np.asarray(sigma_t_scale, np.float32)).astype(np.float32)
+    dens = noise[..., None].astype(np.float32)
     c, r = np.array([0.0, 1.0, 0.0]), 1.0
     sc.media.append(dict(kind=abi.LJ_MEDIUM_HETEROGENEOUS, phase_kind=abi.LJ_PHASE_HG, g=f32(g),
                          albedo=dict(kind=abi.LJ_VOL_CONST, value=[f32(a) for a in albedo]),
                          density=dict(kind=abi.LJ_VOL_GRID, data=dens, p_min=[f32(x) for x in c - r],
-                                      p_max=[f32(x) for x in c + r])))
+                                      p_max=[f32(x) for x in c + r],
+                                      channel_scale=[f32(x) for x in sigma_t_scale])))
     diel = sc.add_material(roughdielectric([1, 1, 1], [1, 1, 1], roughness, eta))
     sc.add_sphere(c, r, diel, interior_medium=0, exterior_medium=-1)
     floor_m = sc.add_material(lambertian([0.6, 0.6, 0.6]))

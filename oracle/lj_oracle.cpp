@@ -839,6 +839,7 @@ struct VolS {
     int res[3] = {1, 1, 1};
     V3 pmin, pmax;
     double scale = 1;
+    V3 cscale{1, 1, 1};          // lj_volume_desc.channel_scale (all zero: 1)
     std::vector<V3> data;
     V3 max_data;
 };
@@ -970,6 +971,9 @@ static VolS vol_from(const lj_volume_desc &v) {
     VolS o;
     o.kind = v.kind;
     o.scale = v.scale;
+    if (v.kind == LJ_VOL_GRID &&
+        (v.channel_scale[0] != 0.0f || v.channel_scale[1] != 0.0f || v.channel_scale[2] != 0.0f))
+        o.cscale = V3{v.channel_scale[0], v.channel_scale[1], v.channel_scale[2]};
     if (v.kind == LJ_VOL_CONST) {
         o.value = V3{v.value[0], v.value[1], v.value[2]};
         o.max_data = o.value;
@@ -1636,7 +1640,7 @@ static V3 vol_lookup(const VolS &v, V3 p) {
            at(x0, y1, z0) * ((1 - dx) * dy * (1 - dz)) + at(x1, y1, z0) * (dx * dy * (1 - dz)) +
            at(x0, y0, z1) * ((1 - dx) * (1 - dy) * dz) + at(x1, y0, z1) * (dx * (1 - dy) * dz) +
            at(x0, y1, z1) * ((1 - dx) * dy * dz) + at(x1, y1, z1) * (dx * dy * dz);
-    return r * v.scale;
+    return r * v.scale * v.cscale;
 }
 // slab test against the grid's box, src/volume.h:124-144
 static bool vol_intersect(const VolS &v, const Ray &r) {
@@ -1655,7 +1659,7 @@ static bool vol_intersect(const VolS &v, const Ray &r) {
 // get_majorant / get_sigma_s / get_sigma_a, src/media/*.inl
 static V3 majorant(const MediumS &m, const Ray &r) {
     if (m.kind == LJ_MEDIUM_HOMOGENEOUS) return m.sigma_a + m.sigma_s;
-    if (vol_intersect(m.density, r)) return m.density.max_data * m.density.scale;
+    if (vol_intersect(m.density, r)) return m.density.max_data * m.density.scale * m.density.cscale;
     return V3{};
 }
 static void sigmas(const MediumS &m, V3 p, V3 &ss, V3 &sa) {
