@@ -288,7 +288,7 @@ def plain_step(gscenes, jobs, out, stream, keep=()):
 def tuned_options(ctx, gscenes):
     """Server options from the autotuner (cached per device and workload)."""
     from lajolla_public_gb300 import gpu
-    tune = scenes.serving_jobs(seed=999, n_jobs=8, n_scenes=WORKLOAD["n_scenes"], resolutions=(128, 256, 512),
+    tune = scenes.serving_jobs(seed=999, n_jobs=8, n_scenes=WORKLOAD["n_scenes"], resolutions=(128, 256, 512, 1024),
                                spps=(4, 16, 64))
     jd = [job_desc(j) for j in tune]
     os.makedirs(os.path.dirname(TUNE_CACHE), exist_ok=True)

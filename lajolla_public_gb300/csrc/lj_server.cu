@@ -406,14 +406,26 @@ struct VolQueueStore {
         r1 = v.ray[2 * i + 1];
         hit = d.vhit[i];
     }
-    // state of a path that waits for its NEE request: kept in place
+    // state of a path that waits for its NEE request: kept in place (the c
+    // step resets the NEE vertex and the pdf products, and takes the PCG
+    // state from the request, so those stay behind)
     LJ_D void save(int i, const VolState &vs) const {
         const VolStateSoA &v = d.vbuf[cur];
         v.beta[i] = vs.beta;
         v.L[i] = vs.L;
-        v.mdir[i] = vs.mdir;
-        v.mnee[i] = vs.mnee;
         v.st[i] = vs.st;
+    }
+    LJ_D void load_c(int i, VolState &vs, float4 &r0, float4 &r1, float4 &hit) const {
+        const VolStateSoA &v = d.vbuf[cur];
+        vs.slot = i;
+        vs.job = v.job[i];
+        vs.pixel = v.pixel[i];
+        vs.beta = v.beta[i];
+        vs.L = v.L[i];
+        vs.st = v.st[i];
+        r0 = v.ray[2 * i];
+        r1 = v.ray[2 * i + 1];
+        hit = d.vhit[i];
     }
     LJ_D void emit(const VolState &vs, bool alive, float4 ray0, float4 ray1) const {
         if (alive) {
@@ -1523,7 +1535,8 @@ int lj_gpu_server_autotune(lj_ctx *ctx, lj_scene *const *scenes, const lj_job_de
             }
         }
     }
-    const int64_t pools[] = {(int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22, (int64_t)1 << 23};
+    const int64_t pools[] = {(int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22, (int64_t)1 << 23,
+                             (int64_t)1 << 24};
     const int32_t blocks[] = {64, 128, 256};
     double best = -1;
     int64_t best_pool = 0;

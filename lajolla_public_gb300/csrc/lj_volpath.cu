@@ -116,14 +116,27 @@ struct VolSlotStore {
         vs.mnee = ps.mnee[p];
         vs.st = ps.st[p];
     }
-    // state of a path that waits for its NEE request
+    // state of a path that waits for its NEE request (the c step resets the
+    // NEE vertex and the pdf products, and takes the PCG state from the
+    // request, so those stay behind)
     LJ_D void save(int, const VolState &vs) const {
         const int p = vs.slot;
         ps.beta[p] = vs.beta;
         ps.L[p] = vs.L;
-        ps.mdir[p] = vs.mdir;
-        ps.mnee[p] = vs.mnee;
         ps.st[p] = vs.st;
+    }
+    LJ_D void load_c(int i, VolState &vs, float4 &r0, float4 &r1, float4 &hit) const {
+        const int p = (cur ? q.path[1] : q.path[0])[i];
+        const float4 *rays = cur ? q.ray[1] : q.ray[0];
+        r0 = rays[2 * i];
+        r1 = rays[2 * i + 1];
+        hit = q.hit[i];
+        vs.slot = p;
+        vs.job = 0;
+        vs.pixel = ps.pixel[p];
+        vs.beta = ps.beta[p];
+        vs.L = ps.L[p];
+        vs.st = ps.st[p];
     }
     LJ_D void emit(const VolState &vs, bool alive, float4 ray0, float4 ray1) const {
         const int p = vs.slot, nxt = cur ^ 1;

@@ -465,7 +465,7 @@ LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const Sha
     const int i = nq.entry[k];
     VolState vs;
     float4 r0, r1, hit;
-    store.load(i, vs, r0, r1, hit);
+    store.load_c(i, vs, r0, r1, hit);
     const float4 o4 = nq.org[k], d4 = nq.dir[k], lp4 = nq.lp[k], ln4 = nq.ln[k], T4 = nq.T[k];
     const int flags = __float_as_int(ln4.w), lid = __float_as_int(lp4.w);
     constexpr bool surface = kSurface;
@@ -519,8 +519,10 @@ LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const Sha
         }
     }
     bool alive = true;
-    V3 next_o{0, 0, 0}, next_d{0, 0, 0}, neep{vs.neep.x, vs.neep.y, vs.neep.z};
-    V3 mdir{vs.mdir.x, vs.mdir.y, vs.mdir.z}, mnee{vs.mnee.x, vs.mnee.y, vs.mnee.z};
+    // the NEE vertex and the pdf products restart at this vertex (a path
+    // that ends here needs neither)
+    V3 next_o{0, 0, 0}, next_d{0, 0, 0}, neep{0, 0, 0};
+    V3 mdir{1, 1, 1}, mnee{1, 1, 1};
     float next_tnear = 0.0f;
     if constexpr (!surface) {
         // phase sampling at the scattering point

@@ -226,7 +226,7 @@ def test_autotune_picks_a_candidate_and_caches_it(ctx, tmp_path):
     jobs = [gpu.job_desc(seed=k, spp=4) for k in range(4)]
     cache = str(tmp_path / "tune.json")
     opt = gpu.autotune(ctx, gs, jobs, [0] * 4, cache_path=cache)
-    assert opt.path_pool in (1 << 20, 1 << 21, 1 << 22, 1 << 23) and opt.block_size in (64, 128, 256)
+    assert opt.path_pool in (1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24) and opt.block_size in (64, 128, 256)
     text = open(cache).read()
     assert "path_pool" in text and "block_size" in text
     again = gpu.autotune(ctx, gs, jobs, [0] * 4, cache_path=cache)
