@@ -7,8 +7,9 @@ Workload (a "step" = serving one batch of render jobs):
            renders one of 6 resident scenes -- in turn a seeded Cornell box
            with tessellated walls, a seeded terrain + icosphere + HDR-envmap
            scene (Disney BSDFs) and a seeded heterogeneous volume (256^3
-           value-noise density, max 20) in a dielectric sphere over a
-           tessellated floor (volumetric path tracer), 10k-2M triangles,
+           FP32 value-noise density, max 20, chromatic sigma_t) in a
+           dielectric sphere over a tessellated floor (volumetric path
+           tracer), 10k-2M triangles,
            log-uniform -- at a square resolution in {128, 256, 512, 1024},
            spp in {4, 16, 64, 256}, max depth uniform in 6..64 (Russian
            roulette from depth 5).  ~0.9e9 camera samples per step, a
