@@ -48,7 +48,7 @@ extern "C" {
 #define LJ_ERR_INVALID_ARG   -1  /* null handle, bad size, bad enum, bad index */
 #define LJ_ERR_CUDA          -2  /* a CUDA runtime call failed                 */
 #define LJ_ERR_OUT_OF_MEMORY -3  /* device allocation or HBM budget exceeded   */
-#define LJ_ERR_UNSUPPORTED   -4  /* feature not available on this build        */
+#define LJ_ERR_UNSUPPORTED   -4  /* feature not available in this library      */
 #define LJ_ERR_DEVICE_LIMIT  -5  /* a bounded device loop hit its limit        */
 #define LJ_ERR_NO_DEVICE     -6  /* no CUDA device / wrong architecture        */
 #define LJ_ERR_QUEUE_FULL    -7  /* server admission queue is full             */
