@@ -371,6 +371,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     g2 = [gpu.GpuScene(ctx, s) for s in pool]
+    torch.cuda.synchronize()
+    upload_s = time.perf_counter() - t0
     sec, _, _ = serve_step(srv_e2e, g2, jobs)
     e2e_s = time.perf_counter() - t0
     srv_e2e.stop()
@@ -433,7 +435,7 @@ def run_ours(args):
         "rel_mse_vs_4096spp": rel_mse,
         "clocks": ck,
         "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h),
+                "d2h_bytes_per_step": int(d2h), "scene_upload_s": round(upload_s, 4),
                 "what": "scene pool uploaded from host (lj_gpu_scene_create, BVH build) + one step served, "
                         "images to host"},
         "gpu_launches": int(launches),

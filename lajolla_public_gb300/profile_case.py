@@ -12,6 +12,9 @@ Cases:
   cbox          seeded Cornell box, 256x256, 64 spp, max depth 6
   terrain       seeded terrain + 16 icospheres + envmap, 1.26M triangles,
                 512x512, 16 spp, max depth 8
+  terrain_full  the full terrain configuration: 2048x1024 grid + 64
+                subdivision-5 icospheres (5.5M triangles), 1024x512 HDR
+                envmap, 1920x1080, 256 spp, max depth 8
   volume        seeded heterogeneous medium (256^3 grid, max density 20) in a
                 dielectric sphere, 512x512, 256 spp, max depth 64 (volpath v6)
   volume_mid    the volume case at 256x256, 16 spp (one wavefront batch)
@@ -41,6 +44,8 @@ def make_case(name):
         return scenes.cornell_box(seed=0, width=256, height=256, spp=64, max_depth=6)
     if name == "cbox_srv":
         return scenes.cornell_box(seed=0, width=256, height=256, spp=64, max_depth=6)
+    if name in ("terrain_full", "terrain_full_srv"):
+        return scenes.terrain_scene(seed=0)
     if name in ("terrain", "terrain_srv"):
         return scenes.resized_terrain_scene(seed=5, n_tris=1261476, width=512, height=512, spp=16, max_depth=8)
     if name in ("volume", "volume_srv"):
