@@ -518,6 +518,67 @@ LJ_HD float bsdf_pdf(const MatParams &m, const BsdfVertex &v, V3 wi, V3 wo) {
     }
     return 0.0f;
 }
+// bsdf_eval and bsdf_pdf of the same directions under one dispatch: each
+// type's two bodies inline side by side, so the terms they share (half
+// vector, microfacet D and G, Fresnel) are computed once.  Same values as
+// the two calls.
+template <uint32_t kMats = kAllMats>
+LJ_HD void bsdf_eval_pdf(const MatParams &m, const BsdfVertex &v, V3 wi, V3 wo, V3 &f, float &pdf) {
+    float ax, ay;
+    switch (m.type) {
+    case 0:
+        if (!has_mat<kMats>(0)) break;
+        f = lambert_eval(m.s[0], v, wi, wo);
+        pdf = lambert_pdf(v, wi, wo);
+        return;
+    case 1:
+        if (!has_mat<kMats>(1)) break;
+        f = plastic_eval(m, v, wi, wo);
+        pdf = plastic_pdf(m, v, wi, wo);
+        return;
+    case 2:
+        if (!has_mat<kMats>(2)) break;
+        f = diel_eval(DielParams{m.s[0], m.s[1], m.eta, true, m.s[2].x, 0, 0}, v, wi, wo, false);
+        pdf = diel_pdf(DielParams{m.s[0], m.s[1], m.eta, true, m.s[2].x, 0, 0}, v, wi, wo);
+        return;
+    case 3:
+        if (!has_mat<kMats>(3)) break;
+        f = ddiffuse_eval(m.s[0], m.s[1].x, m.s[2].x, v, wi, wo);
+        pdf = lambert_pdf(v, wi, wo);
+        return;
+    case 4:
+        if (!has_mat<kMats>(4)) break;
+        disney_alphas(m.s[1].x, m.s[2].x, ax, ay);
+        f = dmetal_eval(m.s[0], ax, ay, v, wi, wo);
+        pdf = dmetal_pdf(ax, ay, v, wi, wo);
+        return;
+    case 5:
+        if (!has_mat<kMats>(5)) break;
+        disney_alphas(m.s[1].x, m.s[2].x, ax, ay);
+        f = diel_eval(DielParams{m.s[0], sqrt3(m.s[0]), m.eta, false, 0, ax, ay}, v, wi, wo, false);
+        pdf = diel_pdf(DielParams{m.s[0], sqrt3(m.s[0]), m.eta, false, 0, ax, ay}, v, wi, wo);
+        return;
+    case 6:
+        if (!has_mat<kMats>(6)) break;
+        ax = dclearcoat_eval(m.s[0].x, v, wi, wo);
+        f = V3{ax, ax, ax};
+        pdf = dclearcoat_pdf(m.s[0].x, v, wi, wo);
+        return;
+    case 7:
+        if (!has_mat<kMats>(7)) break;
+        f = dsheen_eval(m.s[0], m.s[1].x, v, wi, wo);
+        pdf = lambert_pdf(v, wi, wo);
+        return;
+    case 8:
+        if (!has_mat<kMats>(8)) break;
+        f = disney_eval(disney_params(m), v, wi, wo, false);
+        pdf = disney_pdf(disney_params(m), v, wi, wo);
+        return;
+    }
+    f = V3{0, 0, 0};
+    pdf = 0.0f;
+}
+
 template <uint32_t kMats = kAllMats>
 LJ_HD BsdfSample bsdf_sample(const MatParams &m, const BsdfVertex &v, V3 wi, float u0, float u1, float w) {
     float ax, ay;

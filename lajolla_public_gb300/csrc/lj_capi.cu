@@ -143,16 +143,20 @@ void lookup0(const HostImg &im, double u, double v, double out[3]) {
 }
 
 template <typename T>
-int upload(lj_scene *sc, const std::vector<T> &v, const T **dst, std::string *err) {
+int upload(lj_scene *sc, const T *src, size_t n, const T **dst, std::string *err) {
     *dst = nullptr;
-    if (v.empty()) return 0;
+    if (n == 0) return 0;
     void *p = nullptr;
-    LJ_CUDA_TRY(cudaMalloc(&p, sizeof(T) * v.size()));
+    LJ_CUDA_TRY(cudaMalloc(&p, sizeof(T) * n));
     sc->allocs.push_back(p);
-    LJ_CUDA_TRY(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, sc->ctx->stream));
+    LJ_CUDA_TRY(cudaMemcpyAsync(p, src, sizeof(T) * n, cudaMemcpyHostToDevice, sc->ctx->stream));
     *dst = (const T *)p;
-    sc->info.device_bytes += (int64_t)(sizeof(T) * v.size());
+    sc->info.device_bytes += (int64_t)(sizeof(T) * n);
     return 0;
+}
+template <typename T>
+int upload(lj_scene *sc, const std::vector<T> &v, const T **dst, std::string *err) {
+    return upload(sc, v.data(), v.size(), dst, err);
 }
 
 __global__ void k_iota(uint32_t *p, int64_t n) {
@@ -316,6 +320,7 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
     sc->shape_prim_base.assign(d->num_shapes, 0);
     int tri_base = 0, sphere_ord = 0;
     prim_shape.assign((size_t)num_tris + num_spheres, 0);
+    tri_vidx.reserve((size_t)num_tris * 3);
     for (int i = 0; i < d->num_shapes; i++) {
         const lj_shape_desc &s = d->shapes[i];
         ShapeRec &r = shapes[i];
@@ -583,11 +588,10 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
                                     v.channel_scale[2] != 0.0f;
                 float mx[3] = {0, 0, 0};
                 o.channels = v.channels;
-                if (v.channels == 1) {   // one float per voxel
-                    std::vector<float> one(v.data, v.data + n);
-                    for (size_t p = 0; p < n; p++) mx[0] = std::max(mx[0], one[p]);
+                if (v.channels == 1) {   // one float per voxel, uploaded from the caller's array
+                    for (size_t p = 0; p < n; p++) mx[0] = std::max(mx[0], v.data[p]);
                     mx[1] = mx[2] = mx[0];
-                    if (upload(sc, one, &o.data1, &err)) return fail(LJ_ERR_CUDA);
+                    if (upload(sc, v.data, n, &o.data1, &err)) return fail(LJ_ERR_CUDA);
                 } else {
                     std::vector<float4> rgb(n);
                     for (size_t p = 0; p < n; p++) {

@@ -502,8 +502,7 @@ LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const Sha
             V3 f;
             float pdf_dir;
             if constexpr (surface) {
-                f = bsdf_eval<kMats>(mat, bv, wv, dir);
-                pdf_dir = bsdf_pdf<kMats>(mat, bv, wv, dir);
+                bsdf_eval_pdf<kMats>(mat, bv, wv, dir, f, pdf_dir);
             } else {
                 const MediumRec &m = sc.media[medium];
                 float ph = phase_eval(m.phase_kind, m.g, wv, dir);
@@ -548,8 +547,9 @@ LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const Sha
         if (!bs.valid) {
             alive = false;
         } else {
-            V3 f = bsdf_eval<kMats>(mat, bv, wv, bs.dir);
-            float pdf = bsdf_pdf<kMats>(mat, bv, wv, bs.dir);
+            V3 f;
+            float pdf;
+            bsdf_eval_pdf<kMats>(mat, bv, wv, bs.dir, f, pdf);
             if (!(pdf > 0.0f)) {
                 alive = false;
             } else {

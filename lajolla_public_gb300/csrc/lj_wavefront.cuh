@@ -237,9 +237,11 @@ LJ_D void shade_segment(const DevScene &sc, const Paths &paths, int i, const Sha
             }
             if (lid >= 0) p1 = __ldg(sc.light_pmf + lid) * pdf_point_on_light(sc, lid, pl, vx.p);
             if (G > 0.0f && p1 > 0.0f) {
-                V3 f = bsdf_eval<kMats>(mat, bv, wv, dl);
+                V3 f;
+                float pdf_l;
+                bsdf_eval_pdf<kMats>(mat, bv, wv, dl, f, pdf_l);
                 V3 Le = light_emission(sc, lid, -dl, pl);
-                float p2 = bsdf_pdf<kMats>(mat, bv, wv, dl) * G;
+                float p2 = pdf_l * G;
                 float w1 = (p1 * p1) / (p1 * p1 + p2 * p2);
                 V3 c = beta * f * Le * (G * w1 / p1);
                 if (c.x > 0.0f || c.y > 0.0f || c.z > 0.0f)
@@ -250,8 +252,9 @@ LJ_D void shade_segment(const DevScene &sc, const Paths &paths, int i, const Sha
             float bu0 = pcg_uniform(rng), bu1 = pcg_uniform(rng), bwr = pcg_uniform(rng);
             BsdfSample bs = bsdf_sample<kMats>(mat, bv, wv, bu0, bu1, bwr);
             if (bs.valid) {
-                V3 f = bsdf_eval<kMats>(mat, bv, wv, bs.dir);
-                float pdf = bsdf_pdf<kMats>(mat, bv, wv, bs.dir);
+                V3 f;
+                float pdf;
+                bsdf_eval_pdf<kMats>(mat, bv, wv, bs.dir, f, pdf);
                 if (pdf > 0.0f) {
                     if (bs.eta != 0.0f) eta_scale /= (bs.eta * bs.eta);
                     float rr_prob = fminf(max3(beta) / eta_scale, 0.95f);
