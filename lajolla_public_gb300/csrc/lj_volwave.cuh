@@ -1,14 +1,20 @@
-// The shade step of the volumetric path tracer (v6), shared by the
+// The shade steps of the volumetric path tracer (v6), shared by the
 // single-scene renderer (lj_volpath.cu) and the server (lj_server.cu): the
 // GPU form of vol_path_tracing (src/vol_path_tracing.h:59-64, a stub in the
 // reference; the algorithm is the one handouts/homework2.tex:303-816
 // specifies, restated in oracle/lj_oracle.cpp with the same random-number
-// order).  One queue entry: free-flight delta tracking over [0, t_hit) with
-// the chromatic majorant (one channel sampled per segment); then, at a real
-// scattering point or a surface: emission with MIS, NEE with ratio tracking
-// through index-matching surfaces (the shadow traversal runs here), phase /
-// BSDF sampling, Russian roulette, the next ray.  A store decides where the
-// state lives (fixed slots or queue order), as for the path tracer.
+// order).  Per queue entry, after its closest hit:
+//   a  free-flight delta tracking over [0, t_hit) with the chromatic
+//      majorant (one channel sampled per segment), emission with MIS, the
+//      depth limits; index-matching surfaces are passed; at a real
+//      scattering point or a surface with a material, the light sample of
+//      NEE and a request in the NEE queue
+//   b  per request, the shadow ray's walk through index-matching surfaces,
+//      then ratio tracking through media for an unblocked ray
+//   c  per request, the MIS-weighted contribution, phase / BSDF sampling,
+//      Russian roulette, the next ray.
+// A store decides where the state lives (fixed slots or queue order), as
+// for the path tracer.
 #pragma once
 
 #include "../../include/lj_gpu.h"
@@ -113,13 +119,14 @@ LJ_D int update_medium(const Vertex &v, V3 dir, int medium) {
 // A path that reaches a real scattering point or a surface with a material
 // issues one NEE request: vol_segment_a draws the light sample (4 random
 // numbers, as the reference's NEE starts) and appends the request;
-// vol_nee_b runs the shadow loop (closest hits through index-matching
-// surfaces, ratio tracking through media, drawing from the path's stream);
+// vol_nee_b walks the shadow ray through index-matching surfaces and, when
+// no opaque surface or depth limit blocks it, ratio-tracks it through the
+// media, drawing from the path's stream (a blocked ray draws nothing);
 // vol_segment_c turns its transmittance into the MIS-weighted contribution and
 // continues the path with the stream where the shadow loop left it (phase or
 // BSDF sampling, Russian roulette).  The random-number order per path is that
-// of one sequential NEE call; the shadow loop, which does most of the grid
-// lookups, runs in a small kernel of its own.
+// of one sequential NEE call of the oracle; the shadow loop, which does most
+// of the grid lookups, runs in a small kernel of its own.
 // Requests from scattering points fill the queue from its front, requests
 // from surfaces from its back, so that each instance of the c step reads a
 // contiguous range (and the warps of the b step see one kind mostly).
