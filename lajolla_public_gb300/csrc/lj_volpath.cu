@@ -10,8 +10,9 @@
 //               emission with MIS; index-matching surfaces passed; at a
 //               real scattering point or a surface with a material, the
 //               light sample of NEE and a request in the NEE queue
-//   vol_b       per NEE request: the shadow loop (closest hits through
-//               index-matching surfaces, ratio tracking through media)
+//   vol_b       per NEE request: the shadow ray's walk through
+//               index-matching surfaces (closest hits), then ratio
+//               tracking through media unless an opaque surface blocks it
 //   vol_c       per NEE request: the MIS-weighted contribution, phase /
 //               BSDF sampling, Russian roulette, next ray appended to the
 //               other queue.
