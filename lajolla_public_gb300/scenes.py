@@ -269,8 +269,9 @@ class Scene:
                         vd.p_min[c], vd.p_max[c] = v["p_min"][c], v["p_max"][c]
                     vd.data = ptr(data, C.c_float)
                 vd.scale = v.get("scale", 1.0)
+                cs = v.get("channel_scale")
                 for c in range(3):
-                    vd.channel_scale[c] = v.get("channel_scale", (0.0, 0.0, 0.0))[c]
+                    vd.channel_scale[c] = 0.0 if cs is None else cs[c]
         d.num_shapes, d.num_materials = len(self.shapes), len(self.materials)
         d.num_lights, d.num_media, d.num_images = len(self.lights), len(self.media), len(self.images)
         d.envmap_light_id = self.envmap_light_id
@@ -788,6 +789,24 @@ def resized_terrain_scene(seed=0, n_tris=500000, width=256, height=256, spp=64, 
     nz = max(8, int(round(math.sqrt(rest / 4.0))))
     return terrain_scene(seed=seed, width=width, height=height, spp=spp, max_depth=max_depth,
                          grid=(2 * nz, nz), n_spheres=n_spheres, sphere_subdiv=subdiv, env_size=env_size)
+
+
+def with_three_channel_density(sc):
+    """The same scene with every one-channel density grid that carries a
+    channel scale stored as three channels (data * channel scale per voxel,
+    FP32) and no channel scale: the reference's representation of a
+    chromatic grid."""
+    for m in sc.media:
+        d = m.get("density")
+        if d is None or d.get("data") is None or d.get("channel_scale") is None:
+            continue
+        data = np.asarray(d["data"], np.float32)
+        if data.shape[-1] != 1:
+            continue
+        cs = np.asarray(d["channel_scale"], np.float32)
+        d["data"] = (data * cs).astype(np.float32)
+        d["channel_scale"] = None
+    return sc
 
 
 def resized_volume_scene(seed=0, n_tris=10000, width=256, height=256, spp=64, max_depth=64, grid=256):

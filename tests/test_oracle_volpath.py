@@ -64,6 +64,20 @@ def test_shadow_loop_orders_agree(case):
     assert np.all(z < 4.0), (case, m0, m1, z)
 
 
+def test_one_channel_grid_with_channel_scale_equals_three_channel_grid():
+    """A scalar density grid with a chromatic channel scale renders like the
+    same grid stored as three channels (data * scale per voxel): per sample,
+    up to the FP32 rounding of the stored products."""
+    a = scenes.volume_scene(width=16, height=16, spp=4, grid=24, max_depth=16)
+    b = scenes.with_three_channel_density(scenes.volume_scene(width=16, height=16, spp=4, grid=24, max_depth=16))
+    assert a.media[0]["density"]["data"].shape[-1] == 1 and b.media[0]["density"]["data"].shape[-1] == 3
+    px = np.arange(16 * 16, dtype=np.int32)
+    sa = ljo.OracleScene(a).render_samples(px, 4, seed=3).reshape(-1, 3)
+    sb = ljo.OracleScene(b).render_samples(px, 4, seed=3).reshape(-1, 3)
+    err = np.abs(sa - sb) / np.maximum(np.abs(sb), 1e-1)
+    assert (err <= 1e-3).all(axis=1).mean() >= 0.98
+
+
 def test_volpath_without_media_equals_path_tracer():
     sc = scenes.cornell_box(seed=1, width=16, height=16, spp=8, max_depth=6)
     mp, sp = _mean_se(sc, 0, 512, 1)
