@@ -13,9 +13,12 @@
 //      Bittner 2018; below), or -- BvhInput::karras -- the Karras (HPG 2012)
 //      radix tree with bottom-up boxes (atomic arrival counters)
 //   5. level-synchronous collapse into the compressed 8-wide layout of
-//      lj_scene.cuh: greedy largest-area child expansion, octant slot
-//      assignment, 8-bit conservative quantization, leaves of <= 3 primitives
-//      stored contiguously in leaf order.
+//      lj_scene.cuh: the SAH-optimal choice of which binary nodes become wide
+//      nodes, leaves or are opened (Ylitie, Karras and Laine, HPG 2017,
+//      section 3.1: bottom-up cost tables per PLOC round, then top-down
+//      decisions; greedy largest-area child expansion for the Karras tree),
+//      octant slot assignment, 8-bit conservative quantization, leaves of
+//      <= 3 primitives stored contiguously in leaf order.
 #include <cfloat>
 #include <cmath>
 #include <vector>
@@ -452,6 +455,81 @@ __global__ void k_ploc_compact(PlocClusters in, PlocClusters out, const int *nn,
 }
 
 // ---- collapse to the compressed 8-wide layout ----------------------------
+// ---- SAH-optimal collapse: cost tables over the binary tree ---------------
+// C(n, i) = the least SAH cost of the subtree of binary node n as at most i
+// children of a wide node (i = 1..7):
+//   C(n, 1) = min(leaf: A(n) p(n) c_prim if p(n) <= 3 primitives,
+//                 internal: A(n) c_node + D(n, 8))
+//   C(n, i) = min(C(n, i - 1), D(n, i)),
+//   D(n, j) = min over 0 < k < j of C(left, k) + C(right, j - k),
+// A = half the box surface, p = primitives below.  A primitive child is a
+// one-primitive leaf at every i.  dec[8 n + i] records the choice: i = 1:
+// 1 = leaf, 0 = a wide node of its own; i > 1: 0 = as with i - 1 children,
+// else the left child's share k; dec[8 n] = the left child's share of the
+// 8 children when n is a wide node.
+constexpr float kSahNode = 1.0f, kSahPrim = 0.3f;
+
+__device__ __forceinline__ float box_half_area(float4 l, float4 h) {
+    const float dx = h.x - l.x, dy = h.y - l.y, dz = h.z - l.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// The nodes [id_lo, id_hi] of one PLOC round: their children were made in
+// earlier rounds (or are primitives), so their tables are complete.
+__global__ void k_sah_costs(float *cost, uint8_t *dec, const int2 *child, const int2 *range, const float4 *nlo,
+                            const float4 *nhi, const uint32_t *sorted, const float4 *plo, const float4 *phi,
+                            int id_lo, int id_hi) {
+    const int id = id_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (id > id_hi) return;
+    const int2 c = child[id];
+    float cl[8], cr[8];
+    auto load = [&](int enc, float *cc) {
+        if (enc < 0) {
+            const uint32_t g = sorted[~enc];
+            const float a = box_half_area(plo[g], phi[g]) * kSahPrim;
+            for (int i = 1; i < 8; i++) cc[i] = a;
+        } else {
+            for (int i = 1; i < 8; i++) cc[i] = cost[(size_t)enc * 8 + i];
+        }
+    };
+    load(c.x, cl);
+    load(c.y, cr);
+    float D[9];
+    uint8_t K[9];
+    for (int j = 2; j <= 8; j++) {
+        float best = __int_as_float(0x7f800000);
+        int bk = 1;
+        for (int k = 1; k < j; k++) {
+            const float v = cl[k] + cr[j - k];
+            if (v < best) {
+                best = v;
+                bk = k;
+            }
+        }
+        D[j] = best;
+        K[j] = (uint8_t)bk;
+    }
+    const float A = box_half_area(nlo[id], nhi[id]);
+    const int p = range[id].y - range[id].x + 1;
+    const float c_int = A * kSahNode + D[8];
+    const float c_leaf = p <= 3 ? A * (float)p * kSahPrim : __int_as_float(0x7f800000);
+    float C = fminf(c_leaf, c_int);
+    float *co = cost + (size_t)id * 8;
+    uint8_t *de = dec + (size_t)id * 8;
+    co[1] = C;
+    de[1] = c_leaf <= c_int ? 1 : 0;
+    for (int i = 2; i < 8; i++) {
+        if (C <= D[i]) {
+            de[i] = 0;
+        } else {
+            C = D[i];
+            de[i] = K[i];
+        }
+        co[i] = C;
+    }
+    de[0] = K[8];
+}
+
 struct CollapseArgs {
     const int2 *child;      // binary internal nodes
     const int2 *range;
@@ -462,6 +540,7 @@ struct CollapseArgs {
     uint4 *nodes;
     float4 *prims;
     int *node_counter, *prim_counter;
+    const uint8_t *dec;     // SAH decisions (k_sah_costs), or null: greedy expansion
     const int2 *qin;        // (binary node encoded, wide node index)
     const int *qin_count;
     int2 *qout;
@@ -525,32 +604,61 @@ __global__ void k_collapse(CollapseArgs a) {
     if (item >= *a.qin_count) return;
     int2 q = a.qin[item];
     ChildInfo ch[8];
-    int cnt;
+    bool inner[8];   // child k becomes a wide node of its own (else a leaf)
+    int cnt = 0;
     if (q.x < 0) {
         child_info(a, q.x, ch[0]);
         cnt = 1;
+    } else if (a.dec) {
+        // the SAH decisions: 8 children shared between the two subtrees,
+        // each share opened further or taken as fewer children
+        int2 st_enc[16];   // (binary node encoded, children it may fill)
+        int sp = 0;
+        const int2 c = a.child[q.x];
+        const int k8 = a.dec[(size_t)q.x * 8];
+        st_enc[sp++] = make_int2(c.y, 8 - k8);
+        st_enc[sp++] = make_int2(c.x, k8);
+        while (sp > 0 && cnt < 8) {
+            const int2 it = st_enc[--sp];
+            if (it.x < 0 || it.y == 1) {
+                child_info(a, it.x, ch[cnt]);
+                inner[cnt] = it.x >= 0 && a.dec[(size_t)it.x * 8 + 1] == 0;
+                cnt++;
+                continue;
+            }
+            const int d = a.dec[(size_t)it.x * 8 + it.y];
+            if (d == 0) {
+                st_enc[sp++] = make_int2(it.x, it.y - 1);
+            } else {
+                const int2 cc = a.child[it.x];
+                st_enc[sp++] = make_int2(cc.y, it.y - d);
+                st_enc[sp++] = make_int2(cc.x, d);
+            }
+        }
     } else {
         int2 c = a.child[q.x];
         child_info(a, c.x, ch[0]);
         child_info(a, c.y, ch[1]);
         cnt = 2;
-    }
-    // greedy expansion of the largest child that must stay internal
-    while (cnt < 8) {
-        int best = -1;
-        float best_area = -1.0f;
-        for (int k = 0; k < cnt; k++) {
-            if (ch[k].enc >= 0 && ch[k].count > 3) {
-                float ar = half_area(ch[k]);
-                if (ar > best_area) { best_area = ar; best = k; }
+        // greedy expansion of the largest child that must stay internal
+        while (cnt < 8) {
+            int best = -1;
+            float best_area = -1.0f;
+            for (int k = 0; k < cnt; k++) {
+                if (ch[k].enc >= 0 && ch[k].count > 3) {
+                    float ar = half_area(ch[k]);
+                    if (ar > best_area) { best_area = ar; best = k; }
+                }
             }
+            if (best < 0) break;
+            int2 c2 = a.child[ch[best].enc];
+            child_info(a, c2.y, ch[cnt]);
+            child_info(a, c2.x, ch[best]);
+            cnt++;
         }
-        if (best < 0) break;
-        int2 c = a.child[ch[best].enc];
-        child_info(a, c.y, ch[cnt]);
-        child_info(a, c.x, ch[best]);
-        cnt++;
     }
+    if (!a.dec || q.x < 0)
+        for (int k = 0; k < cnt; k++) inner[k] = ch[k].count > 3;
     // node box
     float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (int k = 0; k < cnt; k++)
@@ -582,7 +690,7 @@ __global__ void k_collapse(CollapseArgs a) {
     }
     int n_int = 0, n_prims = 0;
     for (int k = 0; k < cnt; k++) {
-        if (ch[k].count > 3) n_int++;
+        if (inner[k]) n_int++;
         else n_prims += ch[k].count;
     }
     int child_base = n_int ? atomicAdd(a.node_counter, n_int) : 0;
@@ -620,7 +728,7 @@ __global__ void k_collapse(CollapseArgs a) {
             qlo[ax][s] = (uint32_t)ql;
             qhi[ax][s] = (uint32_t)qh;
         }
-        if (c.count > 3) {
+        if (inner[k]) {
             meta[s] = (1u << 5) | (24u + (uint32_t)s);
             imask |= 1u << s;
             int2 e = make_int2(c.enc, child_base + int_rank);
@@ -808,6 +916,9 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
     LJ_CUDA_TRY(cudaMalloc(&out->nodes, sizeof(uint4) * kWideNodeU4 * (size_t)ni));
     LJ_CUDA_TRY(cudaMalloc(&out->prims, sizeof(float4) * kPrimF4 * (size_t)n));
 
+    float *sah_cost = nullptr;
+    uint8_t *sah_dec = nullptr;
+    std::vector<int2> rounds;   // PLOC: the node ids each round made
     k_init_bounds<<<1, 32, 0, s>>>(bounds, 12);
     k_prim_bounds<<<grid_for(n, 256), 256, 0, s>>>(in, plo, phi, cent, bounds);
     k_morton<<<grid_for(n, 256), 256, 0, s>>>(cent, n, bounds, codes, idx);
@@ -849,6 +960,7 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
                 if (err) *err = "BVH build: a clustering round merged nothing";
                 return -5;
             }
+            rounds.push_back(make_int2(n - 2 - merged - tot.y + 1, n - 2 - merged));
             merged += tot.y;
             count = tot.x;
             c ^= 1;
@@ -862,6 +974,13 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
             if (err) *err = "BVH build: clustering left " + std::to_string(n - merged) + " roots";
             return -5;
         }
+        // SAH cost tables, round by round (children before parents)
+        LJ_CUDA_TRY(cudaMallocAsync(&sah_cost, sizeof(float) * 8 * (size_t)ni, s));
+        LJ_CUDA_TRY(cudaMallocAsync(&sah_dec, sizeof(uint8_t) * 8 * (size_t)ni, s));
+        for (const int2 &r : rounds)
+            k_sah_costs<<<grid_for(r.y - r.x + 1, 256), 256, 0, s>>>(sah_cost, sah_dec, child, range, nlo, nhi, idx,
+                                                                       plo, phi, r.x, r.y);
+        LJ_CUDA_TRY(cudaGetLastError());
     } else if (n > 1) {
         k_karras<<<grid_for(n - 1, 256), 256, 0, s>>>(codes, n, child, range, parent_int, parent_leaf);
         k_bottom_up<<<grid_for(n, 256), 256, 0, s>>>(n, child, parent_int, parent_leaf, idx, plo, phi,
@@ -876,6 +995,7 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
     a.child = child; a.range = range; a.nlo = nlo; a.nhi = nhi; a.sorted = idx;
     a.plo = plo; a.phi = phi; a.in = in; a.nodes = out->nodes; a.prims = out->prims;
     a.node_counter = counters; a.prim_counter = counters + 1;
+    a.dec = sah_dec;
     int qcount = 1;
     int2 *qin = q0, *qout = q1;
     int *cin = counters + 2, *cout = counters + 3;
@@ -909,6 +1029,8 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
     cudaFreeAsync(hist, s); cudaFreeAsync(flags, s); cudaFreeAsync(child, s);
     cudaFreeAsync(range, s); cudaFreeAsync(q0, s); cudaFreeAsync(q1, s);
     cudaFreeAsync(parent_int, s); cudaFreeAsync(parent_leaf, s); cudaFreeAsync(counters, s);
+    if (sah_cost) cudaFreeAsync(sah_cost, s);
+    if (sah_dec) cudaFreeAsync(sah_dec, s);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (h_final[1] != n) {
