@@ -320,7 +320,11 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
     sc->shape_prim_base.assign(d->num_shapes, 0);
     int tri_base = 0, sphere_ord = 0;
     prim_shape.assign((size_t)num_tris + num_spheres, 0);
-    tri_vidx.reserve((size_t)num_tris * 3);
+    tri_vidx.resize((size_t)num_tris * 3);
+    // shapes an area light emits from: they need their triangle areas
+    std::vector<char> emits(d->num_shapes, 0);
+    for (int l = 0; l < d->num_lights; l++)
+        if (d->lights[l].kind == LJ_LIGHT_AREA) emits[d->lights[l].shape_id] = 1;
     for (int i = 0; i < d->num_shapes; i++) {
         const lj_shape_desc &s = d->shapes[i];
         ShapeRec &r = shapes[i];
@@ -341,14 +345,15 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
             r.has_uvs = s.uvs != nullptr;
             r.tri_begin = tri_base;
             r.num_tris = s.num_triangles;
-            std::vector<double> areas(s.num_triangles);
+            int *tv = tri_vidx.data() + (size_t)tri_base * 3;
+            for (int t = 0; t < 3 * s.num_triangles; t++) tv[t] = vbase + s.indices[t];
+            std::fill(prim_shape.begin() + tri_base, prim_shape.begin() + tri_base + s.num_triangles, i);
+            // triangle areas: only an emissive mesh samples by area and needs
+            // its total (its light pdf)
+            std::vector<double> areas(s.area_light_id >= 0 || emits[i] ? s.num_triangles : 0);
             double total = 0;
-            for (int t = 0; t < s.num_triangles; t++) {
+            for (int t = 0; t < (int)areas.size(); t++) {
                 int a = s.indices[t * 3], b = s.indices[t * 3 + 1], c = s.indices[t * 3 + 2];
-                tri_vidx.push_back(vbase + a);
-                tri_vidx.push_back(vbase + b);
-                tri_vidx.push_back(vbase + c);
-                prim_shape[tri_base + t] = i;
                 const float *p0 = s.positions + a * 3, *p1 = s.positions + b * 3, *p2 = s.positions + c * 3;
                 double e1[3] = {(double)p1[0] - p0[0], (double)p1[1] - p0[1], (double)p1[2] - p0[2]};
                 double e2[3] = {(double)p2[0] - p0[0], (double)p2[1] - p0[1], (double)p2[2] - p0[2]};
