@@ -14,8 +14,10 @@
 // The order of random numbers per path is the reference's: 2 for the screen
 // position (x then y), then per bounce 4 for light sampling (uv, light, shape),
 // 3 for BSDF sampling (uv, w), 1 for Russian roulette when applicable.
-// A sample's radiance is accumulated in its own slot and reduced per pixel in
-// sample order, so the image is deterministic.
+// Path state travels with its queue entry (every kernel reads its queue
+// contiguously); an ended path leaves its radiance in its sample slot, and
+// the slots are reduced per pixel in sample order, so the image is
+// deterministic.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -28,10 +30,10 @@ namespace lj {
 
 namespace {
 
-__global__ void k_camera(DevScene sc, PathSoA ps, Queues q, int P, int num_pixels, int sample_base,
-                         uint64_t seed) {
+__global__ void k_camera(DevScene sc, Queues q, int P, int num_pixels, int sample_base, uint64_t seed) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
+    const PathSoA &ps = q.st[0];
     int pixel = p % num_pixels;
     int sample = sample_base + p / num_pixels;
     Pcg rng = pcg_keyed(seed, (uint64_t)pixel, (uint64_t)sample);
@@ -41,7 +43,7 @@ __global__ void k_camera(DevScene sc, PathSoA ps, Queues q, int P, int num_pixel
     camera_ray(sc.cam, (x + r1) / sc.cam.w, (y + r2) / sc.cam.h, o, d);
     q.ray[0][2 * p] = make_float4(o.x, o.y, o.z, 0.0f);
     q.ray[0][2 * p + 1] = make_float4(d.x, d.y, d.z, __int_as_float(0x7f800000));
-    q.path[0][p] = p;
+    ps.slot[p] = p;
     ps.pixel[p] = pixel;
     ps.rng[p] = rng.state;
     ps.beta[p] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
@@ -61,12 +63,14 @@ __global__ void __launch_bounds__(128, 8) k_trace_queue(DevBvh bvh, const float4
     trace_queue<false, 128>(io, n, fetch, status);
 }
 
-__global__ void __launch_bounds__(128, 8) k_trace_shadow(DevBvh bvh, const float4 *rays, const int *paths,
+// Lnext: the radiance of the next queue's entries (the paths that go on)
+__global__ void __launch_bounds__(128, 8) k_trace_shadow(DevBvh bvh, const float4 *rays, const int *targets,
                                                       const float4 *contrib, const int *count, int *fetch,
-                                                      float4 *L, unsigned long long *stat, int *status) {
+                                                      float4 *Lnext, float4 *Lres, unsigned long long *stat,
+                                                      int *status) {
     const int n = *count;
     if (blockIdx.x == 0 && threadIdx.x == 0 && stat) atomicAdd(stat, (unsigned long long)n);
-    ShadowQueueIO io{bvh, rays, paths, contrib, L};
+    ShadowQueueIO io{bvh, rays, targets, contrib, Lnext, Lres};
     trace_queue<true, 128>(io, n, fetch, status);
 }
 
@@ -75,16 +79,23 @@ __global__ void __launch_bounds__(128, 8) k_trace_shadow(DevBvh bvh, const float
 template <uint32_t kMats>
 // (the instance for every material type needs more registers: 4 blocks per SM
 // without spills, the others 5)
-__global__ void __launch_bounds__(128, kMats == kAllMats ? 4 : 5) k_shade(DevScene sc, PathSoA ps, Queues q, int cur, float spread0,
-                                                  int *status) {
+__global__ void __launch_bounds__(128, kMats == kAllMats ? 4 : 5) k_shade(DevScene sc, Queues q, int cur, float spread0,
+                                                                         int *status) {
     const int n = q.counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(q.stats + 2, (unsigned long long)n);
     const ShadeCfg cfg{sc.max_depth, sc.rr_depth, spread0};
-    const SlotPaths paths{ps, q, cur};
+    const OrderedPaths paths{q, cur};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         shade_segment<kMats>(sc, paths, i, cfg, status);
 }
-using ShadeKernel = void (*)(DevScene, PathSoA, Queues, int, float, int *);
+using ShadeKernel = void (*)(DevScene, Queues, int, float, int *);
+
+// Paths still in queue cur when the passes end: their radiance to their slots.
+__global__ void k_flush(Queues q, int cur) {
+    const int n = q.counts[cur];
+    const PathSoA &s = q.state(cur);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) q.Lres[s.slot[i]] = s.L[i];
+}
 // the smallest instance whose material set covers the scene's
 ShadeKernel shade_kernel_for(uint32_t mat_mask) {
     if ((mat_mask & ~kLambertMats) == 0) return k_shade<kLambertMats>;
@@ -139,9 +150,12 @@ T *carve(char *&p, size_t n) {
 size_t path_bytes(size_t P) {
     size_t per = 0;
     auto add = [&](size_t b) { per += ((b + 255) / 256) * 256; };
-    add(P * sizeof(int)); add(P * 8); add(P * 16); add(P * 16); add(P * 16); add(P * sizeof(int));
-    add(P * 32); add(P * 32); add(P * 4); add(P * 4); add(P * 16);
-    add(P * 32); add(P * 4); add(P * 16);
+    for (int k = 0; k < 2; k++) {   // state of queue k: slot, pixel, rng, beta, L, prev, nv
+        add(P * 4); add(P * 4); add(P * 8); add(P * 16); add(P * 16); add(P * 16); add(P * 4);
+    }
+    add(P * 32); add(P * 32); add(P * 16);   // rays of both queues, hits
+    add(P * 32); add(P * 4); add(P * 16);    // shadow rays, targets, contributions
+    add(P * 16);                             // radiance per sample slot
     add(64); add(64);
     return per;
 }
@@ -192,22 +206,24 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
         scene->path.bytes = need;
     }
     char *cur = (char *)scene->path.block;
-    PathSoA ps;
-    ps.pixel = carve<int>(cur, P);
-    ps.rng = carve<uint64_t>(cur, P);
-    ps.beta = carve<float4>(cur, P);
-    ps.L = carve<float4>(cur, P);
-    ps.prev = carve<float4>(cur, P);
-    ps.nv = carve<int>(cur, P);
     Queues q;
+    for (int k = 0; k < 2; k++) {
+        PathSoA &ps = q.st[k];
+        ps.slot = carve<int>(cur, P);
+        ps.pixel = carve<int>(cur, P);
+        ps.rng = carve<uint64_t>(cur, P);
+        ps.beta = carve<float4>(cur, P);
+        ps.L = carve<float4>(cur, P);
+        ps.prev = carve<float4>(cur, P);
+        ps.nv = carve<int>(cur, P);
+    }
     q.ray[0] = carve<float4>(cur, 2 * P);
     q.ray[1] = carve<float4>(cur, 2 * P);
-    q.path[0] = carve<int>(cur, P);
-    q.path[1] = carve<int>(cur, P);
     q.hit = carve<float4>(cur, P);
     q.sray = carve<float4>(cur, 2 * P);
-    q.spath = carve<int>(cur, P);
+    q.starget = carve<int>(cur, P);
     q.scontrib = carve<float4>(cur, P);
+    q.Lres = carve<float4>(cur, P);
     q.counts = carve<int>(cur, 16);
     q.stats = carve<unsigned long long>(cur, 8);
 
@@ -247,7 +263,7 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
         int Pb = num_pixels * ns;
         k_set_counts<<<1, 1, 0, s>>>(q.counts, Pb);
         mark_begin(LJ_KERNEL_CAMERA);
-        k_camera<<<(Pb + 255) / 256, 256, 0, s>>>(sc, ps, q, Pb, num_pixels, params->sample_offset + sb,
+        k_camera<<<(Pb + 255) / 256, 256, 0, s>>>(sc, q, Pb, num_pixels, params->sample_offset + sb,
                                                   params->seed);
         mark_end();
         launches += 2;
@@ -261,11 +277,12 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
                                                   q.stats + 0, ctx->d_status);
             mark_end();
             mark_begin(LJ_KERNEL_SHADE);
-            shade<<<g_shade, 128, 0, s>>>(sc, ps, q, curq, spread0, ctx->d_status);
+            shade<<<g_shade, 128, 0, s>>>(sc, q, curq, spread0, ctx->d_status);
             mark_end();
             mark_begin(LJ_KERNEL_SHADOW);
-            k_trace_shadow<<<g_shadow, 128, 0, s>>>(sc.bvh, q.sray, q.spath, q.scontrib, q.counts + 2,
-                                                    q.counts + 9, ps.L, q.stats + 1, ctx->d_status);
+            k_trace_shadow<<<g_shadow, 128, 0, s>>>(sc.bvh, q.sray, q.starget, q.scontrib, q.counts + 2,
+                                                    q.counts + 9, q.st[curq ^ 1].L, q.Lres, q.stats + 1,
+                                                    ctx->d_status);
             mark_end();
             launches += 4;
             class_launches[LJ_KERNEL_OTHER]++;
@@ -282,9 +299,11 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
                 if (c == 0) break;
             }
         }
-        k_resolve<<<(num_pixels + 255) / 256, 256, 0, s>>>(ps.L, num_pixels, ns, d_out);
-        launches++;
-        class_launches[LJ_KERNEL_OTHER]++;
+        // paths the pass limit stopped: their radiance to their slots
+        k_flush<<<g_shade, 128, 0, s>>>(q, curq);
+        k_resolve<<<(num_pixels + 255) / 256, 256, 0, s>>>(q.Lres, num_pixels, ns, d_out);
+        launches += 2;
+        class_launches[LJ_KERNEL_OTHER] += 2;
     }
     int64_t nfl = 3 * (int64_t)num_pixels;
     k_scale<<<(int)((nfl + 255) / 256), 256, 0, s>>>(d_out, nfl, 1.0f / spp);

@@ -242,21 +242,24 @@ struct ClosestQueueIO {
 };
 
 // One scene: shadow rays; an unoccluded ray adds its NEE contribution to its
-// path's radiance (one shadow ray per path per pass, so no two lanes write
-// the same path).
+// path's radiance -- at the path's entry of the next queue (target >= 0) or
+// in the sample slot of a path that ended (~target).  One shadow ray per
+// path per pass, so no two lanes write the same path.
 struct ShadowQueueIO {
     DevBvh b;
     const float4 *rays;
-    const int *paths;
+    const int *targets;
     const float4 *contrib;
-    float4 *L;
+    float4 *Lnext;
+    float4 *Lres;
     LJ_D const DevBvh &bvh(int) const { return b; }
     LJ_D void load(int r, V3 &o, V3 &d, float &tn, float &tf) const { load_ray(rays, r, o, d, tn, tf); }
     LJ_D void store(int r, const Trav &s) const {
         if (s.found) return;
-        const int p = paths[r];
-        const float4 c = contrib[r], l = L[p];
-        L[p] = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
+        const int t = targets[r];
+        float4 *L = t >= 0 ? Lnext + t : Lres + ~t;
+        const float4 c = contrib[r], l = *L;
+        *L = make_float4(l.x + c.x, l.y + c.y, l.z + c.z, l.w);
     }
 };
 

@@ -5,9 +5,11 @@
 // The shade step reads one path's state and hit, and hands the outcome (the
 // next ray, if any, and the NEE shadow ray with its contribution) to a path
 // store, which decides where state lives:
-//   SlotPaths   (single-scene renderer) state in fixed slots, queues carry
-//               slot ids; a finished path's radiance stays in its slot.
-//   the server's store keeps state in queue order instead (lj_server.cu).
+//   OrderedPaths (single-scene renderer) state in queue order: an entry of
+//                the next queue is written with the path's whole state, so
+//                every kernel reads its queue contiguously; a finished
+//                path's radiance goes to its sample slot.
+//   the server's store does the same across jobs (lj_server.cu).
 // The random-number order per path is the reference's: 2 for the screen
 // position, then per bounce 4 for light sampling (uv, light, shape), 3 for
 // BSDF sampling (uv, w), 1 for Russian roulette when applicable.
@@ -21,7 +23,7 @@ namespace lj {
 
 // State of one path between two bounces.
 struct PathState {
-    int slot;        // SlotPaths: the path's slot
+    int slot;        // OrderedPaths: the path's sample slot (pixel + sample * pixels)
     int job;         // server: job table slot
     int pixel;
     uint64_t rng;
@@ -38,7 +40,9 @@ struct ShadeOut {
     int shadow;              // the store's handle of this step's shadow ray, -1 if none
 };
 
+// Path state of the entries of one queue (queue order, SoA).
 struct PathSoA {
+    int *slot;       // sample slot: pixel + sample * pixels
     int *pixel;
     uint64_t *rng;
     float4 *beta;
@@ -48,18 +52,19 @@ struct PathSoA {
 };
 
 struct Queues {
+    PathSoA st[2];                // state of the entries of ray queue 0 / 1
     float4 *ray[2];
-    int *path[2];
     float4 *hit;
     float4 *sray;
-    int *spath;
+    int *starget;                 // the path's entry of the next queue, or ~slot when it ended
     float4 *scontrib;
+    float4 *Lres;                 // radiance per sample slot of the ended paths
     int *counts;                  // [0], [1]: ray queues, [2]: shadow queue
     unsigned long long *stats;    // [0] closest rays, [1] shadow rays, [2] shade segments
     // select with a branch, not an index: indexing a kernel parameter's
     // array with a run-time value would copy the whole struct to local memory
     LJ_HD float4 *rays(int k) const { return k ? ray[1] : ray[0]; }
-    LJ_HD int *paths(int k) const { return k ? path[1] : path[0]; }
+    LJ_HD const PathSoA &state(int k) const { return k ? st[1] : st[0]; }
 };
 
 // Per-job path options: max_depth / rr_depth as in RenderOptions
@@ -90,50 +95,56 @@ LJ_D void counter_add(unsigned long long *counter, unsigned v) {
     if ((int)lane_id() == __ffs(active) - 1 && sum) atomicAdd(counter, (unsigned long long)sum);
 }
 
-// The single-scene renderer's store: queue cur holds (ray, slot) pairs.
-struct SlotPaths {
-    PathSoA ps;
+// The single-scene renderer's store: queue cur holds (ray, state) entries.
+struct OrderedPaths {
     Queues q;
     int cur;
     LJ_D void load(int i, PathState &st, float4 &r0, float4 &r1, float4 &hit) const {
-        const int p = q.paths(cur)[i];
-        st.slot = p;
+        const PathSoA &s = q.state(cur);
+        st.slot = s.slot[i];
         st.job = 0;
-        st.pixel = ps.pixel[p];
-        st.rng = ps.rng[p];
-        st.beta = ps.beta[p];
-        st.L = ps.L[p];
-        st.prev = ps.prev[p];
-        st.nv = ps.nv[p];
+        st.pixel = s.pixel[i];
+        st.rng = s.rng[i];
+        st.beta = s.beta[i];
+        st.L = s.L[i];
+        st.prev = s.prev[i];
+        st.nv = s.nv[i];
         const float4 *rays = q.rays(cur);
         r0 = rays[2 * i];
         r1 = rays[2 * i + 1];
         hit = q.hit[i];
     }
-    // NEE shadow ray: an unoccluded one adds contrib to the path's radiance
-    LJ_D int shadow(const PathState &st, float4 r0, float4 r1, float4 contrib) const {
+    // NEE shadow ray: an unoccluded one adds contrib to the path's radiance,
+    // wherever emit puts the path (the returned handle)
+    LJ_D int shadow(const PathState &, float4 r0, float4 r1, float4 contrib) const {
         const int s = queue_slot(q.counts + 2);
         q.sray[2 * s] = r0;
         q.sray[2 * s + 1] = r1;
-        q.spath[s] = st.slot;
         q.scontrib[s] = contrib;
-        return -1;
+        return s;
     }
     LJ_D void emit(const PathState &st, const ShadeOut &o) const {
-        const int p = st.slot;
-        ps.L[p] = st.L;
-        ps.rng[p] = st.rng;
+        int target;
         if (o.cont) {
-            ps.beta[p] = st.beta;
-            ps.prev[p] = st.prev;
-            ps.nv[p] = st.nv;
             const int nxt = cur ^ 1;
-            const int s = queue_slot(q.counts + nxt);
+            const int e = queue_slot(q.counts + nxt);
+            const PathSoA &s = q.state(nxt);
+            s.slot[e] = st.slot;
+            s.pixel[e] = st.pixel;
+            s.rng[e] = st.rng;
+            s.beta[e] = st.beta;
+            s.L[e] = st.L;
+            s.prev[e] = st.prev;
+            s.nv[e] = st.nv;
             float4 *rays = q.rays(nxt);
-            rays[2 * s] = o.ray0;
-            rays[2 * s + 1] = o.ray1;
-            q.paths(nxt)[s] = p;
+            rays[2 * e] = o.ray0;
+            rays[2 * e + 1] = o.ray1;
+            target = e;
+        } else {
+            q.Lres[st.slot] = st.L;
+            target = ~st.slot;
         }
+        if (o.shadow >= 0) q.starget[o.shadow] = target;
     }
 };
 
