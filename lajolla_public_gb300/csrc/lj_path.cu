@@ -77,9 +77,10 @@ __global__ void __launch_bounds__(128, 8) k_trace_shadow(DevBvh bvh, const float
 // One instance per material set (kMats): a scene of Lambertian surfaces only
 // runs a much smaller kernel than one that may meet every Disney lobe.
 template <uint32_t kMats>
-// (the instance for every material type needs more registers: 4 blocks per SM
-// without spills, the others 5)
-__global__ void __launch_bounds__(128, kMats == kAllMats ? 4 : 5) k_shade(DevScene sc, Queues q, int cur, float spread0,
+// (5 blocks per SM for the instance for every material type, 6 for the others:
+// a few spilled registers cost less than the warps fewer blocks would lose --
+// the shade step waits on memory, -6 to -11 % against 4 and 5 blocks)
+__global__ void __launch_bounds__(128, kMats == kAllMats ? 5 : 6) k_shade(DevScene sc, Queues q, int cur, float spread0,
                                                                          int *status) {
     const int n = q.counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(q.stats + 2, (unsigned long long)n);
