@@ -41,7 +41,10 @@
 extern "C" {
 #endif
 
-#define LJ_GPU_ABI_VERSION 1
+/* 2: lj_volume_desc.channel_scale, the volumetric kernel classes
+ * (LJ_KERNEL_MEDIUM, LJ_KERNEL_NEE) and the volumetric counters of
+ * lj_server_stats */
+#define LJ_GPU_ABI_VERSION 2
 
 /* ---- error codes -------------------------------------------------------- */
 #define LJ_OK                 0

@@ -46,6 +46,9 @@ def lib():
         L.lj_gpu_last_error.argtypes = [vp]
         L.lj_gpu_last_error.restype = C.c_char_p
         L.lj_gpu_abi_version.restype = C.c_int
+        if L.lj_gpu_abi_version() != abi.LJ_GPU_ABI_VERSION:
+            raise LjError(abi.LJ_ERR_UNSUPPORTED, "liblj_gpu.so has ABI version %d, the bindings expect %d"
+                          % (L.lj_gpu_abi_version(), abi.LJ_GPU_ABI_VERSION))
         L.lj_gpu_scene_create.argtypes = [vp, C.POINTER(abi.lj_scene_desc), C.POINTER(vp)]
         L.lj_gpu_scene_destroy.argtypes = [vp]
         L.lj_gpu_scene_info.argtypes = [vp, C.POINTER(abi.lj_scene_info)]
