@@ -1,8 +1,11 @@
-// Render server: continuous batching of path-tracing jobs over one pool of
+// Render server: continuous batching of render jobs over one pool of
 // wavefront queues.  No counterpart in the reference (main.cpp renders one
 // scene per process); the per-path work is path_tracing
-// (src/path_tracing.h:7-325) through shade_segment, exactly as in the
-// single-scene renderer.
+// (src/path_tracing.h:7-325) through shade_segment, or the volumetric path
+// tracer's a / b / c steps (lj_volwave.cuh), exactly as in the single-scene
+// renderers.  Three path classes share the pool: path jobs whose materials
+// are all classic (front of a queue), other path jobs (back of the queue),
+// volumetric path jobs (queues of their own).
 //
 // Device side, one wave (all kernels read their sizes from device memory,
 // so a fixed launch sequence can be captured once and replayed):
@@ -10,13 +13,18 @@
 //            have samples to issue, in the host's scheduling order
 //            (prefix sums over remaining samples), and advance their
 //            issued-sample counters
-//   regen    free slot <- (job, pixel, sample): keyed PCG stream, camera
-//            ray appended to the current ray queue
-//   trace    closest hit; each ray uses the BVH of its job's scene
-//   shade    shade_segment with the job's scene and depth options
-//   shadow   any-hit for the queued NEE rays
+//   regen    new paths in sample order after the ones that go on: keyed
+//            PCG stream, camera ray, state in the current queue of the
+//            job's class
+//   trace    closest hit of every class's rays; each ray uses the BVH of
+//            its job's scene
+//   shade    shade_segment with the job's scene and depth options, one
+//            instance per path class
+//   vol a/b/c  the volumetric steps (one c instance per request kind and
+//            material class)
+//   shadow   any-hit for the queued NEE rays of the path classes
 //   retire   finished paths: 64-bit fixed-point sums into the job's
-//            accumulator, done counter, slot back on the free stack
+//            accumulator, done counter
 // Two waves (ray queues 0 -> 1 -> 0) form one CUDA graph.
 //
 // Host side, a worker thread admits jobs under the HBM budget, keeps the
