@@ -576,36 +576,59 @@ def load_traffic(kernel_name, units_per_launch):
 
 
 # ------------------------------------------------------------ CPU side
-def cpu_sample(pool, target_s):
+class CpuSampler:
     """The oracle restatement on all host cores over random pixels of every
-    scene of the pool (1 spp each, the scenes' own resolution and depth),
-    sized to about target_s seconds.  Returns (Msamples/s, cores, text)."""
-    from oracle import ljo
-    ljo.build()
-    cores = os.cpu_count() or 1
-    rng = np.random.default_rng(7)
-    oss = [ljo.OracleScene(s) for s in pool]
+    scene of the pool (1 spp each, the scenes' own resolution and depth).
+    calibrate() grows the pixel count until one run takes at least 60 % of
+    target_s (at most 4 Mi pixels per scene); run() renders that many."""
 
-    def run(n_px, seed):
+    CAP = 1 << 22
+
+    def __init__(self, pool):
+        from oracle import ljo
+        ljo.build()
+        self.pool = pool
+        self.cores = os.cpu_count() or 1
+        self.rng = np.random.default_rng(7)
+        self.oss = [ljo.OracleScene(s) for s in pool]   # BVH builds on the CPU, once
+        self.n_px = 256
+        self.seed = 0
+
+    def run(self, n_px=None):
+        n_px = self.n_px if n_px is None else n_px
+        self.seed += 1
         t0 = time.perf_counter()
-        for s, o in zip(pool, oss):
-            px = rng.integers(0, s.width * s.height, n_px).astype(np.int32)
-            o.render_samples(px, 1, seed=seed, nthreads=cores)
+        for s, o in zip(self.pool, self.oss):
+            px = self.rng.integers(0, s.width * s.height, n_px).astype(np.int32)
+            o.render_samples(px, 1, seed=self.seed, nthreads=self.cores)
         return time.perf_counter() - t0
 
-    t1 = run(256, 1)
-    n_px = int(max(256, min(1 << 20, 256 * target_s / max(t1, 1e-3))))
-    dt = run(n_px, 2)
-    n = n_px * len(pool)
-    text = ("%d random pixels x 1 spp of each of the %d serving scenes (%d samples, %.1f s); C++ restatement "
-            "of src/path_tracing.h pinned to the reference's renders (and of the volpath v6 handout "
-            "algorithm for the volume scenes), %d threads" % (n_px, len(pool), n, dt, cores))
-    return n / dt / 1e6, cores, text
+    def calibrate(self, target_s):
+        n_px = 256
+        dt = self.run(n_px)
+        while dt < 0.6 * target_s and n_px < self.CAP:
+            n_px = int(min(self.CAP, max(2 * n_px, n_px * 0.8 * target_s / max(dt, 1e-3))))
+            dt = self.run(n_px)
+        self.n_px = n_px
+        return dt
+
+    def describe(self, dt):
+        n = self.n_px * len(self.pool)
+        return ("%d random pixels x 1 spp of each of the %d serving scenes (%d samples, %.1f s); C++ "
+                "restatement of src/path_tracing.h pinned to the reference's renders (and of the volpath v6 "
+                "handout algorithm for the volume scenes), %d threads"
+                % (self.n_px, len(self.pool), n, dt, self.cores))
+
+    def rate(self, dt):
+        return self.n_px * len(self.pool) / dt / 1e6
 
 
 def cpu_baseline(pool, target_s=10.0):
-    v, cores, text = cpu_sample(pool, target_s)
-    return {"value": round(v, 4), "unit": "Msamples/s", "cores": cores, "kind": "port", "sample": text}
+    cs = CpuSampler(pool)
+    cs.calibrate(target_s)
+    dt = cs.run()
+    return {"value": round(cs.rate(dt), 4), "unit": "Msamples/s", "cores": cs.cores, "kind": "port",
+            "sample": cs.describe(dt)}
 
 
 def run_reference(args):
@@ -613,16 +636,18 @@ def run_reference(args):
     if rank != 0:
         return
     pool = make_scenes()
+    cs = CpuSampler(pool)
+    cs.calibrate(args.cpu_seconds / 2)   # each step a bounded sample of about half --cpu-seconds
     for i in range(args.warmup):
-        cpu_sample(pool, 0.5)
+        cs.run(max(256, cs.n_px // 16))
     vals, texts, secs = [], [], []
     for i in range(args.steps):
-        t0 = time.perf_counter()
-        v, cores, text = cpu_sample(pool, 6.0)
-        secs.append(time.perf_counter() - t0)
-        vals.append(v)
-        texts.append(text)
+        dt = cs.run()
+        secs.append(dt)
+        vals.append(cs.rate(dt))
+        texts.append(cs.describe(dt))
     value = statistics.mean(vals)
+    cores = cs.cores
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Msamples/s",
             "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * sum(secs) / args.steps, 3), "higher_is_better": True,
