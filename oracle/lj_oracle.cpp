@@ -1,6 +1,7 @@
 // ORACLE / TEST INFRASTRUCTURE -- not part of the product.  Only tests/,
 // __graft_entry__.smoke() and bench.py's CPU-baseline leg may load this
-// library, and only as the checker / the timed CPU baseline.
+// library, and only as the reference answer in parity checks or as the timed
+// CPU baseline.
 //
 // A double-precision C++ restatement of lajolla's rendering hot path, driven
 // by the same flat lj_scene_desc the GPU library takes.  Each function cites
