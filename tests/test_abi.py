@@ -59,6 +59,29 @@ def test_struct_sizes_match_c():
         assert sizes[n] == abi.STRUCT_SIZES[n], (n, sizes[n], abi.STRUCT_SIZES[n])
 
 
+def test_struct_field_offsets_match_c():
+    """Every field of every ctypes mirror sits at the C compiler's offset (a
+    size match alone would miss two swapped fields of one size)."""
+    fields = []
+    for n in sorted(abi.STRUCT_SIZES):
+        cls = getattr(abi, n)
+        for f in cls._fields_:
+            fields.append((n, f[0], getattr(cls, f[0]).offset))
+    src = "#include <stdio.h>\n#include <stddef.h>\n#include \"lj_gpu.h\"\nint main(void){\n"
+    for n, f, _ in fields:
+        src += '  printf("%%zu\\n", offsetof(%s, %s));\n' % (n, f)
+    src += "  return 0;\n}\n"
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "o.c")
+        exe = os.path.join(d, "o")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    assert len(out) == len(fields) > 50
+    bad = [(n, f, py, int(c)) for (n, f, py), c in zip(fields, out) if py != int(c)]
+    assert not bad, bad
+
+
 def test_init_without_gpu_fails_loudly():
     """No CPU fallback: without a CUDA device the context cannot be created."""
     import torch
