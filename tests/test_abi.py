@@ -82,6 +82,28 @@ def test_struct_field_offsets_match_c():
     assert not bad, bad
 
 
+def test_constants_match_c():
+    """Every LJ_ integer constant of the ctypes mirror (error codes, kinds,
+    kernel classes, the ABI version) has the header's value, and the mirror
+    names every constant the header defines."""
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "lj_gpu.h")).read(), flags=re.S)
+    in_header = set(re.findall(r"\b(LJ_[A-Z0-9_]+)\b", text)) - {"LJ_GPU_H"}
+    names = sorted(k for k in dir(abi) if k.startswith("LJ_") and isinstance(getattr(abi, k), int))
+    assert set(names) == in_header, sorted(set(names) ^ in_header)
+    src = "#include <stdio.h>\n#include \"lj_gpu.h\"\nint main(void){\n"
+    for n in names:
+        src += '  printf("%%lld\\n", (long long)(%s));\n' % n
+    src += "  return 0;\n}\n"
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "k.c")
+        exe = os.path.join(d, "k")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    bad = [(n, getattr(abi, n), int(v)) for n, v in zip(names, out) if getattr(abi, n) != int(v)]
+    assert not bad, bad
+
+
 def test_init_without_gpu_fails_loudly():
     """No CPU fallback: without a CUDA device the context cannot be created."""
     import torch
