@@ -45,6 +45,7 @@ def lib():
         L.lj_gpu_shutdown.argtypes = [vp]
         L.lj_gpu_last_error.argtypes = [vp]
         L.lj_gpu_last_error.restype = C.c_char_p
+        L.lj_gpu_abi_version.argtypes = []
         L.lj_gpu_abi_version.restype = C.c_int
         if L.lj_gpu_abi_version() != abi.LJ_GPU_ABI_VERSION:
             raise LjError(abi.LJ_ERR_UNSUPPORTED, "liblj_gpu.so has ABI version %d, the bindings expect %d"
@@ -59,6 +60,7 @@ def lib():
         L.lj_gpu_trace_any.argtypes = [vp, vp, vp, i64, vp]
         L.lj_gpu_prim_to_shape.argtypes = [vp, i32, C.POINTER(i32), C.POINTER(i32)]
         L.lj_gpu_morton_sort.argtypes = [vp, vp, i64, vp, vp, vp]
+        L.lj_gpu_morton_sort_noalloc.argtypes = [vp, i64, vp, vp, vp]
         L.lj_gpu_trace_counters.argtypes = [vp, vp, i64, i32, C.POINTER(i64), C.POINTER(i64)]
         L.lj_gpu_bsdf_param_count.argtypes = [i32]
         L.lj_gpu_bsdf_batch.argtypes = [vp, C.POINTER(abi.lj_bsdf_batch), i64, vp]

@@ -42,6 +42,23 @@ def test_every_declared_symbol_is_exported():
     assert not missing, missing
 
 
+def test_every_binding_declares_the_header_parameter_count():
+    """gpu.lib() gives every declared function ctypes argument types, as many
+    as the header's prototype has (an undeclared pointer argument would be
+    passed as a 32-bit int)."""
+    L = gpu.lib()
+    protos = {}
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"\b(lj_gpu_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+            args = m.group(2).strip()
+            protos[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    assert set(protos) == set(declared_functions())
+    bad = [(n, k, getattr(L, n).argtypes) for n, k in sorted(protos.items())
+           if getattr(L, n).argtypes is None or len(getattr(L, n).argtypes) != k]
+    assert not bad, bad
+
+
 def test_struct_sizes_match_c():
     names = sorted(abi.STRUCT_SIZES)
     src = "#include <stdio.h>\n#include \"lj_gpu.h\"\nint main(void){\n"
