@@ -7,7 +7,8 @@ Workload (a "step" = serving one batch of render jobs):
            renders one of 6 resident scenes -- in turn a seeded Cornell box
            with tessellated walls, a seeded terrain + icosphere + HDR-envmap
            scene (Disney BSDFs) and a seeded heterogeneous volume (256^3
-           FP32 value-noise density, max 20, chromatic sigma_t) in a
+           one-channel FP32 value-noise density, max 20, scaled per
+           channel by (1.05, 0.9, 0.8) for a chromatic sigma_t) in a
            dielectric sphere over a tessellated floor (volumetric path
            tracer), 10k-2M triangles,
            log-uniform -- at a square resolution in {128, 256, 512, 1024},
