@@ -2306,6 +2306,18 @@ void ljo_pcg(uint64_t stream, uint64_t seed, int k, uint32_t *out) {
 void ljo_set_vol_mis_mode(int mode) { g_vol_mis_mode = mode; }
 void ljo_set_vol_nee_order(int order) { g_vol_nee_order = order; }
 
+// Primary rays of a camera at screen positions (sx, sy) in [0,1)^2:
+// out = org[3], dir[3] per ray (sample_primary, src/camera.cpp:23-47).
+void ljo_camera_batch(const lj_camera_desc *c, const double *screen, int64_t n, double *out) {
+    CameraS cam = make_camera(*c);
+    for (int64_t i = 0; i < n; i++) {
+        Ray r = sample_primary(cam, V2{screen[2 * i], screen[2 * i + 1]});
+        double *o = out + 6 * i;
+        o[0] = r.org.x; o[1] = r.org.y; o[2] = r.org.z;
+        o[3] = r.dir.x; o[4] = r.dir.y; o[5] = r.dir.z;
+    }
+}
+
 void ljo_pcg_keyed(uint64_t job_seed, uint64_t pixel, uint64_t sample, int k, uint32_t *out) {
     Pcg p = pcg_keyed(job_seed, pixel, sample);
     for (int i = 0; i < k; i++) out[i] = pcg_next(p);

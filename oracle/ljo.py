@@ -53,6 +53,7 @@ def lib():
         L.ljo_table2d.argtypes = [vp, C.c_int, C.c_int, vp, C.c_int, vp, vp]
         L.ljo_pcg.argtypes = [u64, u64, C.c_int, vp]
         L.ljo_pcg_keyed.argtypes = [u64, u64, u64, C.c_int, vp]
+        L.ljo_camera_batch.argtypes = [C.POINTER(abi.lj_camera_desc), vp, i64, vp]
         _lib = L
     return _lib
 
@@ -154,6 +155,18 @@ def phase(kind, g, dir_in, dir_out, rnd):
 def pcg(stream, seed, k):
     out = np.zeros(k, np.uint32)
     lib().ljo_pcg(stream, seed, k, _p(out))
+    return out
+
+
+def camera_rays(matrix, fov, width, height, filter_kind, filter_param, screen):
+    """Primary rays (org, dir) per screen position, as an (n, 6) array."""
+    c = abi.lj_camera_desc()
+    c.cam_to_world[:] = [float(x) for x in np.asarray(matrix, np.float64).reshape(-1)]
+    c.fov, c.width, c.height = float(fov), int(width), int(height)
+    c.filter_kind, c.filter_param, c.medium_id = int(filter_kind), float(filter_param), -1
+    screen = np.ascontiguousarray(screen, np.float64).reshape(-1, 2)
+    out = np.zeros((len(screen), 6))
+    lib().ljo_camera_batch(C.byref(c), _p(screen), len(screen), _p(out))
     return out
 
 

@@ -37,6 +37,19 @@ def test_table_dist_matches_reference():
     np.testing.assert_allclose(pdf, g["pdf2"], rtol=1e-13, atol=0)
 
 
+def test_camera_matches_reference():
+    """sample_primary (src/camera.cpp:23-47) with the box, tent and Gaussian
+    pixel filters (src/filters/*.inl) at non-square resolutions: ray origins
+    and directions equal the reference's to FP64 rounding."""
+    g = ljtest.golden("camera")
+    for fk in (abi.LJ_FILTER_BOX, abi.LJ_FILTER_TENT, abi.LJ_FILTER_GAUSSIAN):
+        k = "f%d_" % fk
+        rays = ljo.camera_rays(g[k + "matrix"], g[k + "fov"], g[k + "w"], g[k + "h"], g[k + "filter"],
+                               g[k + "param"], g[k + "screen"])
+        assert rays.shape == g[k + "rays"].shape == (200, 6)
+        np.testing.assert_allclose(rays, g[k + "rays"], rtol=1e-12, atol=1e-13)
+
+
 def test_bsdf_matches_reference():
     g = ljtest.golden("bsdf")
     rec, out = g["inputs"], g["outputs"]
