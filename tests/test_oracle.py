@@ -118,6 +118,23 @@ def test_morton_sort_is_stable_and_sorted():
     np.testing.assert_array_equal(np.sort(order), np.arange(len(tri)))
 
 
+def test_single_triangle_reference_known_answer_cpu():
+    """src/tests/intersection.cpp:4-42 on the oracle: triangle (-1,-1,-1)
+    (1,-1,-1) (0,1,-1); a ray from the origin along -z hits (0, 0, -1), one
+    along +z misses."""
+    sc = scenes.Scene(4, 4, 1, 2, np.eye(4), 45.0)
+    m = sc.add_material(scenes.lambertian([0.5, 0.5, 0.5]))
+    sc.add_mesh(np.array([[-1, -1, -1], [1, -1, -1], [0, 1, -1]], np.float32), np.array([[0, 1, 2]]), m)
+    o = ljo.OracleScene(sc)
+    rays = np.array([[0, 0, 0, 0, 0, 0, -1, np.inf], [0, 0, 0, 0, 0, 0, 1, np.inf]], np.float32)
+    for brute in (True, False):
+        t, prim, _, _, _ = o.trace_closest(rays, brute=brute)
+        assert prim[0] == 0 and prim[1] < 0
+        p = rays[0, :3] + rays[0, 4:7] * t[0]
+        assert np.linalg.norm(p - np.array([0, 0, -1])) < 1e-3
+        np.testing.assert_array_equal(o.trace_any(rays, brute=brute), [1, 0])
+
+
 def test_bvh_matches_brute_force_cpu():
     """The oracle's own BVH traversal agrees with brute force (CPU twin of
     the GPU trace parity test)."""
