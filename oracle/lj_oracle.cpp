@@ -2306,6 +2306,19 @@ void ljo_pcg(uint64_t stream, uint64_t seed, int k, uint32_t *out) {
 void ljo_set_vol_mis_mode(int mode) { g_vol_mis_mode = mode; }
 void ljo_set_vol_nee_order(int order) { g_vol_nee_order = order; }
 
+// Pixel-filter offsets for random pairs u: out = (x, y) per pair
+// (src/filters/box.inl, tent.inl, gaussian.inl).
+void ljo_filter_sample(int kind, double param, const double *u, int64_t n, double *out) {
+    CameraS c;
+    c.filter = kind;
+    c.fparam = param;
+    for (int64_t i = 0; i < n; i++) {
+        V2 s = filter_sample(c, V2{u[2 * i], u[2 * i + 1]});
+        out[2 * i] = s.x;
+        out[2 * i + 1] = s.y;
+    }
+}
+
 // Primary rays of a camera at screen positions (sx, sy) in [0,1)^2:
 // out = org[3], dir[3] per ray (sample_primary, src/camera.cpp:23-47).
 void ljo_camera_batch(const lj_camera_desc *c, const double *screen, int64_t n, double *out) {

@@ -53,6 +53,7 @@ def lib():
         L.ljo_table2d.argtypes = [vp, C.c_int, C.c_int, vp, C.c_int, vp, vp]
         L.ljo_pcg.argtypes = [u64, u64, C.c_int, vp]
         L.ljo_pcg_keyed.argtypes = [u64, u64, u64, C.c_int, vp]
+        L.ljo_filter_sample.argtypes = [C.c_int, C.c_double, vp, i64, vp]
         L.ljo_camera_batch.argtypes = [C.POINTER(abi.lj_camera_desc), vp, i64, vp]
         _lib = L
     return _lib
@@ -167,6 +168,14 @@ def camera_rays(matrix, fov, width, height, filter_kind, filter_param, screen):
     screen = np.ascontiguousarray(screen, np.float64).reshape(-1, 2)
     out = np.zeros((len(screen), 6))
     lib().ljo_camera_batch(C.byref(c), _p(screen), len(screen), _p(out))
+    return out
+
+
+def filter_sample(kind, param, u):
+    """Pixel-filter offsets (n, 2) for random pairs u (n, 2)."""
+    u = np.ascontiguousarray(u, np.float64).reshape(-1, 2)
+    out = np.zeros_like(u)
+    lib().ljo_filter_sample(int(kind), float(param), _p(u), len(u), _p(out))
     return out
 
 

@@ -50,6 +50,31 @@ def test_camera_matches_reference():
         np.testing.assert_allclose(rays, g[k + "rays"], rtol=1e-12, atol=1e-13)
 
 
+def test_filter_sampling_jacobian_reference_method():
+    """The reference's filter test (src/tests/filter.cpp:15-68) on the
+    oracle's filter sampling: the determinant of the sampling map's
+    finite-difference Jacobian equals the inverse of the normalised filter
+    kernel at the sample (width 2 box and tent, standard deviation 2
+    Gaussian), at the reference's point (0.3, 0.4) and at more points."""
+    eps = 1e-6
+    pts = np.array([[0.3, 0.4], [0.1, 0.8], [0.7, 0.2], [0.55, 0.45], [0.9, 0.95]])
+    for kind, w in ((abi.LJ_FILTER_BOX, 2.0), (abi.LJ_FILTER_TENT, 2.0), (abi.LJ_FILTER_GAUSSIAN, 2.0)):
+        s = ljo.filter_sample(kind, w, pts)
+        su = ljo.filter_sample(kind, w, pts + [eps, 0])
+        sv = ljo.filter_sample(kind, w, pts + [0, eps])
+        du, dv = (su - s) / eps, (sv - s) / eps
+        det = np.abs(du[:, 0] * dv[:, 1] - du[:, 1] * dv[:, 0])
+        if kind == abi.LJ_FILTER_BOX:
+            inv_kernel = np.full(len(pts), w * w)
+        elif kind == abi.LJ_FILTER_TENT:
+            h = w / 2
+            inv_kernel = 1 / (((1 - np.abs(s[:, 0]) / h) / h) * ((1 - np.abs(s[:, 1]) / h) / h))
+        else:
+            r2 = (s ** 2).sum(1)
+            inv_kernel = 1 / (np.exp(-r2 / (w * w) / 2) / (w * w * 2 * np.pi))
+        np.testing.assert_allclose(det, inv_kernel, rtol=1e-3, atol=1e-3)
+
+
 def test_bsdf_matches_reference():
     g = ljtest.golden("bsdf")
     rec, out = g["inputs"], g["outputs"]
