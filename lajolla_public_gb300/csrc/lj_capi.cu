@@ -94,7 +94,10 @@ struct HostImg {
     int w = 0, h = 0;
     std::vector<double> px;   // rgb
 };
-// 2x2 box pyramid, <= 8 levels: src/mipmap.h:25-48
+// 2x2 box pyramid, <= 8 levels: src/mipmap.h:25-48.  Where the previous
+// level is one texel high (or wide) and the other side is larger, the
+// reference's 2x2 box reads a row (column) past the image; here that read
+// takes the edge texel instead, which changes no read that is in bounds.
 std::vector<HostImg> make_mips(const lj_image_desc &im) {
     std::vector<HostImg> lv;
     HostImg l0;
@@ -116,7 +119,11 @@ std::vector<HostImg> make_mips(const lj_image_desc &im) {
         for (int y = 0; y < n.h; y++)
             for (int x = 0; x < n.w; x++)
                 for (int c = 0; c < 3; c++) {
-                    auto at = [&](int xx, int yy) { return p.px[((size_t)yy * p.w + xx) * 3 + c]; };
+                    auto at = [&](int xx, int yy) {
+                        xx = std::min(xx, p.w - 1);
+                        yy = std::min(yy, p.h - 1);
+                        return p.px[((size_t)yy * p.w + xx) * 3 + c];
+                    };
                     n.px[((size_t)y * n.w + x) * 3 + c] =
                         (at(2 * x, 2 * y) + at(2 * x + 1, 2 * y) + at(2 * x, 2 * y + 1) + at(2 * x + 1, 2 * y + 1)) / 4.0;
                 }

@@ -199,7 +199,10 @@ static inline double modulo_d(double a, double b) {
     double r = std::fmod(a, b);
     return r < 0.0 ? r + b : r;
 }
-// make_mipmap, src/mipmap.h:25-48
+// make_mipmap, src/mipmap.h:25-48.  Where the previous level is one texel
+// high (or wide) and the other side is larger, the reference's 2x2 box reads
+// a row (column) past the image; here that read takes the edge texel, as
+// the GPU library's pyramid does.
 static Mip3 make_mip(const Img3 &img) {
     Mip3 m;
     int size = std::max(img.w, img.h);
@@ -212,10 +215,11 @@ static Mip3 make_mip(const Img3 &img) {
         n.h = std::max(p.h / 2, 1);
         n.px.resize((size_t)n.w * n.h);
         for (int y = 0; y < n.h; y++)
-            for (int x = 0; x < n.w; x++)
+            for (int x = 0; x < n.w; x++) {
+                int x1 = std::min(2 * x + 1, p.w - 1), y1 = std::min(2 * y + 1, p.h - 1);
                 n.px[(size_t)y * n.w + x] =
-                    (p.at(2 * x, 2 * y) + p.at(2 * x + 1, 2 * y) + p.at(2 * x, 2 * y + 1) +
-                     p.at(2 * x + 1, 2 * y + 1)) / 4.0;
+                    (p.at(2 * x, 2 * y) + p.at(x1, 2 * y) + p.at(2 * x, y1) + p.at(x1, y1)) / 4.0;
+            }
         m.levels.push_back(n);
     }
     return m;
@@ -2305,6 +2309,24 @@ void ljo_pcg(uint64_t stream, uint64_t seed, int k, uint32_t *out) {
 // Test-only: select the volumetric estimator (0 MIS, 1 light only, 2 direction only).
 void ljo_set_vol_mis_mode(int mode) { g_vol_mis_mode = mode; }
 void ljo_set_vol_nee_order(int order) { g_vol_nee_order = order; }
+
+// Mipmap of an RGB image (h x w x 3, FP32, rows top to bottom) looked up at
+// (u, v, level) triples, trilinearly: out = RGB per triple
+// (make_mipmap and lookup, src/mipmap.h:25-88).
+void ljo_mipmap_lookup(const float *rgb, int w, int h, const double *uvl, int64_t n, double *out,
+                       int *num_levels) {
+    Img3 img;
+    img.w = w;
+    img.h = h;
+    img.px.resize((size_t)w * h);
+    for (size_t i = 0; i < img.px.size(); i++) img.px[i] = V3{rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]};
+    Mip3 m = make_mip(img);
+    *num_levels = (int)m.levels.size();
+    for (int64_t i = 0; i < n; i++) {
+        V3 c = mip_lookup(m, uvl[3 * i], uvl[3 * i + 1], uvl[3 * i + 2]);
+        out[3 * i] = c.x; out[3 * i + 1] = c.y; out[3 * i + 2] = c.z;
+    }
+}
 
 // Pixel-filter offsets for random pairs u: out = (x, y) per pair
 // (src/filters/box.inl, tent.inl, gaussian.inl).

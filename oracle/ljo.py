@@ -53,6 +53,7 @@ def lib():
         L.ljo_table2d.argtypes = [vp, C.c_int, C.c_int, vp, C.c_int, vp, vp]
         L.ljo_pcg.argtypes = [u64, u64, C.c_int, vp]
         L.ljo_pcg_keyed.argtypes = [u64, u64, u64, C.c_int, vp]
+        L.ljo_mipmap_lookup.argtypes = [vp, C.c_int, C.c_int, vp, i64, vp, vp]
         L.ljo_filter_sample.argtypes = [C.c_int, C.c_double, vp, i64, vp]
         L.ljo_camera_batch.argtypes = [C.POINTER(abi.lj_camera_desc), vp, i64, vp]
         _lib = L
@@ -169,6 +170,18 @@ def camera_rays(matrix, fov, width, height, filter_kind, filter_param, screen):
     out = np.zeros((len(screen), 6))
     lib().ljo_camera_batch(C.byref(c), _p(screen), len(screen), _p(out))
     return out
+
+
+def mipmap_lookup(img, uvl):
+    """Trilinear lookups (n, 3) of the mipmap of img (h, w, 3) at (u, v,
+    level) triples; also returns the number of levels."""
+    img = np.ascontiguousarray(img, np.float32)
+    h, w = img.shape[:2]
+    uvl = np.ascontiguousarray(uvl, np.float64).reshape(-1, 3)
+    out = np.zeros((len(uvl), 3))
+    nl = C.c_int(0)
+    lib().ljo_mipmap_lookup(_p(img), w, h, _p(uvl), len(uvl), _p(out), C.byref(nl))
+    return out, nl.value
 
 
 def filter_sample(kind, param, u):

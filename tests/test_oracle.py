@@ -75,6 +75,36 @@ def test_filter_sampling_jacobian_reference_method():
         np.testing.assert_allclose(det, inv_kernel, rtol=1e-3, atol=1e-3)
 
 
+def test_mipmap_reference_known_answer_and_box_pyramid():
+    """The reference's mipmap test (src/tests/mipmap.cpp:5-30) on the
+    oracle's mipmap: a constant 64x64 image looks up to 1 at every texel
+    centre of every level l + 0.5.  And for a random 64x32 image: level 0 at
+    texel centres returns the texels, an integer level k returns the mean of
+    the 2^k x 2^k block, and levels past the last clamp to it."""
+    xs = (np.arange(64) + 0.5) / 64
+    uu, vv = np.meshgrid(xs, xs)
+    ones = np.ones((64, 64, 3), np.float32)
+    _, nl = ljo.mipmap_lookup(ones, np.zeros((1, 3)))
+    assert nl == 7
+    for lvl in range(nl):
+        q = np.stack([uu.ravel(), vv.ravel(), np.full(uu.size, lvl + 0.5)], 1)
+        out, _ = ljo.mipmap_lookup(ones, q)
+        assert np.abs(out - 1).max() <= 1e-3
+    rng = np.random.default_rng(3)
+    img = rng.uniform(0, 1, (32, 64, 3)).astype(np.float32)
+    for k in range(4):
+        bw, bh = 64 >> k, 32 >> k
+        block = img.astype(np.float64).reshape(bh, 1 << k, bw, 1 << k, 3).mean(axis=(1, 3))
+        u, v = np.meshgrid((np.arange(bw) + 0.5) / bw, (np.arange(bh) + 0.5) / bh)
+        q = np.stack([u.ravel(), v.ravel(), np.full(u.size, float(k))], 1)
+        out, nl = ljo.mipmap_lookup(img, q)
+        np.testing.assert_allclose(out, block.reshape(-1, 3), rtol=1e-12, atol=1e-12)
+    last = img.astype(np.float64).mean(axis=(0, 1))   # 64x32 -> 7 levels, the last 1x1 holds the mean
+    out, nl = ljo.mipmap_lookup(img, [[0.3, 0.6, 50.0]])
+    assert nl == 7
+    np.testing.assert_allclose(out[0], last, rtol=1e-12)
+
+
 def test_bsdf_matches_reference():
     g = ljtest.golden("bsdf")
     rec, out = g["inputs"], g["outputs"]
