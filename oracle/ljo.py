@@ -13,7 +13,8 @@ import numpy as np
 from lajolla_public_gb300 import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "liblj_oracle.so")
+# LJO_LIB selects another build of the port (e.g. `make asan`'s)
+LIB_PATH = os.environ.get("LJO_LIB") or os.path.join(HERE, "_build", "liblj_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 _lib = None
