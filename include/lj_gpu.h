@@ -243,6 +243,14 @@ int lj_gpu_abi_version(void);
  * table construction (src/scene.cpp:4-53).  Copies the description to the
  * device and builds the BVH there (LBVH -> 8-wide compressed BVH). */
 int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *desc, lj_scene **out);
+/* The checks lj_gpu_scene_create makes before it touches the device, with no
+ * context and no device needed: indices in range (shapes -> materials,
+ * lights, media; lights -> shapes, images; textures -> images), known kinds,
+ * positive sizes.  Returns LJ_OK, or LJ_ERR_INVALID_ARG with the reason in
+ * msg (NUL-terminated, at most msg_size bytes; msg may be NULL).  Where the
+ * reference's parser throws fl_exception (src/flexception.h:24,
+ * src/parsers/parse_scene.cpp) on such input. */
+int lj_gpu_scene_validate(const lj_scene_desc *desc, char *msg, int msg_size);
 /* Replaces Scene::~Scene / rtcReleaseScene (src/scene.cpp:55-59). */
 void lj_gpu_scene_destroy(lj_scene *scene);
 

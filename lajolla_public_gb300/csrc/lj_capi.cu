@@ -200,17 +200,39 @@ int check_desc(const lj_scene_desc *d, std::string &msg) {
             (s.material_id == -1 && d->options.integrator != LJ_INTEGRATOR_VOLPATH)) {
             msg = "shape " + std::to_string(i) + ": material id out of range"; return -1;
         }
-        if (s.area_light_id >= d->num_lights) { msg = "shape " + std::to_string(i) + ": light id out of range"; return -1; }
-        if (s.interior_medium_id >= d->num_media || s.exterior_medium_id >= d->num_media) {
+        if (s.area_light_id < -1 || s.area_light_id >= d->num_lights) {
+            msg = "shape " + std::to_string(i) + ": light id out of range"; return -1;
+        }
+        if (s.interior_medium_id < -1 || s.exterior_medium_id < -1 || s.interior_medium_id >= d->num_media ||
+            s.exterior_medium_id >= d->num_media) {
             msg = "shape " + std::to_string(i) + ": medium id out of range"; return -1;
         }
     }
-    for (int i = 0; i < d->num_materials; i++)
+    for (int i = 0; i < d->num_images; i++) {
+        const lj_image_desc &im = d->images[i];
+        if (im.width <= 0 || im.height <= 0 || !im.data || (im.channels != 1 && im.channels != 3)) {
+            msg = "image " + std::to_string(i) + ": bad size, channel count or data"; return -1;
+        }
+    }
+    for (int i = 0; i < d->num_materials; i++) {
         if (d->materials[i].type < 0 || d->materials[i].type >= LJ_MAT_COUNT) {
             msg = "material " + std::to_string(i) + ": unknown type"; return -1;
         }
+        for (int k = 0; k < LJ_MAT_SLOTS; k++) {
+            const lj_texture_desc &t = d->materials[i].tex[k];
+            if (t.kind != LJ_TEX_CONST && t.kind != LJ_TEX_IMAGE && t.kind != LJ_TEX_CHECKER) {
+                msg = "material " + std::to_string(i) + ": unknown texture kind"; return -1;
+            }
+            if (t.kind == LJ_TEX_IMAGE && (t.image_id < 0 || t.image_id >= d->num_images)) {
+                msg = "material " + std::to_string(i) + ": texture image id out of range"; return -1;
+            }
+        }
+    }
     for (int i = 0; i < d->num_lights; i++) {
         const lj_light_desc &l = d->lights[i];
+        if (l.kind != LJ_LIGHT_AREA && l.kind != LJ_LIGHT_ENVMAP) {
+            msg = "light " + std::to_string(i) + ": unknown kind"; return -1;
+        }
         if (l.kind == LJ_LIGHT_AREA && (l.shape_id < 0 || l.shape_id >= d->num_shapes)) {
             msg = "light " + std::to_string(i) + ": shape id out of range"; return -1;
         }
@@ -218,7 +240,9 @@ int check_desc(const lj_scene_desc *d, std::string &msg) {
             msg = "light " + std::to_string(i) + ": image id out of range"; return -1;
         }
     }
-    if (d->envmap_light_id >= d->num_lights) { msg = "envmap light id out of range"; return -1; }
+    if (d->envmap_light_id < -1 || d->envmap_light_id >= d->num_lights) {
+        msg = "envmap light id out of range"; return -1;
+    }
     if (d->camera.medium_id >= d->num_media || d->camera.medium_id < -1) { msg = "camera medium id out of range"; return -1; }
     for (int i = 0; i < d->num_media; i++) {
         const lj_medium_desc &m = d->media[i];
@@ -294,6 +318,23 @@ void lj_gpu_shutdown(lj_ctx *ctx) {
 }
 
 const char *lj_gpu_last_error(lj_ctx *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+int lj_gpu_scene_validate(const lj_scene_desc *d, char *msg, int msg_size) {
+    std::string m;
+    int rc = LJ_OK;
+    if (!d) {
+        m = "null scene description";
+        rc = LJ_ERR_INVALID_ARG;
+    } else if (check_desc(d, m)) {
+        rc = LJ_ERR_INVALID_ARG;
+    }
+    if (msg && msg_size > 0) {
+        size_t n = std::min(m.size(), (size_t)msg_size - 1);
+        memcpy(msg, m.data(), n);
+        msg[n] = 0;
+    }
+    return rc;
+}
 
 int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
     if (!ctx || !d || !out) return LJ_ERR_INVALID_ARG;

@@ -51,6 +51,7 @@ def lib():
             raise LjError(abi.LJ_ERR_UNSUPPORTED, "liblj_gpu.so has ABI version %d, the bindings expect %d"
                           % (L.lj_gpu_abi_version(), abi.LJ_GPU_ABI_VERSION))
         L.lj_gpu_scene_create.argtypes = [vp, C.POINTER(abi.lj_scene_desc), C.POINTER(vp)]
+        L.lj_gpu_scene_validate.argtypes = [C.POINTER(abi.lj_scene_desc), C.c_char_p, C.c_int]
         L.lj_gpu_scene_destroy.argtypes = [vp]
         L.lj_gpu_scene_info.argtypes = [vp, C.POINTER(abi.lj_scene_info)]
         L.lj_gpu_render.argtypes = [vp, C.POINTER(abi.lj_render_params), vp, C.POINTER(abi.lj_stats)]
@@ -81,6 +82,16 @@ def lib():
                                              C.c_char_p, C.POINTER(abi.lj_server_options)]
         _lib = L
     return _lib
+
+
+def validate_scene(scene):
+    """Checks a scenes.Scene's description the way lj_gpu_scene_create does,
+    without a device; raises LjError with the reason if it is invalid."""
+    desc, keep = scene.desc()
+    buf = C.create_string_buffer(512)
+    rc = lib().lj_gpu_scene_validate(C.byref(desc), buf, len(buf))
+    if rc != abi.LJ_OK:
+        raise LjError(rc, buf.value.decode())
 
 
 def _ptr(t):
