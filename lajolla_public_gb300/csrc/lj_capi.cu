@@ -248,6 +248,17 @@ int check_desc(const lj_scene_desc *d, std::string &msg) {
         const lj_medium_desc &m = d->media[i];
         if (m.kind != LJ_MEDIUM_HOMOGENEOUS && m.kind != LJ_MEDIUM_HETEROGENEOUS) { msg = "medium: unknown kind"; return -1; }
         if (m.phase_kind != LJ_PHASE_ISOTROPIC && m.phase_kind != LJ_PHASE_HG) { msg = "medium: unknown phase"; return -1; }
+        const lj_volume_desc *vols[2] = {&m.albedo, &m.density};
+        for (int k = 0; k < 2 && m.kind == LJ_MEDIUM_HETEROGENEOUS; k++) {
+            const lj_volume_desc &v = *vols[k];
+            if (v.kind != LJ_VOL_CONST && v.kind != LJ_VOL_GRID) {
+                msg = "medium " + std::to_string(i) + ": unknown volume kind"; return -1;
+            }
+            if (v.kind == LJ_VOL_GRID && (v.res[0] <= 0 || v.res[1] <= 0 || v.res[2] <= 0 || !v.data ||
+                                          (v.channels != 1 && v.channels != 3))) {
+                msg = "medium " + std::to_string(i) + ": bad grid volume"; return -1;
+            }
+        }
     }
     return 0;
 }

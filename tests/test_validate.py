@@ -79,6 +79,25 @@ def _first_image_slot(desc):
     raise AssertionError("no image texture")
 
 
+@pytest.mark.parametrize("case", ["grid_res", "grid_channels", "grid_data", "volume_kind"])
+def test_invalid_grid_volumes_are_refused(case):
+    sc = scenes.volume_scene(width=8, height=8, spp=1, grid=8)
+    desc, keep = sc.desc()
+    i = next(k for k in range(desc.num_media) if desc.media[k].kind == abi.LJ_MEDIUM_HETEROGENEOUS)
+    v = desc.media[i].density
+    assert v.kind == abi.LJ_VOL_GRID
+    if case == "grid_res":
+        v.res[0], v.res[1] = -8, -8         # a positive product of negative sizes
+    elif case == "grid_channels":
+        v.channels = 4
+    elif case == "grid_data":
+        v.data = None
+    else:
+        v.kind = 2
+    rc, msg = validate_desc(desc)
+    assert rc == abi.LJ_ERR_INVALID_ARG and "medium %d" % i in msg, msg
+
+
 @pytest.mark.parametrize("case", ["tex_image_id", "tex_kind", "image_channels", "image_size", "image_data",
                                   "light_kind", "shape_light", "shape_medium", "envmap_id", "material_type",
                                   "index_range", "camera"])
