@@ -60,3 +60,9 @@ def test_reference_arm_under_torchrun_prints_once():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["n_gpus"] == 2
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["cores"] >= 1
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "e2e", "cpu_baseline"):
+        assert key in d, key
+    assert d["steps"] == 1 and d["warmup"] == 3 and d["higher_is_better"] is True
+    assert d["unit"] == d["e2e"]["unit"] == d["cpu_baseline"]["unit"] == "Msamples/s"
+    assert d["cpu_baseline"]["kind"] == "port" and d["config"]["workload"].startswith("serving")
