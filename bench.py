@@ -417,10 +417,10 @@ def run_ours(args):
     traffic = load_traffic(kname, units / launches_dom)
     if dom in (abi.LJ_KERNEL_MEDIUM, abi.LJ_KERNEL_NEE):
         note = ("volumetric steps are latency bound, not HBM bound: their dependent density-grid lookups "
-                "(8 x 16 B per tracking step) mostly hit L1/L2 (profiles/ncu_volpath_kernels.md)")
+                "(8 x 16 B per tracking step) mostly hit L1/L2 (ncu of the volume scene's a / b / c steps)")
     else:
         note = ("traversal is instruction-issue bound, not HBM bound: ncu on a terrain job shows "
-                "79% issue active, 3.1 IPC, 2% of DRAM peak (profiles/ncu_srv_trace_terrain.md)")
+                "79% issue active, 3.1 IPC, 2% of DRAM peak")
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,

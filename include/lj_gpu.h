@@ -43,8 +43,9 @@ extern "C" {
 
 /* 2: lj_volume_desc.channel_scale, the volumetric kernel classes
  * (LJ_KERNEL_MEDIUM, LJ_KERNEL_NEE) and the volumetric counters of
- * lj_server_stats */
-#define LJ_GPU_ABI_VERSION 2
+ * lj_server_stats
+ * 3: the emission, camera-ray and medium batches */
+#define LJ_GPU_ABI_VERSION 3
 
 /* ---- error codes -------------------------------------------------------- */
 #define LJ_OK                 0
@@ -380,9 +381,12 @@ int lj_gpu_morton_sort(lj_ctx *ctx, const float *d_tri_vertices, int64_t n,
  * memory is one fixed 2 MiB array inside this library, held on every GPU
  * that loads the library until the process exits.  Hence the limit:
  * n <= LJ_NOALLOC_MORTON_MAX_TRIANGLES, else LJ_ERR_SIZE_LIMIT (nothing is
- * queued).  The first call on each device looks up the array's device
- * address (with that device current) and caches it; make that first call
- * before any stream capture begins.  Every call reuses the same array, so
+ * queued).  The first call in each CUDA context (a device's primary
+ * context, or a driver-API context current on the calling thread) looks up
+ * the array's device address in that context and caches it under the
+ * context's unique id; a context created anew (e.g. after cudaDeviceReset)
+ * gets a new id and a fresh lookup.  Make the first call in a context before
+ * any stream capture begins.  Every call reuses the same array, so
  * calls that overlap on the GPU race: order them (same stream, or events).
  * Errors are returned as codes only (there is no context for a message). */
 #define LJ_NOALLOC_MORTON_MAX_TRIANGLES 65536
@@ -429,6 +433,36 @@ int lj_gpu_light_sample_batch(lj_scene *scene, const float *d_ref_points,
                               const float *d_rnd, int32_t *d_out_light,
                               float *d_out_point, float *d_out_normal,
                               float *d_out_pdf, int64_t n, void *stream);
+
+/* Emission batch: replaces emission(light, view_dir, view_footprint,
+ * point_on_light, scene) (src/light.cpp:56-77; area light
+ * src/lights/diffuse_area_light.inl:15-20, envmap src/lights/envmap.inl:44-73)
+ * for n queries.  d_light: light ids; d_view_dir n*3 (pointing from the
+ * light, as the reference's view_dir); d_point / d_normal n*3 the point on
+ * the light and its normal (an envmap ignores them).  out n*3.  The
+ * reference's envmap footprint never leaves mip level 0 (it is computed from
+ * the direction alone and clamped), so there is no footprint argument.  A
+ * light id outside [0, num_lights) gives NaN. */
+int lj_gpu_light_emission_batch(lj_scene *scene, const int32_t *d_light, const float *d_view_dir,
+                                const float *d_point, const float *d_normal, float *d_out_emission,
+                                int64_t n, void *stream);
+
+/* Camera batch: replaces sample_primary (src/camera.cpp:23-47) with the
+ * scene camera's pixel filter (box / tent / Gaussian, src/filters/*.inl)
+ * for n screen positions d_screen (n*2, in [0,1)^2, x right, y down).
+ * Outputs: ray origins and unit directions, n*3 each. */
+int lj_gpu_camera_ray_batch(lj_scene *scene, const float *d_screen, float *d_out_org,
+                            float *d_out_dir, int64_t n, void *stream);
+
+/* Medium batch: replaces get_sigma_a / get_sigma_s (src/medium.cpp:31-37,
+ * src/media/*.inl, with the GridVolume trilinear lookup of
+ * src/volume.h:44-81) at n points d_points (n*3), and get_majorant
+ * (src/medium.cpp:27-29, the grid box slab test src/volume.h:124-144) for
+ * the n rays (d_points[i], d_dirs[i], tfar = inf), of medium `medium_id` of
+ * the scene.  Outputs n*3 each; any output may be NULL. */
+int lj_gpu_medium_batch(lj_scene *scene, int32_t medium_id, const float *d_points, const float *d_dirs,
+                        float *d_out_sigma_a, float *d_out_sigma_s, float *d_out_majorant,
+                        int64_t n, void *stream);
 
 /* Phase batch: replaces eval / sample_phase_function / pdf_sample_phase
  * (src/phase_function.cpp:30-47) for Henyey-Greenstein (g) or isotropic

@@ -3,10 +3,14 @@
 //   lj_gpu_light_sample_batch  sample_light + sample_point_on_light + pdfs
 //                              (src/scene.cpp:61-67, src/light.cpp:56-77)
 //   lj_gpu_phase_batch         Henyey-Greenstein / isotropic (src/phase_function.cpp:30-47)
+//   lj_gpu_light_emission_batch  emission (src/light.cpp:56-77)
+//   lj_gpu_camera_ray_batch    sample_primary + pixel filters (src/camera.cpp:23-47)
+//   lj_gpu_medium_batch        get_sigma_a / get_sigma_s / get_majorant (src/medium.cpp:27-37)
 // One thread per query; inputs and outputs are flat FP32 arrays in HBM.
 #include "lj_host.h"
 #include "lj_phase.cuh"
 #include "lj_shade.cuh"
+#include "lj_volwave.cuh"
 
 namespace lj {
 namespace {
@@ -93,6 +97,60 @@ __global__ void k_phase_batch(int kind, float g, const float *din, const float *
     }
 }
 
+__global__ void k_emission_batch(DevScene sc, const int32_t *light, const float *view, const float *point,
+                                 const float *normal, float *out, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int lid = light[i];
+    V3 e;
+    if (lid < 0 || lid >= sc.num_lights) {
+        e = V3{__int_as_float(0x7fc00000), __int_as_float(0x7fc00000), __int_as_float(0x7fc00000)};
+    } else {
+        const V3 vd{view[3 * i], view[3 * i + 1], view[3 * i + 2]};
+        PN pn{V3{point[3 * i], point[3 * i + 1], point[3 * i + 2]},
+              V3{normal[3 * i], normal[3 * i + 1], normal[3 * i + 2]}};
+        e = light_emission(sc, lid, vd, pn);
+    }
+    out[3 * i] = e.x; out[3 * i + 1] = e.y; out[3 * i + 2] = e.z;
+}
+
+__global__ void k_camera_batch(CamRec cam, const float *screen, float *org, float *dir, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    V3 o, d;
+    camera_ray(cam, screen[2 * i], screen[2 * i + 1], o, d);
+    org[3 * i] = o.x; org[3 * i + 1] = o.y; org[3 * i + 2] = o.z;
+    dir[3 * i] = d.x; dir[3 * i + 1] = d.y; dir[3 * i + 2] = d.z;
+}
+
+// sigma_a = density * (1 - albedo), sigma_s = density * albedo
+// (src/media/heterogeneous.inl:11-21); the constants of a homogeneous medium.
+__global__ void k_medium_batch(const MediumRec *media, int mid, const float *pts, const float *dirs, float *sa,
+                               float *ss, float *maj, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const MediumRec &m = media[mid];
+    const V3 p{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+    if (sa || ss) {
+        V3 a, s;
+        if (m.kind == LJ_MEDIUM_HOMOGENEOUS) {
+            a = V3{m.sigma_a[0], m.sigma_a[1], m.sigma_a[2]};
+            s = V3{m.sigma_s[0], m.sigma_s[1], m.sigma_s[2]};
+        } else {
+            const V3 d = vol_lookup(m.density, p), al = vol_lookup(m.albedo, p);
+            s = d * al;
+            a = d * (V3{1, 1, 1} - al);
+        }
+        if (sa) { sa[3 * i] = a.x; sa[3 * i + 1] = a.y; sa[3 * i + 2] = a.z; }
+        if (ss) { ss[3 * i] = s.x; ss[3 * i + 1] = s.y; ss[3 * i + 2] = s.z; }
+    }
+    if (maj) {
+        const V3 d{dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]};
+        const V3 mj = majorant(m, p, d);
+        maj[3 * i] = mj.x; maj[3 * i + 1] = mj.y; maj[3 * i + 2] = mj.z;
+    }
+}
+
 inline int blocks(int64_t n) { return (int)((n + 255) / 256); }
 
 }  // namespace
@@ -150,6 +208,46 @@ int lj_gpu_phase_batch(lj_ctx *ctx, int32_t kind, float g, const float *d_dir_in
     k_phase_batch<<<blocks(n), 256, 0, s>>>(kind, g, d_dir_in, d_dir_out, d_rnd, d_out_value, d_out_pdf,
                                             d_out_dir, n);
     if (cudaGetLastError() != cudaSuccess) return set_error(ctx, LJ_ERR_CUDA, "phase_batch launch failed");
+    return LJ_OK;
+}
+
+int lj_gpu_light_emission_batch(lj_scene *sc, const int32_t *d_light, const float *d_view_dir, const float *d_point,
+                                const float *d_normal, float *d_out, int64_t n, void *stream) {
+    if (!sc || n < 0 || (n > 0 && (!d_light || !d_view_dir || !d_point || !d_normal || !d_out)))
+        return LJ_ERR_INVALID_ARG;
+    if (n == 0) return LJ_OK;
+    cudaSetDevice(sc->ctx->device);
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
+    k_emission_batch<<<blocks(n), 256, 0, s>>>(sc->dev, d_light, d_view_dir, d_point, d_normal, d_out, n);
+    if (cudaGetLastError() != cudaSuccess) return set_error(sc->ctx, LJ_ERR_CUDA, "light_emission_batch launch failed");
+    return LJ_OK;
+}
+
+int lj_gpu_camera_ray_batch(lj_scene *sc, const float *d_screen, float *d_out_org, float *d_out_dir, int64_t n,
+                            void *stream) {
+    if (!sc || n < 0 || (n > 0 && (!d_screen || !d_out_org || !d_out_dir))) return LJ_ERR_INVALID_ARG;
+    if (n == 0) return LJ_OK;
+    cudaSetDevice(sc->ctx->device);
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
+    k_camera_batch<<<blocks(n), 256, 0, s>>>(sc->dev.cam, d_screen, d_out_org, d_out_dir, n);
+    if (cudaGetLastError() != cudaSuccess) return set_error(sc->ctx, LJ_ERR_CUDA, "camera_ray_batch launch failed");
+    return LJ_OK;
+}
+
+int lj_gpu_medium_batch(lj_scene *sc, int32_t medium_id, const float *d_points, const float *d_dirs,
+                        float *d_out_sigma_a, float *d_out_sigma_s, float *d_out_majorant, int64_t n,
+                        void *stream) {
+    if (!sc || n < 0) return LJ_ERR_INVALID_ARG;
+    if (medium_id < 0 || medium_id >= sc->dev.num_media)
+        return set_error(sc->ctx, LJ_ERR_INVALID_ARG, "medium_batch: medium id out of range");
+    if (n > 0 && (!d_points || (d_out_majorant && !d_dirs)))
+        return set_error(sc->ctx, LJ_ERR_INVALID_ARG, "medium_batch: missing input buffer");
+    if (n == 0 || (!d_out_sigma_a && !d_out_sigma_s && !d_out_majorant)) return LJ_OK;
+    cudaSetDevice(sc->ctx->device);
+    cudaStream_t s = (cudaStream_t)stream;   // NULL: the legacy default stream
+    k_medium_batch<<<blocks(n), 256, 0, s>>>(sc->dev.media, medium_id, d_points, d_dirs, d_out_sigma_a,
+                                             d_out_sigma_s, d_out_majorant, n);
+    if (cudaGetLastError() != cudaSuccess) return set_error(sc->ctx, LJ_ERR_CUDA, "medium_batch launch failed");
     return LJ_OK;
 }
 

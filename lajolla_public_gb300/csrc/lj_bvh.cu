@@ -31,9 +31,9 @@ namespace lj {
 
 namespace {
 
-constexpr int kRsThreads = 256;
-constexpr int kRsItems = 8;
-constexpr int kRsTile = kRsThreads * kRsItems;
+constexpr int kRsThreads = kRadixThreads;
+constexpr int kRsItems = kRadixItems;
+constexpr int kRsTile = kRadixTile;
 
 __device__ __forceinline__ uint32_t f2o(float f) {
     uint32_t u = __float_as_uint(f);
@@ -833,11 +833,6 @@ int launch_trace_counters(const DevBvh &bvh, const void *rays, int64_t n, bool a
     if (any) k_trace_count<true><<<grid_for(n, 128), 128, 0, s>>>(bvh, (const float4 *)rays, n, d_counts, d_status);
     else k_trace_count<false><<<grid_for(n, 128), 128, 0, s>>>(bvh, (const float4 *)rays, n, d_counts, d_status);
     return cudaGetLastError() == cudaSuccess ? 0 : -2;
-}
-
-size_t radix_hist_entries(int64_t n) {
-    int64_t tiles = (n + kRsTile - 1) / kRsTile;
-    return (size_t)256 * (size_t)(tiles > 0 ? tiles : 1);
 }
 
 int radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tmp_keys, uint32_t *tmp_vals,

@@ -28,9 +28,16 @@ enum : int {
     } while (0)
 
 // ---- radix sort (lj_bvh.cu) ----
+// Keys per tile of the sort's block passes: 256 threads x 8 keys.
+constexpr int kRadixThreads = 256;
+constexpr int kRadixItems = 8;
+constexpr int kRadixTile = kRadixThreads * kRadixItems;
+// Histogram entries the sort needs for n keys: 256 buckets per tile.
+constexpr size_t radix_hist_entries(int64_t n) {
+    return (size_t)256 * (size_t)(n > 0 ? (n + kRadixTile - 1) / kRadixTile : 1);
+}
 // Stable LSD sort of (key, value) pairs on bits [0, 32) of the key, 8 bits
 // per pass.  tmp_keys/tmp_vals: n entries; hist: radix_hist_entries(n).
-size_t radix_hist_entries(int64_t n);
 int radix_sort_pairs(uint32_t *keys, uint32_t *vals, uint32_t *tmp_keys, uint32_t *tmp_vals,
                      uint32_t *hist, int64_t n, cudaStream_t s, std::string *err);
 

@@ -14,10 +14,14 @@
 // requests are rejected with LJ_ERR_SIZE_LIMIT before any work is queued.
 //
 // Host code cannot use the array's name as a device address (on the host it
-// names a shadow variable), so the first call on each device, with that
-// device current, asks the runtime for the address with cudaGetSymbolAddress
-// and caches it; later calls on that device reuse it.  Make that first call
-// before any stream capture begins.
+// names a shadow variable), so the first call in each CUDA context (the
+// runtime's primary context of a device, or a driver-API context the caller
+// made current) asks the runtime for the address with cudaGetSymbolAddress
+// and caches it under that context's unique id (cuCtxGetId); later calls in
+// the same context reuse it.  A context that is destroyed and created again
+// -- cudaDeviceReset, or cuCtxDestroy + cuCtxCreate -- has a new id, so the
+// first call after it looks the address up again.  Make the first call in
+// a context before any stream capture begins.
 //
 // All calls share the one array and it keeps whatever the previous call left
 // in it; each call initialises what it reads (the centroid bounds are reset,
@@ -27,6 +31,8 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "lj_host.h"
 
@@ -34,42 +40,84 @@ namespace {
 
 constexpr size_t kNoallocScratchBytes = (size_t)2 << 20;
 constexpr int64_t kNoallocMaxTris = LJ_NOALLOC_MORTON_MAX_TRIANGLES;
-constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
-std::mutex g_noalloc_mutex;
-void *g_noalloc_ptr[kMaxDevices] = {};
-
-size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 
 // bytes used for n triangles: bounds | centroids | keys | tmp keys | tmp values | histogram
-size_t noalloc_bytes(int64_t n) {
+constexpr size_t noalloc_bytes(int64_t n) {
     return 256 + round256(sizeof(float4) * n) + 3 * round256(sizeof(uint32_t) * n) +
            round256(sizeof(uint32_t) * lj::radix_hist_entries(n));
 }
+static_assert(noalloc_bytes(kNoallocMaxTris) <= kNoallocScratchBytes,
+              "scratch array too small for LJ_NOALLOC_MORTON_MAX_TRIANGLES");
 
 __global__ void k_noalloc_iota(uint32_t *p, int64_t n) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = (uint32_t)i;
 }
 
-// Device address of the scratch array on the current device (set-up on the
-// first call per device).
+// Driver entry points, fetched through the runtime so that the library does
+// not link libcuda itself (it must load, for its exports to be checked, on
+// machines without a GPU driver).
+typedef int (*CtxGetCurrentFn)(void **ctx);                       // cuCtxGetCurrent
+typedef int (*CtxGetIdFn)(void *ctx, unsigned long long *id);     // cuCtxGetId
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+std::once_flag g_entry_once;
+
+void load_entry_points() {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        g_ctx_get_current = (CtxGetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+        g_ctx_get_id = (CtxGetIdFn)f;
+    cudaGetLastError();
+}
+
+// Unique id of the CUDA context current on this thread; false if there is
+// none yet or the driver cannot say.
+bool current_context_id(unsigned long long *id) {
+    std::call_once(g_entry_once, load_entry_points);
+    if (!g_ctx_get_current || !g_ctx_get_id) return false;
+    void *ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != 0 || !ctx) return false;
+    return g_ctx_get_id(ctx, id) == 0;
+}
+
+std::mutex g_noalloc_mutex;
+std::vector<std::pair<unsigned long long, void *>> g_noalloc_ptr;   // context id -> address
+
+// Device address of the scratch array in the current context (looked up
+// with cudaGetSymbolAddress on the first call in each context).
 int scratch_address(unsigned char **out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return LJ_ERR_NO_DEVICE;
+    unsigned long long id = 0;
+    bool known = current_context_id(&id);
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return LJ_ERR_CUDA;
+    if (known) {
+        for (auto &e : g_noalloc_ptr) {
+            if (e.first == id) {
+                *out = (unsigned char *)e.second;
+                return LJ_OK;
+            }
         }
-        g_noalloc_ptr[dev] = p;
     }
-    *out = (unsigned char *)g_noalloc_ptr[dev];
+    // The lookup makes the runtime bind a context to this thread if none is
+    // current yet (the device's primary context), so the id is read again
+    // after it.
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver ? LJ_ERR_NO_DEVICE : LJ_ERR_CUDA;
+    }
+    if (current_context_id(&id)) g_noalloc_ptr.emplace_back(id, p);
+    *out = (unsigned char *)p;
     return LJ_OK;
 }
 
@@ -77,9 +125,6 @@ int scratch_address(unsigned char **out) {
 
 extern "C" int lj_gpu_morton_sort_noalloc(const float *d_tri_vertices, int64_t n, uint32_t *d_codes,
                                           uint32_t *d_order, void *stream) {
-    static_assert(256 + (size_t)16 * kNoallocMaxTris + 3 * (size_t)4 * kNoallocMaxTris +
-                          (size_t)4 * 256 * ((kNoallocMaxTris + 2047) / 2048) <= kNoallocScratchBytes,
-                  "scratch array too small for LJ_NOALLOC_MORTON_MAX_TRIANGLES");
     if (n < 0 || (n > 0 && (!d_tri_vertices || !d_codes || !d_order))) return LJ_ERR_INVALID_ARG;
     if (n > kNoallocMaxTris) return LJ_ERR_SIZE_LIMIT;
     if (n == 0) return LJ_OK;

@@ -67,6 +67,9 @@ def lib():
         L.lj_gpu_bsdf_batch.argtypes = [vp, C.POINTER(abi.lj_bsdf_batch), i64, vp]
         L.lj_gpu_light_sample_batch.argtypes = [vp, vp, vp, vp, vp, vp, vp, i64, vp]
         L.lj_gpu_phase_batch.argtypes = [vp, i32, C.c_float, vp, vp, vp, vp, vp, vp, i64, vp]
+        L.lj_gpu_light_emission_batch.argtypes = [vp, vp, vp, vp, vp, vp, i64, vp]
+        L.lj_gpu_camera_ray_batch.argtypes = [vp, vp, vp, vp, i64, vp]
+        L.lj_gpu_medium_batch.argtypes = [vp, i32, vp, vp, vp, vp, vp, i64, vp]
         L.lj_gpu_server_start.argtypes = [vp, C.POINTER(abi.lj_server_options), C.POINTER(vp)]
         L.lj_gpu_server_submit.argtypes = [vp, vp, C.POINTER(abi.lj_job_desc), C.POINTER(i64)]
         L.lj_gpu_server_poll.argtypes = [vp, i64, C.POINTER(abi.lj_job_status)]
@@ -274,6 +277,34 @@ class GpuScene:
         self.ctx.check(lib().lj_gpu_light_sample_batch(self.h, _ptr(ref_points), _ptr(rnd), _ptr(lid),
                                                        _ptr(pt), _ptr(nr), _ptr(pdf), n, stream))
         return lid, pt, nr, pdf
+
+    def light_emission(self, light_ids, view_dirs, points, normals, stream=None):
+        """emission(light, view_dir, footprint, point_on_light) per query
+        (int32 ids, (n, 3) float32 tensors) -> (n, 3)."""
+        import torch
+        out = torch.empty((light_ids.shape[0], 3), dtype=torch.float32, device=light_ids.device)
+        self.ctx.check(lib().lj_gpu_light_emission_batch(self.h, _ptr(light_ids), _ptr(view_dirs), _ptr(points),
+                                                         _ptr(normals), _ptr(out), light_ids.shape[0], stream))
+        return out
+
+    def camera_rays(self, screen, stream=None):
+        """sample_primary at (n, 2) screen positions -> (origins, directions)."""
+        import torch
+        n = screen.shape[0]
+        org = torch.empty((n, 3), dtype=torch.float32, device=screen.device)
+        d = torch.empty((n, 3), dtype=torch.float32, device=screen.device)
+        self.ctx.check(lib().lj_gpu_camera_ray_batch(self.h, _ptr(screen), _ptr(org), _ptr(d), n, stream))
+        return org, d
+
+    def medium(self, medium_id, points, dirs, stream=None):
+        """(sigma_a, sigma_s) at `points` and the majorant along rays
+        (points, dirs) of medium `medium_id`, each (n, 3)."""
+        import torch
+        n = points.shape[0]
+        out = [torch.empty((n, 3), dtype=torch.float32, device=points.device) for _ in range(3)]
+        self.ctx.check(lib().lj_gpu_medium_batch(self.h, int(medium_id), _ptr(points), _ptr(dirs), _ptr(out[0]),
+                                                 _ptr(out[1]), _ptr(out[2]), n, stream))
+        return tuple(out)
 
     def trace_counters(self, rays, any_hit=False):
         """(nodes fetched, primitives tested) over a batch of rays."""

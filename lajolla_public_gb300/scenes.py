@@ -72,6 +72,27 @@ def rgbe_image(rng, h, w, exponent=128):
     return (k * 2.0 ** (exponent - 136)).astype(np.float32)
 
 
+def rgbe_sky(rng, h, w, exponent=129):
+    """Lat-long sky (y up, lajolla's mapping src/lights/envmap.inl:7-20)
+    whose texels survive a Radiance RGBE round trip exactly: every channel is
+    k * 2^(exponent - 136) with k in [16, 255].  A horizon-to-zenith gradient
+    over a dim ground plus a seeded sun lobe at k = 255, 16x the darkest
+    texel."""
+    u = (np.arange(w) + 0.5) / w
+    v = (np.arange(h) + 0.5) / h
+    az, el = u * 2 * np.pi, v * np.pi
+    dirs = np.stack([np.sin(az)[None, :] * np.sin(el)[:, None], np.cos(el)[:, None] * np.ones((1, w)),
+                     -np.cos(az)[None, :] * np.sin(el)[:, None]], axis=-1)
+    up = np.clip(dirs[..., 1], 0, 1)[..., None]
+    sky = np.where(dirs[..., 1:2] > 0, np.array([120, 110, 100]) * (1 - up) + np.array([40, 70, 150]) * up,
+                   np.array([24, 20, 16]))
+    sun_el, sun_az = np.radians(rng.uniform(30, 60)), rng.uniform(0, 2 * np.pi)
+    sd = np.array([np.sin(sun_az) * np.cos(sun_el), np.sin(sun_el), -np.cos(sun_az) * np.cos(sun_el)])
+    lobe = np.exp(-(1 - np.clip(dirs @ sd, -1, 1)) / (1 - np.cos(np.radians(12.0))))[..., None]
+    k = np.clip(np.rint(sky + (255 - sky) * lobe), 16, 255)
+    return (k * 2.0 ** (exponent - 136)).astype(np.float32)
+
+
 def write_hdr(path, img):
     """Flat (not run-length encoded) Radiance RGBE file of an image made by
     rgbe_image; row 0 of `img` is the first scanline."""
@@ -91,6 +112,23 @@ def write_hdr(path, img):
         f.write(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n")
         f.write(f"-Y {h} +X {w}\n".encode())
         f.write(rgbe.tobytes())
+
+
+def write_vol(path, data, p_min, p_max):
+    """Binary grid volume in the layout lajolla's loader reads
+    (src/volume.cpp:6-104): 'VOL', version byte 3, int32 type 1 (FP32),
+    int32 x, y, z resolution and channel count, the grid's box as six FP32
+    (min xyz, max xyz), then the FP32 voxels, x fastest, channels
+    interleaved.  `data` is (z, y, x, channels)."""
+    data = np.ascontiguousarray(data, np.float32)
+    if data.ndim == 3:
+        data = data[..., None]
+    nz, ny, nx, ch = data.shape
+    with open(path, "wb") as f:
+        f.write(b"VOL" + bytes([3]))
+        f.write(np.array([1, nx, ny, nz, ch], "<i4").tobytes())
+        f.write(np.array(list(p_min) + list(p_max), "<f4").tobytes())
+        f.write(data.astype("<f4").tobytes())
 
 
 def lambertian(rgb):
@@ -395,6 +433,18 @@ class Scene:
                 em = self.lights[s["area_light_id"]]["intensity"]
                 out.append(f'    <emitter type="area"><rgb name="radiance" value="{vec(em)}"/></emitter>')
             out.append('  </shape>')
+        # the parser numbers lights in document order (area lights with their
+        # shapes), so the envmap, the last light here, comes after the shapes
+        if self.envmap_light_id >= 0:
+            if self.envmap_light_id != len(self.lights) - 1:
+                raise ValueError("write_mitsuba: the envmap must be the last light")
+            l = self.lights[self.envmap_light_id]
+            fn = os.path.join(directory, f'{name}_img{l["image_id"]}.hdr')
+            out += ['  <emitter type="envmap">', f'    <string name="filename" value="{fn}"/>',
+                    '    <transform name="toWorld">',
+                    '      <matrix value="' + " ".join(r(float(x)) for x in np.asarray(l["to_world"]).reshape(-1))
+                    + '"/>', '    </transform>', f'    <float name="scale" value="{r(float(l.get("scale", 1.0)))}"/>',
+                    '  </emitter>']
         out.append('</scene>')
         path = os.path.join(directory, f"{name}.xml")
         with open(path, "w") as f:
@@ -493,6 +543,47 @@ def textured_scene(seed=0, width=64, height=64, spp=16, max_depth=6, integrator=
     sc.add_sphere([-0.35, 1.45, -0.3], 0.22, sc.add_material(dict(type=abi.LJ_MAT_LAMBERTIAN, eta=1.0,
                                                                   tex=[image_tex(1, 3.0, 2.0)])))
     return sc
+
+
+def envmap_scene(seed=0, width=64, height=48, spp=16, max_depth=6, with_area_light=True):
+    """Seeded outdoor scene lit by a rotated HDR envmap (scale 2, an
+    RGBE-exact sky from rgbe_sky) and, with `with_area_light`, a small quad
+    light: a Lambertian ground quad, a RoughPlastic analytic sphere, a
+    Lambertian box and a smooth-shaded RoughPlastic icosphere.  The camera
+    sees the sky above the horizon, so the miss path's emission shows."""
+    rng = np.random.default_rng(seed)
+    sc = Scene(width, height, spp, max_depth, look_at([0.4, 1.2, 4.0], [0, 0.6, 0], [0, 1, 0]), 50.0)
+    ground = sc.add_material(lambertian([f32(x) for x in rng.uniform(0.3, 0.7, 3)]))
+    sc.add_mesh(*_quad([-4, 0, 4], [4, 0, 4], [4, 0, -4], [-4, 0, -4]), ground)
+    plastic = sc.add_material(roughplastic([f32(x) for x in rng.uniform(0.2, 0.8, 3)], [0.8, 0.8, 0.8],
+                                           f32(rng.uniform(0.05, 0.3)), 1.5))
+    sc.add_sphere([-0.7, 0.5, 0.2], 0.5, plastic)
+    pos, idx = _box([0.7, 0.35, -0.3], [0.7, 0.7, 0.7], float(rng.uniform(10, 40)))
+    sc.add_mesh(pos, idx, sc.add_material(lambertian([f32(x) for x in rng.uniform(0.2, 0.8, 3)])))
+    v, f = icosphere(2)
+    sc.add_mesh(v * 0.3 + np.array([0.2, 0.3, 0.9]), f,
+                sc.add_material(roughplastic([0.3, 0.5, 0.7], [0.9, 0.9, 0.9], 0.2, 1.45)), normals=v)
+    if with_area_light:
+        lpos, lidx = _quad([1.2, 2.0, 0.5], [1.6, 2.0, 0.5], [1.6, 2.0, 0.1], [1.2, 2.0, 0.1])
+        sc.add_mesh(lpos, lidx, sc.add_material(lambertian([0.5, 0.5, 0.5])), emission=[12, 10, 8])
+    sc.images.append(rgbe_sky(rng, 32, 64))
+    # FP32 entries: lajolla's parser reads matrices with std::stof
+    tw = _rotation(float(rng.uniform(20, 70)), [0.1, 1.0, 0.2]).astype(np.float32).astype(np.float64)
+    sc.lights.append(dict(kind=abi.LJ_LIGHT_ENVMAP, image_id=len(sc.images) - 1, scale=2.0, to_world=tw,
+                          to_local=np.linalg.inv(tw)))
+    sc.envmap_light_id = len(sc.lights) - 1
+    return sc
+
+
+def _rotation(angle_deg, axis):
+    """4x4 rotation about `axis` (src/transform.cpp:21-56's rotate)."""
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    s, c = np.sin(np.radians(angle_deg)), np.cos(np.radians(angle_deg))
+    m = np.eye(4)
+    m[:3, :3] = c * np.eye(3) + (1 - c) * np.outer(a, a) + s * np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]],
+                                                                         [-a[1], a[0], 0]])
+    return m
 
 
 def triangle_soup(seed, n_tris, offset_sigma=0.01):

@@ -14,18 +14,24 @@
 //                                  pdf_point_on_light + emission on a scene with a
 //                                  triangle-mesh light, a sphere light and an envmap
 //   golden_harness camera in out   sample_primary (src/camera.cpp:23-47)
+//   golden_harness medium in out d1.vol d3.vol a3.vol
+//                                  get_sigma_a / get_sigma_s / get_majorant
+//                                  (src/medium.cpp:27-37) on grid volumes the
+//                                  reference's .vol loader reads (src/volume.cpp)
 //
 // Input/output files are flat little-endian arrays; layouts are documented per
 // mode below and mirrored in make_golden.py.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <vector>
 
 #include "camera.h"
 #include "light.h"
 #include "material.h"
+#include "medium.h"
 #include "pcg.h"
 #include "phase_function.h"
 #include "scene.h"
@@ -209,9 +215,39 @@ static void run_camera(const std::vector<double> &in, std::vector<double> &out) 
     }
 }
 
+// medium: argv = d1.vol (1 channel), d3.vol (3 channels), a3.vol (3 channels)
+//   in: header s0, s1, albedo0[3], sigma_a[3], sigma_s[3] (11), then records
+//   p[3], d[3] (6)
+//   out per record, for media 0, 1, 2: sigma_a[3], sigma_s[3], majorant[3] (27)
+// Media (as parse_medium builds them, src/parsers/parse_scene.cpp:694-741):
+//   0 heterogeneous: density = d1.vol with scale s0, constant albedo0
+//   1 heterogeneous: density = d3.vol with scale s1, albedo = a3.vol
+//   2 homogeneous sigma_a, sigma_s
+// The majorant is taken along the ray (p, d) with tnear 0, tfar = inf.
+static void run_medium(const std::vector<double> &in, std::vector<double> &out, char **vols) {
+    VolumeSpectrum d1 = load_volume_from_file<Spectrum>(vols[0]);
+    VolumeSpectrum d3 = load_volume_from_file<Spectrum>(vols[1]);
+    VolumeSpectrum a3 = load_volume_from_file<Spectrum>(vols[2]);
+    set_scale(d1, in[0]);
+    set_scale(d3, in[1]);
+    std::vector<Medium> media = {
+        HeterogeneousMedium{{HenyeyGreenstein{0.3}}, ConstantVolume<Spectrum>{Vector3{in[2], in[3], in[4]}}, d1},
+        HeterogeneousMedium{{HenyeyGreenstein{0.3}}, a3, d3},
+        HomogeneousMedium{{IsotropicPhase{}}, Vector3{in[5], in[6], in[7]}, Vector3{in[8], in[9], in[10]}}};
+    for (size_t k = 11; k + 6 <= in.size(); k += 6) {
+        Vector3 p{in[k], in[k + 1], in[k + 2]}, d{in[k + 3], in[k + 4], in[k + 5]};
+        Ray r{p, d, Real(0), std::numeric_limits<Real>::infinity()};
+        for (const Medium &m : media) {
+            Spectrum sa = get_sigma_a(m, p), ss = get_sigma_s(m, p), mj = get_majorant(m, r);
+            out.insert(out.end(), {sa.x, sa.y, sa.z, ss.x, ss.y, ss.z, mj.x, mj.y, mj.z});
+        }
+    }
+}
+
 int main(int argc, char **argv) {
-    if (argc != 4) {
-        fprintf(stderr, "usage: golden_harness <bsdf|phase|table|pcg|light|camera> in out\n");
+    if (argc < 4 || (std::string(argv[1]) == "medium" ? argc != 7 : argc != 4)) {
+        fprintf(stderr, "usage: golden_harness <bsdf|phase|table|pcg|light|camera> in out\n"
+                        "       golden_harness medium in out d1.vol d3.vol a3.vol\n");
         return 2;
     }
     std::string mode = argv[1];
@@ -222,6 +258,7 @@ int main(int argc, char **argv) {
     else if (mode == "pcg") run_pcg(in, out);
     else if (mode == "light") run_light(in, out);
     else if (mode == "camera") run_camera(in, out);
+    else if (mode == "medium") run_medium(in, out, argv + 4);
     else { fprintf(stderr, "unknown mode\n"); return 2; }
     write_all(argv[3], out);
     return 0;

@@ -19,6 +19,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <optional>
 #include <thread>
@@ -2264,6 +2265,41 @@ int ljo_light_sample_batch(void *s, const float *ref, const float *rnd, int32_t 
         out_point[i * 3] = pn.p.x; out_point[i * 3 + 1] = pn.p.y; out_point[i * 3 + 2] = pn.p.z;
         out_normal[i * 3] = pn.n.x; out_normal[i * 3 + 1] = pn.n.y; out_normal[i * 3 + 2] = pn.n.z;
         out_pdf[i] = sc->light_dist.pmf[lid] * pdf_point_on_light(*sc, l, pn, p);
+    }
+    return 0;
+}
+
+// emission(light, view_dir, 0, point_on_light) per query (src/light.cpp:56-77),
+// matching lj_gpu_light_emission_batch: out = RGB.
+int ljo_light_emission_batch(void *s, const int32_t *light, const double *view, const double *point,
+                             const double *normal, int64_t n, double *out) {
+    Scene *sc = (Scene *)s;
+    for (int64_t i = 0; i < n; i++) {
+        const LightS &l = sc->lights[light[i]];
+        PN pn{V3{point[3 * i], point[3 * i + 1], point[3 * i + 2]},
+              V3{normal[3 * i], normal[3 * i + 1], normal[3 * i + 2]}};
+        V3 e = light_emission(*sc, l, V3{view[3 * i], view[3 * i + 1], view[3 * i + 2]}, 0, pn);
+        out[3 * i] = e.x; out[3 * i + 1] = e.y; out[3 * i + 2] = e.z;
+    }
+    return 0;
+}
+
+// get_sigma_a / get_sigma_s at points and get_majorant along the rays
+// (point, dir, tnear 0, tfar inf) of medium `mid` (src/medium.cpp:27-37),
+// matching lj_gpu_medium_batch: each output RGB per query.
+int ljo_medium_batch(void *s, int mid, const double *pts, const double *dirs, int64_t n, double *sa, double *ss,
+                     double *maj) {
+    Scene *sc = (Scene *)s;
+    const MediumS &m = sc->media[mid];
+    for (int64_t i = 0; i < n; i++) {
+        V3 p{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+        V3 vs, va;
+        sigmas(m, p, vs, va);
+        Ray r{p, V3{dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]}, 0, std::numeric_limits<double>::infinity()};
+        V3 mj = majorant(m, r);
+        sa[3 * i] = va.x; sa[3 * i + 1] = va.y; sa[3 * i + 2] = va.z;
+        ss[3 * i] = vs.x; ss[3 * i + 1] = vs.y; ss[3 * i + 2] = vs.z;
+        maj[3 * i] = mj.x; maj[3 * i + 1] = mj.y; maj[3 * i + 2] = mj.z;
     }
     return 0;
 }

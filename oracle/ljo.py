@@ -6,6 +6,7 @@ __graft_entry__.smoke() and bench.py's CPU-baseline leg import this module.
 """
 import ctypes as C
 import os
+import re
 import subprocess
 
 import numpy as np
@@ -25,9 +26,20 @@ def build():
     subprocess.run(["make", "-C", HERE, "-s", "port"], check=True)
 
 
+def reference_dir():
+    """Directory of the reference sources: $LJ_REFERENCE_DIR, else the
+    default the oracle Makefile names.  None where no sources are there (the
+    reference exists only in the development container)."""
+    d = os.environ.get("LJ_REFERENCE_DIR")
+    if not d:
+        m = re.search(r"^LJ_REFERENCE_DIR \?= *(\S+)", open(os.path.join(HERE, "Makefile")).read(), re.M)
+        d = m.group(1) if m else ""
+    return d if d and os.path.isdir(os.path.join(d, "src")) else None
+
+
 def build_ref():
-    """Compile the reference renderer + golden harness from /root/reference
-    (development container only)."""
+    """Compile the reference renderer + golden harness from the reference
+    sources (reference_dir(); development container only)."""
     subprocess.run(["make", "-C", HERE, "-s", "-j8", "ref"], check=True)
 
 
@@ -57,6 +69,8 @@ def lib():
         L.ljo_mipmap_lookup.argtypes = [vp, C.c_int, C.c_int, vp, i64, vp, vp]
         L.ljo_filter_sample.argtypes = [C.c_int, C.c_double, vp, i64, vp]
         L.ljo_camera_batch.argtypes = [C.POINTER(abi.lj_camera_desc), vp, i64, vp]
+        L.ljo_light_emission_batch.argtypes = [vp, vp, vp, vp, vp, i64, vp]
+        L.ljo_medium_batch.argtypes = [vp, C.c_int, vp, vp, i64, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -119,6 +133,20 @@ class OracleScene:
         pt, nr, pdf = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
         lib().ljo_light_sample_batch(self.h, _p(ref_points), _p(rnd), _p(lid), _p(pt), _p(nr), _p(pdf), n)
         return lid, pt, nr, pdf
+
+    def light_emission(self, light_ids, view_dirs, points, normals):
+        lid = np.ascontiguousarray(light_ids, np.int32)
+        v, p, nr = (np.ascontiguousarray(a, np.float64) for a in (view_dirs, points, normals))
+        out = np.zeros((len(lid), 3))
+        lib().ljo_light_emission_batch(self.h, _p(lid), _p(v), _p(p), _p(nr), len(lid), _p(out))
+        return out
+
+    def medium(self, medium_id, points, dirs):
+        """(sigma_a, sigma_s, majorant) of a medium, as lj_gpu_medium_batch."""
+        p, d = np.ascontiguousarray(points, np.float64), np.ascontiguousarray(dirs, np.float64)
+        out = [np.zeros((len(p), 3)) for _ in range(3)]
+        lib().ljo_medium_batch(self.h, int(medium_id), _p(p), _p(d), len(p), _p(out[0]), _p(out[1]), _p(out[2]))
+        return tuple(out)
 
 
 def morton(tri_vertices):

@@ -26,11 +26,11 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "golden_harness")
 
 
-def harness(mode, inp):
+def harness(mode, inp, extra=()):
     with tempfile.TemporaryDirectory() as d:
         fi, fo = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
         np.asarray(inp, np.float64).tofile(fi)
-        subprocess.run([HARNESS, mode, fi, fo], check=True)
+        subprocess.run([HARNESS, mode, fi, fo] + list(extra), check=True)
         return np.fromfile(fo, np.float64)
 
 
@@ -179,6 +179,67 @@ def make_camera(rng):
     return flat
 
 
+def make_medium(rng):
+    """get_sigma_a / get_sigma_s / get_majorant (src/medium.cpp:27-37) of two
+    heterogeneous media over grid volumes read by the reference's .vol loader
+    (src/volume.cpp:6-104) from files written by scenes.write_vol, and one
+    homogeneous medium.  Medium 0: a one-channel density grid (the loader
+    repeats it into three channels) with scale s0 and a constant albedo;
+    medium 1: a three-channel density grid with scale s1 and a three-channel
+    albedo grid on a box of its own.  Half the points fill a box larger than
+    the grids' (many fall outside: zero density), half a box mostly inside
+    them; directions are uniform on the
+    sphere, and each majorant is taken along the ray (point, direction)."""
+    grids = {
+        "d1": dict(data=f32(rng.uniform(0.1, 3.0, (6, 5, 7, 1))), p_min=f32([-0.6, -0.3, -0.4]),
+                   p_max=f32([0.7, 0.5, 0.9])),
+        "d3": dict(data=f32(rng.uniform(0.1, 3.0, (4, 6, 5, 3))), p_min=f32([-0.5, -0.6, -0.5]),
+                   p_max=f32([0.6, 0.4, 0.3])),
+        "a3": dict(data=f32(rng.uniform(0.1, 0.95, (5, 4, 4, 3))), p_min=f32([-0.7, -0.5, -0.6]),
+                   p_max=f32([0.5, 0.6, 0.5])),
+    }
+    s0, s1 = 2.5, 0.75   # exact in FP32, the type lj_volume_desc.scale has
+    albedo0 = f32(rng.uniform(0.2, 0.9, 3))
+    sigma_a, sigma_s = f32(rng.uniform(0.1, 2.0, 3)), f32(rng.uniform(0.1, 2.0, 3))
+    n = 800
+    pts = f32(np.concatenate([rng.uniform(-1.0, 1.0, (n // 2, 3)), rng.uniform(-0.5, 0.5, (n - n // 2, 3))]))
+    dirs = f32(sphere_dirs(rng, n))
+    header = np.concatenate([[s0, s1], albedo0, sigma_a, sigma_s])
+    with tempfile.TemporaryDirectory() as d:
+        paths = []
+        for k in ("d1", "d3", "a3"):
+            paths.append(os.path.join(d, k + ".vol"))
+            scenes.write_vol(paths[-1], grids[k]["data"], grids[k]["p_min"], grids[k]["p_max"])
+        out = harness("medium", np.concatenate([header, np.concatenate([pts, dirs], 1).reshape(-1)]), paths)
+    out = out.reshape(n, 3, 9)
+    flat = dict(points=pts, dirs=dirs, s0=s0, s1=s1, albedo0=albedo0, sigma_a=sigma_a, sigma_s=sigma_s,
+                outputs=out)
+    for k, g in grids.items():
+        for kk, vv in g.items():
+            flat[k + "_" + kk] = vv
+    return flat
+
+
+def medium_scene(g):
+    """A scene holding the three media of the `medium` golden (a single
+    triangle and no lights: only the media are queried)."""
+    sc = scenes.Scene(8, 8, 1, 2, np.eye(4), 45.0, integrator=abi.LJ_INTEGRATOR_VOLPATH, vol_path_version=6)
+    m = sc.add_material(scenes.lambertian([0.5, 0.5, 0.5]))
+    sc.add_mesh(np.array([[5, 5, 5], [6, 5, 5], [5, 6, 5]], np.float32), np.array([[0, 1, 2]]), m)
+
+    def grid(k, scale=1.0):
+        return dict(kind=abi.LJ_VOL_GRID, data=g[k + "_data"], p_min=list(g[k + "_p_min"]),
+                    p_max=list(g[k + "_p_max"]), scale=float(scale))
+    sc.media.append(dict(kind=abi.LJ_MEDIUM_HETEROGENEOUS, phase_kind=abi.LJ_PHASE_HG, g=0.3,
+                         albedo=dict(kind=abi.LJ_VOL_CONST, value=list(g["albedo0"])),
+                         density=grid("d1", g["s0"])))
+    sc.media.append(dict(kind=abi.LJ_MEDIUM_HETEROGENEOUS, phase_kind=abi.LJ_PHASE_HG, g=0.3,
+                         albedo=grid("a3"), density=grid("d3", g["s1"])))
+    sc.media.append(dict(kind=abi.LJ_MEDIUM_HOMOGENEOUS, phase_kind=abi.LJ_PHASE_ISOTROPIC,
+                         sigma_a=list(g["sigma_a"]), sigma_s=list(g["sigma_s"])))
+    return sc
+
+
 def mixed_scene(seed, w, h, spp, max_depth):
     """Cornell box whose boxes are RoughPlastic / RoughDielectric, plus a
     sphere light: exercises every implemented reference material."""
@@ -201,6 +262,9 @@ RENDER_CASES = {
     # image and checkerboard textures, vertex normals, UVs; the reference's
     # Disney materials are stubs, so this path case has none
     "textured": lambda: scenes.textured_scene(4, 40, 32, 16, 6, clearcoat=False),
+    # a rotated HDR envmap (miss-path emission, table_dist sampling) beside a
+    # quad light, over Lambertian and RoughPlastic surfaces
+    "envmap": lambda: scenes.envmap_scene(5, 40, 32, 16, 6),
 }
 
 # aux_render (src/render.cpp:12-69), one case per auxiliary integrator
@@ -224,21 +288,25 @@ def make_renders(cases=RENDER_CASES):
     return out
 
 
-def main():
+def main(which=()):
+    """Regenerates every fixture, or only those named (e.g. `medium renders`):
+    the functions share one seeded stream in a fixed order, so each fixture
+    comes out the same whichever subset is written."""
     ljo.build_ref()
     rng = np.random.default_rng(20261203)
-    np.savez_compressed(os.path.join(OUT, "bsdf.npz"), **make_bsdf(rng))
-    np.savez_compressed(os.path.join(OUT, "phase.npz"), **make_phase(rng))
-    np.savez_compressed(os.path.join(OUT, "table.npz"), **make_table(rng))
-    np.savez_compressed(os.path.join(OUT, "pcg.npz"), **make_pcg())
-    np.savez_compressed(os.path.join(OUT, "light.npz"), **make_light(rng))
-    np.savez_compressed(os.path.join(OUT, "camera.npz"), **make_camera(rng))
-    np.savez_compressed(os.path.join(OUT, "renders.npz"), **make_renders())
-    np.savez_compressed(os.path.join(OUT, "aux.npz"), **make_renders(AUX_CASES))
+    makers = [("bsdf", lambda: make_bsdf(rng)), ("phase", lambda: make_phase(rng)),
+              ("table", lambda: make_table(rng)), ("pcg", make_pcg), ("light", lambda: make_light(rng)),
+              ("camera", lambda: make_camera(rng)), ("renders", make_renders),
+              ("aux", lambda: make_renders(AUX_CASES)),
+              ("medium", lambda: make_medium(np.random.default_rng(20261204)))]
+    for name, mk in makers:
+        data = mk()
+        if not which or name in which:
+            np.savez_compressed(os.path.join(OUT, name + ".npz"), **data)
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -43,3 +43,19 @@ def rel_err(a, b, floor):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return np.abs(a - b) / np.maximum(np.abs(b), floor)
+
+
+def emission_queries(g):
+    """(light ids, points, normals, view directions) of the light golden's
+    samples, with the view direction its harness used: from the reference
+    point's side for area lights, the stored "from light" direction for the
+    envmap (golden_harness.cpp, mode light)."""
+    out = g["outputs"]
+    ref = g["inputs"][:, 0:3].astype(np.float64)
+    lid = out[:, 0].astype(np.int32)
+    pt, nr = out[:, 1:4], out[:, 4:7]
+    d = ref - pt
+    view = d / np.linalg.norm(d, axis=1, keepdims=True)
+    env = lid == 2
+    view[env] = nr[env]
+    return lid, pt, nr, view

@@ -35,7 +35,8 @@ def sample_match(sc, ctx, sample_index, rtol, seed=11):
 # Per-path relative tolerance: 1e-3 for diffuse scenes; 1e-2 where glossy
 # lobes (GGX with alpha^2 ~ 1e-3) amplify FP32 rounding of the half vector.
 # A logic error changes a path's radiance by O(1), not by these amounts.
-@pytest.mark.parametrize("case,rtol", [("cbox", 1e-3), ("cbox_rr", 1e-3), ("mixed", 1e-2), ("textured", 1e-3)])
+@pytest.mark.parametrize("case,rtol", [("cbox", 1e-3), ("cbox_rr", 1e-3), ("mixed", 1e-2), ("textured", 1e-3),
+                                       ("envmap", 1e-2)])
 def test_per_sample_parity_with_oracle(ctx, case, rtol):
     sc = make_golden.RENDER_CASES[case]()
     for k in (0, 5):
@@ -44,7 +45,7 @@ def test_per_sample_parity_with_oracle(ctx, case, rtol):
     assert st.samples == sc.width * sc.height
 
 
-@pytest.mark.parametrize("case", ["cbox", "mixed", "textured"])
+@pytest.mark.parametrize("case", ["cbox", "mixed", "textured", "envmap"])
 def test_statistical_parity_with_reference_render(ctx, case):
     ref = ljtest.golden("renders")[case].astype(np.float64)
     sc = make_golden.RENDER_CASES[case]()

@@ -83,3 +83,25 @@ def test_volpath_versions_1_to_5_are_rejected(ctx):
     with pytest.raises(gpu.LjError) as e:
         g.render(seed=1)
     assert e.value.code == abi.LJ_ERR_UNSUPPORTED
+
+
+def test_volpath_without_media_equals_path_tracer_on_gpu(ctx):
+    """With no participating media the volumetric path tracer (v6) is an
+    unbiased estimator of the same image as the path tracer
+    (src/path_tracing.h): per pixel within 4 standard errors, and the image
+    means within 4 standard errors.  Standard errors come from the oracle's
+    per-sample variance of the path tracer."""
+    sc = scenes.cornell_box(seed=1, width=16, height=16, spp=8, max_depth=6)
+    n = 4096
+    mp, _ = gpu.GpuScene(ctx, sc).render(seed=1, spp=n)
+    sc.integrator, sc.vol_path_version = abi.LJ_INTEGRATOR_VOLPATH, 6
+    mv, _ = gpu.GpuScene(ctx, sc).render(seed=2, spp=n)
+    sc.integrator = abi.LJ_INTEGRATOR_PATH
+    s = ljo.OracleScene(sc).render_samples(np.arange(16 * 16, dtype=np.int32), 256, seed=3)
+    var = s.var(axis=1).reshape(16, 16, 3)
+    se = np.sqrt(2 * var / n) + 1e-6
+    z = np.abs(mp - mv) / se
+    assert (z < 4).all(axis=2).mean() >= 0.99, z.max()
+    se_mean = np.sqrt(2 * var.mean(axis=(0, 1)) / (n * 256))
+    assert np.all(np.abs(mp.mean(axis=(0, 1)) - mv.mean(axis=(0, 1))) <= 4 * se_mean), (mp.mean((0, 1)),
+                                                                                          mv.mean((0, 1)))

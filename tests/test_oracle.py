@@ -150,6 +150,31 @@ def test_light_sampling_matches_reference():
     np.testing.assert_allclose(pdf, out[:, 7], rtol=1e-9)
 
 
+def test_light_emission_matches_reference():
+    """emission (src/light.cpp:56-77) of the reference's sampled light points:
+    one-sided area-light radiance and the envmap's lookup
+    (src/lights/envmap.inl:44-73), on the light golden's outputs."""
+    g = ljtest.golden("light")
+    o = ljo.OracleScene(ljtest.light_scene(g["env"], g["to_world"]))
+    lid, pt, nr, view = ljtest.emission_queries(g)
+    np.testing.assert_allclose(o.light_emission(lid, view, pt, nr), g["outputs"][:, 8:11], rtol=1e-9, atol=1e-12)
+    assert (g["outputs"][lid == 2, 8:11] > 0).all()   # envmap samples are lit
+
+
+def test_medium_matches_reference():
+    """get_sigma_a / get_sigma_s / get_majorant (src/medium.cpp:27-37) with
+    the GridVolume lookup and slab test (src/volume.h:44-144) on grids the
+    reference's .vol loader read, and a homogeneous medium."""
+    g = ljtest.golden("medium")
+    o = ljo.OracleScene(make_golden.medium_scene(g))
+    for k in range(3):
+        sa, ss, mj = o.medium(k, g["points"], g["dirs"])
+        want = g["outputs"][:, k]
+        np.testing.assert_allclose(sa, want[:, 0:3], rtol=1e-6, atol=1e-12)
+        np.testing.assert_allclose(ss, want[:, 3:6], rtol=1e-6, atol=1e-12)
+        np.testing.assert_array_equal(mj, want[:, 6:9])
+
+
 @pytest.mark.parametrize("case", sorted(make_golden.RENDER_CASES))
 def test_render_matches_reference_sample_for_sample(case):
     """Tile-mode RNG reproduces the reference renderer's own image exactly

@@ -32,11 +32,14 @@ def _tris(seed, n):
     return torch.from_numpy(pos[idx].reshape(-1, 9).copy()).cuda()
 
 
-def _run_noalloc(tri):
+def _run_noalloc(tri, stream=None):
     n = tri.shape[0]
     codes = torch.full((n,), -1, dtype=torch.int32, device="cuda")
     order = torch.full((n,), -1, dtype=torch.int32, device="cuda")
-    rc = _noalloc()(tri.data_ptr(), n, codes.data_ptr(), order.data_ptr(), None)
+    handle = None if stream is None else stream.cuda_stream
+    if stream is not None:
+        stream.wait_stream(torch.cuda.current_stream())
+    rc = _noalloc()(tri.data_ptr(), n, codes.data_ptr(), order.data_ptr(), handle)
     assert rc == abi.LJ_OK, rc
     torch.cuda.synchronize()
     return codes.cpu().numpy(), order.cpu().numpy()
@@ -61,3 +64,15 @@ def test_noalloc_rejects_sizes_beyond_its_fixed_scratch(ctx):
     assert rc == abi.LJ_ERR_SIZE_LIMIT
     torch.cuda.synchronize()
     assert bool((codes == 7).all()) and bool((order == 7).all())
+
+
+def test_noalloc_smallest_sizes_and_a_side_stream(ctx):
+    # n = 1 skips the sort (only the codes and the identity order are
+    # written), n = 2 sorts one pair; then a call on a stream of its own
+    side = torch.cuda.Stream()
+    for seed, n, stream in ((21, 1, None), (22, 2, None), (23, 2, None), (24, 5000, side), (25, 1, side)):
+        tri = _tris(seed, n)
+        got_codes, got_order = _run_noalloc(tri, stream)
+        want_codes, want_order = ctx.morton_sort(tri)
+        np.testing.assert_array_equal(got_codes, want_codes.cpu().numpy())
+        np.testing.assert_array_equal(got_order, want_order.cpu().numpy())
