@@ -44,7 +44,8 @@ extern "C" {
 /* 2: lj_volume_desc.channel_scale, the volumetric kernel classes
  * (LJ_KERNEL_MEDIUM, LJ_KERNEL_NEE) and the volumetric counters of
  * lj_server_stats
- * 3: the emission, camera-ray and medium batches */
+ * 3: the emission, camera-ray and medium batches; LJ_RENDER_COUNT_BVH and
+ * the lj_stats.bvh_* counters */
 #define LJ_GPU_ABI_VERSION 3
 
 /* ---- error codes -------------------------------------------------------- */
@@ -272,6 +273,10 @@ int lj_gpu_scene_info(lj_scene *scene, lj_scene_info *out);
 
 /* lj_render_params.flags */
 #define LJ_RENDER_PROFILE 1      /* time each kernel class with CUDA events (adds event records) */
+#define LJ_RENDER_COUNT_BVH 2    /* after each traversal launch, an instrumented traversal of every
+                                    LJ_COUNT_BVH_STRIDE-th queue entry counts the BVH bytes it reads
+                                    (lj_stats.bvh_*; measurement only: extra launches) */
+#define LJ_COUNT_BVH_STRIDE 16
 
 typedef struct lj_render_params {
     uint64_t seed;               /* job seed; RNG is keyed on (seed, pixel, sample) */
@@ -306,6 +311,11 @@ typedef struct lj_stats {
     int64_t real_collisions;     /* volpath: real scattering events           */
     double class_ms[LJ_KERNEL_CLASSES];        /* LJ_RENDER_PROFILE only */
     int64_t class_launches[LJ_KERNEL_CLASSES]; /* LJ_RENDER_PROFILE only */
+    /* LJ_RENDER_COUNT_BVH only, [0] closest-hit queues, [1] shadow-ray
+     * queues (the path tracer's; the volumetric NEE loop is not counted):
+     * rays counted, 80-byte wide nodes fetched and 48-byte leaf records
+     * tested by those rays. */
+    int64_t bvh_rays[2], bvh_nodes[2], bvh_prims[2];
 } lj_stats;
 
 /* Replaces Image3 render(const Scene&) (src/render.cpp:155-170).  Writes the

@@ -18,6 +18,8 @@ LJ_ERR_TIMEOUT = -9
 LJ_ERR_CANCELLED = -10
 LJ_ERR_SIZE_LIMIT = -11
 LJ_NOALLOC_MORTON_MAX_TRIANGLES = 65536
+LJ_RENDER_COUNT_BVH = 2
+LJ_COUNT_BVH_STRIDE = 16
 
 LJ_TEX_CONST, LJ_TEX_IMAGE, LJ_TEX_CHECKER = 0, 1, 2
 (LJ_MAT_LAMBERTIAN, LJ_MAT_ROUGHPLASTIC, LJ_MAT_ROUGHDIELECTRIC, LJ_MAT_DISNEY_DIFFUSE,
@@ -146,7 +148,8 @@ class lj_stats(C.Structure):
                 ("path_segments", C.c_int64), ("kernel_launches", C.c_int64),
                 ("null_collisions", C.c_int64), ("real_collisions", C.c_int64),
                 ("class_ms", C.c_double * LJ_KERNEL_CLASSES),
-                ("class_launches", C.c_int64 * LJ_KERNEL_CLASSES)]
+                ("class_launches", C.c_int64 * LJ_KERNEL_CLASSES),
+                ("bvh_rays", C.c_int64 * 2), ("bvh_nodes", C.c_int64 * 2), ("bvh_prims", C.c_int64 * 2)]
 
 
 class lj_ray(C.Structure):

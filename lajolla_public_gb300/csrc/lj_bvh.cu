@@ -823,9 +823,44 @@ __global__ void k_trace_count(DevBvh bvh, const float4 *rays, int64_t n, unsigne
     }
 }
 
+template <bool kAny>
+__global__ void k_trace_count_queue(DevBvh bvh, const float4 *rays, const int *count, int stride,
+                                    unsigned long long *counts, int *status) {
+    const int64_t n = *count;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * stride;
+    uint32_t nn = 0, np = 0, nr = 0;
+    if (i < n) {
+        float4 r0 = rays[2 * i], r1 = rays[2 * i + 1];
+        TraceHit h{0.0f, -1, 0.0f, 0.0f};
+        int ovf = 0;
+        trace_bvh<kAny, true>(bvh, V3{r0.x, r0.y, r0.z}, V3{r1.x, r1.y, r1.z}, r0.w, r1.w, h, &ovf, &nn, &np);
+        if (ovf) atomicOr(status, kStatusStackOverflow);
+        nr = 1;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        nr += __shfl_xor_sync(0xffffffffu, nr, o);
+        nn += __shfl_xor_sync(0xffffffffu, nn, o);
+        np += __shfl_xor_sync(0xffffffffu, np, o);
+    }
+    if ((threadIdx.x & 31) == 0 && nr) {
+        atomicAdd(counts, (unsigned long long)nr);
+        atomicAdd(counts + 1, (unsigned long long)nn);
+        atomicAdd(counts + 2, (unsigned long long)np);
+    }
+}
+
 inline int grid_for(int64_t n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
+
+int launch_trace_counters_queue(const DevBvh &bvh, const void *rays, const int *d_count, int64_t cap, int stride,
+                                bool any, unsigned long long *d_counts, int *d_status, cudaStream_t s) {
+    if (cap <= 0 || stride <= 0) return 0;
+    const int g = grid_for((cap + stride - 1) / stride, 128);
+    if (any) k_trace_count_queue<true><<<g, 128, 0, s>>>(bvh, (const float4 *)rays, d_count, stride, d_counts, d_status);
+    else k_trace_count_queue<false><<<g, 128, 0, s>>>(bvh, (const float4 *)rays, d_count, stride, d_counts, d_status);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+}
 
 int launch_trace_counters(const DevBvh &bvh, const void *rays, int64_t n, bool any,
                           unsigned long long *d_counts, int *d_status, cudaStream_t s) {

@@ -75,5 +75,10 @@ int launch_trace_any(const DevBvh &bvh, const void *rays, uint8_t *occ, int64_t 
 // instrumented traversal: d_counts[0] += nodes fetched, d_counts[1] += prims tested
 int launch_trace_counters(const DevBvh &bvh, const void *rays, int64_t n, bool any,
                           unsigned long long *d_counts, int *d_status, cudaStream_t s);
+// the same over every stride-th entry of a ray queue whose length is in
+// device memory (*d_count <= cap): d_counts[0] += rays counted, [1] += nodes
+// fetched, [2] += prims tested
+int launch_trace_counters_queue(const DevBvh &bvh, const void *rays, const int *d_count, int64_t cap, int stride,
+                                bool any, unsigned long long *d_counts, int *d_status, cudaStream_t s);
 
 }  // namespace lj

@@ -259,6 +259,13 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
         if (profile) cudaEventRecord(marks.back().second.second, s);
     };
     int64_t class_launches[LJ_KERNEL_CLASSES] = {};
+    // LJ_RENDER_COUNT_BVH: rays / nodes / prims of closest [0..2] and shadow [3..5] queues
+    const bool count_bvh = timed && (params->flags & LJ_RENDER_COUNT_BVH);
+    unsigned long long *bvhc = nullptr;
+    if (count_bvh) {
+        LJ_CUDA_TRY(cudaMallocAsync(&bvhc, 6 * sizeof(unsigned long long), s));
+        LJ_CUDA_TRY(cudaMemsetAsync(bvhc, 0, 6 * sizeof(unsigned long long), s));
+    }
     for (int sb = 0; sb < spp; sb += nsamp) {
         int ns = std::min(nsamp, spp - sb);
         int Pb = num_pixels * ns;
@@ -277,6 +284,9 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
             k_trace_queue<<<g_trace, 128, 0, s>>>(sc.bvh, q.ray[curq], q.hit, q.counts + curq, q.counts + 8,
                                                   q.stats + 0, ctx->d_status);
             mark_end();
+            if (count_bvh)
+                launch_trace_counters_queue(sc.bvh, q.ray[curq], q.counts + curq, Pb, LJ_COUNT_BVH_STRIDE, false,
+                                            bvhc, ctx->d_status, s);
             mark_begin(LJ_KERNEL_SHADE);
             shade<<<g_shade, 128, 0, s>>>(sc, q, curq, spread0, ctx->d_status);
             mark_end();
@@ -285,6 +295,9 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
                                                     q.counts + 9, q.st[curq ^ 1].L, q.Lres, q.stats + 1,
                                                     ctx->d_status);
             mark_end();
+            if (count_bvh)
+                launch_trace_counters_queue(sc.bvh, q.sray, q.counts + 2, Pb, LJ_COUNT_BVH_STRIDE, true, bvhc + 3,
+                                            ctx->d_status, s);
             launches += 4;
             class_launches[LJ_KERNEL_OTHER]++;
             class_launches[LJ_KERNEL_TRACE]++;
@@ -326,6 +339,17 @@ int render_path(lj_scene *scene, const lj_render_params *params, float *d_out, c
         stats->rays_shadow = (int64_t)st[1];
         stats->path_segments = (int64_t)st[2];
         stats->kernel_launches = launches;
+        if (count_bvh) {
+            unsigned long long c[6];
+            LJ_CUDA_TRY(cudaMemcpyAsync(c, bvhc, sizeof(c), cudaMemcpyDeviceToHost, s));
+            LJ_CUDA_TRY(cudaFreeAsync(bvhc, s));
+            LJ_CUDA_TRY(cudaStreamSynchronize(s));
+            for (int k = 0; k < 2; k++) {
+                stats->bvh_rays[k] = (int64_t)c[3 * k];
+                stats->bvh_nodes[k] = (int64_t)c[3 * k + 1];
+                stats->bvh_prims[k] = (int64_t)c[3 * k + 2];
+            }
+        }
         for (int c = 0; c < LJ_KERNEL_CLASSES; c++) {
             stats->class_launches[c] = class_launches[c];
             stats->class_ms[c] = 0.0;

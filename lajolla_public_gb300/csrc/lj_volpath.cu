@@ -334,6 +334,13 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
     const bool profile = stats && (params->flags & LJ_RENDER_PROFILE);
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
     int64_t class_launches[LJ_KERNEL_CLASSES] = {};
+    // LJ_RENDER_COUNT_BVH: rays / nodes / prims of the closest-hit queues
+    const bool count_bvh = stats && (params->flags & LJ_RENDER_COUNT_BVH);
+    unsigned long long *bvhc = nullptr;
+    if (count_bvh) {
+        LJ_CUDA_TRY(cudaMallocAsync(&bvhc, 3 * sizeof(unsigned long long), s));
+        LJ_CUDA_TRY(cudaMemsetAsync(bvhc, 0, 3 * sizeof(unsigned long long), s));
+    }
     auto mark_begin = [&](int cls) {
         class_launches[cls]++;
         if (!profile) return;
@@ -364,6 +371,9 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
             k_vol_trace<<<g_trace, 128, 0, s>>>(sc.bvh, q.ray[curq], q.hit, q.counts + curq, q.counts + 8,
                                                 q.stats + 0, ctx->d_status);
             mark_end();
+            if (count_bvh)
+                launch_trace_counters_queue(sc.bvh, q.ray[curq], q.counts + curq, Pb, LJ_COUNT_BVH_STRIDE, false,
+                                            bvhc, ctx->d_status, s);
             mark_begin(LJ_KERNEL_MEDIUM);
             k_vol_a<<<g_a, 128, 0, s>>>(sc, ps, q, curq, spread0, ctx->d_status);
             mark_end();
@@ -412,6 +422,15 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
         stats->null_collisions = (int64_t)st[3];
         stats->real_collisions = (int64_t)st[4];
         stats->kernel_launches = launches;
+        if (count_bvh) {
+            unsigned long long c[3];
+            LJ_CUDA_TRY(cudaMemcpyAsync(c, bvhc, sizeof(c), cudaMemcpyDeviceToHost, s));
+            LJ_CUDA_TRY(cudaFreeAsync(bvhc, s));
+            LJ_CUDA_TRY(cudaStreamSynchronize(s));
+            stats->bvh_rays[0] = (int64_t)c[0];
+            stats->bvh_nodes[0] = (int64_t)c[1];
+            stats->bvh_prims[0] = (int64_t)c[2];
+        }
         for (int c = 0; c < LJ_KERNEL_CLASSES; c++) {
             stats->class_launches[c] = class_launches[c];
             stats->class_ms[c] = 0.0;

@@ -2077,6 +2077,47 @@ int ljo_render_samples(void *s, uint64_t seed, const int32_t *pixels, int64_t n,
     return 0;
 }
 
+// Samples of one render job at the job's own resolution (same camera and
+// fov, as the GPU's job camera) and path-length options: out[i] = the
+// radiance of sample samples[i] of pixel pixels[i] (y * width + x), keyed
+// on (seed, pixel, sample) like the GPU.  Non-finite samples are returned
+// as they are.  The scene's camera and options are swapped for the call's
+// duration, so calls on one scene must not overlap.
+int ljo_render_job_samples(void *s, const lj_camera_desc *cam_desc, uint64_t seed, int width, int height,
+                           int max_depth, int rr_depth, const int32_t *pixels, const int32_t *samples, int64_t n,
+                           int nthreads, double *out) {
+    Scene *sc = (Scene *)s;
+    lj_camera_desc cd = *cam_desc;
+    cd.width = width;
+    cd.height = height;
+    CameraS saved_cam = sc->cam;
+    lj_render_options saved_opt = sc->opt;
+    sc->cam = make_camera(cd);
+    sc->opt.max_depth = max_depth;
+    sc->opt.rr_depth = rr_depth;
+    if (nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();
+    std::atomic<int64_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            int64_t i0 = next.fetch_add(16);
+            if (i0 >= n) break;
+            for (int64_t i = i0; i < std::min(n, i0 + 16); i++) {
+                int p = pixels[i];
+                Rng rng{pcg_keyed(seed, (uint64_t)p, (uint64_t)samples[i]), true};
+                V3 L = sc->opt.integrator == LJ_INTEGRATOR_VOLPATH ? vol_path_tracing(*sc, p % width, p / width, rng)
+                                                                   : path_tracing(*sc, p % width, p / width, rng, false);
+                out[i * 3] = L.x; out[i * 3 + 1] = L.y; out[i * 3 + 2] = L.z;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int i = 0; i < nthreads; i++) th.emplace_back(worker);
+    for (auto &t : th) t.join();
+    sc->cam = saved_cam;
+    sc->opt = saved_opt;
+    return 0;
+}
+
 // Closest hit.  brute != 0: test every primitive (the BVH oracle); also
 // reports in ties[i] how many primitives share the minimal t.
 int ljo_trace_closest(void *s, const lj_ray *rays, lj_hit *hits, int64_t n, int brute,

@@ -71,6 +71,8 @@ def lib():
         L.ljo_camera_batch.argtypes = [C.POINTER(abi.lj_camera_desc), vp, i64, vp]
         L.ljo_light_emission_batch.argtypes = [vp, vp, vp, vp, vp, i64, vp]
         L.ljo_medium_batch.argtypes = [vp, C.c_int, vp, vp, i64, vp, vp, vp]
+        L.ljo_render_job_samples.argtypes = [vp, C.POINTER(abi.lj_camera_desc), u64, C.c_int, C.c_int, C.c_int,
+                                             C.c_int, vp, vp, i64, C.c_int, vp]
         _lib = L
     return _lib
 
@@ -107,6 +109,16 @@ class OracleScene:
         out = np.zeros((len(pixels), spp, 3))
         lib().ljo_render_samples(self.h, seed, _p(pixels), len(pixels), spp, sample_offset,
                                  nthreads, _p(out))
+        return out
+
+    def render_job_samples(self, seed, width, height, max_depth, rr_depth, pixels, samples, nthreads=0):
+        """Radiance of (pixel, sample index) keys of a render job at its own
+        resolution and depth options (the GPU's keyed samples): (n, 3)."""
+        px = np.ascontiguousarray(pixels, np.int32)
+        sm = np.ascontiguousarray(samples, np.int32)
+        out = np.zeros((len(px), 3))
+        lib().ljo_render_job_samples(self.h, C.byref(self._desc.camera), seed, width, height, max_depth, rr_depth,
+                                     _p(px), _p(sm), len(px), nthreads, _p(out))
         return out
 
     def trace_closest(self, rays, brute=False, nthreads=0):
