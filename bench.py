@@ -26,8 +26,7 @@ Our arm (--impl ours):
   plain     the same jobs through the single-scene wavefront renderer, one at
             a time in arrival order (lj_gpu_render_job_device + image to
             host).  Both arms trace the same keyed samples, so their images
-            (and errors) match: rel_mse reports both against a 4096-spp
-            render for a few jobs.
+            (and errors) match (matched_error).
   latency   p50 / p99 of (completion - arrival) per job, both arms.
   e2e       one step through the C ABI from host memory: the scene pool is
             uploaded (lj_gpu_scene_create: descriptors from host, device BVH
@@ -36,10 +35,23 @@ Our arm (--impl ours):
             (LJ_SERVER_PROFILE: CUDA events around every kernel on the
             server's stream), compulsory algorithmic bytes per launch
             (include/lj_bytes_model.h) / average launch time, against the
-            measured HBM copy bandwidth (MEASURED_PEAKS.json).
+            measured HBM copy bandwidth (MEASURED_PEAKS.json); with_bvh adds
+            the BVH bytes per ray counted on the same jobs
+            (LJ_RENDER_COUNT_BVH), issue_bound the instruction-issue ceiling
+            of the kernel's ncu capture.
+  quality   per-image relative MSE of one 128^2 job per scene kind at spp 4
+            .. 4096, batched and plain, against a 64k-spp render validated
+            against the oracle at 3 standard errors; the spp that reaches
+            1e-3 is marked.
+  single_scene  the Cornell box (256^2, 64 spp), full terrain (5.5M
+            triangles, 1080p, 256 spp) and volume (256^3, 512^2, 256 spp)
+            configurations, and the intersection + BSDF microbenchmark.
   cpu_baseline  the oracle's C++ restatement of the reference path tracer
             (oracle/lj_oracle.cpp, FP64, all host threads) on a bounded
-            sample of the same scenes.
+            sample drawn from the GPU arm's own work: (job, pixel, sample)
+            keys uniform over a step's W*H*spp, each at its job's resolution
+            and depth with the GPU's keyed random numbers; per_sample_parity
+            compares a subset of such samples with the GPU's.
 The working set (path pool ~1 GB, scenes up to 2M triangles, accumulators)
 is larger than L2.
 
@@ -47,7 +59,7 @@ Reference arm (--impl reference): the reference's CPU path tracer on the
 host cores -- the reference renderer cannot be built on the benchmark machine
 (its sources are not present there), so its C++ restatement in oracle/ runs
 instead, pinned sample-for-sample to the reference's own renders
-(tests/golden), on a bounded sample of the serving scenes per step.
+(tests/golden); step i samples the work of the GPU arm's timed step i.
 
 Multi-GPU: replicas only (each rank serves its own copy of the job stream;
 no collective on the data path); value sums all ranks' samples over the
@@ -182,6 +194,8 @@ BYTES_NEE_RESULT = 56
 BYTES_VOL_SEGMENT = (2 * (BYTES_RAY + BYTES_HIT + BYTES_VOL_STATE) + 2 * (BYTES_VOL_STATE + BYTES_RAY)
                      + 2 * BYTES_NEE_REQUEST + BYTES_NEE_RESULT)
 BYTES_NEE_SHADOW_LOOP = BYTES_NEE_REQUEST + BYTES_NEE_RESULT
+BYTES_NODE = 80         # compressed 8-wide BVH node
+BYTES_LEAF = 48         # leaf primitive record
 
 
 def kernel_bytes(cls, samples, rays_closest, rays_shadow, segments, vol_segments=0, nee_requests=0):
@@ -238,10 +252,10 @@ def pct(xs, q):
     return float(np.percentile(np.asarray(xs, np.float64), q)) if xs else None
 
 
-def job_desc(j, profile=False):
+def job_desc(j, profile=False, count_bvh=False):
     from lajolla_public_gb300 import gpu
     return gpu.job_desc(seed=j["seed"], spp=j["spp"], width=j["width"], height=j["height"],
-                        max_depth=j["max_depth"], rr_depth=j["rr_depth"], profile=profile)
+                        max_depth=j["max_depth"], rr_depth=j["rr_depth"], profile=profile, count_bvh=count_bvh)
 
 
 def serve_step(srv, gscenes, jobs, keep=()):
@@ -298,6 +312,121 @@ def tuned_options(ctx, gscenes):
     return gpu.autotune(ctx, gscenes, jd, [j["scene"] for j in tune], cache_path=TUNE_CACHE, options=opt)
 
 
+SCENE_KINDS = ("cornell box", "terrain + envmap", "volume")   # serving_scenes cycles through them
+
+
+def quality(srv, gscenes, pool, cs, out, stream, res=128, depth=16, ref_spp=65536,
+            spps=(4, 16, 64, 256, 1024, 4096), check_px=1024, check_spp=64):
+    """Per-image relative MSE (sum of squared errors / sum of squares of the
+    reference) of one 128 x 128 job per scene kind against a 64k-spp render
+    of the same job by the plain GPU renderer with an independent seed.
+    Each reference is first checked against the oracle: on `check_px` random
+    pixels, its value lies within 3 standard errors of the oracle's mean of
+    `check_spp` keyed samples.  The job is then rendered at each spp by the
+    server (batched) and by the plain renderer; both trace the same keyed
+    samples, so their errors match.  rel_mse x spp stays flat when the error
+    is the estimator's variance (no bias)."""
+    from lajolla_public_gb300 import gpu
+    rows = []
+    n = res * res * 3
+    for kind_i, kind in enumerate(SCENE_KINDS):
+        si = kind_i   # first scene of each kind
+        sc = pool[si]
+        seed = 4242 + si
+        job = dict(scene=si, seed=seed, width=res, height=res, max_depth=depth, rr_depth=5)
+        t0 = time.perf_counter()
+        gscenes[si].render_job_device(out[:n], job_desc(dict(job, spp=ref_spp, seed=seed ^ 0x5bd1e995)),
+                                      stream=stream)
+        ref = out[:n].cpu().numpy().reshape(res, res, 3).astype(np.float64)
+        ref_s = time.perf_counter() - t0
+        # the reference against the oracle
+        px = cs.rng.integers(0, res * res, check_px).astype(np.int32)
+        osm = cs.oss[si].render_job_samples(seed ^ 0x1234567, res, res, depth, 5, np.repeat(px, check_spp),
+                                            np.tile(np.arange(check_spp, dtype=np.int32), check_px),
+                                            nthreads=cs.cores).reshape(check_px, check_spp, 3)
+        osm = np.where(np.isfinite(osm), osm, 0.0)
+        m_o, sd_o = osm.mean(axis=1), osm.std(axis=1)
+        se = np.sqrt(sd_o ** 2 / check_spp + sd_o ** 2 / ref_spp) + 1e-9
+        within = float((np.abs(ref.reshape(-1, 3)[px] - m_o) <= 3 * se).all(axis=1).mean())
+        den = float(np.mean(ref ** 2)) + 1e-30
+        per_spp, first_ok = [], None
+        for spp in spps:
+            jb = dict(job, spp=spp)
+            jid = srv.submit(gscenes[si], job_desc(jb))
+            img_b, _ = srv.wait(jid, timeout=600)
+            gscenes[si].render_job_device(out[:n], job_desc(jb), stream=stream)
+            img_p = out[:n].cpu().numpy().reshape(res, res, 3)
+            rb = float(np.mean((img_b - ref) ** 2) / den)
+            rp = float(np.mean((img_p - ref) ** 2) / den)
+            ok = max(rb, rp) <= 1e-3
+            if ok and first_ok is None:
+                first_ok = spp
+            per_spp.append({"spp": spp, "batched": rb, "plain": rp, "rel_mse_x_spp": round(rb * spp, 4),
+                            "meets_1e-3": ok,
+                            "batched_vs_plain_max_abs": float(np.abs(img_b - img_p).max())})
+        rows.append({"scene": kind, "scene_triangles": sc.num_triangles,
+                     "job": "%dx%d, max depth %d, RR from 5" % (res, res, depth), "ref_spp": ref_spp,
+                     "ref_render_s": round(ref_s, 3),
+                     "ref_vs_oracle_within_3se": round(within, 4),
+                     "ref_vs_oracle": "%d pixels x %d oracle samples" % (check_px, check_spp),
+                     "rel_mse": per_spp, "min_spp_meeting_1e-3": first_ok})
+    return rows
+
+
+def bvh_bytes(gscenes, jobs, out, stream):
+    """BVH bytes per ray of the plain renderer over `jobs` (the same keyed
+    paths the server traces): an instrumented traversal of every 16th entry
+    of every closest-hit and shadow-ray queue (LJ_RENDER_COUNT_BVH) counts
+    the 80-byte wide nodes fetched and the 48-byte leaf records tested."""
+    tot = np.zeros((3, 2), np.int64)
+    for j in jobs:
+        n = j["width"] * j["height"] * 3
+        st = gscenes[j["scene"]].render_job_device(out[:n], job_desc(j, count_bvh=True), stream=stream, stats=True)
+        tot += np.array([list(st.bvh_rays), list(st.bvh_nodes), list(st.bvh_prims)], np.int64)
+    res = {}
+    for k, name in ((0, "closest"), (1, "shadow")):
+        r = max(1, int(tot[0, k]))
+        res[name] = {"rays_counted": int(tot[0, k]), "nodes_per_ray": round(tot[1, k] / r, 3),
+                     "leaf_records_per_ray": round(tot[2, k] / r, 3),
+                     "bvh_bytes_per_ray": round((BYTES_NODE * tot[1, k] + BYTES_LEAF * tot[2, k]) / r, 1)}
+    return res
+
+
+def single_scene_configs(ctx, stream):
+    """The single-scene configurations through lj_gpu_render_device: a
+    timed render (CUDA events around the call's kernels, after a warm-up
+    render) and a profiled one (events around every kernel) for the class
+    split."""
+    import torch
+    from lajolla_public_gb300 import gpu
+    cases = (("cornell_box", "seeded Cornell box (36 triangles, fits in L2), 256x256, 64 spp, max depth 6",
+              lambda: scenes.cornell_box(seed=0)),
+             ("terrain", "2048x1024-grid fractal terrain + 64 subdivision-5 icospheres (5.5M triangles), Disney "
+                         "BSDFs, 1024x512 HDR envmap, 1920x1080, 256 spp, max depth 8",
+              lambda: scenes.terrain_scene(seed=0)),
+             ("volume", "256^3 heterogeneous chromatic medium (max density 20, HG g 0.7) in a dielectric sphere "
+                        "(eta 1.33) over a plane, sphere light, 512x512, 256 spp, max depth 64 (volpath v6)",
+              lambda: scenes.volume_scene(seed=0)))
+    rows = {}
+    for name, what, mk in cases:
+        sc = mk()
+        g = gpu.GpuScene(ctx, sc)
+        out = torch.empty(sc.width * sc.height * 3, dtype=torch.float32, device="cuda")
+        g.render_device(out, seed=1, spp=4, stream=stream)
+        st = g.render_device(out, seed=2, stream=stream)
+        sp = g.render_device(out, seed=3, stream=stream, profile=True)
+        rays = st.rays_closest + st.rays_shadow
+        rows[name] = {"what": what, "msamples_per_s": round(st.samples / st.device_ms / 1e3, 2),
+                      "mrays_per_s": round(rays / st.device_ms / 1e3, 1), "device_ms": round(st.device_ms, 2),
+                      "samples": int(st.samples), "rays_closest": int(st.rays_closest),
+                      "rays_shadow": int(st.rays_shadow), "bvh_build_ms": round(g.info().build_ms, 2),
+                      "kernel_ms_profiled": {abi.KERNEL_CLASS_NAMES[c]: round(sp.class_ms[c], 2)
+                                             for c in range(abi.LJ_KERNEL_CLASSES) if sp.class_launches[c]}}
+        g.close()
+        del out
+    return rows
+
+
 def run_ours(args):
     import torch
     from lajolla_public_gb300 import gpu
@@ -328,19 +457,20 @@ def run_ours(args):
     barrier(world)
     b_secs, b_lat, p_secs, p_lat = [], [], [], []
     samples = 0
-    keep_imgs = None
+    match = 0.0
     for i in range(args.steps):
         jobs = make_jobs(1000 + i)
         samples += job_samples(jobs)
-        keep = tuple(sorted(range(len(jobs)), key=lambda k: jobs[k]["width"] * jobs[k]["spp"])[:3]) if i == 0 else ()
+        keep = tuple(range(len(jobs))) if i == 0 else ()
         sec, lat, bimgs = serve_step(srv, gscenes, jobs, keep)
         b_secs.append(sec)
         b_lat += lat
         sec, lat, pimgs = plain_step(gscenes, jobs, out, stream, keep)
         p_secs.append(sec)
         p_lat += lat
-        if i == 0:
-            keep_imgs = (jobs, keep, bimgs, pimgs)
+        for k in keep:   # batched and plain images of the same jobs (same keyed samples)
+            match = max(match, float(np.abs(bimgs[k] - pimgs[k]).max() / (np.abs(pimgs[k]).max() + 1e-30)))
+        del bimgs, pimgs
     barrier(world)
     ck = clocks.stop()
     st1 = srv.stats()
@@ -349,21 +479,6 @@ def run_ours(args):
     value = samples * world / b_total / 1e6
     plain_value = samples * world / p_total / 1e6
     launches = st1.kernel_launches - st0.kernel_launches
-
-    # matched error: a few jobs of the first step against 4096-spp renders
-    jobs0, keep, bimgs, pimgs = keep_imgs
-    rel_mse = []
-    for k in keep:
-        j = dict(jobs0[k])
-        ref_job = dict(j, spp=4096, seed=j["seed"] ^ 0x5bd1e995)
-        n = j["width"] * j["height"] * 3
-        gscenes[j["scene"]].render_job_device(out[:n], job_desc(ref_job), stream=stream)
-        ref = out[:n].cpu().numpy().reshape(j["height"], j["width"], 3).astype(np.float64)
-        den = float(np.mean(ref ** 2)) + 1e-30
-        rel_mse.append({"job": "%dx%d %d spp depth %d" % (j["width"], j["height"], j["spp"], j["max_depth"]),
-                        "batched": float(np.mean((bimgs[k] - ref) ** 2) / den),
-                        "plain": float(np.mean((pimgs[k] - ref) ** 2) / den),
-                        "batched_vs_plain_max_abs": float(np.abs(bimgs[k] - pimgs[k]).max())})
 
     # e2e: upload the scene pool from host memory inside the timed region,
     # then serve the first timed step's jobs
@@ -401,6 +516,7 @@ def run_ours(args):
         plain_rays[0] += st.rays_closest
         plain_rays[1] += st.rays_shadow
         plain_rays[2] += st.path_segments
+    bvh = bvh_bytes(gscenes, jobs, out, stream)
     peak, peak_kind = measured_peaks()
     cls_ms = list(ps.class_ms)
     dom = max((c for c in range(abi.LJ_KERNEL_CLASSES) if c != abi.LJ_KERNEL_OTHER), key=lambda c: cls_ms[c])
@@ -415,6 +531,18 @@ def run_ours(args):
     kname = {abi.LJ_KERNEL_CAMERA: "k_srv_regen", abi.LJ_KERNEL_MEDIUM: "k_srv_vol_a + k_srv_vol_c",
              abi.LJ_KERNEL_NEE: "k_srv_vol_b"}.get(dom, "k_srv_" + abi.KERNEL_CLASS_NAMES[dom])
     traffic = load_traffic(kname, units / launches_dom)
+    with_bvh = None
+    if dom in (abi.LJ_KERNEL_TRACE, abi.LJ_KERNEL_SHADOW):
+        key = "closest" if dom == abi.LJ_KERNEL_TRACE else "shadow"
+        nb_bvh = nb + units * bvh[key]["bvh_bytes_per_ray"]
+        ach_bvh = nb_bvh / launches_dom / avg_launch_s / 1e9
+        with_bvh = {"achieved": round(ach_bvh, 1), "frac": round(ach_bvh / peak, 4),
+                    "bytes_per_launch": round(nb_bvh / launches_dom),
+                    "bvh_bytes_per_ray": bvh[key]["bvh_bytes_per_ray"],
+                    "how": "compulsory bytes + 80 B per wide node fetched + 48 B per leaf record tested, per ray "
+                           "counted by an instrumented traversal of every 16th queue entry of the plain renderer "
+                           "on the same jobs"}
+    issue = load_issue(kname)
     if dom in (abi.LJ_KERNEL_MEDIUM, abi.LJ_KERNEL_NEE):
         note = ("volumetric steps are latency bound, not HBM bound: their dependent density-grid lookups "
                 "(8 x 16 B per tracking step) mostly hit L1/L2 (ncu of the volume scene's a / b / c steps)")
@@ -433,7 +561,6 @@ def run_ours(args):
                   "latency_ms": {"p50": round(pct(p_lat, 50), 2), "p99": round(pct(p_lat, 99), 2)},
                   "what": "same jobs, one at a time, lj_gpu_render_job_device + image to host"},
         "batched_over_plain": round(value / plain_value, 3),
-        "rel_mse_vs_4096spp": rel_mse,
         "clocks": ck,
         "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "scene_upload_s": round(upload_s, 4),
@@ -446,8 +573,13 @@ def run_ours(args):
                      else "fallback 6800 GB/s", "traffic": traffic,
                      "bytes_per_launch": round(nb / launches_dom), "avg_launch_us": round(avg_launch_s * 1e6, 2),
                      "bytes": "compulsory (queues, hits, path state, shading records); BVH and density-grid "
-                              "bytes excluded",
+                              "bytes excluded (with_bvh adds the BVH bytes)",
+                     "with_bvh": with_bvh, "issue_bound": issue,
                      "note": note},
+        "bvh_bytes_per_ray": bvh,
+        "matched_error": {"batched_vs_plain_max_rel_diff": match,
+                          "what": "largest |batched - plain| / max |plain| over the first timed step's job images: "
+                                  "both forms trace the same keyed samples, so their errors match"},
         "kernel_ms_per_step": {abi.KERNEL_CLASS_NAMES[c]: round(cls_ms[c], 3) for c in range(abi.LJ_KERNEL_CLASSES)},
         "plain_kernel_ms_per_step": {abi.KERNEL_CLASS_NAMES[c]: round(plain_ms[c], 3)
                                      for c in range(abi.LJ_KERNEL_CLASSES)},
@@ -458,12 +590,17 @@ def run_ours(args):
         "mrays_per_s": round((st1.rays_closest - st0.rays_closest + st1.rays_shadow - st0.rays_shadow)
                              / b_total / 1e6, 1),
     }
-    srv.stop()
     if args.microbench:
         line["microbench"] = microbench(ctx)
+    if args.configs:
+        line["single_scene"] = single_scene_configs(ctx, stream)
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(pool, target_s=args.cpu_seconds)
+        line["cpu_baseline"], cs = cpu_baseline(pool, make_jobs(1000), target_s=args.cpu_seconds)
+        line["per_sample_parity"] = per_sample_parity(cs, gscenes, make_jobs(1000), out, stream)
+        if args.quality:
+            line["quality"] = quality(srv, gscenes, pool, cs, out, stream)
         print(json.dumps(line), flush=True)
+    srv.stop()
     for g in gscenes:
         g.close()
     ctx.close()
@@ -562,6 +699,21 @@ def scene_host_bytes(sc):
     return int(b)
 
 
+def load_issue(kernel_name):
+    """Instruction-issue ceiling of the dominant kernel from its committed
+    ncu capture (profiles/traffic.json): issue-active fraction x active
+    threads per warp instruction / 32 is the fraction of the SMs' lane
+    slots doing work; None if not captured."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        v = json.load(open(p)).get(kernel_name)
+        if isinstance(v, dict) and v.get("issue_active") and v.get("threads_per_inst"):
+            return {"issue_active": v["issue_active"], "threads_per_inst": v["threads_per_inst"],
+                    "lane_utilisation": round(v["issue_active"] * v["threads_per_inst"] / 32, 3),
+                    "source": v.get("issue_source", "ncu")}
+    return None
+
+
 def load_traffic(kernel_name, units_per_launch):
     """DRAM bytes per launch of the dominant kernel: the per-unit figure of
     the committed ncu capture (profiles/traffic.json, measured on a smaller
@@ -578,10 +730,14 @@ def load_traffic(kernel_name, units_per_launch):
 
 # ------------------------------------------------------------ CPU side
 class CpuSampler:
-    """The oracle restatement on all host cores over random pixels of every
-    scene of the pool (1 spp each, the scenes' own resolution and depth).
-    calibrate() grows the pixel count until one run takes at least 60 % of
-    target_s (at most 4 Mi pixels per scene); run() renders that many."""
+    """The oracle's restatement of the reference path tracer (and of the
+    volpath v6 algorithm for the volume scenes) on all host cores, over
+    exactly the GPU arm's work: a run draws n keys (job, pixel, sample index)
+    uniformly over the camera samples of a step's jobs (so jobs are weighted
+    by W * H * spp), and renders each at its job's resolution, max depth and
+    Russian-roulette depth with the GPU's keyed random numbers
+    (job seed, pixel, sample).  calibrate() grows n until one run takes at
+    least 60 % of the target time (at most 4 Mi keys)."""
 
     CAP = 1 << 22
 
@@ -592,44 +748,107 @@ class CpuSampler:
         self.cores = os.cpu_count() or 1
         self.rng = np.random.default_rng(7)
         self.oss = [ljo.OracleScene(s) for s in pool]   # BVH builds on the CPU, once
-        self.n_px = 256
-        self.seed = 0
+        self.n = 256
+        self.split = {}
 
-    def run(self, n_px=None):
-        n_px = self.n_px if n_px is None else n_px
-        self.seed += 1
-        t0 = time.perf_counter()
-        for s, o in zip(self.pool, self.oss):
-            px = self.rng.integers(0, s.width * s.height, n_px).astype(np.int32)
-            o.render_samples(px, 1, seed=self.seed, nthreads=self.cores)
-        return time.perf_counter() - t0
+    def draw(self, jobs, n):
+        """n keys uniform over the jobs' camera samples, grouped by job:
+        [(job index, pixels, sample indices)]."""
+        w = np.array([j["width"] * j["height"] * j["spp"] for j in jobs], np.float64)
+        ji = self.rng.choice(len(jobs), size=n, p=w / w.sum())
+        out = []
+        for k in np.unique(ji):
+            cnt = int((ji == k).sum())
+            j = jobs[k]
+            out.append((int(k), self.rng.integers(0, j["width"] * j["height"], cnt).astype(np.int32),
+                        self.rng.integers(0, j["spp"], cnt).astype(np.int32)))
+        return out
 
-    def calibrate(self, target_s):
-        n_px = 256
-        dt = self.run(n_px)
-        while dt < 0.6 * target_s and n_px < self.CAP:
-            n_px = int(min(self.CAP, max(2 * n_px, n_px * 0.8 * target_s / max(dt, 1e-3))))
-            dt = self.run(n_px)
-        self.n_px = n_px
+    def render(self, jobs, keys):
+        """Renders the keys; returns ({job index: (n, 3) radiance}, seconds,
+        {class: [samples, seconds]})."""
+        vals, split = {}, {"path": [0, 0.0], "volpath": [0, 0.0]}
+        t_all = time.perf_counter()
+        for k, px, sm in keys:
+            j = jobs[k]
+            cls = "volpath" if self.pool[j["scene"]].integrator == abi.LJ_INTEGRATOR_VOLPATH else "path"
+            t0 = time.perf_counter()
+            vals[k] = self.oss[j["scene"]].render_job_samples(j["seed"], j["width"], j["height"], j["max_depth"],
+                                                             j["rr_depth"], px, sm, nthreads=self.cores)
+            split[cls][0] += len(px)
+            split[cls][1] += time.perf_counter() - t0
+        return vals, time.perf_counter() - t_all, split
+
+    def run(self, jobs, n=None):
+        keys = self.draw(jobs, self.n if n is None else n)
+        _, dt, split = self.render(jobs, keys)
+        self.split = split
+        return dt
+
+    def calibrate(self, jobs, target_s):
+        n = 256
+        dt = self.run(jobs, n)
+        while dt < 0.6 * target_s and n < self.CAP:
+            n = int(min(self.CAP, max(2 * n, n * 0.8 * target_s / max(dt, 1e-3))))
+            dt = self.run(jobs, n)
+        self.n = n
         return dt
 
     def describe(self, dt):
-        n = self.n_px * len(self.pool)
-        return ("%d random pixels x 1 spp of each of the %d serving scenes (%d samples, %.1f s); C++ "
-                "restatement of src/path_tracing.h pinned to the reference's renders (and of the volpath v6 "
-                "handout algorithm for the volume scenes), %d threads"
-                % (self.n_px, len(self.pool), n, dt, self.cores))
+        sp = ", ".join("%s %d samples in %.2f s" % (c, v[0], v[1]) for c, v in self.split.items() if v[0])
+        return ("%d (job, pixel, sample) keys drawn uniformly over the step's %d jobs' W*H*spp camera samples "
+                "(the GPU arm's sample distribution), each at its job's resolution, max depth and RR depth with "
+                "the GPU's keyed random numbers (%.1f s: %s); C++ restatement of src/path_tracing.h pinned to "
+                "the reference's renders (and of the volpath v6 handout algorithm for the volume scenes), "
+                "%d threads" % (self.n, WORKLOAD["n_jobs"], dt, sp, self.cores))
 
     def rate(self, dt):
-        return self.n_px * len(self.pool) / dt / 1e6
+        return self.n / dt / 1e6
 
 
-def cpu_baseline(pool, target_s=10.0):
+def cpu_baseline(pool, jobs, target_s=10.0):
     cs = CpuSampler(pool)
-    cs.calibrate(target_s)
-    dt = cs.run()
+    cs.calibrate(jobs, target_s)
+    dt = cs.run(jobs)
+    split = {c: {"samples": v[0], "seconds": round(v[1], 3),
+                 "msamples_per_s": round(v[0] / v[1] / 1e6, 4) if v[1] > 0 else None} for c, v in cs.split.items()}
     return {"value": round(cs.rate(dt), 4), "unit": "Msamples/s", "cores": cs.cores, "kind": "port",
-            "sample": cs.describe(dt)}
+            "sample": cs.describe(dt), "split": split}, cs
+
+
+def per_sample_parity(cs, gscenes, jobs, out, stream, per_job=256, rtol=1e-2, floor=1e-1):
+    """The CPU sampler's values against the GPU's for the same keys, on one
+    job of each scene: the GPU renders the job's whole image at one sample
+    index (spp 1), the oracle the same sample of `per_job` random pixels.
+    A sample agrees when it is within rtol relative (floor absolute); FP32
+    against FP64 may flip a path's branch (roulette, a CDF boundary, a
+    null collision), so a few do not."""
+    from lajolla_public_gb300 import gpu
+    seen, n_all, n_ok, rows = set(), 0, 0, []
+    for k, j in enumerate(jobs):
+        if j["scene"] in seen:
+            continue
+        seen.add(j["scene"])
+        smp = int(cs.rng.integers(0, j["spp"]))
+        n = j["width"] * j["height"] * 3
+        gscenes[j["scene"]].render_job_device(out[:n], gpu.job_desc(seed=j["seed"], spp=1, sample_offset=smp,
+                                                                      width=j["width"], height=j["height"],
+                                                                      max_depth=j["max_depth"],
+                                                                      rr_depth=j["rr_depth"]), stream=stream)
+        img = out[:n].cpu().numpy().reshape(-1, 3).astype(np.float64)
+        px = cs.rng.integers(0, j["width"] * j["height"], per_job).astype(np.int32)
+        vals, _, _ = cs.render(jobs, [(k, px, np.full(per_job, smp, np.int32))])
+        ref = vals[k]
+        fin = np.isfinite(ref).all(axis=1)
+        ref = np.where(fin[:, None], ref, 0.0)    # the GPU drops non-finite samples
+        ok = (np.abs(img[px] - ref) <= rtol * np.maximum(np.abs(ref), floor)).all(axis=1)
+        n_all += per_job
+        n_ok += int(ok.sum())
+        rows.append({"scene": int(j["scene"]), "job": "%dx%d depth %d sample %d" % (j["width"], j["height"],
+                                                                                  j["max_depth"], smp),
+                     "agree": round(float(ok.mean()), 4)})
+    return {"samples": n_all, "agree_fraction": round(n_ok / max(1, n_all), 4),
+            "tolerance": "%g relative, %g absolute floor" % (rtol, floor), "jobs": rows}
 
 
 def run_reference(args):
@@ -638,15 +857,19 @@ def run_reference(args):
         return
     pool = make_scenes()
     cs = CpuSampler(pool)
-    cs.calibrate(args.cpu_seconds / 2)   # each step a bounded sample of about half --cpu-seconds
+    cs.calibrate(make_jobs(1000), args.cpu_seconds / 2)   # each step a bounded sample of about half --cpu-seconds
     for i in range(args.warmup):
-        cs.run(max(256, cs.n_px // 16))
+        cs.run(make_jobs(100 + i), max(256, cs.n // 16))
     vals, texts, secs = [], [], []
+    split = {"path": [0, 0.0], "volpath": [0, 0.0]}
     for i in range(args.steps):
-        dt = cs.run()
+        dt = cs.run(make_jobs(1000 + i))   # the jobs of our arm's timed step i
         secs.append(dt)
         vals.append(cs.rate(dt))
         texts.append(cs.describe(dt))
+        for c in split:
+            split[c][0] += cs.split[c][0]
+            split[c][1] += cs.split[c][1]
     value = statistics.mean(vals)
     cores = cs.cores
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Msamples/s",
@@ -655,12 +878,14 @@ def run_reference(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene generator)",
             "config": config_dict(pool),
             "cpu_baseline": {"value": round(value, 4), "unit": "Msamples/s", "cores": cores, "kind": "port",
-                             "sample": "per step: " + texts[-1]},
+                             "sample": "per step: " + texts[-1],
+                             "split": {c: {"samples": v[0], "seconds": round(v[1], 3)} for c, v in split.items()}},
             "e2e": {"value": round(value, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "the reference renderer cannot be built on the benchmark machine (its sources are not "
-                    "there); its C++ restatement in oracle/ runs instead, on a bounded sample of the "
-                    "serving scenes (the reference has no server: it renders one scene per process)"}
+            "note": "same sample distribution as the GPU arm (step i draws from the jobs of the GPU arm's timed "
+                    "step i); the reference renderer cannot be built on the benchmark machine (its sources are "
+                    "not there), so its C++ restatement in oracle/ runs instead (the reference has no server: "
+                    "it renders one scene per process)"}
     print(json.dumps(line), flush=True)
 
 
@@ -673,6 +898,10 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-microbench", dest="microbench", action="store_false",
                     help="skip the intersection + BSDF microbenchmark")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip the single-scene configurations (Cornell box, full terrain, volume)")
+    ap.add_argument("--no-quality", dest="quality", action="store_false",
+                    help="skip the relative-MSE measurement against 64k-spp references")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

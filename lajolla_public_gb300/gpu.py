@@ -319,9 +319,11 @@ class GpuScene:
         return s.value, l.value
 
 
-def job_desc(seed=0, spp=0, sample_offset=0, width=0, height=0, max_depth=None, rr_depth=None, profile=False):
+def job_desc(seed=0, spp=0, sample_offset=0, width=0, height=0, max_depth=None, rr_depth=None, profile=False,
+             count_bvh=False):
     j = abi.lj_job_desc(seed=seed, spp=spp, sample_offset=sample_offset, width=width, height=height,
-                        flags=abi.LJ_RENDER_PROFILE if profile else 0)
+                        flags=(abi.LJ_RENDER_PROFILE if profile else 0) |
+                        (abi.LJ_RENDER_COUNT_BVH if count_bvh else 0))
     if max_depth is not None:
         j.override_depth = 1
         j.max_depth = max_depth

@@ -288,6 +288,55 @@ def make_renders(cases=RENDER_CASES):
     return out
 
 
+# The reference's own scene files, parsed by the reference's parser and
+# flattened by the adapter (lajolla_public_gb300/adapter) as a lajolla build
+# with the GPU path would: file under scenes/, and the reduced resolution
+# and sample count of the fixture.
+REF_SCENES = {
+    "cbox": ("cbox/cbox.xml", 128, 128, 64),
+    "veach_mi": ("veach_mi/mi.xml", 192, 128, 64),
+    "pixel_filter": ("pixel_filter_test/pixel_filter_test.xml", 160, 120, 64),
+}
+ADAPTER = os.path.join(ROOT, "oracle", "_ref", "adapter_check")
+
+
+def reference_scene_variant(rel, w, h, spp, directory):
+    """The reference's scene file with another film size and sample count,
+    written into `directory`; relative file names point back at the
+    original's directory."""
+    import re
+    src = os.path.join(ljo.reference_dir(), "scenes", rel)
+    xml = open(src).read()
+    for name, v in (("width", w), ("height", h), ("sampleCount", spp)):
+        xml = re.sub(r'(<integer name="%s" value=")\d+' % name, r"\g<1>%d" % v, xml)
+    base = os.path.dirname(src)
+    xml = re.sub(r'value="((?!/)[^"]+\.(?:obj|ply|serialized|exr|hdr|png|jpg|tga|vol))"',
+                 lambda m: 'value="%s"' % os.path.join(base, m.group(1)), xml)
+    out = os.path.join(directory, os.path.basename(rel))
+    open(out, "w").write(xml)
+    return out
+
+
+def flatten_reference_scene(xml):
+    """adapter_check flatten: the flattened descriptor's bytes."""
+    with tempfile.TemporaryDirectory() as d:
+        f = os.path.join(d, "scene.flat")
+        subprocess.run([ADAPTER, "flatten", xml, f], check=True, capture_output=True)
+        return open(f, "rb").read()
+
+
+def make_refscenes():
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-s", "-j8", "adapter"], check=True)
+    out = {}
+    for name, (rel, w, h, spp) in REF_SCENES.items():
+        with tempfile.TemporaryDirectory() as d:
+            xml = reference_scene_variant(rel, w, h, spp, d)
+            out[name + "_flat"] = np.frombuffer(flatten_reference_scene(xml), np.uint8)
+            img, _ = ljo.run_reference(xml, os.path.join(d, "out.pfm"), threads=8)
+        out[name + "_render"] = img.astype(np.float32)
+    return out
+
+
 def main(which=()):
     """Regenerates every fixture, or only those named (e.g. `medium renders`):
     the functions share one seeded stream in a fixed order, so each fixture
@@ -298,7 +347,8 @@ def main(which=()):
               ("table", lambda: make_table(rng)), ("pcg", make_pcg), ("light", lambda: make_light(rng)),
               ("camera", lambda: make_camera(rng)), ("renders", make_renders),
               ("aux", lambda: make_renders(AUX_CASES)),
-              ("medium", lambda: make_medium(np.random.default_rng(20261204)))]
+              ("medium", lambda: make_medium(np.random.default_rng(20261204))),
+              ("refscenes", make_refscenes)]
     for name, mk in makers:
         data = mk()
         if not which or name in which:
