@@ -252,10 +252,11 @@ def pct(xs, q):
     return float(np.percentile(np.asarray(xs, np.float64), q)) if xs else None
 
 
-def job_desc(j, profile=False, count_bvh=False):
+def job_desc(j, profile=False, count_bvh=False, sample_offset=0):
     from lajolla_public_gb300 import gpu
-    return gpu.job_desc(seed=j["seed"], spp=j["spp"], width=j["width"], height=j["height"],
-                        max_depth=j["max_depth"], rr_depth=j["rr_depth"], profile=profile, count_bvh=count_bvh)
+    return gpu.job_desc(seed=j["seed"], spp=j["spp"], sample_offset=sample_offset, width=j["width"],
+                        height=j["height"], max_depth=j["max_depth"], rr_depth=j["rr_depth"], profile=profile,
+                        count_bvh=count_bvh)
 
 
 def serve_step(srv, gscenes, jobs, keep=()):
@@ -316,16 +317,19 @@ SCENE_KINDS = ("cornell box", "terrain + envmap", "volume")   # serving_scenes c
 
 
 def quality(srv, gscenes, pool, cs, out, stream, res=128, depth=16, ref_spp=65536,
-            spps=(4, 16, 64, 256, 1024, 4096), check_px=1024, check_spp=64):
+            spps=(4, 16, 64, 256, 1024, 4096), check_px=128, check_spp=4096, key_px=512, key_samples=2):
     """Per-image relative MSE (sum of squared errors / sum of squares of the
     reference) of one 128 x 128 job per scene kind against a 64k-spp render
     of the same job by the plain GPU renderer with an independent seed.
-    Each reference is first checked against the oracle: on `check_px` random
-    pixels, its value lies within 3 standard errors of the oracle's mean of
-    `check_spp` keyed samples.  The job is then rendered at each spp by the
-    server (batched) and by the plain renderer; both trace the same keyed
-    samples, so their errors match.  rel_mse x spp stays flat when the error
-    is the estimator's variance (no bias)."""
+    Each reference is first checked against the oracle twice: per pixel, on
+    `check_px` random pixels its value lies within 3 standard errors of the
+    oracle's mean of `check_spp` keyed samples (enough samples that
+    heavy-tailed pixels show their tails); and per sample, the GPU's samples
+    of the reference's own keys (whole images at `key_samples` sample
+    indices) equal the oracle's on `key_px` pixels each.  The job is then
+    rendered at each spp by the server (batched) and by the plain renderer;
+    both trace the same keyed samples, so their errors match.  rel_mse x spp
+    stays flat when the error is the estimator's variance (no bias)."""
     from lajolla_public_gb300 import gpu
     rows = []
     n = res * res * 3
@@ -339,7 +343,7 @@ def quality(srv, gscenes, pool, cs, out, stream, res=128, depth=16, ref_spp=6553
                                       stream=stream)
         ref = out[:n].cpu().numpy().reshape(res, res, 3).astype(np.float64)
         ref_s = time.perf_counter() - t0
-        # the reference against the oracle
+        # the reference against the oracle: per pixel (independent keys) ...
         px = cs.rng.integers(0, res * res, check_px).astype(np.int32)
         osm = cs.oss[si].render_job_samples(seed ^ 0x1234567, res, res, depth, 5, np.repeat(px, check_spp),
                                             np.tile(np.arange(check_spp, dtype=np.int32), check_px),
@@ -348,6 +352,18 @@ def quality(srv, gscenes, pool, cs, out, stream, res=128, depth=16, ref_spp=6553
         m_o, sd_o = osm.mean(axis=1), osm.std(axis=1)
         se = np.sqrt(sd_o ** 2 / check_spp + sd_o ** 2 / ref_spp) + 1e-9
         within = float((np.abs(ref.reshape(-1, 3)[px] - m_o) <= 3 * se).all(axis=1).mean())
+        # ... and per sample (the reference's own keys)
+        agree = []
+        for _ in range(key_samples):
+            k = int(cs.rng.integers(0, ref_spp))
+            gscenes[si].render_job_device(out[:n], job_desc(dict(job, spp=1, seed=seed ^ 0x5bd1e995),
+                                                            sample_offset=k), stream=stream)
+            g1 = out[:n].cpu().numpy().reshape(-1, 3).astype(np.float64)
+            kp = cs.rng.integers(0, res * res, key_px).astype(np.int32)
+            o1 = cs.oss[si].render_job_samples(seed ^ 0x5bd1e995, res, res, depth, 5, kp,
+                                               np.full(key_px, k, np.int32), nthreads=cs.cores)
+            o1 = np.where(np.isfinite(o1).all(axis=1, keepdims=True), o1, 0.0)
+            agree.append((np.abs(g1[kp] - o1) <= 1e-2 * np.maximum(np.abs(o1), 1e-1)).all(axis=1).mean())
         den = float(np.mean(ref ** 2)) + 1e-30
         per_spp, first_ok = [], None
         for spp in spps:
@@ -369,6 +385,9 @@ def quality(srv, gscenes, pool, cs, out, stream, res=128, depth=16, ref_spp=6553
                      "ref_render_s": round(ref_s, 3),
                      "ref_vs_oracle_within_3se": round(within, 4),
                      "ref_vs_oracle": "%d pixels x %d oracle samples" % (check_px, check_spp),
+                     "ref_keys_vs_oracle_agree": round(float(np.mean(agree)), 4),
+                     "ref_keys_vs_oracle": "%d sample indices x %d pixels of the reference's keys, 1e-2 relative"
+                                           % (key_samples, key_px),
                      "rel_mse": per_spp, "min_spp_meeting_1e-3": first_ok})
     return rows
 

@@ -45,7 +45,7 @@ extern "C" {
  * (LJ_KERNEL_MEDIUM, LJ_KERNEL_NEE) and the volumetric counters of
  * lj_server_stats
  * 3: the emission, camera-ray and medium batches; LJ_RENDER_COUNT_BVH and
- * the lj_stats.bvh_* counters */
+ * the lj_stats.bvh_* counters; lj_gpu_scene_update_mesh */
 #define LJ_GPU_ABI_VERSION 3
 
 /* ---- error codes -------------------------------------------------------- */
@@ -253,6 +253,22 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *desc, lj_scene **out);
  * reference's parser throws fl_exception (src/flexception.h:24,
  * src/parsers/parse_scene.cpp) on such input. */
 int lj_gpu_scene_validate(const lj_scene_desc *desc, char *msg, int msg_size);
+/* New vertex positions (and, when not NULL, normals) of mesh `shape_id`
+ * of a resident scene, num_vertices * 3 host floats (the mesh's vertex count
+ * at creation), with the BVH brought up to date on the device without
+ * uploading the scene again: LJ_UPDATE_REFIT keeps the tree's topology and
+ * recomputes its boxes bottom-up (fast; traversal slows down as the motion
+ * grows), LJ_UPDATE_REBUILD builds a new tree from the new positions.  The
+ * scene's bounds, bounding sphere, shadow epsilon, the mesh's emitter areas
+ * and the light-selection table follow the new positions, so the scene
+ * renders as one created with them would.  Waits for the device's queued
+ * work first.  Refused (LJ_ERR_INVALID_ARG) while the scene is registered
+ * with a running server.  Replaces rtcUpdateGeometryBuffer +
+ * rtcCommitGeometry + rtcCommitScene, Embree's path for moved geometry (the
+ * reference builds its Embree scene once, src/scene.cpp:19-34). */
+enum { LJ_UPDATE_REFIT = 0, LJ_UPDATE_REBUILD = 1 };
+int lj_gpu_scene_update_mesh(lj_scene *scene, int32_t shape_id, const float *positions, const float *normals,
+                             int32_t num_vertices, int32_t mode);
 /* Replaces Scene::~Scene / rtcReleaseScene (src/scene.cpp:55-59). */
 void lj_gpu_scene_destroy(lj_scene *scene);
 

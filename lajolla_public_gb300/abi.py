@@ -19,6 +19,7 @@ LJ_ERR_CANCELLED = -10
 LJ_ERR_SIZE_LIMIT = -11
 LJ_NOALLOC_MORTON_MAX_TRIANGLES = 65536
 LJ_RENDER_COUNT_BVH = 2
+LJ_UPDATE_REFIT, LJ_UPDATE_REBUILD = 0, 1
 LJ_COUNT_BVH_STRIDE = 16
 
 LJ_TEX_CONST, LJ_TEX_IMAGE, LJ_TEX_CHECKER = 0, 1, 2

@@ -599,6 +599,37 @@ __device__ void write_prim(const CollapseArgs &a, int sorted_pos, int slot) {
     }
 }
 
+// Quantisation frame of a wide node over its box [lo, hi]: per axis a
+// power-of-two step s (exponent e, stored biased by 127) with lo + 255 s >= hi.
+__device__ void quant_frame(const float lo[3], const float hi[3], uint32_t ebits[3], float sc[3]) {
+    for (int ax = 0; ax < 3; ax++) {
+        float ext = hi[ax] - lo[ax];
+        int e = ext > 0.0f ? (int)ceilf(log2f(ext / 255.0f)) : -126;
+        e = max(-126, min(127, e));
+        float s = ldexpf(1.0f, e);
+        while (lo[ax] + 255.0f * s < hi[ax] && e < 127) { e++; s = ldexpf(1.0f, e); }
+        ebits[ax] = (uint32_t)(e + 127);
+        sc[ax] = s;
+    }
+}
+// Conservative 8-bit planes of a child box [clo, chi] in that frame: the
+// dequantised box always contains the child's.
+__device__ void quant_child(const float clo[3], const float chi[3], const float lo[3], const float sc[3],
+                            uint32_t ql_out[3], uint32_t qh_out[3]) {
+    for (int ax = 0; ax < 3; ax++) {
+        float fl = floorf((clo[ax] - lo[ax]) / sc[ax]);
+        float fh = ceilf((chi[ax] - lo[ax]) / sc[ax]);
+        int ql = (int)fmaxf(0.0f, fminf(255.0f, fl));
+        int qh = (int)fmaxf(0.0f, fminf(255.0f, fh));
+        while (ql > 0 && lo[ax] + (float)ql * sc[ax] > clo[ax]) ql--;
+        while (qh < 255 && lo[ax] + (float)qh * sc[ax] < chi[ax]) qh++;
+        if (qh <= ql) { if (qh < 255) qh = ql + 1; else ql = qh - 1; }
+        ql_out[ax] = (uint32_t)ql;
+        qh_out[ax] = (uint32_t)qh;
+    }
+}
+__device__ uint32_t pack4(const uint32_t *b) { return b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24); }
+
 __global__ void k_collapse(CollapseArgs a) {
     int item = blockIdx.x * blockDim.x + threadIdx.x;
     if (item >= *a.qin_count) return;
@@ -699,15 +730,7 @@ __global__ void k_collapse(CollapseArgs a) {
     // quantization frame: per-axis power-of-two scale with 255 * s >= extent
     uint32_t ebits[3];
     float sc[3];
-    for (int ax = 0; ax < 3; ax++) {
-        float ext = hi[ax] - lo[ax];
-        int e = ext > 0.0f ? (int)ceilf(log2f(ext / 255.0f)) : -126;
-        e = max(-126, min(127, e));
-        float s = ldexpf(1.0f, e);
-        while (lo[ax] + 255.0f * s < hi[ax] && e < 127) { e++; s = ldexpf(1.0f, e); }
-        ebits[ax] = (uint32_t)(e + 127);
-        sc[ax] = s;
-    }
+    quant_frame(lo, hi, ebits, sc);
     uint32_t meta[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     uint32_t qlo[3][8], qhi[3][8];
     uint32_t imask = 0;
@@ -717,16 +740,13 @@ __global__ void k_collapse(CollapseArgs a) {
         int k = child_in_slot[s];
         if (k < 0) continue;
         const ChildInfo &c = ch[k];
-        for (int ax = 0; ax < 3; ax++) {
-            float fl = floorf((c.lo[ax] - lo[ax]) / sc[ax]);
-            float fh = ceilf((c.hi[ax] - lo[ax]) / sc[ax]);
-            int ql = (int)fmaxf(0.0f, fminf(255.0f, fl));
-            int qh = (int)fmaxf(0.0f, fminf(255.0f, fh));
-            while (ql > 0 && lo[ax] + (float)ql * sc[ax] > c.lo[ax]) ql--;
-            while (qh < 255 && lo[ax] + (float)qh * sc[ax] < c.hi[ax]) qh++;
-            if (qh <= ql) { if (qh < 255) qh = ql + 1; else ql = qh - 1; }
-            qlo[ax][s] = (uint32_t)ql;
-            qhi[ax][s] = (uint32_t)qh;
+        {
+            uint32_t ql[3], qh[3];
+            quant_child(c.lo, c.hi, lo, sc, ql, qh);
+            for (int ax = 0; ax < 3; ax++) {
+                qlo[ax][s] = ql[ax];
+                qhi[ax][s] = qh[ax];
+            }
         }
         if (inner[k]) {
             meta[s] = (1u << 5) | (24u + (uint32_t)s);
@@ -755,16 +775,107 @@ __global__ void k_collapse(CollapseArgs a) {
             prim_off += c.count;
         }
     }
-    auto pack = [](const uint32_t *b) {
-        return b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24);
-    };
     uint4 *dst = a.nodes + (size_t)q.y * kWideNodeU4;
     dst[0] = make_uint4(__float_as_uint(lo[0]), __float_as_uint(lo[1]), __float_as_uint(lo[2]),
                         ebits[0] | (ebits[1] << 8) | (ebits[2] << 16) | (imask << 24));
-    dst[1] = make_uint4((uint32_t)child_base, (uint32_t)prim_base, pack(meta), pack(meta + 4));
-    dst[2] = make_uint4(pack(qlo[0]), pack(qlo[0] + 4), pack(qlo[1]), pack(qlo[1] + 4));
-    dst[3] = make_uint4(pack(qlo[2]), pack(qlo[2] + 4), pack(qhi[0]), pack(qhi[0] + 4));
-    dst[4] = make_uint4(pack(qhi[1]), pack(qhi[1] + 4), pack(qhi[2]), pack(qhi[2] + 4));
+    dst[1] = make_uint4((uint32_t)child_base, (uint32_t)prim_base, pack4(meta), pack4(meta + 4));
+    dst[2] = make_uint4(pack4(qlo[0]), pack4(qlo[0] + 4), pack4(qlo[1]), pack4(qlo[1] + 4));
+    dst[3] = make_uint4(pack4(qlo[2]), pack4(qlo[2] + 4), pack4(qhi[0]), pack4(qhi[0] + 4));
+    dst[4] = make_uint4(pack4(qhi[1]), pack4(qhi[1] + 4), pack4(qhi[2]), pack4(qhi[2] + 4));
+}
+
+// ---- refit: the tree keeps its topology, boxes follow moved vertices ----
+// Leaf records of triangles rewritten from the vertex array (as write_prim
+// does at build time); sphere records are unchanged.
+__global__ void k_refit_prims(BvhInput in, float4 *prims, int n) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    float4 *dst = prims + (size_t)r * kPrimF4;
+    const int g = __float_as_int(dst[0].w);
+    if (g >= in.num_tris) return;
+    const int i0 = in.tri_vidx[g * 3], i1 = in.tri_vidx[g * 3 + 1], i2 = in.tri_vidx[g * 3 + 2];
+    V3 p0{in.vpos[i0 * 3], in.vpos[i0 * 3 + 1], in.vpos[i0 * 3 + 2]};
+    V3 p1{in.vpos[i1 * 3], in.vpos[i1 * 3 + 1], in.vpos[i1 * 3 + 2]};
+    V3 p2{in.vpos[i2 * 3], in.vpos[i2 * 3 + 1], in.vpos[i2 * 3 + 2]};
+    V3 e1 = xsub(p1, p0), e2 = xsub(p2, p0);
+    dst[0] = make_float4(p0.x, p0.y, p0.z, __int_as_float(g));
+    dst[1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+    dst[2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+}
+
+// Box of primitive g from the vertex array (triangles) or its record (spheres).
+__device__ void prim_box(const BvhInput &in, const float4 *rec, int g, float lo[3], float hi[3]) {
+    if (g < in.num_tris) {
+        for (int k = 0; k < 3; k++) {
+            const int v = in.tri_vidx[g * 3 + k];
+            for (int ax = 0; ax < 3; ax++) {
+                const float x = in.vpos[v * 3 + ax];
+                lo[ax] = fminf(lo[ax], x);
+                hi[ax] = fmaxf(hi[ax], x);
+            }
+        }
+    } else {
+        const float c[3] = {rec[0].x, rec[0].y, rec[0].z}, r = rec[1].x;
+        for (int ax = 0; ax < 3; ax++) {
+            lo[ax] = fminf(lo[ax], c[ax] - r);
+            hi[ax] = fmaxf(hi[ax], c[ax] + r);
+        }
+    }
+}
+
+// One level of wide nodes [begin, end), children (deeper levels) done: each
+// child's box (leaf primitives from the records, inner children from nbox),
+// the node's new frame and planes; topology (child_base, prim_base, meta,
+// slots) unchanged.  nbox[2 i], nbox[2 i + 1] = node i's lo, hi.
+__global__ void k_refit_nodes(BvhInput in, uint4 *nodes, const float4 *prims, float4 *nbox, int begin, int end) {
+    const int i = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= end) return;
+    uint4 *nd = nodes + (size_t)i * kWideNodeU4;
+    const uint4 w0 = nd[0], w1 = nd[1];
+    const uint32_t imask = w0.w >> 24;
+    const uint32_t child_base = w1.x, prim_base = w1.y;
+    float clo[8][3], chi[8][3];
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int s = 0; s < 8; s++) {
+        const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * (s & 3))) & 0xffu;
+        for (int ax = 0; ax < 3; ax++) { clo[s][ax] = FLT_MAX; chi[s][ax] = -FLT_MAX; }
+        if (meta == 0) continue;
+        if (imask & (1u << s)) {
+            const int c = (int)child_base + __popc(imask & ((1u << s) - 1u));
+            const float4 a = nbox[2 * c], b = nbox[2 * c + 1];
+            clo[s][0] = a.x; clo[s][1] = a.y; clo[s][2] = a.z;
+            chi[s][0] = b.x; chi[s][1] = b.y; chi[s][2] = b.z;
+        } else {
+            const int count = __popc(meta >> 5), off = (int)(meta & 31u);
+            for (int m = 0; m < count; m++) {
+                const float4 *rec = prims + (size_t)(prim_base + off + m) * kPrimF4;
+                prim_box(in, rec, __float_as_int(rec[0].w), clo[s], chi[s]);
+            }
+        }
+        for (int ax = 0; ax < 3; ax++) {
+            lo[ax] = fminf(lo[ax], clo[s][ax]);
+            hi[ax] = fmaxf(hi[ax], chi[s][ax]);
+        }
+    }
+    uint32_t ebits[3];
+    float sc[3];
+    quant_frame(lo, hi, ebits, sc);
+    uint32_t qlo[3][8], qhi[3][8];
+    for (int s = 0; s < 8; s++) {
+        uint32_t ql[3] = {0, 0, 0}, qh[3] = {0, 0, 0};
+        if (clo[s][0] <= chi[s][0]) quant_child(clo[s], chi[s], lo, sc, ql, qh);
+        for (int ax = 0; ax < 3; ax++) {
+            qlo[ax][s] = ql[ax];
+            qhi[ax][s] = qh[ax];
+        }
+    }
+    nd[0] = make_uint4(__float_as_uint(lo[0]), __float_as_uint(lo[1]), __float_as_uint(lo[2]),
+                       ebits[0] | (ebits[1] << 8) | (ebits[2] << 16) | (imask << 24));
+    nd[2] = make_uint4(pack4(qlo[0]), pack4(qlo[0] + 4), pack4(qlo[1]), pack4(qlo[1] + 4));
+    nd[3] = make_uint4(pack4(qlo[2]), pack4(qlo[2] + 4), pack4(qhi[0]), pack4(qhi[0] + 4));
+    nd[4] = make_uint4(pack4(qhi[1]), pack4(qhi[1] + 4), pack4(qhi[2]), pack4(qhi[2] + 4));
+    nbox[2 * i] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+    nbox[2 * i + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
 }
 
 __global__ void k_set_int(int *p, int v) { *p = v; }
@@ -852,6 +963,27 @@ __global__ void k_trace_count_queue(DevBvh bvh, const float4 *rays, const int *c
 inline int grid_for(int64_t n, int b) { return (int)((n + b - 1) / b); }
 
 }  // namespace
+
+int refit_bvh(const BvhInput &in, uint4 *nodes, float4 *prims, int num_prims, const std::vector<int> &level_start,
+              float lo[3], float hi[3], cudaStream_t s, std::string *err) {
+    if (num_prims <= 0 || level_start.size() < 2) return 0;
+    const int num_nodes = level_start.back();
+    k_refit_prims<<<grid_for(num_prims, 256), 256, 0, s>>>(in, prims, num_prims);
+    float4 *nbox = nullptr;
+    LJ_CUDA_TRY(cudaMallocAsync(&nbox, sizeof(float4) * 2 * (size_t)num_nodes, s));
+    for (int l = (int)level_start.size() - 2; l >= 0; l--) {
+        const int b = level_start[l], e = level_start[l + 1];
+        k_refit_nodes<<<grid_for(e - b, 128), 128, 0, s>>>(in, nodes, prims, nbox, b, e);
+    }
+    float4 root[2];
+    LJ_CUDA_TRY(cudaMemcpyAsync(root, nbox, sizeof(root), cudaMemcpyDeviceToHost, s));
+    LJ_CUDA_TRY(cudaFreeAsync(nbox, s));
+    LJ_CUDA_TRY(cudaStreamSynchronize(s));
+    LJ_CUDA_TRY(cudaGetLastError());
+    lo[0] = root[0].x; lo[1] = root[0].y; lo[2] = root[0].z;
+    hi[0] = root[1].x; hi[1] = root[1].y; hi[2] = root[1].z;
+    return 0;
+}
 
 int launch_trace_counters_queue(const DevBvh &bvh, const void *rays, const int *d_count, int64_t cap, int stride,
                                 bool any, unsigned long long *d_counts, int *d_status, cudaStream_t s) {
@@ -1029,12 +1161,18 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
     int qcount = 1;
     int2 *qin = q0, *qout = q1;
     int *cin = counters + 2, *cout = counters + 3;
+    // one launch per level; the launch for level L allocates all of level
+    // L + 1's nodes, so every level is one contiguous index range
+    out->level_start.assign({0, 1});
     for (int level = 0; level < 4096 && qcount > 0; level++) {
         k_set_int<<<1, 1, 0, s>>>(cout, 0);
         a.qin = qin; a.qin_count = cin; a.qout = qout; a.qout_count = cout;
         k_collapse<<<grid_for(qcount, 128), 128, 0, s>>>(a);
+        int nodes_so_far = 0;
         LJ_CUDA_TRY(cudaMemcpyAsync(&qcount, cout, sizeof(int), cudaMemcpyDeviceToHost, s));
+        LJ_CUDA_TRY(cudaMemcpyAsync(&nodes_so_far, counters, sizeof(int), cudaMemcpyDeviceToHost, s));
         LJ_CUDA_TRY(cudaStreamSynchronize(s));
+        if (nodes_so_far > out->level_start.back()) out->level_start.push_back(nodes_so_far);
         std::swap(qin, qout);
         std::swap(cin, cout);
     }

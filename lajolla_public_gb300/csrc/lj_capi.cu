@@ -377,6 +377,9 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
         else num_spheres++;
     sc->num_spheres = num_spheres;
     sc->shape_prim_base.assign(d->num_shapes, 0);
+    sc->shape_vbase.assign(d->num_shapes, -1);
+    sc->shape_nverts.assign(d->num_shapes, 0);
+    sc->emitter_indices.assign(d->num_shapes, {});
     int tri_base = 0, sphere_ord = 0;
     prim_shape.assign((size_t)num_tris + num_spheres, 0);
     tri_vidx.resize((size_t)num_tris * 3);
@@ -395,6 +398,10 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
         r.exterior_medium_id = s.exterior_medium_id;
         if (s.kind == LJ_SHAPE_MESH) {
             int vbase = (int)(vpos.size() / 3);
+            sc->shape_vbase[i] = vbase;
+            sc->shape_nverts[i] = s.num_vertices;
+            if (emits[i] || s.area_light_id >= 0)
+                sc->emitter_indices[i].assign(s.indices, s.indices + (size_t)s.num_triangles * 3);
             vpos.insert(vpos.end(), s.positions, s.positions + (size_t)s.num_vertices * 3);
             if (s.normals) vnrm.insert(vnrm.end(), s.normals, s.normals + (size_t)s.num_vertices * 3);
             else vnrm.insert(vnrm.end(), (size_t)s.num_vertices * 3, 0.0f);
@@ -448,6 +455,8 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
         return fail(LJ_ERR_CUDA);
     const float *d_spheres = nullptr;
     if (upload(sc, spheres, &d_spheres, &err)) return fail(LJ_ERR_CUDA);
+    sc->d_spheres = d_spheres;
+    sc->shapes_host = shapes;
     ds.num_tris = num_tris;
     ds.num_prims = num_tris + num_spheres;
     ds.num_shapes = d->num_shapes;
@@ -463,6 +472,7 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
     ds.bvh.prims = bout.prims;
     ds.bvh.num_nodes = bout.num_nodes;
     ds.bvh.num_leaf_prims = ds.num_prims;
+    sc->bvh_levels = bout.level_start;
     sc->info.num_wide_nodes = bout.num_nodes;
     sc->info.num_binary_nodes = bout.num_binary;
     sc->info.build_ms = bout.build_ms;
@@ -532,6 +542,7 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
     // ---- lights + power table (src/scene.cpp:47-52) ----
     std::vector<LightRec> lights(d->num_lights);
     std::vector<double> power(d->num_lights);
+    sc->light_factor.assign(d->num_lights, 0.0);
     ds.env.light_id = -1;
     for (int i = 0; i < d->num_lights; i++) {
         const lj_light_desc &l = d->lights[i];
@@ -551,7 +562,8 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
             double area = shapes[l.shape_id].total_area;
             if (d->shapes[l.shape_id].kind == LJ_SHAPE_SPHERE)
                 area = 4 * M_PI * (double)d->shapes[l.shape_id].radius * d->shapes[l.shape_id].radius;
-            power[i] = luminance_d(l.intensity[0], l.intensity[1], l.intensity[2]) * area * M_PI;
+            sc->light_factor[i] = luminance_d(l.intensity[0], l.intensity[1], l.intensity[2]) * M_PI;
+            power[i] = sc->light_factor[i] * area;
         } else {
             // envmap sampling table from luminance * sin(elevation) at level 0
             const HostImg &im = mips[l.image_id][0];
@@ -603,7 +615,8 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
             ds.env.light_id = i;
             ds.env.num_levels = (int)mips[l.image_id].size();
             for (int k = 0; k < ds.env.num_levels; k++) ds.env.levels[k] = levels[l.image_id * 8 + k];
-            power[i] = M_PI * sc->info.bsphere_radius * sc->info.bsphere_radius * total / ((double)w * h);
+            sc->light_factor[i] = M_PI * total / ((double)w * h);
+            power[i] = sc->light_factor[i] * sc->info.bsphere_radius * sc->info.bsphere_radius;
         }
     }
     if (d->envmap_light_id >= 0 && ds.env.light_id != d->envmap_light_id)
@@ -689,6 +702,150 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
     }
     ctx->scenes.push_back(sc);
     *out = sc;
+    return LJ_OK;
+}
+
+int lj_gpu_scene_update_mesh(lj_scene *sc, int32_t shape_id, const float *positions, const float *normals,
+                             int32_t num_vertices, int32_t mode) {
+    if (!sc) return LJ_ERR_INVALID_ARG;
+    lj_ctx *ctx = sc->ctx;
+    if (shape_id < 0 || shape_id >= (int)sc->shapes_host.size() || sc->shapes_host[shape_id].kind != LJ_SHAPE_MESH)
+        return set_error(ctx, LJ_ERR_INVALID_ARG, "scene_update_mesh: shape_id is not a mesh of the scene");
+    if (!positions || num_vertices != sc->shape_nverts[shape_id])
+        return set_error(ctx, LJ_ERR_INVALID_ARG, "scene_update_mesh: positions must hold the mesh's " +
+                                                      std::to_string(sc->shape_nverts[shape_id]) + " vertices");
+    if (mode != LJ_UPDATE_REFIT && mode != LJ_UPDATE_REBUILD)
+        return set_error(ctx, LJ_ERR_INVALID_ARG, "scene_update_mesh: unknown mode");
+    if (normals && !sc->shapes_host[shape_id].has_normals)
+        return set_error(ctx, LJ_ERR_INVALID_ARG, "scene_update_mesh: the mesh was created without normals");
+    if (sc->server_refs.load() > 0)
+        return set_error(ctx, LJ_ERR_INVALID_ARG, "scene_update_mesh: the scene is registered with a running server");
+    const size_t nv = (size_t)num_vertices;
+    for (size_t k = 0; k < nv * 3; k++)
+        if (!std::isfinite(positions[k]))
+            return set_error(ctx, LJ_ERR_INVALID_ARG, "scene_update_mesh: a position is not finite");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    std::string err;
+    // work queued on any stream may still read the scene
+    if (cudaDeviceSynchronize() != cudaSuccess) return set_error(ctx, LJ_ERR_CUDA, "scene_update_mesh: device error");
+    DevScene &ds = sc->dev;
+    const size_t vbase = (size_t)sc->shape_vbase[shape_id];
+    if (cudaMemcpyAsync(const_cast<float *>(ds.vpos) + vbase * 3, positions, sizeof(float) * nv * 3,
+                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        (normals && cudaMemcpyAsync(const_cast<float *>(ds.vnrm) + vbase * 3, normals, sizeof(float) * nv * 3,
+                                    cudaMemcpyHostToDevice, s) != cudaSuccess))
+        return set_error(ctx, LJ_ERR_CUDA, "scene_update_mesh: upload failed");
+
+    // ---- BVH: refit in place, or rebuild ----
+    BvhInput bin{ds.vpos, ds.tri_vidx, sc->d_spheres, ds.num_tris, sc->num_spheres};
+    float lo[3], hi[3];
+    if (mode == LJ_UPDATE_REFIT) {
+        if (refit_bvh(bin, const_cast<uint4 *>(ds.bvh.nodes), const_cast<float4 *>(ds.bvh.prims), ds.num_prims,
+                      sc->bvh_levels, lo, hi, s, &err))
+            return set_error(ctx, LJ_ERR_CUDA, "scene_update_mesh: " + err);
+    } else {
+        BvhOutput bout;
+        int rc = build_bvh(bin, &bout, s, &err);
+        if (rc) {
+            if (bout.nodes) cudaFree(bout.nodes);
+            if (bout.prims) cudaFree(bout.prims);
+            return set_error(ctx, rc == -5 ? LJ_ERR_DEVICE_LIMIT : LJ_ERR_CUDA, "scene_update_mesh: " + err);
+        }
+        for (void *&a : sc->allocs) {
+            if (a == (void *)ds.bvh.nodes) {
+                cudaFree(a);
+                a = bout.nodes;
+            } else if (a == (void *)ds.bvh.prims) {
+                cudaFree(a);
+                a = bout.prims;
+            }
+        }
+        sc->info.device_bytes += ((int64_t)bout.num_nodes - ds.bvh.num_nodes) * 80;
+        ds.bvh.nodes = bout.nodes;
+        ds.bvh.prims = bout.prims;
+        ds.bvh.num_nodes = bout.num_nodes;
+        sc->bvh_levels = bout.level_start;
+        sc->info.num_wide_nodes = bout.num_nodes;
+        sc->info.num_binary_nodes = bout.num_binary;
+        sc->info.build_ms = bout.build_ms;
+        for (int k = 0; k < 3; k++) {
+            lo[k] = bout.lo[k];
+            hi[k] = bout.hi[k];
+        }
+    }
+    // ---- bounds, bounding sphere and shadow epsilon (src/scene.cpp:29-34,
+    // src/scene.h:99-105) follow the new geometry ----
+    {
+        double dd = 0;
+        for (int k = 0; k < 3; k++) {
+            sc->info.bounds_lower[k] = lo[k];
+            sc->info.bounds_upper[k] = hi[k];
+            dd += ((double)hi[k] - lo[k]) * ((double)hi[k] - lo[k]);
+        }
+        sc->info.bsphere_radius = std::sqrt(dd) / 2;
+        for (int k = 0; k < 3; k++) sc->info.bsphere_center[k] = ((double)lo[k] + hi[k]) / 2;
+        ds.bradius = (float)sc->info.bsphere_radius;
+        for (int k = 0; k < 3; k++) ds.bcenter[k] = (float)sc->info.bsphere_center[k];
+        ds.eps = (float)std::min(sc->info.bsphere_radius * 1e-5, 0.01);
+    }
+    // ---- an emitting mesh's triangle areas and sampling table ----
+    ShapeRec &r = sc->shapes_host[shape_id];
+    const std::vector<int32_t> &idx = sc->emitter_indices[shape_id];
+    if (!idx.empty()) {
+        const int nt = (int)(idx.size() / 3);
+        std::vector<double> areas(nt);
+        double total = 0;
+        for (int t = 0; t < nt; t++) {
+            const float *p0 = positions + idx[t * 3] * 3, *p1 = positions + idx[t * 3 + 1] * 3,
+                        *p2 = positions + idx[t * 3 + 2] * 3;
+            double e1[3] = {(double)p1[0] - p0[0], (double)p1[1] - p0[1], (double)p1[2] - p0[2]};
+            double e2[3] = {(double)p2[0] - p0[0], (double)p2[1] - p0[1], (double)p2[2] - p0[2]};
+            double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                   cz = e1[0] * e2[1] - e1[1] * e2[0];
+            areas[t] = std::sqrt(cx * cx + cy * cy + cz * cz) / 2;
+            total += areas[t];
+        }
+        r.total_area = (float)total;
+        if (cudaMemcpyAsync(const_cast<ShapeRec *>(ds.shapes) + shape_id, &r, sizeof(ShapeRec),
+                            cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return set_error(ctx, LJ_ERR_CUDA, "scene_update_mesh: upload failed");
+        if (r.sampler_offset >= 0) {
+            std::vector<float> pmf, cdf;
+            table_1d(areas, pmf, cdf);
+            if (cudaMemcpyAsync(const_cast<float *>(ds.tri_cdf) + r.sampler_offset, cdf.data(),
+                                sizeof(float) * cdf.size(), cudaMemcpyHostToDevice, s) != cudaSuccess)
+                return set_error(ctx, LJ_ERR_CUDA, "scene_update_mesh: upload failed");
+        }
+    }
+    // ---- light-selection table (src/scene.cpp:47-52): area lights by their
+    // shapes' areas, the envmap by the bounding radius ----
+    if (ds.num_lights > 0) {
+        std::vector<double> power(ds.num_lights);
+        std::vector<LightRec> lr(ds.num_lights);
+        if (cudaMemcpyAsync(lr.data(), ds.lights, sizeof(LightRec) * lr.size(), cudaMemcpyDeviceToHost, s) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return set_error(ctx, LJ_ERR_CUDA, "scene_update_mesh: light table read failed");
+        for (int i = 0; i < ds.num_lights; i++) {
+            if (lr[i].kind == LJ_LIGHT_AREA) {
+                const ShapeRec &sh = sc->shapes_host[lr[i].shape_id];
+                double area = sh.kind == LJ_SHAPE_SPHERE ? 4 * M_PI * (double)sh.radius * sh.radius : sh.total_area;
+                power[i] = sc->light_factor[i] * area;
+            } else {
+                power[i] = sc->light_factor[i] * sc->info.bsphere_radius * sc->info.bsphere_radius;
+            }
+        }
+        std::vector<float> lpmf, lcdf;
+        table_1d(power, lpmf, lcdf);
+        if (cudaMemcpyAsync(const_cast<float *>(ds.light_pmf), lpmf.data(), sizeof(float) * lpmf.size(),
+                            cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(const_cast<float *>(ds.light_cdf), lcdf.data(), sizeof(float) * lcdf.size(),
+                            cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return set_error(ctx, LJ_ERR_CUDA, "scene_update_mesh: upload failed");
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess)
+        return set_error(ctx, LJ_ERR_CUDA, "scene_update_mesh: stream synchronize failed");
     return LJ_OK;
 }
 

@@ -46,6 +46,18 @@ struct lj_scene {
     lj_camera_desc camera{};
     uint32_t mat_mask = 0;             // bit t: a material of type t exists
     std::atomic<int> server_refs{0};   // servers this scene is registered with
+    // kept for lj_gpu_scene_update_mesh: the BVH's levels and sphere records,
+    // where each mesh's vertices start, the host copy of the shape records
+    // and the triangle indices of emitting meshes (their areas feed the
+    // light tables), and each light's power factor (area light: luminance x
+    // pi, times its shape's area; envmap: pi x mean table value, times the
+    // bounding radius squared)
+    const float *d_spheres = nullptr;
+    std::vector<int> bvh_levels;
+    std::vector<int> shape_vbase, shape_nverts;
+    std::vector<lj::ShapeRec> shapes_host;
+    std::vector<std::vector<int32_t>> emitter_indices;
+    std::vector<double> light_factor;
 };
 
 namespace lj {

@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <string>
+#include <vector>
 
 #include "lj_scene.cuh"
 
@@ -64,8 +65,15 @@ struct BvhOutput {
     int num_binary = 0;
     float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // scene AABB (rtcGetSceneBounds)
     double build_ms = 0;
+    // wide nodes level by level: level l is [level_start[l], level_start[l + 1])
+    std::vector<int> level_start;
 };
 int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *err);
+// Refit of a built tree to moved vertices (in.vpos): leaf records rewritten,
+// node boxes recomputed level by level from the deepest, topology kept;
+// lo / hi receive the new root box.
+int refit_bvh(const BvhInput &in, uint4 *nodes, float4 *prims, int num_prims, const std::vector<int> &level_start,
+              float lo[3], float hi[3], cudaStream_t s, std::string *err);
 
 // ---- batch trace (lj_bvh.cu) ----
 int launch_trace_closest(const DevBvh &bvh, const void *rays, void *hits, int64_t n,

@@ -378,14 +378,20 @@ __global__ void __launch_bounds__(B, 1024 / B) k_srv_trace(SrvDev d, int cur) {
 // The scene and job tables are read-only here (restrict: the stores of the
 // shade step cannot alias them, so their fields need not be re-read).
 // One instance per material class: class 0 (the queue's front) runs the
-// smaller kernel compiled for kClassicMats.
-template <int B, int kClass>
-__global__ void __launch_bounds__(B, (kClass == 0 ? 640 : 512) / B)
+// smaller kernel compiled for kClassicMats.  The shade kernels run at
+// kShadeBlock threads whatever the server's block size, with the single-
+// scene renderer's occupancy (6 blocks per SM, 5 for every material type:
+// a few spilled registers cost less than the warps fewer blocks would lose).
+// One compiled instance per class keeps a job's arithmetic -- and so its
+// image -- independent of the block size the other kernels use.
+constexpr int kShadeBlock = 128;
+template <int kClass>
+__global__ void __launch_bounds__(kShadeBlock, kClass == 0 ? 6 : 5)
     k_srv_shade(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
     const int n = d.counts[kClass == 0 ? cur : 10 + cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 2, (unsigned long long)n);
     const QueuePaths<kClass> paths{d, cur};
-    for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
+    for (int i = blockIdx.x * kShadeBlock + threadIdx.x; i < n; i += gridDim.x * kShadeBlock) {
         const int e = kClass == 0 ? i : d.back(i);
         const SrvJob &jb = jobs[d.buf[cur].job[e]];
         const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
@@ -556,7 +562,7 @@ struct KernelSet {
 };
 template <int B>
 KernelSet kernel_set() {
-    return KernelSet{k_srv_regen<B>,      k_srv_trace<B>,       k_srv_shade<B, 0>,    k_srv_shade<B, 1>,
+    return KernelSet{k_srv_regen<B>,      k_srv_trace<B>,       k_srv_shade<0>,       k_srv_shade<1>,
                      k_srv_vol_a<B>,      k_srv_vol_b<B>,       k_srv_vol_c<B, 0>,    k_srv_vol_c<B, 1>,
                      k_srv_vol_c<B, 2>,   k_srv_shadow<B>,      k_srv_retire<B>};
 }
@@ -742,10 +748,10 @@ void launch_wave(lj_server *s, int cur) {
     s->ks.trace<<<s->grid[1], B, 0, s->stream>>>(s->dev, cur);
     mark(s, LJ_KERNEL_TRACE, false);
     mark(s, LJ_KERNEL_SHADE, true);
-    s->ks.shade0<<<s->grid[2], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    s->ks.shade0<<<s->grid[2], kShadeBlock, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
     mark(s, LJ_KERNEL_SHADE, false);
     mark(s, LJ_KERNEL_SHADE, true);
-    s->ks.shade1<<<s->grid[5], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
+    s->ks.shade1<<<s->grid[5], kShadeBlock, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
     mark(s, LJ_KERNEL_SHADE, false);
     mark(s, LJ_KERNEL_MEDIUM, true);
     s->ks.vol_a<<<s->grid[6], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
@@ -897,8 +903,8 @@ std::string build_device(lj_server *s) {
     SRV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
     s->grid[0] = occupancy_grid((const void *)s->ks.regen, s->block, sms);
     s->grid[1] = occupancy_grid((const void *)s->ks.trace, s->block, sms);
-    s->grid[2] = occupancy_grid((const void *)s->ks.shade0, s->block, sms);
-    s->grid[5] = occupancy_grid((const void *)s->ks.shade1, s->block, sms);
+    s->grid[2] = occupancy_grid((const void *)s->ks.shade0, kShadeBlock, sms);
+    s->grid[5] = occupancy_grid((const void *)s->ks.shade1, kShadeBlock, sms);
     s->grid[6] = occupancy_grid((const void *)s->ks.vol_a, s->block, sms);
     s->grid[7] = occupancy_grid((const void *)s->ks.vol_b, s->block, sms);
     s->grid[8] = occupancy_grid((const void *)s->ks.vol_c0, s->block, sms);

@@ -53,6 +53,7 @@ def lib():
         L.lj_gpu_scene_create.argtypes = [vp, C.POINTER(abi.lj_scene_desc), C.POINTER(vp)]
         L.lj_gpu_scene_validate.argtypes = [C.POINTER(abi.lj_scene_desc), C.c_char_p, C.c_int]
         L.lj_gpu_scene_destroy.argtypes = [vp]
+        L.lj_gpu_scene_update_mesh.argtypes = [vp, i32, vp, vp, i32, i32]
         L.lj_gpu_scene_info.argtypes = [vp, C.POINTER(abi.lj_scene_info)]
         L.lj_gpu_render.argtypes = [vp, C.POINTER(abi.lj_render_params), vp, C.POINTER(abi.lj_stats)]
         L.lj_gpu_render_device.argtypes = [vp, C.POINTER(abi.lj_render_params), vp, vp,
@@ -207,6 +208,17 @@ class GpuScene:
             self.close()
         except Exception:
             pass
+
+    def update_mesh(self, shape_id, positions, normals=None, rebuild=False):
+        """New vertex positions (and normals) of mesh `shape_id`; the BVH is
+        refitted (or rebuilt) on the device.  The host-side scene
+        description is not changed."""
+        pos = np.ascontiguousarray(positions, np.float32)
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+        self.ctx.check(lib().lj_gpu_scene_update_mesh(
+            self.h, int(shape_id), pos.ctypes.data_as(C.c_void_p),
+            None if nrm is None else nrm.ctypes.data_as(C.c_void_p), len(pos),
+            abi.LJ_UPDATE_REBUILD if rebuild else abi.LJ_UPDATE_REFIT))
 
     def info(self):
         inf = abi.lj_scene_info()
