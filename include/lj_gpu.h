@@ -528,8 +528,13 @@ typedef struct lj_server_options {
     int32_t use_graphs;          /* 1 = replay captured CUDA graphs, 0 = plain launches    */
     int32_t flags;               /* LJ_SERVER_PROFILE: time each kernel class with CUDA
                                     events (plain launches, a host sync per poll)          */
-    int32_t pad;
+    int32_t tune_objective;      /* lj_gpu_server_autotune: LJ_TUNE_*                      */
 } lj_server_options;
+/* Autotuner objectives.  BALANCED: among the candidates within 3% of the
+ * highest throughput, the one with the lowest median job latency (a larger
+ * path pool often buys a little throughput with much later small jobs);
+ * THROUGHPUT: the highest Msamples/s; LATENCY: the lowest median latency. */
+enum { LJ_TUNE_BALANCED = 0, LJ_TUNE_THROUGHPUT = 1, LJ_TUNE_LATENCY = 2 };
 #define LJ_SERVER_PROFILE 1
 #define LJ_SERVER_ONE_SHADE_KERNEL 2   /* every job through the all-materials shade kernel */
 
@@ -596,10 +601,13 @@ int lj_gpu_server_stop(lj_server *server);
 int lj_gpu_render_job_device(lj_scene *scene, const lj_job_desc *job, float *d_out_rgb, void *stream,
                              lj_stats *stats);
 
-/* Autotuner: runs the given job mix (job i renders scenes[job_scene[i]])
- * once per candidate (path pool x block size) and writes the fastest into
- * *options (other fields are kept).  With cache_path, results are read from
- * and stored in that JSON file, keyed by device and workload size. */
+/* Autotuner: runs the given job mix (job i renders scenes[job_scene[i]],
+ * all submitted at once) once per candidate path pool x block size, then
+ * waves between polls for the best of those, and writes the choice that
+ * options->tune_objective ranks first into *options (other fields are
+ * kept).  With cache_path, results are read from and stored in that JSON
+ * file, keyed by device, objective and workload (total samples, largest
+ * scene, share of volumetric samples, mean max depth). */
 int lj_gpu_server_autotune(lj_ctx *ctx, lj_scene *const *scenes, const lj_job_desc *jobs,
                            const int32_t *job_scene, int32_t n_jobs, const char *cache_path,
                            lj_server_options *options);

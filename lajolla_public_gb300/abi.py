@@ -20,6 +20,7 @@ LJ_ERR_SIZE_LIMIT = -11
 LJ_NOALLOC_MORTON_MAX_TRIANGLES = 65536
 LJ_RENDER_COUNT_BVH = 2
 LJ_UPDATE_REFIT, LJ_UPDATE_REBUILD = 0, 1
+LJ_TUNE_BALANCED, LJ_TUNE_THROUGHPUT, LJ_TUNE_LATENCY = 0, 1, 2
 LJ_COUNT_BVH_STRIDE = 16
 
 LJ_TEX_CONST, LJ_TEX_IMAGE, LJ_TEX_CHECKER = 0, 1, 2
@@ -182,7 +183,8 @@ class lj_server_options(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_int64), ("path_pool", C.c_int64),
                 ("block_size", C.c_int32), ("max_live_jobs", C.c_int32),
                 ("max_queued_jobs", C.c_int32), ("waves_per_poll", C.c_int32),
-                ("policy", C.c_int32), ("use_graphs", C.c_int32), ("flags", C.c_int32), ("pad", C.c_int32)]
+                ("policy", C.c_int32), ("use_graphs", C.c_int32), ("flags", C.c_int32),
+                ("tune_objective", C.c_int32)]
 
 
 class lj_job_desc(C.Structure):

@@ -1511,23 +1511,39 @@ int lj_gpu_server_autotune(lj_ctx *ctx, lj_scene *const *scenes, const lj_job_de
                            const int32_t *job_scene, int32_t n_jobs, const char *cache_path,
                            lj_server_options *options) {
     if (!ctx || !scenes || !jobs || !job_scene || n_jobs <= 0 || !options) return LJ_ERR_INVALID_ARG;
-    // workload key: device, SM count, total samples and largest scene (log2 buckets)
+    const int objective = options->tune_objective;
+    if (objective < LJ_TUNE_BALANCED || objective > LJ_TUNE_LATENCY)
+        return set_error(ctx, LJ_ERR_INVALID_ARG, "autotune: unknown objective");
+    // workload key: device, SM count, objective, total samples and largest
+    // scene (log2 buckets), share of volumetric samples (tenths), mean max
+    // depth (log2 bucket)
     cudaDeviceProp prop{};
     if (cudaGetDeviceProperties(&prop, ctx->device) != cudaSuccess)
         return set_error(ctx, LJ_ERR_CUDA, "autotune: cannot query the device");
-    double total = 0, max_prims = 1;
+    double total = 0, max_prims = 1, vol = 0, depth = 0;
     for (int i = 0; i < n_jobs; i++) {
         const lj_scene *sc = scenes[job_scene[i]];
         double w = jobs[i].width > 0 ? jobs[i].width : sc->width;
         double h = jobs[i].height > 0 ? jobs[i].height : sc->height;
         double spp = jobs[i].spp > 0 ? jobs[i].spp : sc->options.samples_per_pixel;
         total += w * h * spp;
+        if (sc->options.integrator == LJ_INTEGRATOR_VOLPATH) vol += w * h * spp;
+        int md = jobs[i].override_depth ? jobs[i].max_depth : sc->options.max_depth;
+        depth += md < 0 ? 64 : md;
         max_prims = std::max(max_prims, (double)sc->info.num_prims);
     }
     std::ostringstream key;
-    key << prop.name << "|sm" << prop.multiProcessorCount << "|samples2^" << (int)std::lround(std::log2(total + 1))
-        << "|prims2^" << (int)std::lround(std::log2(max_prims));
+    key << prop.name << "|sm" << prop.multiProcessorCount << "|obj" << objective << "|samples2^"
+        << (int)std::lround(std::log2(total + 1)) << "|prims2^" << (int)std::lround(std::log2(max_prims))
+        << "|vol" << (int)std::lround(10 * vol / std::max(total, 1.0)) << "|depth2^"
+        << (int)std::lround(std::log2(depth / n_jobs + 1));
     std::map<std::string, std::string> cache;
+    auto field = [](const std::string &v, const char *name, long long *out) {
+        size_t p = v.find(std::string("\"") + name + "\":");
+        if (p == std::string::npos) return false;
+        *out = std::strtoll(v.c_str() + p + std::strlen(name) + 3, nullptr, 10);
+        return true;
+    };
     if (cache_path) {
         std::ifstream f(cache_path);
         std::string line;
@@ -1539,53 +1555,96 @@ int lj_gpu_server_autotune(lj_ctx *ctx, lj_scene *const *scenes, const lj_job_de
             cache[line.substr(a + 1, b - a - 1)] = line.substr(c, d - c + 1);
         }
         auto it = cache.find(key.str());
-        if (it != cache.end()) {
-            const std::string &v = it->second;
-            size_t pp = v.find("\"path_pool\":"), bb = v.find("\"block_size\":");
-            if (pp != std::string::npos && bb != std::string::npos) {
-                options->path_pool = std::strtoll(v.c_str() + pp + 12, nullptr, 10);
-                options->block_size = (int32_t)std::strtol(v.c_str() + bb + 13, nullptr, 10);
-                return LJ_OK;
-            }
+        long long pool = 0, blk = 0, wpp = 0;
+        if (it != cache.end() && field(it->second, "path_pool", &pool) && field(it->second, "block_size", &blk) &&
+            field(it->second, "waves_per_poll", &wpp)) {
+            options->path_pool = pool;
+            options->block_size = (int32_t)blk;
+            options->waves_per_poll = (int32_t)wpp;
+            return LJ_OK;
         }
     }
+    struct Cand {
+        int64_t pool;
+        int32_t block, wpp;
+        double rate, latency;   // Msamples/s, median job latency (ms)
+    };
+    // one run of the job mix, all jobs submitted at once
+    auto run = [&](Cand &c, std::string *why) {
+        lj_server_options o = *options;
+        o.path_pool = c.pool;
+        o.block_size = c.block;
+        o.waves_per_poll = c.wpp;
+        lj_server *srv = nullptr;
+        if (lj_gpu_server_start(ctx, &o, &srv) != LJ_OK) return 1;   // e.g. pool above the budget
+        auto t0 = std::chrono::steady_clock::now();
+        std::vector<int64_t> ids(n_jobs, 0);
+        std::vector<double> lat;
+        bool ok = true;
+        for (int i = 0; i < n_jobs && ok; i++)
+            ok = lj_gpu_server_submit(srv, scenes[job_scene[i]], &jobs[i], &ids[i]) == LJ_OK;
+        for (int i = 0; i < n_jobs && ok; i++) {
+            lj_job_status st{};
+            ok = lj_gpu_server_wait(srv, ids[i], 600.0, nullptr, &st) == LJ_OK;
+            lat.push_back(st.finish_ms - st.submit_ms);
+        }
+        double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        *why = lj_gpu_server_last_error(srv);
+        if (lj_gpu_server_stop(srv) != LJ_OK) ok = false;
+        if (!ok) return -1;
+        std::sort(lat.begin(), lat.end());
+        c.rate = total / sec * 1e-6;
+        c.latency = lat[lat.size() / 2];
+        return 0;
+    };
+    auto better = [&](const Cand &a, const Cand &b, double best_rate) {   // is a preferred to b?
+        if (objective == LJ_TUNE_THROUGHPUT) return a.rate > b.rate;
+        if (objective == LJ_TUNE_LATENCY) return a.latency < b.latency;
+        const bool ia = a.rate >= 0.97 * best_rate, ib = b.rate >= 0.97 * best_rate;
+        if (ia != ib) return ia;
+        return ia ? a.latency < b.latency : a.rate > b.rate;
+    };
+    auto pick = [&](std::vector<Cand> &cs) {
+        double best_rate = 0;
+        for (const Cand &c : cs) best_rate = std::max(best_rate, c.rate);
+        size_t k = 0;
+        for (size_t i = 1; i < cs.size(); i++)
+            if (better(cs[i], cs[k], best_rate)) k = i;
+        return cs[k];
+    };
     const int64_t pools[] = {(int64_t)1 << 20, (int64_t)1 << 21, (int64_t)1 << 22, (int64_t)1 << 23,
                              (int64_t)1 << 24};
     const int32_t blocks[] = {64, 128, 256};
-    double best = -1;
-    int64_t best_pool = 0;
-    int32_t best_block = 0;
-    for (int64_t pool : pools) {
+    const int32_t wpps[] = {4, 8, 16};
+    std::vector<Cand> done;
+    std::string why;
+    // path pool x block size at 8 waves per poll, then waves per poll for the
+    // best of those (the poll interval hardly interacts with the other two)
+    for (int64_t pool : pools)
         for (int32_t blk : blocks) {
-            lj_server_options o = *options;
-            o.path_pool = pool;
-            o.block_size = blk;
-            lj_server *srv = nullptr;
-            if (lj_gpu_server_start(ctx, &o, &srv) != LJ_OK) continue;   // e.g. pool above the budget
-            auto t0 = std::chrono::steady_clock::now();
-            std::vector<int64_t> ids(n_jobs, 0);
-            bool ok = true;
-            for (int i = 0; i < n_jobs && ok; i++)
-                ok = lj_gpu_server_submit(srv, scenes[job_scene[i]], &jobs[i], &ids[i]) == LJ_OK;
-            for (int i = 0; i < n_jobs && ok; i++) ok = lj_gpu_server_wait(srv, ids[i], 600.0, nullptr, nullptr) == LJ_OK;
-            double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-            std::string srv_err = lj_gpu_server_last_error(srv);
-            if (lj_gpu_server_stop(srv) != LJ_OK) ok = false;
-            if (!ok) return set_error(ctx, LJ_ERR_CUDA, "autotune: candidate run failed: " + srv_err);
-            double rate = total / sec * 1e-6;
-            if (rate > best) {
-                best = rate;
-                best_pool = pool;
-                best_block = blk;
-            }
+            Cand c{pool, blk, 8, 0, 0};
+            int rc = run(c, &why);
+            if (rc < 0) return set_error(ctx, LJ_ERR_CUDA, "autotune: candidate run failed: " + why);
+            if (rc == 0) done.push_back(c);
         }
+    if (done.empty()) return set_error(ctx, LJ_ERR_OUT_OF_MEMORY, "autotune: no candidate fits the HBM budget");
+    const Cand first = pick(done);
+    for (int32_t w : wpps) {
+        if (w == first.wpp) continue;
+        Cand c{first.pool, first.block, w, 0, 0};
+        int rc = run(c, &why);
+        if (rc < 0) return set_error(ctx, LJ_ERR_CUDA, "autotune: candidate run failed: " + why);
+        if (rc == 0) done.push_back(c);
     }
-    if (best < 0) return set_error(ctx, LJ_ERR_OUT_OF_MEMORY, "autotune: no candidate fits the HBM budget");
-    options->path_pool = best_pool;
-    options->block_size = best_block;
+    const Cand best = pick(done);
+    options->path_pool = best.pool;
+    options->block_size = best.block;
+    options->waves_per_poll = best.wpp;
     if (cache_path) {
         std::ostringstream v;
-        v << "{\"path_pool\": " << best_pool << ", \"block_size\": " << best_block << ", \"msamples_s\": " << best << "}";
+        v << "{\"path_pool\": " << best.pool << ", \"block_size\": " << best.block << ", \"waves_per_poll\": "
+          << best.wpp << ", \"msamples_s\": " << best.rate << ", \"median_latency_ms\": " << best.latency
+          << ", \"candidates\": " << done.size() << "}";
         cache[key.str()] = v.str();
         std::ofstream f(cache_path);
         f << "{\n";

@@ -345,12 +345,13 @@ def job_desc(seed=0, spp=0, sample_offset=0, width=0, height=0, max_depth=None, 
 
 def server_options(hbm_budget_bytes=0, path_pool=0, block_size=0, max_live_jobs=0, max_queued_jobs=0,
                    waves_per_poll=0, policy=abi.LJ_SCHED_FIFO, use_graphs=True, profile=False,
-                   one_shade_kernel=False):
+                   one_shade_kernel=False, tune_objective=abi.LJ_TUNE_BALANCED):
     return abi.lj_server_options(hbm_budget_bytes=hbm_budget_bytes, path_pool=path_pool, block_size=block_size,
                                  max_live_jobs=max_live_jobs, max_queued_jobs=max_queued_jobs,
                                  waves_per_poll=waves_per_poll, policy=policy, use_graphs=1 if use_graphs else 0,
                                  flags=(abi.LJ_SERVER_PROFILE if profile else 0) |
-                                 (abi.LJ_SERVER_ONE_SHADE_KERNEL if one_shade_kernel else 0))
+                                 (abi.LJ_SERVER_ONE_SHADE_KERNEL if one_shade_kernel else 0),
+                                 tune_objective=tune_objective)
 
 
 class Server:

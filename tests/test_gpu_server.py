@@ -227,7 +227,16 @@ def test_autotune_picks_a_candidate_and_caches_it(ctx, tmp_path):
     cache = str(tmp_path / "tune.json")
     opt = gpu.autotune(ctx, gs, jobs, [0] * 4, cache_path=cache)
     assert opt.path_pool in (1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24) and opt.block_size in (64, 128, 256)
+    assert opt.waves_per_poll in (4, 8, 16)
     text = open(cache).read()
-    assert "path_pool" in text and "block_size" in text
+    assert "path_pool" in text and "block_size" in text and "median_latency_ms" in text
     again = gpu.autotune(ctx, gs, jobs, [0] * 4, cache_path=cache)
-    assert (again.path_pool, again.block_size) == (opt.path_pool, opt.block_size)
+    assert (again.path_pool, again.block_size, again.waves_per_poll) == \
+        (opt.path_pool, opt.block_size, opt.waves_per_poll)
+    # another objective is another cache entry
+    lat = gpu.autotune(ctx, gs, jobs, [0] * 4, cache_path=cache,
+                       options=gpu.server_options(tune_objective=abi.LJ_TUNE_LATENCY))
+    assert lat.block_size in (64, 128, 256)
+    assert open(cache).read().count("|obj") == 2
+    with pytest.raises(gpu.LjError):
+        gpu.autotune(ctx, gs, jobs, [0] * 4, options=gpu.server_options(tune_objective=9))
