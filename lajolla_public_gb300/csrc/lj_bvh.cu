@@ -474,14 +474,11 @@ __device__ __forceinline__ float box_half_area(float4 l, float4 h) {
     return dx * dy + dy * dz + dz * dx;
 }
 
-// The nodes [id_lo, id_hi] of one PLOC round: their children were made in
-// earlier rounds (or are primitives), so their tables are complete.
-__global__ void k_sah_costs(float *cost, uint8_t *dec, const int2 *child, const int2 *range, const float4 *nlo,
-                            const float4 *nhi, const uint32_t *sorted, const float4 *plo, const float4 *phi,
-                            int id_lo, int id_hi) {
-    const int id = id_lo + blockIdx.x * blockDim.x + threadIdx.x;
-    if (id > id_hi) return;
-    const int2 c = child[id];
+// The cost table of binary node id, its children's tables complete.  Reads
+// bypass L1 (the bottom-up walk reads what other SMs wrote).
+__device__ void sah_table(float *cost, uint8_t *dec, const int2 *child, const int2 *range, const float4 *nlo,
+                          const float4 *nhi, const uint32_t *sorted, const float4 *plo, const float4 *phi, int id) {
+    const int2 c = __ldcg(child + id);
     float cl[8], cr[8];
     auto load = [&](int enc, float *cc) {
         if (enc < 0) {
@@ -489,7 +486,7 @@ __global__ void k_sah_costs(float *cost, uint8_t *dec, const int2 *child, const 
             const float a = box_half_area(plo[g], phi[g]) * kSahPrim;
             for (int i = 1; i < 8; i++) cc[i] = a;
         } else {
-            for (int i = 1; i < 8; i++) cc[i] = cost[(size_t)enc * 8 + i];
+            for (int i = 1; i < 8; i++) cc[i] = __ldcg(cost + (size_t)enc * 8 + i);
         }
     };
     load(c.x, cl);
@@ -509,8 +506,9 @@ __global__ void k_sah_costs(float *cost, uint8_t *dec, const int2 *child, const 
         D[j] = best;
         K[j] = (uint8_t)bk;
     }
-    const float A = box_half_area(nlo[id], nhi[id]);
-    const int p = range[id].y - range[id].x + 1;
+    const float A = box_half_area(__ldcg(nlo + id), __ldcg(nhi + id));
+    const int2 rg = __ldcg(range + id);
+    const int p = rg.y - rg.x + 1;
     const float c_int = A * kSahNode + D[8];
     const float c_leaf = p <= 3 ? A * (float)p * kSahPrim : __int_as_float(0x7f800000);
     float C = fminf(c_leaf, c_int);
@@ -530,6 +528,188 @@ __global__ void k_sah_costs(float *cost, uint8_t *dec, const int2 *child, const 
     de[0] = K[8];
 }
 
+// Cost tables bottom-up: one thread per primitive walks towards the root;
+// the second thread to reach a node (both subtrees done) fills its table.
+__global__ void k_sah_costs_up(float *cost, uint8_t *dec, const int2 *child, const int2 *range, const float4 *nlo,
+                               const float4 *nhi, const uint32_t *sorted, const float4 *plo, const float4 *phi,
+                               const int *parent_int, const int *parent_leaf, int *visit, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int id = __ldcg(parent_leaf + i);
+    while (id >= 0) {
+        __threadfence();
+        if (atomicAdd(visit + id, 1) == 0) return;
+        __threadfence();
+        sah_table(cost, dec, child, range, nlo, nhi, sorted, plo, phi, id);
+        id = __ldcg(parent_int + id);
+    }
+}
+
+// ---- treelet restructuring (Karras and Aila, "Fast Parallel Construction
+// of High-Quality Bounding Volume Hierarchies", HPG 2013) ------------------
+// Bottom-up over the binary tree; at a node with at least min_prims
+// primitives below, the treelet of its kTreeletLeaves largest descendants
+// (grown by opening the largest-area inner leaf until there are 7) is
+// rebuilt with the topology of least SAH cost, found exactly by dynamic
+// programming over the 127 subsets of its leaves; the treelet's inner node
+// ids are reused.  Costs: binary SAH, kSahNode per node, kSahPrim per
+// primitive, areas as half surface areas.
+constexpr int kTreeletLeaves = 7;
+
+struct TreeletArgs {
+    int2 *child, *range;
+    float4 *nlo, *nhi;
+    float *sahc;            // binary SAH cost of each inner node's subtree
+    int *parent_int, *parent_leaf, *visit;
+    const uint32_t *sorted;
+    const float4 *plo, *phi;
+};
+
+__device__ void treelet_leaf(const TreeletArgs &a, int enc, float4 &lo, float4 &hi, int &cnt, float &cost) {
+    if (enc < 0) {
+        const uint32_t g = a.sorted[~enc];
+        lo = a.plo[g];
+        hi = a.phi[g];
+        cnt = 1;
+        cost = box_half_area(lo, hi) * kSahPrim;
+    } else {
+        lo = __ldcg(a.nlo + enc);
+        hi = __ldcg(a.nhi + enc);
+        const int2 r = __ldcg(a.range + enc);
+        cnt = r.y - r.x + 1;
+        cost = __ldcg(a.sahc + enc);
+    }
+}
+
+__device__ void treelet_at(const TreeletArgs &a, int R, int min_prims) {
+    int leaf[kTreeletLeaves], inner[kTreeletLeaves - 1];
+    float4 llo[kTreeletLeaves], lhi[kTreeletLeaves];
+    int lcnt[kTreeletLeaves];
+    float lcost[kTreeletLeaves];
+    const int2 cR = __ldcg(a.child + R);
+    leaf[0] = cR.x;
+    leaf[1] = cR.y;
+    treelet_leaf(a, leaf[0], llo[0], lhi[0], lcnt[0], lcost[0]);
+    treelet_leaf(a, leaf[1], llo[1], lhi[1], lcnt[1], lcost[1]);
+    const float AR = box_half_area(__ldcg(a.nlo + R), __ldcg(a.nhi + R));
+    const float current = AR * kSahNode + lcost[0] + lcost[1];
+    int nl = 2, nin = 1;
+    inner[0] = R;
+    if (lcnt[0] + lcnt[1] >= min_prims) {
+        while (nl < kTreeletLeaves) {
+            int best = -1;
+            float ba = -1.0f;
+            for (int k = 0; k < nl; k++) {
+                if (leaf[k] < 0) continue;
+                const float ar = box_half_area(llo[k], lhi[k]);
+                if (ar > ba) { ba = ar; best = k; }
+            }
+            if (best < 0) break;
+            const int e = leaf[best];
+            inner[nin++] = e;
+            const int2 c = __ldcg(a.child + e);
+            leaf[best] = c.x;
+            treelet_leaf(a, c.x, llo[best], lhi[best], lcnt[best], lcost[best]);
+            leaf[nl] = c.y;
+            treelet_leaf(a, c.y, llo[nl], lhi[nl], lcnt[nl], lcost[nl]);
+            nl++;
+        }
+    }
+    if (nl < 4) {   // two or three leaves: every topology is the same up to order
+        __stcg(a.sahc + R, current);
+        return;
+    }
+    // subsets of the nl leaves: area of the union box, least cost, best split
+    float area[1 << kTreeletLeaves], cost[1 << kTreeletLeaves];
+    uint8_t split[1 << kTreeletLeaves];
+    const int full = (1 << nl) - 1;
+    for (int sset = 1; sset <= full; sset++) {
+        float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int k = 0; k < nl; k++) {
+            if (!(sset & (1 << k))) continue;
+            lo[0] = fminf(lo[0], llo[k].x); lo[1] = fminf(lo[1], llo[k].y); lo[2] = fminf(lo[2], llo[k].z);
+            hi[0] = fmaxf(hi[0], lhi[k].x); hi[1] = fmaxf(hi[1], lhi[k].y); hi[2] = fmaxf(hi[2], lhi[k].z);
+        }
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        area[sset] = dx * dy + dy * dz + dz * dx;
+    }
+    for (int k = 0; k < nl; k++) cost[1 << k] = lcost[k];
+    for (int sset = 3; sset <= full; sset++) {
+        if (__popc(sset) < 2) continue;
+        const int low = sset & -sset;
+        float best = FLT_MAX;
+        int bp = low;
+        // each split {p, sset ^ p} once: p holds the lowest leaf of sset
+        for (int p = (sset - 1) & sset; p > 0; p = (p - 1) & sset) {
+            if (!(p & low)) continue;
+            const float c = cost[p] + cost[sset ^ p];
+            if (c < best) { best = c; bp = p; }
+        }
+        cost[sset] = area[sset] * kSahNode + best;
+        split[sset] = (uint8_t)bp;
+    }
+    if (!(cost[full] < current * (1.0f - 1e-6f))) {
+        __stcg(a.sahc + R, current);
+        return;
+    }
+    // rebuild: each subset of two or more leaves becomes an inner node (the
+    // full set keeps R); box, primitive count and cost follow from the subset
+    int st[kTreeletLeaves], ids[kTreeletLeaves], sp = 0, next = 1;
+    st[sp] = full;
+    ids[sp++] = R;
+    while (sp > 0) {
+        --sp;
+        const int sset = st[sp], id = ids[sp];
+        int enc[2];
+        const int part[2] = {split[sset], sset ^ split[sset]};
+        for (int h = 0; h < 2; h++) {
+            if (__popc(part[h]) == 1) {
+                enc[h] = leaf[__ffs(part[h]) - 1];
+            } else {
+                enc[h] = inner[next++];
+                st[sp] = part[h];
+                ids[sp++] = enc[h];
+            }
+            if (enc[h] >= 0) __stcg(a.parent_int + enc[h], id);
+            else __stcg(a.parent_leaf + ~enc[h], id);
+        }
+        float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+        int cnt = 0;
+        for (int k = 0; k < nl; k++) {
+            if (!(sset & (1 << k))) continue;
+            lo.x = fminf(lo.x, llo[k].x); lo.y = fminf(lo.y, llo[k].y); lo.z = fminf(lo.z, llo[k].z);
+            hi.x = fmaxf(hi.x, lhi[k].x); hi.y = fmaxf(hi.y, lhi[k].y); hi.z = fmaxf(hi.z, lhi[k].z);
+            cnt += lcnt[k];
+        }
+        __stcg(a.child + id, make_int2(enc[0], enc[1]));
+        __stcg(a.nlo + id, lo);
+        __stcg(a.nhi + id, hi);
+        __stcg(a.range + id, make_int2(0, cnt - 1));
+        __stcg(a.sahc + id, cost[sset]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_treelets(TreeletArgs a, int n, int min_prims) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int id = __ldcg(a.parent_leaf + i);
+    while (id >= 0) {
+        __threadfence();
+        if (atomicAdd(a.visit + id, 1) == 0) return;
+        __threadfence();
+        treelet_at(a, id, min_prims);
+        id = __ldcg(a.parent_int + id);
+    }
+}
+
+__global__ void k_parents(const int2 *child, int ni, int *parent_int, int *parent_leaf) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= ni) return;
+    const int2 c = child[id];
+    if (c.x >= 0) parent_int[c.x] = id; else parent_leaf[~c.x] = id;
+    if (c.y >= 0) parent_int[c.y] = id; else parent_leaf[~c.y] = id;
+}
+
 struct CollapseArgs {
     const int2 *child;      // binary internal nodes
     const int2 *range;
@@ -540,7 +720,7 @@ struct CollapseArgs {
     uint4 *nodes;
     float4 *prims;
     int *node_counter, *prim_counter;
-    const uint8_t *dec;     // SAH decisions (k_sah_costs), or null: greedy expansion
+    const uint8_t *dec;     // SAH decisions (sah_table), or null: greedy expansion
     const int2 *qin;        // (binary node encoded, wide node index)
     const int *qin_count;
     int2 *qout;
@@ -1080,7 +1260,6 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
 
     float *sah_cost = nullptr;
     uint8_t *sah_dec = nullptr;
-    std::vector<int2> rounds;   // PLOC: the node ids each round made
     k_init_bounds<<<1, 32, 0, s>>>(bounds, 12);
     k_prim_bounds<<<grid_for(n, 256), 256, 0, s>>>(in, plo, phi, cent, bounds);
     k_morton<<<grid_for(n, 256), 256, 0, s>>>(cent, n, bounds, codes, idx);
@@ -1122,7 +1301,6 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
                 if (err) *err = "BVH build: a clustering round merged nothing";
                 return -5;
             }
-            rounds.push_back(make_int2(n - 2 - merged - tot.y + 1, n - 2 - merged));
             merged += tot.y;
             count = tot.x;
             c ^= 1;
@@ -1136,12 +1314,24 @@ int build_bvh(const BvhInput &in, BvhOutput *out, cudaStream_t s, std::string *e
             if (err) *err = "BVH build: clustering left " + std::to_string(n - merged) + " roots";
             return -5;
         }
-        // SAH cost tables, round by round (children before parents)
+        // parent links (the root, node 0, keeps -1), then treelet passes
+        // with a growing minimum subtree size (7, 14, 28 primitives)
+        k_parents<<<grid_for(ni, 256), 256, 0, s>>>(child, ni, parent_int, parent_leaf);
+        float *sahc = nullptr;
+        int *visit = (int *)flags;
+        LJ_CUDA_TRY(cudaMallocAsync(&sahc, sizeof(float) * (size_t)ni, s));
+        TreeletArgs ta{child, range, nlo, nhi, sahc, parent_int, parent_leaf, visit, idx, plo, phi};
+        for (int pass = 0; pass < in.treelet_passes; pass++) {
+            LJ_CUDA_TRY(cudaMemsetAsync(visit, 0, sizeof(int) * ni, s));
+            k_treelets<<<grid_for(n, 128), 128, 0, s>>>(ta, n, kTreeletLeaves << pass);
+        }
+        LJ_CUDA_TRY(cudaFreeAsync(sahc, s));
+        // SAH cost tables of the 8-wide collapse, bottom-up
         LJ_CUDA_TRY(cudaMallocAsync(&sah_cost, sizeof(float) * 8 * (size_t)ni, s));
         LJ_CUDA_TRY(cudaMallocAsync(&sah_dec, sizeof(uint8_t) * 8 * (size_t)ni, s));
-        for (const int2 &r : rounds)
-            k_sah_costs<<<grid_for(r.y - r.x + 1, 256), 256, 0, s>>>(sah_cost, sah_dec, child, range, nlo, nhi, idx,
-                                                                       plo, phi, r.x, r.y);
+        LJ_CUDA_TRY(cudaMemsetAsync(visit, 0, sizeof(int) * ni, s));
+        k_sah_costs_up<<<grid_for(n, 256), 256, 0, s>>>(sah_cost, sah_dec, child, range, nlo, nhi, idx, plo, phi,
+                                                         parent_int, parent_leaf, visit, n);
         LJ_CUDA_TRY(cudaGetLastError());
     } else if (n > 1) {
         k_karras<<<grid_for(n - 1, 256), 256, 0, s>>>(codes, n, child, range, parent_int, parent_leaf);

@@ -57,6 +57,7 @@ struct BvhInput {
     const float *spheres;   // device, 4 floats (c, r) per sphere (prims num_tris ..)
     int num_tris, num_spheres;
     int karras = 0;         // 1: Karras radix tree over the Morton order, 0: PLOC clustering
+    int treelet_passes = 3; // PLOC: treelet restructuring passes before the collapse
 };
 struct BvhOutput {
     uint4 *nodes = nullptr;     // device, owned by the scene
