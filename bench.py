@@ -549,7 +549,7 @@ def run_ours(args):
              abi.LJ_KERNEL_NEE: ps.nee_requests}.get(dom, job_samples(jobs))
     kname = {abi.LJ_KERNEL_CAMERA: "k_srv_regen", abi.LJ_KERNEL_MEDIUM: "k_srv_vol_a + k_srv_vol_c",
              abi.LJ_KERNEL_NEE: "k_srv_vol_b"}.get(dom, "k_srv_" + abi.KERNEL_CLASS_NAMES[dom])
-    traffic = load_traffic(kname, units / launches_dom)
+    traffic, traffic_src = load_traffic(kname, units / launches_dom)
     with_bvh = None
     if dom in (abi.LJ_KERNEL_TRACE, abi.LJ_KERNEL_SHADOW):
         key = "closest" if dom == abi.LJ_KERNEL_TRACE else "shadow"
@@ -589,7 +589,7 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                     else "fallback 6800 GB/s", "traffic": traffic,
+                     else "fallback 6800 GB/s", "traffic": traffic, "traffic_source": traffic_src,
                      "bytes_per_launch": round(nb / launches_dom), "avg_launch_us": round(avg_launch_s * 1e6, 2),
                      "bytes": "compulsory (queues, hits, path state, shading records); BVH and density-grid "
                               "bytes excluded (with_bvh adds the BVH bytes)",
@@ -734,17 +734,19 @@ def load_issue(kernel_name):
 
 
 def load_traffic(kernel_name, units_per_launch):
-    """DRAM bytes per launch of the dominant kernel: the per-unit figure of
-    the committed ncu capture (profiles/traffic.json, measured on a smaller
-    case of the same kernel) times the units of an average launch here, or
-    None."""
+    """DRAM bytes per launch of the dominant kernel from its committed ncu
+    capture (profiles/traffic.json): the mean over every launch of the
+    kernel in one step of this workload where that was captured, else the
+    per-unit figure of a smaller case times the units of an average launch
+    here; with the figure's source, or (None, None)."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
-        d = json.load(open(p))
-        v = d.get(kernel_name)
+        v = json.load(open(p)).get(kernel_name)
+        if isinstance(v, dict) and v.get("dram_bytes_per_launch"):
+            return round(float(v["dram_bytes_per_launch"])), v.get("source")
         if isinstance(v, dict) and v.get("dram_bytes_per_unit"):
-            return round(float(v["dram_bytes_per_unit"]) * units_per_launch)
-    return None
+            return round(float(v["dram_bytes_per_unit"]) * units_per_launch), v.get("source")
+    return None, None
 
 
 # ------------------------------------------------------------ CPU side

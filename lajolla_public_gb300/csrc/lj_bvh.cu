@@ -581,7 +581,19 @@ __device__ void treelet_leaf(const TreeletArgs &a, int enc, float4 &lo, float4 &
     }
 }
 
-__device__ void treelet_at(const TreeletArgs &a, int R, int min_prims) {
+// Per-warp scratch of the subset DP (shared memory).
+struct TreeletSmem {
+    float area[1 << kTreeletLeaves];
+    float cost[1 << kTreeletLeaves];
+    uint8_t split[1 << kTreeletLeaves];
+};
+
+// The treelet at R, by the whole warp: every lane forms the treelet (same
+// loads, uniform control flow), the lanes share the subsets' union areas
+// and, size by size, their least costs; the full set's splits are spread
+// over the lanes and reduced.  Lane 0 writes the new topology.
+__device__ void treelet_at_warp(const TreeletArgs &a, int R, int min_prims, TreeletSmem &sm, int lane) {
+    const unsigned kFull = 0xffffffffu;
     int leaf[kTreeletLeaves], inner[kTreeletLeaves - 1];
     float4 llo[kTreeletLeaves], lhi[kTreeletLeaves];
     int lcnt[kTreeletLeaves];
@@ -616,14 +628,13 @@ __device__ void treelet_at(const TreeletArgs &a, int R, int min_prims) {
         }
     }
     if (nl < 4) {   // two or three leaves: every topology is the same up to order
-        __stcg(a.sahc + R, current);
+        if (lane == 0) __stcg(a.sahc + R, current);
+        __syncwarp();
         return;
     }
-    // subsets of the nl leaves: area of the union box, least cost, best split
-    float area[1 << kTreeletLeaves], cost[1 << kTreeletLeaves];
-    uint8_t split[1 << kTreeletLeaves];
     const int full = (1 << nl) - 1;
-    for (int sset = 1; sset <= full; sset++) {
+    // union areas, 4 subsets per lane
+    for (int sset = lane + 1; sset <= full; sset += 32) {
         float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
         for (int k = 0; k < nl; k++) {
             if (!(sset & (1 << k))) continue;
@@ -631,74 +642,127 @@ __device__ void treelet_at(const TreeletArgs &a, int R, int min_prims) {
             hi[0] = fmaxf(hi[0], lhi[k].x); hi[1] = fmaxf(hi[1], lhi[k].y); hi[2] = fmaxf(hi[2], lhi[k].z);
         }
         const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
-        area[sset] = dx * dy + dy * dz + dz * dx;
+        sm.area[sset] = dx * dy + dy * dz + dz * dx;
+        if (__popc(sset) == 1) sm.cost[sset] = lcost[__ffs(sset) - 1];
     }
-    for (int k = 0; k < nl; k++) cost[1 << k] = lcost[k];
-    for (int sset = 3; sset <= full; sset++) {
-        if (__popc(sset) < 2) continue;
-        const int low = sset & -sset;
-        float best = FLT_MAX;
-        int bp = low;
-        // each split {p, sset ^ p} once: p holds the lowest leaf of sset
-        for (int p = (sset - 1) & sset; p > 0; p = (p - 1) & sset) {
-            if (!(p & low)) continue;
-            const float c = cost[p] + cost[sset ^ p];
-            if (c < best) { best = c; bp = p; }
+    __syncwarp();
+    // least costs of the proper subsets, size by size (each split {p, s ^ p}
+    // once: p holds the lowest leaf of s)
+    for (int size = 2; size < nl; size++) {
+        for (int sset = lane + 1; sset < full; sset += 32) {
+            if (__popc(sset) != size) continue;
+            const int low = sset & -sset;
+            float best = FLT_MAX;
+            int bp = low;
+            for (int p = (sset - 1) & sset; p > 0; p = (p - 1) & sset) {
+                if (!(p & low)) continue;
+                const float c = sm.cost[p] + sm.cost[sset ^ p];
+                if (c < best) { best = c; bp = p; }
+            }
+            sm.cost[sset] = sm.area[sset] * kSahNode + best;
+            sm.split[sset] = (uint8_t)bp;
         }
-        cost[sset] = area[sset] * kSahNode + best;
-        split[sset] = (uint8_t)bp;
+        __syncwarp();
     }
-    if (!(cost[full] < current * (1.0f - 1e-6f))) {
-        __stcg(a.sahc + R, current);
+    // the full set: its 2^(nl-1) - 1 splits over the lanes, then the least
+    // (ties to the larger split, the one the sequential order meets first)
+    float best = FLT_MAX;
+    int bp = 0;
+    for (int j = lane; j < (1 << (nl - 1)) - 1; j += 32) {
+        const int p = (j << 1) | 1;   // the splits holding leaf 0, j over the other leaves (not all of them)
+        const float c = sm.cost[p] + sm.cost[full ^ p];
+        if (c < best || (c == best && p > bp)) { best = c; bp = p; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(kFull, best, o);
+        const int op = __shfl_xor_sync(kFull, bp, o);
+        if (ob < best || (ob == best && op > bp)) { best = ob; bp = op; }
+    }
+    const float cfull = sm.area[full] * kSahNode + best;
+    if (lane == 0) {
+        sm.cost[full] = cfull;
+        sm.split[full] = (uint8_t)bp;
+    }
+    __syncwarp();
+    if (!(cfull < current * (1.0f - 1e-6f))) {
+        if (lane == 0) __stcg(a.sahc + R, current);
+        __syncwarp();
         return;
     }
-    // rebuild: each subset of two or more leaves becomes an inner node (the
-    // full set keeps R); box, primitive count and cost follow from the subset
-    int st[kTreeletLeaves], ids[kTreeletLeaves], sp = 0, next = 1;
-    st[sp] = full;
-    ids[sp++] = R;
-    while (sp > 0) {
-        --sp;
-        const int sset = st[sp], id = ids[sp];
-        int enc[2];
-        const int part[2] = {split[sset], sset ^ split[sset]};
-        for (int h = 0; h < 2; h++) {
-            if (__popc(part[h]) == 1) {
-                enc[h] = leaf[__ffs(part[h]) - 1];
-            } else {
-                enc[h] = inner[next++];
-                st[sp] = part[h];
-                ids[sp++] = enc[h];
+    if (lane == 0) {
+        // rebuild: each subset of two or more leaves becomes an inner node (the
+        // full set keeps R); box, primitive count and cost follow from the subset
+        int st[kTreeletLeaves], ids[kTreeletLeaves], sp = 0, next = 1;
+        st[sp] = full;
+        ids[sp++] = R;
+        while (sp > 0) {
+            --sp;
+            const int sset = st[sp], id = ids[sp];
+            int enc[2];
+            const int part[2] = {sm.split[sset], sset ^ sm.split[sset]};
+            for (int h = 0; h < 2; h++) {
+                if (__popc(part[h]) == 1) {
+                    enc[h] = leaf[__ffs(part[h]) - 1];
+                } else {
+                    enc[h] = inner[next++];
+                    st[sp] = part[h];
+                    ids[sp++] = enc[h];
+                }
+                if (enc[h] >= 0) __stcg(a.parent_int + enc[h], id);
+                else __stcg(a.parent_leaf + ~enc[h], id);
             }
-            if (enc[h] >= 0) __stcg(a.parent_int + enc[h], id);
-            else __stcg(a.parent_leaf + ~enc[h], id);
+            float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f),
+                   hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
+            int cnt = 0;
+            for (int k = 0; k < nl; k++) {
+                if (!(sset & (1 << k))) continue;
+                lo.x = fminf(lo.x, llo[k].x); lo.y = fminf(lo.y, llo[k].y); lo.z = fminf(lo.z, llo[k].z);
+                hi.x = fmaxf(hi.x, lhi[k].x); hi.y = fmaxf(hi.y, lhi[k].y); hi.z = fmaxf(hi.z, lhi[k].z);
+                cnt += lcnt[k];
+            }
+            __stcg(a.child + id, make_int2(enc[0], enc[1]));
+            __stcg(a.nlo + id, lo);
+            __stcg(a.nhi + id, hi);
+            __stcg(a.range + id, make_int2(0, cnt - 1));
+            __stcg(a.sahc + id, sm.cost[sset]);
         }
-        float4 lo = make_float4(FLT_MAX, FLT_MAX, FLT_MAX, 0.0f), hi = make_float4(-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f);
-        int cnt = 0;
-        for (int k = 0; k < nl; k++) {
-            if (!(sset & (1 << k))) continue;
-            lo.x = fminf(lo.x, llo[k].x); lo.y = fminf(lo.y, llo[k].y); lo.z = fminf(lo.z, llo[k].z);
-            hi.x = fmaxf(hi.x, lhi[k].x); hi.y = fmaxf(hi.y, lhi[k].y); hi.z = fmaxf(hi.z, lhi[k].z);
-            cnt += lcnt[k];
-        }
-        __stcg(a.child + id, make_int2(enc[0], enc[1]));
-        __stcg(a.nlo + id, lo);
-        __stcg(a.nhi + id, hi);
-        __stcg(a.range + id, make_int2(0, cnt - 1));
-        __stcg(a.sahc + id, cost[sset]);
     }
+    __syncwarp();
 }
 
+// Bottom-up with whole warps: each lane walks from its primitive towards the
+// root (the second lane to reach a node goes on); in each step the warp
+// handles, one after another and all lanes together, the nodes its lanes
+// reached.  Lanes that are done stay in the loop for the warp's work.
 __global__ void __launch_bounds__(128) k_treelets(TreeletArgs a, int n, int min_prims) {
+    __shared__ TreeletSmem smem[4];
+    const unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    TreeletSmem &sm = smem[threadIdx.x >> 5];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int id = __ldcg(a.parent_leaf + i);
-    while (id >= 0) {
+    int node = -1;
+    bool alive = false;
+    if (i < n) {
+        node = __ldcg(a.parent_leaf + i);
         __threadfence();
-        if (atomicAdd(a.visit + id, 1) == 0) return;
+        alive = node >= 0 && atomicAdd(a.visit + node, 1) != 0;
+    }
+    for (;;) {   // a step per tree level: alive lanes move up one node each step
+        unsigned todo = __ballot_sync(kFull, alive);
+        if (!todo) break;
         __threadfence();
-        treelet_at(a, id, min_prims);
-        id = __ldcg(a.parent_int + id);
+        while (todo) {
+            const int leader = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int R = __shfl_sync(kFull, node, leader);
+            treelet_at_warp(a, R, min_prims, sm, lane);
+        }
+        if (alive) {
+            const int p = __ldcg(a.parent_int + node);
+            __threadfence();
+            alive = p >= 0 && atomicAdd(a.visit + p, 1) != 0;
+            node = p;
+        }
     }
 }
 
