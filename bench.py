@@ -514,6 +514,7 @@ def run_ours(args):
     for g in g2:
         g.close()
     e2e_value = job_samples(jobs) * world / max_over_ranks(e2e_s, world) / 1e6
+    update = scene_update_times(ctx, pool)
     h2d = sum(scene_host_bytes(s) for s in pool) + len(jobs) * 40
     d2h = sum(j["width"] * j["height"] * 12 for j in jobs)
 
@@ -585,6 +586,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(d2h), "scene_upload_s": round(upload_s, 4),
                 "what": "scene pool uploaded from host (lj_gpu_scene_create, BVH build) + one step served, "
                         "images to host"},
+        "scene_update": update,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
@@ -694,6 +696,40 @@ def microbench(ctx, n_tris=1 << 20, n_rays=1 << 24, n_bsdf=1 << 24, reps=3):
             ms = timed(lambda: ctx.bsdf(mtype, op, params, wi, dir_out=wo, rnd=rnd, stream=stream))
             out["%s_%s_mcalls_s" % (name, opname)] = round(n_bsdf / ms / 1e3, 1)
     g.close()
+    return out
+
+
+def scene_update_times(ctx, pool):
+    """A resident scene whose geometry moved, brought up to date in place
+    (lj_gpu_scene_update_mesh: the largest mesh of the pool's largest scene
+    displaced, BVH refitted or rebuilt) against creating it again from host
+    memory (lj_gpu_scene_create); host clock, device synchronized."""
+    import torch
+    from lajolla_public_gb300 import gpu
+    sc = max(pool, key=lambda x: x.num_triangles)
+    mesh = max((i for i, s in enumerate(sc.shapes) if s["kind"] == abi.LJ_SHAPE_MESH),
+               key=lambda i: len(sc.shapes[i]["indices"]))
+    p = sc.shapes[mesh]["positions"]
+    moved = (p + np.random.default_rng(5).normal(0, 1e-3, p.shape)).astype(np.float32)
+    out = {"scene_triangles": sc.num_triangles, "mesh_triangles": int(len(sc.shapes[mesh]["indices"]))}
+    for name in ("create", "refit", "rebuild"):
+        best = None
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if name == "create":
+                g = gpu.GpuScene(ctx, sc)
+                torch.cuda.synchronize()
+                dt = time.perf_counter() - t0
+            else:
+                g = gpu.GpuScene(ctx, sc)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                g.update_mesh(mesh, moved, rebuild=(name == "rebuild"))
+                dt = time.perf_counter() - t0
+            g.close()
+            best = dt if best is None else min(best, dt)
+        out[name + "_ms"] = round(best * 1e3, 2)
     return out
 
 
