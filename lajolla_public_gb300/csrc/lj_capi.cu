@@ -149,6 +149,33 @@ void lookup0(const HostImg &im, double u, double v, double out[3]) {
     }
 }
 
+// Host -> device copy of a caller's (pageable) array.  Large arrays are
+// page-locked for the copy (cudaHostRegister, read-only where the device
+// allows it) and released after it: a pageable copy of tens of MB runs at
+// a fraction of the link's rate.  Memory that is already page-locked, or
+// that cannot be registered, is copied as it is.
+int h2d(void *dst, const void *src, size_t bytes, cudaStream_t s, std::string *err) {
+    if (bytes >= ((size_t)4 << 20)) {
+        void *h = const_cast<void *>(src);
+        cudaError_t e = cudaHostRegister(h, bytes, cudaHostRegisterReadOnly);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            e = cudaHostRegister(h, bytes, cudaHostRegisterDefault);
+        }
+        if (e == cudaSuccess) {
+            cudaError_t c = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+            cudaError_t w = cudaStreamSynchronize(s);
+            cudaHostUnregister(h);
+            LJ_CUDA_TRY(c);
+            LJ_CUDA_TRY(w);
+            return 0;
+        }
+        cudaGetLastError();
+    }
+    LJ_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    return 0;
+}
+
 template <typename T>
 int upload(lj_scene *sc, const T *src, size_t n, const T **dst, std::string *err) {
     *dst = nullptr;
@@ -156,10 +183,35 @@ int upload(lj_scene *sc, const T *src, size_t n, const T **dst, std::string *err
     void *p = nullptr;
     LJ_CUDA_TRY(cudaMalloc(&p, sizeof(T) * n));
     sc->allocs.push_back(p);
-    LJ_CUDA_TRY(cudaMemcpyAsync(p, src, sizeof(T) * n, cudaMemcpyHostToDevice, sc->ctx->stream));
+    if (h2d(p, src, sizeof(T) * n, sc->ctx->stream, err)) return -2;
     *dst = (const T *)p;
     sc->info.device_bytes += (int64_t)(sizeof(T) * n);
     return 0;
+}
+
+// Per-channel maximum of a grid volume's values and at least zero (the
+// reference's load_volume starts its maximum at zero, src/volume.cpp:72-97),
+// and for three channels the one-float4-per-voxel layout.  mx: 3 uints,
+// zeroed; non-negative floats order like their bit patterns.
+__global__ void k_grid_prep(const float *src, size_t n, int channels, float4 *rgb, unsigned int *mx) {
+    float m[3] = {0.0f, 0.0f, 0.0f};
+    for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
+        if (channels == 1) {
+            m[0] = fmaxf(m[0], src[p]);
+        } else {
+            const float x = src[3 * p], y = src[3 * p + 1], z = src[3 * p + 2];
+            m[0] = fmaxf(m[0], x);
+            m[1] = fmaxf(m[1], y);
+            m[2] = fmaxf(m[2], z);
+            rgb[p] = make_float4(x, y, z, 0.0f);
+        }
+    }
+    for (int c = 0; c < 3; c++) {
+        float v = m[c];
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (!(v > 0.0f)) v = 0.0f;   // also turns -0 into +0
+        if ((threadIdx.x & 31) == 0 && v > 0.0f) atomicMax(mx + c, __float_as_uint(v));
+    }
 }
 template <typename T>
 int upload(lj_scene *sc, const std::vector<T> &v, const T **dst, std::string *err) {
@@ -665,21 +717,47 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
                                     v.channel_scale[2] != 0.0f;
                 float mx[3] = {0, 0, 0};
                 o.channels = v.channels;
-                if (v.channels == 1) {   // one float per voxel, uploaded from the caller's array
-                    for (size_t p = 0; p < n; p++) mx[0] = std::max(mx[0], v.data[p]);
-                    mx[1] = mx[2] = mx[0];
-                    if (upload(sc, v.data, n, &o.data1, &err)) return fail(LJ_ERR_CUDA);
-                } else {
-                    std::vector<float4> rgb(n);
-                    for (size_t p = 0; p < n; p++) {
-                        float x[3];
-                        for (int c = 0; c < 3; c++) {
-                            x[c] = v.data[p * 3 + c];
-                            mx[c] = std::max(mx[c], x[c]);
-                        }
-                        rgb[p] = make_float4(x[0], x[1], x[2], 0.0f);
+                // the caller's values to the device as they are; maxima (and
+                // the float4 layout of three channels) computed there
+                unsigned int *d_mx = nullptr, h_mx[3] = {0, 0, 0};
+                const float *raw = nullptr;
+                float4 *rgb = nullptr;
+                const int gblocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+                bool ok = cudaMalloc(&d_mx, sizeof(h_mx)) == cudaSuccess &&
+                          cudaMemsetAsync(d_mx, 0, sizeof(h_mx), ctx->stream) == cudaSuccess;
+                if (ok && v.channels == 1) {   // one float per voxel, uploaded from the caller's array
+                    ok = upload(sc, v.data, n, &o.data1, &err) == 0;
+                    raw = o.data1;
+                } else if (ok) {
+                    void *tmp = nullptr;
+                    ok = cudaMalloc(&tmp, sizeof(float) * 3 * n) == cudaSuccess &&
+                         h2d(tmp, v.data, sizeof(float) * 3 * n, ctx->stream, &err) == 0 &&
+                         cudaMalloc((void **)&rgb, sizeof(float4) * n) == cudaSuccess;
+                    if (rgb) {
+                        sc->allocs.push_back(rgb);
+                        sc->info.device_bytes += (int64_t)(sizeof(float4) * n);
+                        o.data = rgb;
                     }
-                    if (upload(sc, rgb, &o.data, &err)) return fail(LJ_ERR_CUDA);
+                    raw = (const float *)tmp;
+                }
+                if (ok) {
+                    k_grid_prep<<<gblocks, 256, 0, ctx->stream>>>(raw, n, v.channels, rgb, d_mx);
+                    ok = cudaGetLastError() == cudaSuccess &&
+                         cudaMemcpyAsync(h_mx, d_mx, sizeof(h_mx), cudaMemcpyDeviceToHost, ctx->stream) ==
+                             cudaSuccess &&
+                         cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+                }
+                if (v.channels == 3 && raw) cudaFree(const_cast<float *>(raw));
+                if (d_mx) cudaFree(d_mx);
+                if (!ok) {
+                    cudaGetLastError();
+                    if (err.empty()) err = "medium " + std::to_string(i) + ": grid upload failed";
+                    return fail(LJ_ERR_CUDA);
+                }
+                for (int c = 0; c < 3; c++) {
+                    float f;
+                    memcpy(&f, &h_mx[v.channels == 1 ? 0 : c], sizeof(f));
+                    mx[c] = f;
                 }
                 for (int c = 0; c < 3; c++) {
                     o.res[c] = v.res[c];
