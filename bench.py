@@ -798,9 +798,9 @@ class CpuSampler:
     by W * H * spp), and renders each at its job's resolution, max depth and
     Russian-roulette depth with the GPU's keyed random numbers
     (job seed, pixel, sample).  calibrate() grows n until one run takes at
-    least 60 % of the target time (at most 4 Mi keys)."""
+    least 60 % of the target time (at most 32 Mi keys)."""
 
-    CAP = 1 << 22
+    CAP = 1 << 25
 
     def __init__(self, pool):
         from oracle import ljo
