@@ -1132,7 +1132,7 @@ struct AnyBatchIO {
     uint8_t *occ;
     LJ_D const DevBvh &bvh(int) const { return b; }
     LJ_D void load(int r, V3 &o, V3 &d, float &tn, float &tf) const { load_ray(rays, r, o, d, tn, tf); }
-    LJ_D void store(int r, const Trav &s) const { occ[r] = s.found ? 1 : 0; }
+    LJ_D void store(int r, const Trav &s) const { occ[r] = s.found() ? 1 : 0; }
 };
 
 __global__ void __launch_bounds__(128, 8) k_trace_closest(DevBvh bvh, const float4 *rays, float4 *hits, int n,

@@ -301,7 +301,7 @@ struct SrvShadowIO {
     LJ_D const DevBvh &bvh(int r) const { return d.scenes[d.jobs[job_of(r)].scene].bvh; }
     LJ_D void load(int r, V3 &o, V3 &dir, float &tn, float &tf) const { load_ray(d.sray, r, o, dir, tn, tf); }
     LJ_D void store(int r, const Trav &s) const {
-        if (s.found) return;
+        if (s.found()) return;
         const int t = d.starget[r];
         float4 *L = t < 0 ? d.rL + (t & 0x7fffffff) : d.buf[nxt].L + t;
         const float4 c = d.scontrib[r], l = *L;
@@ -366,13 +366,14 @@ struct QueuePaths {
     }
 };
 
-// traversal: 64 registers (full-SM occupancy of 50%, no spills)
+// traversal: 64 registers (full-SM occupancy of 50%); the per-ray scene
+// lookup leaves no room for the packed child test's registers
 template <int B>
 __global__ void __launch_bounds__(B, 1024 / B) k_srv_trace(SrvDev d, int cur) {
     const int n0 = d.counts[cur], n01 = n0 + d.counts[10 + cur], n = n01 + d.counts[12 + cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 0, (unsigned long long)n);
     SrvClosestIO io{d, cur, n0, n01};
-    trace_queue<false, B>(io, n, d.counts + 8, d.status);
+    trace_queue<false, B, false>(io, n, d.counts + 8, d.status);
 }
 
 // The scene and job tables are read-only here (restrict: the stores of the

@@ -177,16 +177,110 @@ LJ_D float fmin3(float a, float b, float c) {
 // Box slack of the traversal: a child box is entered when
 // max(near planes, tnear) * (1 - 1e-6) <= min(far planes, tfar (1 + 1e-6)) *
 // (1 + 1e-6), i.e. ~8 ulps either side, so hits on box faces and hits at
-// exactly the current closest distance (ties) are never culled; written as
-// one multiply by their quotient.
+// exactly the current closest distance (ties) are never culled; applied as
+// one factor, their quotient, on the near side.
 constexpr float kBoxSlack = (1.0f - 1.0e-6f) / (1.0f + 1.0e-6f);
 
-LJ_D uint32_t extract_byte(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
-// Byte i of w as a float, exactly: one byte permute puts it into the
-// mantissa of 2^23 (bits 0x4B000000), one add removes the 2^23.  Cheaper
-// than an integer extract + int-to-float conversion.
-LJ_D float byte_to_float(uint32_t w, int i) {
-    return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)i)) - 8388608.0f;
+// Pairs of FP32 values in one 64-bit register pair, for the packed FP32
+// instructions of this GPU (PTX add / fma .f32x2): each half is rounded
+// exactly like the scalar instruction, two lanes of work per issue slot.
+typedef unsigned long long f32x2;
+LJ_D f32x2 pk2(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+LJ_D float2 upk2(f32x2 r) {
+    float2 f;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(r));
+    return f;
+}
+LJ_D f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+LJ_D f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// Byte i of w placed in the mantissa of 2^23 (bits 0x4B000000): the float
+// 2^23 + byte, exactly, in one byte permute.
+LJ_D float byte_biased(uint32_t w, int i) { return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + (uint32_t)i)); }
+LJ_D uint32_t byte_of(uint32_t w, int i) { return __byte_perm(w, 0u, 0x4440u + (uint32_t)i); }
+
+// Box test of the 8 children of one wide node (node words c0..c4) for one
+// ray: returns the node's hit mask -- bits 24-31 the hit internal children
+// at slot ^ (7 - octant), bits 0-23 the hit leaf primitives (prim_base +
+// bit).  oct_inv4 is (7 - octant) in every byte; inv the reciprocal
+// direction; tfar_s = tfar * (1 + 1e-6).
+//
+// Plane t = q * a + b with a = 2^e / d, b = (p - o) / d per axis (q the
+// plane's byte).  kPacked: the x and y planes of one side (near or far)
+// form one packed pair with the coefficient pairs (a_x, a_y), (b_x, b_y),
+// so one packed add removes the 2^23 bias of both bytes and one packed FMA
+// gives both t; z goes alone.  The packed form needs a few more live
+// registers: it pays in the any-hit traversal, while the closest-hit one
+// (more state per ray) spills with it and runs the scalar form.  Both give
+// the same t, bit for bit.
+// The mask bits follow Ylitie, Karras and Laine (HPG 2017): a child's meta
+// byte is (unary prim count << 5) | offset for a leaf, (1 << 5) | (24 +
+// slot) for an internal child; XOR-ing the offset of internal children
+// with the octant gives the bit index of every child in one byte op per
+// four children.  Empty slots have meta 0 and add no bit.
+template <bool kPacked>
+LJ_D uint32_t child_hits(uint4 c0, uint4 c1, uint4 c2, uint4 c3, uint4 c4, V3 o, V3 inv, uint32_t oct_inv4,
+                         float tnear, float tfar_s) {
+    const float px = __uint_as_float(c0.x), py = __uint_as_float(c0.y), pz = __uint_as_float(c0.z);
+    const float sx = __uint_as_float((c0.w & 0xffu) << 23);
+    const float sy = __uint_as_float(((c0.w >> 8) & 0xffu) << 23);
+    const float sz = __uint_as_float(((c0.w >> 16) & 0xffu) << 23);
+    const float ax = sx * inv.x, bx = (px - o.x) * inv.x;
+    const float ay = sy * inv.y, by = (py - o.y) * inv.y;
+    const float az = sz * inv.z, bz = (pz - o.z) * inv.z;
+    const f32x2 AXY = pk2(ax, ay), BXY = pk2(bx, by);
+    const f32x2 BIAS = pk2(-8388608.0f, -8388608.0f);
+    // the words holding the near / far plane bytes of the 8 children, per
+    // axis (lo planes are near for a positive direction component)
+    const bool negx = inv.x < 0.0f, negy = inv.y < 0.0f, negz = inv.z < 0.0f;
+    const uint32_t nx0 = negx ? c3.z : c2.x, nx1 = negx ? c3.w : c2.y;
+    const uint32_t fx0 = negx ? c2.x : c3.z, fx1 = negx ? c2.y : c3.w;
+    const uint32_t ny0 = negy ? c4.x : c2.z, ny1 = negy ? c4.y : c2.w;
+    const uint32_t fy0 = negy ? c2.z : c4.x, fy1 = negy ? c2.w : c4.y;
+    const uint32_t nz0 = negz ? c4.z : c3.x, nz1 = negz ? c4.w : c3.y;
+    const uint32_t fz0 = negz ? c3.x : c4.z, fz1 = negz ? c3.y : c4.w;
+    uint32_t hits = 0;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        // per four children: bit index and prim bits of each child's mask entry
+        const uint32_t m = h == 0 ? c1.z : c1.w;
+        const uint32_t inner7 = (((m & (m << 1)) >> 4) & 0x01010101u) * 7u;   // 7 in internal children's bytes
+        const uint32_t bit4 = (m ^ (oct_inv4 & inner7)) & 0x1f1f1f1fu;
+        const uint32_t cnt4 = (m >> 5) & 0x07070707u;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            float2 n, f;
+            if (kPacked) {
+                n = upk2(fma2(add2(pk2(byte_biased(h ? nx1 : nx0, k), byte_biased(h ? ny1 : ny0, k)), BIAS), AXY, BXY));
+                f = upk2(fma2(add2(pk2(byte_biased(h ? fx1 : fx0, k), byte_biased(h ? fy1 : fy0, k)), BIAS), AXY, BXY));
+            } else {
+                n.x = fmaf(byte_biased(h ? nx1 : nx0, k) - 8388608.0f, ax, bx);
+                n.y = fmaf(byte_biased(h ? ny1 : ny0, k) - 8388608.0f, ay, by);
+                f.x = fmaf(byte_biased(h ? fx1 : fx0, k) - 8388608.0f, ax, bx);
+                f.y = fmaf(byte_biased(h ? fy1 : fy0, k) - 8388608.0f, ay, by);
+            }
+            const float nz = fmaf(byte_biased(h ? nz1 : nz0, k) - 8388608.0f, az, bz);
+            const float fz = fmaf(byte_biased(h ? fz1 : fz0, k) - 8388608.0f, az, bz);
+            // slack of ~8 ulps (kBoxSlack): hits on box faces, and hits at
+            // exactly the current closest distance (ties), are never culled
+            const float tmin = fmaxf(fmax3(n.x, n.y, nz), tnear) * kBoxSlack;
+            const float tmax = fmin3(f.x, f.y, fminf(fz, tfar_s));
+            if (tmin <= tmax) hits |= byte_of(cnt4, k) << byte_of(bit4, k);
+        }
+    }
+    return hits;
 }
 
 // Returns true on hit.  kAny: stop at the first hit (occlusion query).
@@ -206,7 +300,7 @@ LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, Trac
     V3 inv = V3{1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z};
     const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
     const uint32_t oct_xor = 7u - oct;
-    const bool negx = inv.x < 0.0f, negy = inv.y < 0.0f, negz = inv.z < 0.0f;
+    const uint32_t oct_inv4 = oct_xor * 0x01010101u;
 
     uint2 stack[kTraversalStack];
     int sp = 0;
@@ -236,45 +330,9 @@ LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, Trac
             const uint4 *np = bvh.nodes + (size_t)child * kWideNodeU4;
             uint4 c0 = __ldg(np + 0), c1 = __ldg(np + 1), c2 = __ldg(np + 2),
                   c3 = __ldg(np + 3), c4 = __ldg(np + 4);
-            float px = __uint_as_float(c0.x), py = __uint_as_float(c0.y), pz = __uint_as_float(c0.z);
-            float sx = __uint_as_float((c0.w & 0xffu) << 23);
-            float sy = __uint_as_float(((c0.w >> 8) & 0xffu) << 23);
-            float sz = __uint_as_float(((c0.w >> 16) & 0xffu) << 23);
-            uint32_t nimask = c0.w >> 24;
-            // plane t = q * a + b
-            float ax = sx * inv.x, bx = (px - o.x) * inv.x;
-            float ay = sy * inv.y, by = (py - o.y) * inv.y;
-            float az = sz * inv.z, bz = (pz - o.z) * inv.z;
-            uint32_t node_hits = 0, prim_hits = 0;
-            // near / far plane words per axis (see trav_step)
-            const uint32_t nx0 = negx ? c3.z : c2.x, nx1 = negx ? c3.w : c2.y;
-            const uint32_t fx0 = negx ? c2.x : c3.z, fx1 = negx ? c2.y : c3.w;
-            const uint32_t ny0 = negy ? c4.x : c2.z, ny1 = negy ? c4.y : c2.w;
-            const uint32_t fy0 = negy ? c2.z : c4.x, fy1 = negy ? c2.w : c4.y;
-            const uint32_t nz0 = negz ? c4.z : c3.x, nz1 = negz ? c4.w : c3.y;
-            const uint32_t fz0 = negz ? c3.x : c4.z, fz1 = negz ? c3.y : c4.w;
-#pragma unroll
-            for (int i = 0; i < 8; i++) {
-                uint32_t meta = extract_byte(i < 4 ? c1.z : c1.w, i & 3);
-                if (meta == 0u) continue;
-                float nx = fmaf(byte_to_float(i < 4 ? nx0 : nx1, i & 3), ax, bx);
-                float fx = fmaf(byte_to_float(i < 4 ? fx0 : fx1, i & 3), ax, bx);
-                float ny = fmaf(byte_to_float(i < 4 ? ny0 : ny1, i & 3), ay, by);
-                float fy = fmaf(byte_to_float(i < 4 ? fy0 : fy1, i & 3), ay, by);
-                float nz = fmaf(byte_to_float(i < 4 ? nz0 : nz1, i & 3), az, bz);
-                float fz = fmaf(byte_to_float(i < 4 ? fz0 : fz1, i & 3), az, bz);
-                // slack of ~8 ulps (kBoxSlack): hits on box faces, and hits at
-                // exactly the current closest distance (ties), are never culled
-                float tmin = fmaxf(fmax3(nx, ny, nz), tnear) * kBoxSlack;
-                float tmax = fmin3(fx, fy, fminf(fz, tfar * (1.0f + 1.0e-6f)));
-                if (tmin <= tmax) {
-                    uint32_t off = meta & 0x1fu;
-                    if (off >= 24u) node_hits |= 1u << (24u + ((uint32_t)i ^ oct_xor));
-                    else prim_hits |= ((meta >> 5) & 7u) << off;
-                }
-            }
-            ngroup = make_uint2(c1.x, node_hits | nimask);
-            tgroup = make_uint2(c1.y, prim_hits);
+            const uint32_t hm = child_hits<kAny>(c0, c1, c2, c3, c4, o, inv, oct_inv4, tnear, tfar * (1.0f + 1.0e-6f));
+            ngroup = make_uint2(c1.x, (hm & 0xff000000u) | (c0.w >> 24));
+            tgroup = make_uint2(c1.y, hm & 0x00ffffffu);
         } else {
             tgroup = ngroup;
             ngroup = make_uint2(0u, 0u);

@@ -41,8 +41,11 @@ struct Trav {
     int iter;
     const uint4 *nodes;
     const float4 *prims;
-    TraceHit hit;
-    bool found;
+    // closest hit so far: its primitive (-1: none), barycentrics; its
+    // distance is tfar (the search interval shrinks to it)
+    int prim;
+    float u, v;
+    LJ_D bool found() const { return prim >= 0; }
 };
 
 LJ_D void trav_init(Trav &s, const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar) {
@@ -61,13 +64,15 @@ LJ_D void trav_init(Trav &s, const DevBvh &bvh, V3 o, V3 d, float tnear, float t
     s.iter = 0;
     s.nodes = bvh.nodes;
     s.prims = bvh.prims;
-    s.hit = TraceHit{0.0f, -1, 0.0f, 0.0f};
-    s.found = false;
+    s.prim = -1;
+    s.u = 0.0f;
+    s.v = 0.0f;
 }
 
 // One step: visit one node (or take the pending primitive group) and test
 // the primitives it yields.  Returns true when the ray is finished.
-template <bool kAny>
+// kPacked: the child box test's packed form (child_hits).
+template <bool kAny, bool kPacked>
 LJ_D bool trav_step(Trav &s, TravStack &stack, int *status) {
     if (++s.iter > (1 << 22)) {   // a well-formed tree needs far fewer steps
         atomicOr(status, kStatusStackOverflow);
@@ -87,47 +92,10 @@ LJ_D bool trav_step(Trav &s, TravStack &stack, int *status) {
         const uint4 *np = s.nodes + (size_t)child * kWideNodeU4;
         const uint4 c0 = __ldg(np + 0), c1 = __ldg(np + 1), c2 = __ldg(np + 2), c3 = __ldg(np + 3),
                     c4 = __ldg(np + 4);
-        const float px = __uint_as_float(c0.x), py = __uint_as_float(c0.y), pz = __uint_as_float(c0.z);
-        const float sx = __uint_as_float((c0.w & 0xffu) << 23);
-        const float sy = __uint_as_float(((c0.w >> 8) & 0xffu) << 23);
-        const float sz = __uint_as_float(((c0.w >> 16) & 0xffu) << 23);
-        const uint32_t nimask = c0.w >> 24;
-        const float ax = sx * s.inv.x, bx = (px - s.o.x) * s.inv.x;
-        const float ay = sy * s.inv.y, by = (py - s.o.y) * s.inv.y;
-        const float az = sz * s.inv.z, bz = (pz - s.o.z) * s.inv.z;
-        const bool negx = s.inv.x < 0.0f, negy = s.inv.y < 0.0f, negz = s.inv.z < 0.0f;
-        // the words holding the near / far plane bytes of the 8 children, per
-        // axis (lo planes are near for a positive direction component)
-        const uint32_t nx0 = negx ? c3.z : c2.x, nx1 = negx ? c3.w : c2.y;
-        const uint32_t fx0 = negx ? c2.x : c3.z, fx1 = negx ? c2.y : c3.w;
-        const uint32_t ny0 = negy ? c4.x : c2.z, ny1 = negy ? c4.y : c2.w;
-        const uint32_t fy0 = negy ? c2.z : c4.x, fy1 = negy ? c2.w : c4.y;
-        const uint32_t nz0 = negz ? c4.z : c3.x, nz1 = negz ? c4.w : c3.y;
-        const uint32_t fz0 = negz ? c3.x : c4.z, fz1 = negz ? c3.y : c4.w;
-        const float tnear = s.tnear, tfar = s.tfar * (1.0f + 1.0e-6f);
-        uint32_t node_hits = 0, prim_hits = 0;
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const uint32_t meta = extract_byte(i < 4 ? c1.z : c1.w, i & 3);
-            if (meta == 0u) continue;
-            const float nx = fmaf(byte_to_float(i < 4 ? nx0 : nx1, i & 3), ax, bx);
-            const float fx = fmaf(byte_to_float(i < 4 ? fx0 : fx1, i & 3), ax, bx);
-            const float ny = fmaf(byte_to_float(i < 4 ? ny0 : ny1, i & 3), ay, by);
-            const float fy = fmaf(byte_to_float(i < 4 ? fy0 : fy1, i & 3), ay, by);
-            const float nz = fmaf(byte_to_float(i < 4 ? nz0 : nz1, i & 3), az, bz);
-            const float fz = fmaf(byte_to_float(i < 4 ? fz0 : fz1, i & 3), az, bz);
-            // slack of ~8 ulps (kBoxSlack): hits on box faces, and hits at
-            // exactly the current closest distance (ties), are never culled
-            const float tmin = fmaxf(fmax3(nx, ny, nz), tnear) * kBoxSlack;
-            const float tmax = fmin3(fx, fy, fminf(fz, tfar));
-            if (tmin <= tmax) {
-                const uint32_t off = meta & 0x1fu;
-                if (off >= 24u) node_hits |= 1u << (24u + ((uint32_t)i ^ s.oct_xor));
-                else prim_hits |= ((meta >> 5) & 7u) << off;
-            }
-        }
-        s.ngroup = make_uint2(c1.x, node_hits | nimask);
-        tgroup = make_uint2(c1.y, prim_hits);
+        const uint32_t hm = child_hits<kPacked>(c0, c1, c2, c3, c4, s.o, s.inv, s.oct_xor * 0x01010101u, s.tnear,
+                                       s.tfar * (1.0f + 1.0e-6f));
+        s.ngroup = make_uint2(c1.x, (hm & 0xff000000u) | (c0.w >> 24));
+        tgroup = make_uint2(c1.y, hm & 0x00ffffffu);
     } else {
         tgroup = s.ngroup;
         s.ngroup = make_uint2(0u, 0u);
@@ -141,22 +109,25 @@ LJ_D bool trav_step(Trav &s, TravStack &stack, int *status) {
         if (f1.w == 0.0f) {
             const float4 f2 = __ldg(pp + 2);
             float t, u, v;
-            // equal distances go to the lower primitive index
+            // equal distances go to the lower primitive index (prim < s.prim
+            // is false while there is no hit: s.prim is -1)
             if (tri_intersect(V3{f0.x, f0.y, f0.z}, V3{f1.x, f1.y, f1.z}, V3{f2.x, f2.y, f2.z}, s.o, s.d, s.tnear,
                               s.tfar, t, u, v) &&
-                (t < s.tfar || (!kAny && s.found && prim < s.hit.prim))) {
-                s.found = true;
+                (t < s.tfar || (!kAny && prim < s.prim))) {
+                s.prim = prim;
                 if (kAny) return true;
                 s.tfar = t;
-                s.hit = TraceHit{t, prim, u, v};
+                s.u = u;
+                s.v = v;
             }
         } else {
             const float t = sphere_hit(V3{f0.x, f0.y, f0.z}, f1.x, s.o, s.d, s.tnear, s.tfar);
             if (t >= 0.0f) {
-                s.found = true;
+                s.prim = prim;
                 if (kAny) return true;
                 s.tfar = t;
-                s.hit = TraceHit{t, prim, 0.0f, 0.0f};   // sphere uv is recomputed from the hit point
+                s.u = 0.0f;   // sphere uv is recomputed from the hit point
+                s.v = 0.0f;
             }
         }
     }
@@ -170,10 +141,11 @@ LJ_D bool trav_step(Trav &s, TravStack &stack, int *status) {
 // Traces rays [0, n) of a queue.  IO supplies, per ray index r:
 //   const DevBvh &bvh(int r)                  the BVH to trace against
 //   void load(int r, V3 &o, V3 &d, float &tnear, float &tfar)
-//   void store(int r, const Trav &s)          s.found / s.hit hold the result
+//   void store(int r, const Trav &s)          s.found(), s.prim / tfar / u / v hold the result
 // *fetch must be 0 at launch; every warp of the grid must call this, with
-// blockDim.x == kBlock.
-template <bool kAny, int kBlock, class IO>
+// blockDim.x == kBlock.  kPacked selects the child box test's packed form:
+// fastest where the kernel's registers allow it without spilling.
+template <bool kAny, int kBlock, bool kPacked = true, class IO>
 LJ_D void trace_queue(IO &io, int n, int *fetch, int *status) {
     const unsigned kFull = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -208,7 +180,7 @@ LJ_D void trace_queue(IO &io, int n, int *fetch, int *status) {
         unsigned act = __ballot_sync(kFull, ray >= 0);
         if (act == 0) break;
         do {
-            if (ray >= 0 && trav_step<kAny>(s, stack, status)) {
+            if (ray >= 0 && trav_step<kAny, kPacked>(s, stack, status)) {
                 io.store(ray, s);
                 ray = -1;
             }
@@ -227,7 +199,7 @@ LJ_D void load_ray(const float4 *rays, int r, V3 &o, V3 &d, float &tn, float &tf
     tf = r1.w;
 }
 LJ_D float4 hit_record(const Trav &s) {
-    return s.found ? make_float4(s.hit.t, __int_as_float(s.hit.prim), s.hit.u, s.hit.v)
+    return s.found() ? make_float4(s.tfar, __int_as_float(s.prim), s.u, s.v)
                    : make_float4(0.0f, __int_as_float(-1), 0.0f, 0.0f);
 }
 
@@ -255,7 +227,7 @@ struct ShadowQueueIO {
     LJ_D const DevBvh &bvh(int) const { return b; }
     LJ_D void load(int r, V3 &o, V3 &d, float &tn, float &tf) const { load_ray(rays, r, o, d, tn, tf); }
     LJ_D void store(int r, const Trav &s) const {
-        if (s.found) return;
+        if (s.found()) return;
         const int t = targets[r];
         float4 *L = t >= 0 ? Lnext + t : Lres + ~t;
         const float4 c = contrib[r], l = *L;
