@@ -376,6 +376,25 @@ __global__ void __launch_bounds__(B, 1024 / B) k_srv_trace(SrvDev d, int cur) {
     trace_queue<false, B, false>(io, n, d.counts + 8, d.status);
 }
 
+// A path store whose entry was loaded before the step runs: the kernel loads
+// the entry's state first and looks its job (and so its scene and options)
+// up from the loaded job index, so the state loads and the job lookup are in
+// flight together instead of one after the other.
+template <class Paths>
+struct PreloadedPaths {
+    const Paths &p;
+    const PathState &st;
+    float4 r0, r1, hit;
+    LJ_D void load(int, PathState &s, float4 &a, float4 &b, float4 &h) const {
+        s = st;
+        a = r0;
+        b = r1;
+        h = hit;
+    }
+    LJ_D int shadow(const PathState &s, float4 a, float4 b, float4 c) const { return p.shadow(s, a, b, c); }
+    LJ_D void emit(const PathState &s, const ShadeOut &o) const { p.emit(s, o); }
+};
+
 // The scene and job tables are read-only here (restrict: the stores of the
 // shade step cannot alias them, so their fields need not be re-read).
 // One instance per material class: class 0 (the queue's front) runs the
@@ -394,9 +413,13 @@ __global__ void __launch_bounds__(kShadeBlock, kClass == 0 ? 6 : 5)
     const QueuePaths<kClass> paths{d, cur};
     for (int i = blockIdx.x * kShadeBlock + threadIdx.x; i < n; i += gridDim.x * kShadeBlock) {
         const int e = kClass == 0 ? i : d.back(i);
-        const SrvJob &jb = jobs[d.buf[cur].job[e]];
+        PathState st;
+        float4 r0, r1, hit;
+        paths.load(e, st, r0, r1, hit);
+        const SrvJob &jb = jobs[st.job];
         const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
-        shade_segment<kClass == 0 ? kClassicMats : kAllMats>(scenes[jb.scene], paths, e, cfg, d.status);
+        const PreloadedPaths<QueuePaths<kClass>> pre{paths, st, r0, r1, hit};
+        shade_segment<kClass == 0 ? kClassicMats : kAllMats>(scenes[jb.scene], pre, e, cfg, d.status);
     }
 }
 
@@ -467,6 +490,28 @@ struct VolQueueStore {
     }
 };
 
+// The volumetric store with the entry's state loaded up front (as
+// PreloadedPaths): load / load_c return it, the rest is the store's.
+struct PreloadedVol {
+    const VolQueueStore &p;
+    const VolState &vs;
+    float4 r0, r1, hit;
+    LJ_D void load(int, VolState &s, float4 &a, float4 &b, float4 &h) const {
+        s = vs;
+        a = r0;
+        b = r1;
+        h = hit;
+    }
+    LJ_D void load_c(int, VolState &s, float4 &a, float4 &b, float4 &h) const {
+        s = vs;
+        a = r0;
+        b = r1;
+        h = hit;
+    }
+    LJ_D void save(int i, const VolState &s) const { p.save(i, s); }
+    LJ_D void emit(const VolState &s, bool alive, float4 a, float4 b) const { p.emit(s, alive, a, b); }
+};
+
 // Volumetric paths: the a / b / c steps of lj_volwave.cuh over the volpath
 // queue and the wave's NEE requests.
 template <int B>
@@ -476,9 +521,13 @@ __global__ void __launch_bounds__(B, 512 / B)
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 3, (unsigned long long)n);
     const VolQueueStore store{d, cur};
     for (int i = blockIdx.x * B + threadIdx.x; i < n; i += gridDim.x * B) {
-        const SrvJob &jb = jobs[d.vbuf[cur].job[i]];
+        VolState vs;
+        float4 r0, r1, hit;
+        store.load(i, vs, r0, r1, hit);
+        const SrvJob &jb = jobs[vs.job];
         const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
-        vol_segment_a(scenes[jb.scene], store, i, cfg, d.nee, d.status, d.stats + 4);
+        const PreloadedVol pre{store, vs, r0, r1, hit};
+        vol_segment_a(scenes[jb.scene], pre, i, cfg, d.nee, d.status, d.stats + 4);
     }
 }
 template <int B>
@@ -502,10 +551,22 @@ __global__ void __launch_bounds__(B, 384 / B)
     const VolQueueStore store{d, cur};
     for (int r = blockIdx.x * B + threadIdx.x; r < n; r += gridDim.x * B) {
         const int k = kKind == 0 ? r : d.nee.cap - 1 - r;
-        const SrvJob &jb = jobs[d.vbuf[cur].job[d.nee.entry[k]]];
-        if (kKind != 0 && jb.all_mats != kKind - 1) continue;
-        const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
-        vol_segment_c<kKind == 1 ? kClassicMats : kAllMats, kKind != 0>(scenes[jb.scene], store, k, cfg, d.nee);
+        if (kKind == 0) {
+            VolState vs;
+            float4 r0, r1, hit;
+            store.load_c(d.nee.entry[k], vs, r0, r1, hit);
+            const SrvJob &jb = jobs[vs.job];
+            const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
+            const PreloadedVol pre{store, vs, r0, r1, hit};
+            vol_segment_c<kAllMats, false>(scenes[jb.scene], pre, k, cfg, d.nee);
+        } else {
+            // the two surface instances share the request range: the job's
+            // material class decides before any state is read
+            const SrvJob &jb = jobs[d.vbuf[cur].job[d.nee.entry[k]]];
+            if (jb.all_mats != kKind - 1) continue;
+            const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
+            vol_segment_c<kKind == 1 ? kClassicMats : kAllMats, true>(scenes[jb.scene], store, k, cfg, d.nee);
+        }
     }
 }
 
