@@ -570,9 +570,12 @@ def run_ours(args):
     if dom in (abi.LJ_KERNEL_MEDIUM, abi.LJ_KERNEL_NEE):
         note = ("volumetric steps are latency bound, not HBM bound: their dependent density-grid lookups "
                 "(8 x 16 B per tracking step) mostly hit L1/L2 (ncu of the volume scene's a / b / c steps)")
+    elif issue:
+        note = ("traversal is instruction-issue bound, not HBM bound: ncu of a full secondary-ray wave shows "
+                "%d%% issue active with %.1f of 32 lanes busy, DRAM a few %% of peak, L2 serving most BVH reads"
+                % (round(100 * issue["issue_active"]), issue["threads_per_inst"]))
     else:
-        note = ("traversal is instruction-issue bound, not HBM bound: ncu on a terrain job shows "
-                "79% issue active, 3.1 IPC, 2% of DRAM peak")
+        note = "traversal is instruction-issue bound, not HBM bound (DRAM a few % of peak)"
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world,
