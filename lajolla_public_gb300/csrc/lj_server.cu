@@ -71,6 +71,8 @@ struct SrvJob {
     float clamp;                 // |sample| bound that keeps the sums inside int64
     int mclass;                  // shade kernel: 0 path, kClassicMats materials; 1 path, any; 2 volpath
     int all_mats;                // volpath: materials outside kClassicMats occur
+    int lambert;                 // class 0, every material Lambertian: the class-0 kernel's
+                                 // Lambertian-only code shades the job
 };
 
 // Material classes of the server's two path shade kernel instances
@@ -398,15 +400,19 @@ struct PreloadedPaths {
 // The scene and job tables are read-only here (restrict: the stores of the
 // shade step cannot alias them, so their fields need not be re-read).
 // One instance per material class: class 0 (the queue's front) runs the
-// smaller kernel compiled for kClassicMats.  The shade kernels run at
-// kShadeBlock threads whatever the server's block size, with the single-
-// scene renderer's occupancy (6 blocks per SM, 5 for every material type:
-// a few spilled registers cost less than the warps fewer blocks would lose).
-// One compiled instance per class keeps a job's arithmetic -- and so its
-// image -- independent of the block size the other kernels use.
+// smaller kernel compiled for kClassicMats, with a branch of code compiled
+// for Lambertian materials alone that the jobs whose materials are all
+// Lambertian take (per lane: a job's paths always run the same branch,
+// whichever other jobs share their warp).  The shade kernels run at
+// kShadeBlock threads whatever the server's block size, 5 blocks per SM (96
+// registers): class 0 at the 6 blocks of the single-scene classic kernel
+// spilled 3x the bytes with its second branch and ran 3 % slower, at 4 it
+// lost more warps than the spills cost.  One compiled instance per class
+// keeps a job's arithmetic -- and so its image -- independent of the block
+// size the other kernels use.
 constexpr int kShadeBlock = 128;
 template <int kClass>
-__global__ void __launch_bounds__(kShadeBlock, kClass == 0 ? 6 : 5)
+__global__ void __launch_bounds__(kShadeBlock, 5)
     k_srv_shade(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
     const int n = d.counts[kClass == 0 ? cur : 10 + cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 2, (unsigned long long)n);
@@ -419,7 +425,9 @@ __global__ void __launch_bounds__(kShadeBlock, kClass == 0 ? 6 : 5)
         const SrvJob &jb = jobs[st.job];
         const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
         const PreloadedPaths<QueuePaths<kClass>> pre{paths, st, r0, r1, hit};
-        shade_segment<kClass == 0 ? kClassicMats : kAllMats>(scenes[jb.scene], pre, e, cfg, d.status);
+        // a job always runs the same branch, whatever its warp shares
+        if (kClass == 0 && jb.lambert) shade_segment<kLambertMats>(scenes[jb.scene], pre, e, cfg, d.status);
+        else shade_segment<kClass == 0 ? kClassicMats : kAllMats>(scenes[jb.scene], pre, e, cfg, d.status);
     }
 }
 
@@ -1040,6 +1048,7 @@ std::string admit(lj_server *s, HostJob *j) {
     if (j->scene->options.integrator == LJ_INTEGRATOR_VOLPATH) h.mclass = 2;
     else h.mclass = classic ? 0 : 1;
     h.all_mats = classic ? 0 : 1;
+    h.lambert = classic && (j->scene->mat_mask & ~kLambertMats) == 0;
     SRV_CUDA(cudaMemcpyAsync(s->d_jobs + slot, &h, sizeof(SrvJob), cudaMemcpyHostToDevice, s->stream));
     SRV_CUDA(cudaMemsetAsync(s->d_ctr + slot, 0, sizeof(SrvCtr), s->stream));
     SRV_CUDA(cudaMemsetAsync(s->d_cancel + slot, 0, sizeof(int), s->stream));
