@@ -37,8 +37,9 @@ struct Trav {
     float tnear, tfar;
     uint32_t oct_xor;
     uint2 ngroup;
-    int sp;
-    int iter;
+    // bits 0-7: stack entries in use; bits 8-31: steps taken (one register
+    // for both: the traversal's live state is what limits its occupancy)
+    int spi;
     const uint4 *nodes;
     const float4 *prims;
     // closest hit so far: its primitive (-1: none), barycentrics; its
@@ -60,8 +61,7 @@ LJ_D void trav_init(Trav &s, const DevBvh &bvh, V3 o, V3 d, float tnear, float t
     const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
     s.oct_xor = 7u - oct;
     s.ngroup = bvh.num_nodes > 0 ? make_uint2(0u, (1u << (24u + (0u ^ s.oct_xor))) | 1u) : make_uint2(0u, 0u);
-    s.sp = 0;
-    s.iter = 0;
+    s.spi = 0;
     s.nodes = bvh.nodes;
     s.prims = bvh.prims;
     s.prim = -1;
@@ -74,7 +74,8 @@ LJ_D void trav_init(Trav &s, const DevBvh &bvh, V3 o, V3 d, float tnear, float t
 // kPacked: the child box test's packed form (child_hits).
 template <bool kAny, bool kPacked>
 LJ_D bool trav_step(Trav &s, TravStack &stack, int *status) {
-    if (++s.iter > (1 << 22)) {   // a well-formed tree needs far fewer steps
+    s.spi += 256;
+    if (s.spi > (1 << 30)) {   // 2^22 steps: a well-formed tree needs far fewer
         atomicOr(status, kStatusStackOverflow);
         return true;
     }
@@ -86,7 +87,7 @@ LJ_D bool trav_step(Trav &s, TravStack &stack, int *status) {
         const uint32_t child = s.ngroup.x + __popc(imask & ((1u << slot) - 1u));
         s.ngroup.y &= ~(1u << k);
         if (s.ngroup.y > 0x00ffffffu) {
-            if (s.sp < kTraversalStack) stack.put(s.sp++, s.ngroup);
+            if ((s.spi & 0xff) < kTraversalStack) stack.put((s.spi++) & 0xff, s.ngroup);
             else atomicOr(status, kStatusStackOverflow);
         }
         const uint4 *np = s.nodes + (size_t)child * kWideNodeU4;
@@ -132,8 +133,8 @@ LJ_D bool trav_step(Trav &s, TravStack &stack, int *status) {
         }
     }
     if (s.ngroup.y <= 0x00ffffffu) {
-        if (s.sp == 0) return true;
-        s.ngroup = stack.get(--s.sp);
+        if ((s.spi & 0xff) == 0) return true;
+        s.ngroup = stack.get((--s.spi) & 0xff);
     }
     return false;
 }
