@@ -46,6 +46,8 @@ Our arm (--impl ours):
   single_scene  the Cornell box (256^2, 64 spp), full terrain (5.5M
             triangles, 1080p, 256 spp) and volume (256^3, 512^2, 256 spp)
             configurations, and the intersection + BSDF microbenchmark.
+  small_jobs  a burst of 64 small jobs ({64,128,256}^2, 1-16 spp) served
+            and rendered plain: batching where no job fills the GPU alone.
   cpu_baseline  the oracle's C++ restatement of the reference path tracer
             (oracle/lj_oracle.cpp, FP64, all host threads) on a bounded
             sample drawn from the GPU arm's own work: (job, pixel, sample)
@@ -301,6 +303,28 @@ def plain_step(gscenes, jobs, out, stream, keep=()):
             imgs[k] = img.numpy().reshape(j["height"], j["width"], 3)
     torch.cuda.synchronize()
     return time.perf_counter() - t0, lat, imgs
+
+
+def small_jobs(srv, gscenes, out, stream, reps=3):
+    """Batching where it matters most: a burst of 64 small jobs (resolution
+    {64,128,256}^2, spp {1,4,16}, max depth 6-16, all arriving at once) over
+    the same resident scenes, served by the benchmark's server and rendered
+    one at a time by the plain renderer; best of `reps` passes each."""
+    jobs = scenes.serving_jobs(seed=77, n_jobs=64, n_scenes=WORKLOAD["n_scenes"], rate=1e9,
+                               resolutions=(64, 128, 256), spps=(1, 4, 16), depth=(6, 16))
+    n = job_samples(jobs)
+    b = min(serve_step(srv, gscenes, jobs)[0] for _ in range(reps))
+    p = min(plain_step(gscenes, jobs, out, stream)[0] for _ in range(reps))
+    _, lat_b, _ = serve_step(srv, gscenes, jobs)
+    _, lat_p, _ = plain_step(gscenes, jobs, out, stream)
+    return {"what": "burst of 64 jobs: resolution {64,128,256}^2, spp {1,4,16}, max depth 6-16, all arriving "
+                    "at once; same scenes and server options as the headline",
+            "samples": n, "batched_msamples_s": round(n / b / 1e6, 1), "plain_msamples_s": round(n / p / 1e6, 1),
+            "batched_over_plain": round(p / b, 3),
+            "latency_ms": {"batched_p50": round(float(np.percentile(lat_b, 50)), 2),
+                           "batched_p99": round(float(np.percentile(lat_b, 99)), 2),
+                           "plain_p50": round(float(np.percentile(lat_p, 50)), 2),
+                           "plain_p99": round(float(np.percentile(lat_p, 99)), 2)}}
 
 
 def tuned_options(ctx, gscenes):
@@ -618,6 +642,7 @@ def run_ours(args):
         "mrays_per_s": round((st1.rays_closest - st0.rays_closest + st1.rays_shadow - st0.rays_shadow)
                              / b_total / 1e6, 1),
     }
+    line["small_jobs"] = small_jobs(srv, gscenes, out, stream)
     if args.microbench:
         line["microbench"] = microbench(ctx)
     if args.configs:
