@@ -432,6 +432,7 @@ constexpr uint32_t kAllMats = (1u << 9) - 1u;
 constexpr uint32_t kLambertMats = 1u << LJ_MAT_LAMBERTIAN;
 constexpr uint32_t kClassicMats =
     (1u << LJ_MAT_LAMBERTIAN) | (1u << LJ_MAT_ROUGHPLASTIC) | (1u << LJ_MAT_ROUGHDIELECTRIC);
+constexpr uint32_t kDisneyBsdfMats = 1u << LJ_MAT_DISNEY_BSDF;   // the combined Disney BSDF alone
 template <uint32_t kMats>
 LJ_HD constexpr bool has_mat(int t) { return (kMats >> t) & 1u; }
 // texture slots a material type reads (the slot table in lj_gpu.h)
