@@ -20,8 +20,9 @@
 //            its job's scene
 //   shade    shade_segment with the job's scene and depth options, one
 //            instance per path class
-//   vol a/b/c  the volumetric steps (one c instance per request kind and
-//            material class)
+//   vol a/b/c  the volumetric steps (b finishes the requests from
+//            scattering points; one c instance per material class for the
+//            requests from surfaces)
 //   shadow   any-hit for the queued NEE rays of the path classes
 //   retire   finished paths: 64-bit fixed-point sums into the job's
 //            accumulator, done counter
@@ -499,18 +500,12 @@ struct VolQueueStore {
 };
 
 // The volumetric store with the entry's state loaded up front (as
-// PreloadedPaths): load / load_c return it, the rest is the store's.
+// PreloadedPaths): load returns it, the rest is the store's.
 struct PreloadedVol {
     const VolQueueStore &p;
     const VolState &vs;
     float4 r0, r1, hit;
     LJ_D void load(int, VolState &s, float4 &a, float4 &b, float4 &h) const {
-        s = vs;
-        a = r0;
-        b = r1;
-        h = hit;
-    }
-    LJ_D void load_c(int, VolState &s, float4 &a, float4 &b, float4 &h) const {
         s = vs;
         a = r0;
         b = r1;
@@ -543,38 +538,35 @@ __global__ void __launch_bounds__(B, 512 / B)
     k_srv_vol_b(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
     const int nf = d.counts[16], n = nf + d.counts[17];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 4, (unsigned long long)n);
+    const VolQueueStore store{d, cur};
     for (int r = blockIdx.x * B + threadIdx.x; r < n; r += gridDim.x * B) {
         const int k = d.nee.req(r, nf);
         const SrvJob &jb = jobs[d.vbuf[cur].job[d.nee.entry[k]]];
-        vol_nee_b(scenes[jb.scene], d.nee, k, jb.max_depth, d.status, d.stats + 5);
+        if (r < nf) {   // from a scattering point: its c step follows here (NeeToPhase)
+            const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
+            vol_nee_b(scenes[jb.scene], d.nee, k, jb.max_depth, d.status, d.stats + 5,
+                      NeeToPhase<VolQueueStore>{scenes[jb.scene], store, d.nee, cfg});
+        } else {
+            vol_nee_b(scenes[jb.scene], d.nee, k, jb.max_depth, d.status, d.stats + 5, NeeToQueue{d.nee});
+        }
     }
 }
-// Three instances: kKind = 0 continues the requests from scattering points
-// (no material code), kKind = 1 / 2 those from surfaces of jobs whose
-// materials are all in kClassicMats (smaller code) / the others.
+// The c step of the requests from surfaces, in two instances: kKind = 1 / 2
+// for jobs whose materials are all in kClassicMats (smaller code) / the
+// others.  (Requests from scattering points finish in k_srv_vol_b.)
 template <int B, int kKind>
 __global__ void __launch_bounds__(B, 384 / B)
     k_srv_vol_c(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
-    const int n = d.counts[kKind == 0 ? 16 : 17];
+    const int n = d.counts[17];
     const VolQueueStore store{d, cur};
     for (int r = blockIdx.x * B + threadIdx.x; r < n; r += gridDim.x * B) {
-        const int k = kKind == 0 ? r : d.nee.cap - 1 - r;
-        if (kKind == 0) {
-            VolState vs;
-            float4 r0, r1, hit;
-            store.load_c(d.nee.entry[k], vs, r0, r1, hit);
-            const SrvJob &jb = jobs[vs.job];
-            const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
-            const PreloadedVol pre{store, vs, r0, r1, hit};
-            vol_segment_c<kAllMats, false>(scenes[jb.scene], pre, k, cfg, d.nee);
-        } else {
-            // the two surface instances share the request range: the job's
-            // material class decides before any state is read
-            const SrvJob &jb = jobs[d.vbuf[cur].job[d.nee.entry[k]]];
-            if (jb.all_mats != kKind - 1) continue;
-            const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
-            vol_segment_c<kKind == 1 ? kClassicMats : kAllMats, true>(scenes[jb.scene], store, k, cfg, d.nee);
-        }
+        const int k = d.nee.cap - 1 - r;
+        // the two instances share the request range: the job's material
+        // class decides before any state is read
+        const SrvJob &jb = jobs[d.vbuf[cur].job[d.nee.entry[k]]];
+        if (jb.all_mats != kKind - 1) continue;
+        const ShadeCfg cfg{jb.max_depth, jb.rr_depth, jb.spread0};
+        vol_segment_c<kKind == 1 ? kClassicMats : kAllMats, true>(scenes[jb.scene], store, k, cfg, d.nee);
     }
 }
 
@@ -624,7 +616,6 @@ struct KernelSet {
     void (*shade1)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*vol_a)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*vol_b)(SrvDev, const DevScene *, const SrvJob *, int);
-    void (*vol_c0)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*vol_c1)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*vol_c2)(SrvDev, const DevScene *, const SrvJob *, int);
     void (*shadow)(SrvDev, int);
@@ -633,7 +624,7 @@ struct KernelSet {
 template <int B>
 KernelSet kernel_set() {
     return KernelSet{k_srv_regen<B>,      k_srv_trace<B>,       k_srv_shade<0>,       k_srv_shade<1>,
-                     k_srv_vol_a<B>,      k_srv_vol_b<B>,       k_srv_vol_c<B, 0>,    k_srv_vol_c<B, 1>,
+                     k_srv_vol_a<B>,      k_srv_vol_b<B>,       k_srv_vol_c<B, 1>,
                      k_srv_vol_c<B, 2>,   k_srv_shadow<B>,      k_srv_retire<B>};
 }
 
@@ -830,9 +821,6 @@ void launch_wave(lj_server *s, int cur) {
     s->ks.vol_b<<<s->grid[7], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
     mark(s, LJ_KERNEL_NEE, false);
     mark(s, LJ_KERNEL_MEDIUM, true);
-    s->ks.vol_c0<<<s->grid[8], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
-    mark(s, LJ_KERNEL_MEDIUM, false);
-    mark(s, LJ_KERNEL_MEDIUM, true);
     s->ks.vol_c1<<<s->grid[9], B, 0, s->stream>>>(s->dev, s->d_scenes, s->d_jobs, cur);
     mark(s, LJ_KERNEL_MEDIUM, false);
     mark(s, LJ_KERNEL_MEDIUM, true);
@@ -977,7 +965,6 @@ std::string build_device(lj_server *s) {
     s->grid[5] = occupancy_grid((const void *)s->ks.shade1, kShadeBlock, sms);
     s->grid[6] = occupancy_grid((const void *)s->ks.vol_a, s->block, sms);
     s->grid[7] = occupancy_grid((const void *)s->ks.vol_b, s->block, sms);
-    s->grid[8] = occupancy_grid((const void *)s->ks.vol_c0, s->block, sms);
     s->grid[9] = occupancy_grid((const void *)s->ks.vol_c1, s->block, sms);
     s->grid[10] = occupancy_grid((const void *)s->ks.vol_c2, s->block, sms);
     s->grid[3] = occupancy_grid((const void *)s->ks.shadow, s->block, sms);
@@ -1255,7 +1242,7 @@ void worker_main(lj_server *s) {
         if (e == cudaSuccess) e = collect_marks(s);
         lk.lock();
         s->waves += 2 * pairs;
-        s->kernel_launches += 24 * pairs;
+        s->kernel_launches += 22 * pairs;
         if (s->graph) s->graph_launches += pairs;
         const int b = s->poll_next;
         s->poll_next = (b + 1) % kPollsInFlight;

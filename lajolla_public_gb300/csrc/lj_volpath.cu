@@ -167,10 +167,18 @@ __global__ void __launch_bounds__(128, 4) k_vol_a(DevScene sc, VolSoA ps, VolQue
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         vol_segment_a(sc, store, i, cfg, q.nee, status, q.stats);
 }
-__global__ void __launch_bounds__(128, 4) k_vol_b(DevScene sc, VolQueues q, int *status) {
+// The requests from scattering points finish their c step here too
+// (NeeToPhase); those from surfaces go on to k_vol_c<..., true>.
+__global__ void __launch_bounds__(128, 4) k_vol_b(DevScene sc, VolSoA ps, VolQueues q, int cur, float spread0,
+                                                  int *status) {
     const int nf = q.counts[2], n = nf + q.counts[3];
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
-        vol_nee_b(sc, q.nee, q.nee.req(r, nf), sc.max_depth, status, q.stats + 1);
+    const ShadeCfg cfg{sc.max_depth, sc.rr_depth, spread0};
+    const VolSlotStore store{ps, q, cur};
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const int k = q.nee.req(r, nf);
+        if (r < nf) vol_nee_b(sc, q.nee, k, sc.max_depth, status, q.stats + 1, NeeToPhase<VolSlotStore>{sc, store, q.nee, cfg});
+        else vol_nee_b(sc, q.nee, k, sc.max_depth, status, q.stats + 1, NeeToQueue{q.nee});
+    }
 }
 // kSurface = false: requests from scattering points (front); true: from
 // surfaces (back)
@@ -315,10 +323,8 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
     const int g_trace = grid_for_kernel((const void *)k_vol_trace, 128);
     const VolCKernel k_cs =
         (scene->mat_mask & ~kClassicMats) == 0 ? k_vol_c<kClassicMats, true> : k_vol_c<kAllMats, true>;
-    const VolCKernel k_cm = k_vol_c<kAllMats, false>;   // no material code
     const int g_a = grid_for_kernel((const void *)k_vol_a, 128);
     const int g_b = grid_for_kernel((const void *)k_vol_b, 128);
-    const int g_cm = grid_for_kernel((const void *)k_cm, 128);
     const int g_cs = grid_for_kernel((const void *)k_cs, 128);
     const bool unbounded = sc.max_depth == -1;
     const int passes = unbounded ? LJ_MAX_BOUNCES + 2 : std::max(1, sc.max_depth);
@@ -378,15 +384,12 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
             k_vol_a<<<g_a, 128, 0, s>>>(sc, ps, q, curq, spread0, ctx->d_status);
             mark_end();
             mark_begin(LJ_KERNEL_NEE);
-            k_vol_b<<<g_b, 128, 0, s>>>(sc, q, ctx->d_status);
-            mark_end();
-            mark_begin(LJ_KERNEL_MEDIUM);
-            k_cm<<<g_cm, 128, 0, s>>>(sc, ps, q, curq, spread0);
+            k_vol_b<<<g_b, 128, 0, s>>>(sc, ps, q, curq, spread0, ctx->d_status);
             mark_end();
             mark_begin(LJ_KERNEL_MEDIUM);
             k_cs<<<g_cs, 128, 0, s>>>(sc, ps, q, curq, spread0);
             mark_end();
-            launches += 6;
+            launches += 5;
             curq ^= 1;
             // stop once every path of the batch has ended
             if ((pass & 3) == 3 && pass + 1 < passes) {

@@ -150,9 +150,26 @@ struct NeeQueue {
     LJ_D int req(int r, int n_front) const { return r < n_front ? r : cap - 1 - (r - n_front); }
 };
 
-// Shadow loop of request k (b step).  max_depth: the job's.
+// The b step's result of request k for the c step: written to the request.
+struct NeeToQueue {
+    const NeeQueue &nq;
+    LJ_D void operator()(int k, uint64_t rng, V3 T, bool blocked, V3 p_nee, V3 p_dir, float4, float4, float4,
+                         float4) const {
+        nq.rng[k] = rng;
+        nq.T[k] = make_float4(T.x, T.y, T.z, blocked ? 1.0f : 0.0f);
+        nq.pn[k] = make_float4(p_nee.x, p_nee.y, p_nee.z, 0.0f);
+        nq.pd[k] = make_float4(p_dir.x, p_dir.y, p_dir.z, 0.0f);
+    }
+};
+
+// Shadow loop of request k (b step).  max_depth: the job's.  finish(k, PCG
+// state, transmittance, blocked, ratio-tracking pdf product, free-flight pdf
+// product, and the request's org / dir / lp / ln as read here) receives the
+// result: NeeToQueue hands it to a c step through the request, a caller may
+// instead continue the path at once.
+template <class Finish = NeeToQueue>
 LJ_D void vol_nee_b(const DevScene &sc, const NeeQueue &nq, int k, int max_depth, int *status,
-                    unsigned long long *seg_stat) {
+                    unsigned long long *seg_stat, const Finish &finish) {
     const float4 o4 = nq.org[k], d4 = nq.dir[k], lp4 = nq.lp[k], ln4 = nq.ln[k];
     const int4 md = nq.med[k];
     const int flags = __float_as_int(ln4.w);
@@ -297,10 +314,7 @@ LJ_D void vol_nee_b(const DevScene &sc, const NeeQueue &nq, int k, int max_depth
         }
         if (seg_stat) counter_add(seg_stat, blocked ? 0u : (unsigned)segs);
     }
-    nq.rng[k] = rng.state;
-    nq.T[k] = make_float4(T.x, T.y, T.z, blocked ? 1.0f : 0.0f);
-    nq.pn[k] = make_float4(p_nee.x, p_nee.y, p_nee.z, 0.0f);
-    nq.pd[k] = make_float4(p_dir.x, p_dir.y, p_dir.z, 0.0f);
+    finish(k, rng.state, T, blocked, p_nee, p_dir, o4, d4, lp4, ln4);
 }
 
 // a step: one queue entry up to its NEE request.  Free-flight delta
@@ -466,14 +480,46 @@ LJ_D void vol_segment_a(const DevScene &sc, const Store &store, int i, const Sha
 // phase (kSurface = false: a request from a scattering point) or BSDF
 // sampling, Russian roulette and the next ray.
 // kMats: the material types the scenes can hold (kAllMats: any).
+// The request fields the c step uses: where the light sample points, what
+// the b step found (T.w = 1: blocked), sigma_s at a scattering point, the
+// PCG state after the shadow loop.
+struct NeeReq {
+    float4 org, dir, lp, ln, T;
+    V3 pn, pd;
+    float4 ss;
+    uint64_t rng;
+};
+LJ_D NeeReq load_req(const NeeQueue &nq, int k, bool surface) {
+    NeeReq q;
+    q.org = nq.org[k];
+    q.dir = nq.dir[k];
+    q.lp = nq.lp[k];
+    q.ln = nq.ln[k];
+    q.T = nq.T[k];
+    const float4 pn4 = nq.pn[k], pd4 = nq.pd[k];
+    q.pn = V3{pn4.x, pn4.y, pn4.z};
+    q.pd = V3{pd4.x, pd4.y, pd4.z};
+    q.ss = surface ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : nq.ss[k];
+    q.rng = nq.rng[k];
+    return q;
+}
+
+template <uint32_t kMats, bool kSurface, class Store>
+LJ_D void vol_c_core(const DevScene &sc, const Store &store, int i, const NeeReq &rq, const ShadeCfg &cfg);
+
 template <uint32_t kMats, bool kSurface, class Store>
 LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const ShadeCfg &cfg, const NeeQueue &nq) {
+    vol_c_core<kMats, kSurface>(sc, store, nq.entry[k], load_req(nq, k, kSurface), cfg);
+}
+
+// The c step of one request of path entry i, from its fields rq.
+template <uint32_t kMats, bool kSurface, class Store>
+LJ_D void vol_c_core(const DevScene &sc, const Store &store, int i, const NeeReq &rq, const ShadeCfg &cfg) {
     const float inf = __int_as_float(0x7f800000);
-    const int i = nq.entry[k];
     VolState vs;
     float4 r0, r1, hit;
     store.load_c(i, vs, r0, r1, hit);
-    const float4 o4 = nq.org[k], d4 = nq.dir[k], lp4 = nq.lp[k], ln4 = nq.ln[k], T4 = nq.T[k];
+    const float4 o4 = rq.org, d4 = rq.dir, lp4 = rq.lp, ln4 = rq.ln, T4 = rq.T;
     const int flags = __float_as_int(ln4.w), lid = __float_as_int(lp4.w);
     constexpr bool surface = kSurface;
     const V3 ro{r0.x, r0.y, r0.z}, rd{r1.x, r1.y, r1.z};
@@ -483,7 +529,7 @@ LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const Sha
     int medium = vs.st.x, bounces = vs.st.y;
     bool never_scatter = vs.st.z != 0;
     Pcg rng;
-    rng.state = nq.rng[k];
+    rng.state = rq.rng;
     rng.inc = ((uint64_t)vs.pixel << 1u) | 1u;
     const V3 wv = -rd;
     Vertex vx;
@@ -517,9 +563,8 @@ LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const Sha
                 pdf_dir = ph;
             }
             V3 Le = light_emission(sc, lid, -dir, pl);
-            const float4 pn4 = nq.pn[k], pd4 = nq.pd[k];
-            float pn = pdf_nee * avg3(V3{pn4.x, pn4.y, pn4.z});
-            float pd = pdf_dir * G * avg3(V3{pd4.x, pd4.y, pd4.z});
+            float pn = pdf_nee * avg3(rq.pn);
+            float pd = pdf_dir * G * avg3(rq.pd);
             float w = (pn * pn) / (pn * pn + pd * pd);
             nee = T * f * Le * (G * w / pn);
         }
@@ -532,8 +577,7 @@ LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const Sha
     float next_tnear = 0.0f;
     if constexpr (!surface) {
         // phase sampling at the scattering point
-        const float4 ss4 = nq.ss[k];
-        const V3 ss{ss4.x, ss4.y, ss4.z};
+        const V3 ss{rq.ss.x, rq.ss.y, rq.ss.z};
         const MediumRec &m = sc.media[medium];
         L += beta * ss * nee;
         float u0 = pcg_uniform(rng), u1 = pcg_uniform(rng);
@@ -592,5 +636,40 @@ LJ_D void vol_segment_c(const DevScene &sc, const Store &store, int k, const Sha
     store.emit(vs, alive, make_float4(next_o.x, next_o.y, next_o.z, next_tnear),
                make_float4(next_d.x, next_d.y, next_d.z, inf));
 }
+
+// A value the compiler must take as it is: no multiply that produced it is
+// fused into an add that uses it, as when it went through memory.
+LJ_D float opaque(float x) {
+    asm volatile("" : "+f"(x));
+    return x;
+}
+
+// The b step of a request from a scattering point goes on with its c step at
+// once (phase sampling needs no material code): the transmittance and the
+// pdf products stay in registers instead of a round trip through the
+// request, and the request is not read again.  The pdf products pass
+// through opaque() so that the c step rounds them exactly as when they were
+// stored, and the path's image does not change.
+template <class Store>
+struct NeeToPhase {
+    const DevScene &sc;
+    const Store &store;
+    const NeeQueue &nq;
+    ShadeCfg cfg;
+    LJ_D void operator()(int k, uint64_t rng, V3 T, bool blocked, V3 p_nee, V3 p_dir, float4 o4, float4 d4,
+                         float4 lp4, float4 ln4) const {
+        NeeReq rq;
+        rq.org = o4;
+        rq.dir = d4;
+        rq.lp = lp4;
+        rq.ln = ln4;
+        rq.T = make_float4(T.x, T.y, T.z, blocked ? 1.0f : 0.0f);
+        rq.pn = V3{opaque(p_nee.x), opaque(p_nee.y), opaque(p_nee.z)};
+        rq.pd = V3{opaque(p_dir.x), opaque(p_dir.y), opaque(p_dir.z)};
+        rq.ss = nq.ss[k];
+        rq.rng = rng;
+        vol_c_core<kAllMats, false>(sc, store, nq.entry[k], rq, cfg);
+    }
+};
 
 }  // namespace lj
