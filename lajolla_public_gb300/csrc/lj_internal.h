@@ -11,6 +11,14 @@
 
 namespace lj {
 
+// Paths in flight of one wavefront batch of the single-scene renderers when
+// the caller does not say (lj_render_params.max_paths_in_flight = 0): 16 Mi
+// paths (~4.8 GB of path state and queues for the path tracer, ~6 GB for
+// the volumetric one).  Larger batches spread each bounce's launch and its
+// last, half-empty warps over more paths: the 1080p x 256 spp terrain
+// renders 16 % faster than with 4 Mi, 32 Mi adds 2 % more.
+constexpr int64_t kDefaultPathsInFlight = (int64_t)1 << 24;
+
 // Status word bits written by bounded device loops.
 enum : int {
     kStatusStackOverflow = 1,

@@ -273,7 +273,7 @@ int render_volpath(lj_scene *scene, const lj_render_params *params, float *d_out
     const int num_pixels = W * H;
     const int spp = params->spp > 0 ? params->spp : scene->options.samples_per_pixel;
     if (spp <= 0) return set_error(ctx, LJ_ERR_INVALID_ARG, "render: samples per pixel must be positive");
-    int64_t cap = params->max_paths_in_flight > 0 ? params->max_paths_in_flight : (int64_t)1 << 22;
+    int64_t cap = params->max_paths_in_flight > 0 ? params->max_paths_in_flight : kDefaultPathsInFlight;
     int nsamp = (int)std::max<int64_t>(1, std::min<int64_t>(spp, cap / std::max(1, num_pixels)));
     size_t P = (size_t)num_pixels * nsamp;
     size_t need = vol_bytes(P);
