@@ -17,7 +17,7 @@ import torch
 
 import ljtest
 from golden import make_golden
-from lajolla_public_gb300 import gpu, scenes
+from lajolla_public_gb300 import abi, gpu, scenes
 from oracle import ljo
 
 pytestmark = pytest.mark.gpu
@@ -43,6 +43,17 @@ def test_per_sample_parity_with_oracle(ctx, case, rtol):
         frac, st = sample_match(sc, ctx, k, rtol)
         assert frac >= 0.99, (case, k, frac)
     assert st.samples == sc.width * sc.height
+
+
+def test_per_sample_parity_disney_only_scene(ctx):
+    """A scene whose materials are all combined Disney BSDFs (terrain +
+    icospheres + envmap) runs the single-scene renderer's Disney-only shade
+    instance; per sample it matches the oracle like the other cases."""
+    sc = scenes.resized_terrain_scene(seed=3, n_tris=20000, width=48, height=32, spp=4, env_size=(64, 32))
+    assert all(m["type"] == abi.LJ_MAT_DISNEY_BSDF for m in sc.materials)
+    for k in (0, 5):
+        frac, _ = sample_match(sc, ctx, k, 1e-2)
+        assert frac >= 0.99, (k, frac)
 
 
 @pytest.mark.parametrize("case", ["cbox", "mixed", "textured", "envmap"])
