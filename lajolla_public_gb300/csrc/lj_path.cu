@@ -78,12 +78,13 @@ __global__ void __launch_bounds__(128, 8) k_trace_shadow(DevBvh bvh, const float
 // runs a much smaller kernel than one that may meet every Disney lobe, and a
 // scene of combined Disney BSDFs alone one without the other eight types.
 template <uint32_t kMats>
-// (5 blocks per SM for the instance for every material type, 6 for the others:
-// a few spilled registers cost less than the warps fewer blocks would lose --
-// the shade step waits on memory, -6 to -11 % against 4 and 5 blocks; the
-// Disney-BSDF instance at 6 blocks shades a Disney scene 6 % faster than the
-// every-type instance at 5)
-__global__ void __launch_bounds__(128, kMats == kAllMats ? 5 : 6) k_shade(DevScene sc, Queues q, int cur, float spread0,
+// (8 blocks per SM (64 registers) for the instances with Disney code, 6 for
+// the others: spilled registers cost less than the warps fewer blocks would
+// lose -- the shade step waits on memory; the Lambertian / classic
+// instances at 6 are -6 to -11 % against 4 and 5 blocks and gain nothing at
+// 8, the Disney-BSDF instance at 8 shades the full terrain 9 % faster than
+// at 6, and 6 % faster at 6 than the every-type instance at 5)
+__global__ void __launch_bounds__(128, (kMats & ~kClassicMats) != 0 ? 8 : 6) k_shade(DevScene sc, Queues q, int cur, float spread0,
                                                                          int *status) {
     const int n = q.counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(q.stats + 2, (unsigned long long)n);

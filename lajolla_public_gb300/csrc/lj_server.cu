@@ -405,15 +405,17 @@ struct PreloadedPaths {
 // for Lambertian materials alone that the jobs whose materials are all
 // Lambertian take (per lane: a job's paths always run the same branch,
 // whichever other jobs share their warp).  The shade kernels run at
-// kShadeBlock threads whatever the server's block size, 5 blocks per SM (96
-// registers): class 0 at the 6 blocks of the single-scene classic kernel
-// spilled 3x the bytes with its second branch and ran 3 % slower, at 4 it
-// lost more warps than the spills cost.  One compiled instance per class
-// keeps a job's arithmetic -- and so its image -- independent of the block
-// size the other kernels use.
+// kShadeBlock threads whatever the server's block size: class 0 at 5 blocks
+// per SM (96 registers; at the 6 blocks of the single-scene classic kernel
+// it spilled 3x the bytes with its second branch and ran 3 % slower, at 4
+// it lost more warps than the spills cost), class 1 at 8 (64 registers: its
+// Disney code waits on memory, and the warps gain more than the spills
+// cost -- a terrain job's shading 16 % faster than at 5).  One compiled
+// instance per class keeps a job's arithmetic -- and so its image --
+// independent of the block size the other kernels use.
 constexpr int kShadeBlock = 128;
 template <int kClass>
-__global__ void __launch_bounds__(kShadeBlock, 5)
+__global__ void __launch_bounds__(kShadeBlock, kClass == 0 ? 5 : 8)
     k_srv_shade(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
     const int n = d.counts[kClass == 0 ? cur : 10 + cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(d.stats + 2, (unsigned long long)n);
@@ -553,9 +555,12 @@ __global__ void __launch_bounds__(B, 512 / B)
 }
 // The c step of the requests from surfaces, in two instances: kKind = 1 / 2
 // for jobs whose materials are all in kClassicMats (smaller code) / the
-// others.  (Requests from scattering points finish in k_srv_vol_b.)
+// others.  (Requests from scattering points finish in k_srv_vol_b.)  At 64
+// registers and full occupancy: its material code waits on memory, and the
+// warps gain more than the spills cost (the serving step's volumetric time
+// -9 % against 128 registers).
 template <int B, int kKind>
-__global__ void __launch_bounds__(B, 384 / B)
+__global__ void __launch_bounds__(B, 1024 / B)
     k_srv_vol_c(SrvDev d, const DevScene *__restrict__ scenes, const SrvJob *__restrict__ jobs, int cur) {
     const int n = d.counts[17];
     const VolQueueStore store{d, cur};

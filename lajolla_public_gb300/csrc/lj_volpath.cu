@@ -181,9 +181,9 @@ __global__ void __launch_bounds__(128, 4) k_vol_b(DevScene sc, VolSoA ps, VolQue
     }
 }
 // kSurface = false: requests from scattering points (front); true: from
-// surfaces (back)
+// surfaces (back).  64 registers, full occupancy (as the server's c step).
 template <uint32_t kMats, bool kSurface>
-__global__ void __launch_bounds__(128, 3) k_vol_c(DevScene sc, VolSoA ps, VolQueues q, int cur, float spread0) {
+__global__ void __launch_bounds__(128, 8) k_vol_c(DevScene sc, VolSoA ps, VolQueues q, int cur, float spread0) {
     const int n = q.counts[kSurface ? 3 : 2];
     const ShadeCfg cfg{sc.max_depth, sc.rr_depth, spread0};
     const VolSlotStore store{ps, q, cur};
