@@ -25,7 +25,8 @@
 //            requests from surfaces)
 //   shadow   any-hit for the queued NEE rays of the path classes
 //   retire   finished paths: 64-bit fixed-point sums into the job's
-//            accumulator, done counter
+//            accumulator (one plane per channel: a warp's atomics for one
+//            channel land on consecutive words), done counter
 // Two waves (ray queues 0 -> 1 -> 0) form one CUDA graph.
 //
 // Host side, a worker thread admits jobs under the HBM budget, keeps the
@@ -65,7 +66,7 @@ struct SrvJob {
     CamRec cam;
     unsigned long long seed;
     long long total;             // npix * spp
-    unsigned long long *accum;   // npix * 3 sums in units of 2^-32
+    unsigned long long *accum;   // 3 planes of npix sums (R, G, B) in units of 2^-32
     int scene, npix, spp, sample_offset;
     int max_depth, rr_depth;
     float spread0;
@@ -596,22 +597,32 @@ __global__ void __launch_bounds__(B) k_srv_retire(SrvDev d) {
         const SrvJob &jb = d.jobs[j];
         const float4 L = d.rL[i];
         if (isfinite(L.x) && isfinite(L.y) && isfinite(L.z)) {
-            unsigned long long *a = jb.accum + 3 * (size_t)d.rpixel[i];
+            // integer sums: the same totals in any order or layout
+            unsigned long long *a = jb.accum + d.rpixel[i];
+            const size_t np = (size_t)jb.npix;
             atomicAdd(a, to_fixed(L.x, jb.clamp));
-            atomicAdd(a + 1, to_fixed(L.y, jb.clamp));
-            atomicAdd(a + 2, to_fixed(L.z, jb.clamp));
+            atomicAdd(a + np, to_fixed(L.y, jb.clamp));
+            atomicAdd(a + 2 * np, to_fixed(L.z, jb.clamp));
         } else {
             atomicAdd(&d.ctr[j].dropped, 1ULL);
         }
+        // one done-counter atomic per job per warp; most warps hold one job
         const unsigned active = __activemask();
-        const unsigned same = __match_any_sync(active, j);
-        if ((int)(threadIdx.x & 31u) == __ffs(same) - 1) atomicAdd(&d.ctr[j].done, (unsigned long long)__popc(same));
+        const int lead = __ffs(active) - 1;
+        if (__all_sync(active, j == __shfl_sync(active, j, lead))) {
+            if ((int)(threadIdx.x & 31u) == lead) atomicAdd(&d.ctr[j].done, (unsigned long long)__popc(active));
+        } else {
+            const unsigned same = __match_any_sync(active, j);
+            if ((int)(threadIdx.x & 31u) == __ffs(same) - 1)
+                atomicAdd(&d.ctr[j].done, (unsigned long long)__popc(same));
+        }
     }
 }
 
+// n = 3 * npix: HWC image element i from plane i % 3, pixel i / 3
 __global__ void k_srv_finalize(const unsigned long long *acc, float *img, long long n, double scale) {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) img[i] = (float)((double)(long long)acc[i] * scale);
+    if (i < n) img[i] = (float)((double)(long long)acc[(i % 3) * (n / 3) + i / 3] * scale);
 }
 
 struct KernelSet {
