@@ -67,6 +67,8 @@ struct SrvJob {
     unsigned long long seed;
     long long total;             // npix * spp
     unsigned long long *accum;   // 3 planes of npix sums (R, G, B) in units of 2^-32
+    DevBvh bvh;                  // the scene's BVH (a copy: a ray fetched by the
+                                 // traversal finds its tree one load sooner)
     int scene, npix, spp, sample_offset;
     int max_depth, rr_depth;
     float spread0;
@@ -284,7 +286,7 @@ struct SrvClosestIO {
     int cur, n0, n01;   // class-0 entries; class-0 + class-1 entries of queue cur
     LJ_D const DevBvh &bvh(int r) const {
         const int job = r < n01 ? d.buf[cur].job[d.entry(r, n0)] : d.vbuf[cur].job[r - n01];
-        return d.scenes[d.jobs[job].scene].bvh;
+        return d.jobs[job].bvh;
     }
     LJ_D void load(int r, V3 &o, V3 &dir, float &tn, float &tf) const {
         if (r < n01) load_ray(d.buf[cur].ray, d.entry(r, n0), o, dir, tn, tf);
@@ -302,7 +304,7 @@ struct SrvShadowIO {
         const int t = d.starget[r];
         return t < 0 ? d.rjob[t & 0x7fffffff] : d.buf[nxt].job[t];
     }
-    LJ_D const DevBvh &bvh(int r) const { return d.scenes[d.jobs[job_of(r)].scene].bvh; }
+    LJ_D const DevBvh &bvh(int r) const { return d.jobs[job_of(r)].bvh; }
     LJ_D void load(int r, V3 &o, V3 &dir, float &tn, float &tf) const { load_ray(d.sray, r, o, dir, tn, tf); }
     LJ_D void store(int r, const Trav &s) const {
         if (s.found()) return;
@@ -1040,6 +1042,7 @@ std::string admit(lj_server *s, HostJob *j) {
     h.total = j->total;
     h.accum = j->d_accum;
     h.scene = j->scene_slot;
+    h.bvh = j->scene->dev.bvh;   // a served scene's BVH does not change (updates refused)
     h.npix = (int)npix;
     h.spp = j->spp;
     h.sample_offset = j->sample_offset;
