@@ -29,8 +29,9 @@ Our arm (--impl ours):
             (and errors) match (matched_error).
   latency   p50 / p99 of (completion - arrival) per job, both arms.
   e2e       one step through the C ABI from host memory: the scene pool is
-            uploaded (lj_gpu_scene_create: descriptors from host, device BVH
-            build) inside the timed region, then the jobs are served.
+            uploaded (lj_gpu_scene_create_many: descriptors from host, device
+            BVH builds, the scenes' uploads overlapped) inside the timed
+            region, then the jobs are served.
   roofline  the dominant kernel class of a profiled server step
             (LJ_SERVER_PROFILE: CUDA events around every kernel on the
             server's stream), compulsory algorithmic bytes per launch
@@ -533,7 +534,7 @@ def run_ours(args):
     jobs = make_jobs(1000)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    g2 = [gpu.GpuScene(ctx, s) for s in pool]
+    g2 = gpu.create_scenes(ctx, pool)
     torch.cuda.synchronize()
     upload_s = time.perf_counter() - t0
     sec, _, _ = serve_step(srv_e2e, g2, jobs)
@@ -615,7 +616,7 @@ def run_ours(args):
         "clocks": ck,
         "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "scene_upload_s": round(upload_s, 4),
-                "what": "scene pool uploaded from host (lj_gpu_scene_create, BVH build) + one step served, "
+                "what": "scene pool uploaded from host (lj_gpu_scene_create_many, BVH builds) + one step served, "
                         "images to host"},
         "scene_update": update,
         "gpu_launches": int(launches),

@@ -45,8 +45,9 @@ extern "C" {
  * (LJ_KERNEL_MEDIUM, LJ_KERNEL_NEE) and the volumetric counters of
  * lj_server_stats
  * 3: the emission, camera-ray and medium batches; LJ_RENDER_COUNT_BVH and
- * the lj_stats.bvh_* counters; lj_gpu_scene_update_mesh */
-#define LJ_GPU_ABI_VERSION 3
+ * the lj_stats.bvh_* counters; lj_gpu_scene_update_mesh
+ * 4: lj_gpu_scene_create_many */
+#define LJ_GPU_ABI_VERSION 4
 
 /* ---- error codes -------------------------------------------------------- */
 #define LJ_OK                 0
@@ -245,6 +246,18 @@ int lj_gpu_abi_version(void);
  * table construction (src/scene.cpp:4-53).  Copies the description to the
  * device and builds the BVH there (LBVH -> 8-wide compressed BVH). */
 int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *desc, lj_scene **out);
+/* n scenes at once, each exactly as lj_gpu_scene_create makes it (the same
+ * BVH, tables and device records), with their copies and device builds on
+ * streams of their own and their host-side tables on threads of their own
+ * (up to 8), so that a server's resident pool loads in about the time of
+ * its largest scene: a BVH build is a chain of small dependent launches,
+ * and the chains of several scenes overlap.  Every description is checked
+ * first (lj_gpu_scene_validate's checks); on any error no scene is kept,
+ * out[0..n) are all NULL and the message names the failing description's
+ * index.  Returns when every scene is on the device.  Replaces n
+ * Scene::Scene constructions (src/scene.cpp:4-53), one per scene file a
+ * server keeps resident. */
+int lj_gpu_scene_create_many(lj_ctx *ctx, int32_t n, const lj_scene_desc *const *descs, lj_scene **out);
 /* The checks lj_gpu_scene_create makes before it touches the device, with no
  * context and no device needed: indices in range (shapes -> materials,
  * lights, media; lights -> shapes, images; textures -> images), known kinds,

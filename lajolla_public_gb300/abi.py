@@ -131,7 +131,7 @@ class lj_scene_info(C.Structure):
                 ("device_bytes", C.c_int64), ("build_ms", C.c_double)]
 
 
-LJ_GPU_ABI_VERSION = 3       # the structs below mirror this version of include/lj_gpu.h
+LJ_GPU_ABI_VERSION = 4       # the structs below mirror this version of include/lj_gpu.h
 LJ_RENDER_PROFILE = 1
 (LJ_KERNEL_CAMERA, LJ_KERNEL_TRACE, LJ_KERNEL_SHADE, LJ_KERNEL_SHADOW, LJ_KERNEL_OTHER, LJ_KERNEL_MEDIUM,
  LJ_KERNEL_NEE) = range(7)

@@ -8,9 +8,12 @@
 // src/scene.h:99-105).  Tables are built in double precision, as the
 // reference does, and stored as FP32.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
+#include <thread>
 
 #include "lj_host.h"
 
@@ -153,8 +156,13 @@ void lookup0(const HostImg &im, double u, double v, double out[3]) {
 // page-locked for the copy (cudaHostRegister, read-only where the device
 // allows it) and released after it: a pageable copy of tens of MB runs at
 // a fraction of the link's rate.  Memory that is already page-locked, or
-// that cannot be registered, is copied as it is.
+// that cannot be registered, is copied as it is.  One copy at a time in the
+// process (scene creations may run on several threads): a range locked for
+// one copy is never seen, half-released, by a copy of an overlapping range
+// that a caller's two descriptions share.
+std::mutex g_h2d_mutex;
 int h2d(void *dst, const void *src, size_t bytes, cudaStream_t s, std::string *err) {
+    std::lock_guard<std::mutex> lock(g_h2d_mutex);
     if (bytes >= ((size_t)4 << 20)) {
         void *h = const_cast<void *>(src);
         cudaError_t e = cudaHostRegister(h, bytes, cudaHostRegisterReadOnly);
@@ -183,7 +191,7 @@ int upload(lj_scene *sc, const T *src, size_t n, const T **dst, std::string *err
     void *p = nullptr;
     LJ_CUDA_TRY(cudaMalloc(&p, sizeof(T) * n));
     sc->allocs.push_back(p);
-    if (h2d(p, src, sizeof(T) * n, sc->ctx->stream, err)) return -2;
+    if (h2d(p, src, sizeof(T) * n, sc->upload_stream, err)) return -2;
     *dst = (const T *)p;
     sc->info.device_bytes += (int64_t)(sizeof(T) * n);
     return 0;
@@ -399,22 +407,37 @@ int lj_gpu_scene_validate(const lj_scene_desc *d, char *msg, int msg_size) {
     return rc;
 }
 
-int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
-    if (!ctx || !d || !out) return LJ_ERR_INVALID_ARG;
-    *out = nullptr;
-    std::string msg;
-    if (check_desc(d, msg)) return set_error(ctx, LJ_ERR_INVALID_ARG, msg);
+namespace {
+
+// Frees a scene that never joined its context's list (its creation failed,
+// or another scene of the same lj_gpu_scene_create_many call did).
+void discard_scene(lj_scene *sc) {
+    cudaStreamSynchronize(sc->upload_stream);
+    for (void *p : sc->allocs) cudaFree(p);
+    delete sc;
+}
+
+// One scene from a checked description, every copy and kernel on `stream`,
+// the host-side tables built on the calling thread.  Touches nothing of the
+// context but its device and stream-independent settings, so that several
+// run at once; on failure the scene's allocations are freed and msg says why.
+int create_scene(lj_ctx *ctx, const lj_scene_desc *d, cudaStream_t stream, lj_scene **out, std::string &msg) {
     cudaSetDevice(ctx->device);
     lj_scene *sc = new (std::nothrow) lj_scene();
-    if (!sc) return set_error(ctx, LJ_ERR_OUT_OF_MEMORY, "host allocation failed");
+    if (!sc) {
+        msg = "host allocation failed";
+        return LJ_ERR_OUT_OF_MEMORY;
+    }
     sc->ctx = ctx;
+    sc->upload_stream = stream;
     sc->options = d->options;
     sc->width = d->camera.width;
     sc->height = d->camera.height;
     std::string err;
     auto fail = [&](int code) {
-        lj_gpu_scene_destroy(sc);
-        return set_error(ctx, code, err.empty() ? "scene upload failed" : err);
+        discard_scene(sc);
+        msg = err.empty() ? "scene upload failed" : err;
+        return code;
     };
     DevScene &ds = sc->dev;
 
@@ -516,7 +539,7 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
     // ---- BVH ----
     BvhInput bin{ds.vpos, ds.tri_vidx, d_spheres, num_tris, num_spheres};
     BvhOutput bout;
-    int rc = build_bvh(bin, &bout, ctx->stream, &err);
+    int rc = build_bvh(bin, &bout, stream, &err);
     if (bout.nodes) sc->allocs.push_back(bout.nodes);
     if (bout.prims) sc->allocs.push_back(bout.prims);
     if (rc) return fail(rc == -5 ? LJ_ERR_DEVICE_LIMIT : LJ_ERR_CUDA);
@@ -724,14 +747,14 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
                 float4 *rgb = nullptr;
                 const int gblocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
                 bool ok = cudaMalloc(&d_mx, sizeof(h_mx)) == cudaSuccess &&
-                          cudaMemsetAsync(d_mx, 0, sizeof(h_mx), ctx->stream) == cudaSuccess;
+                          cudaMemsetAsync(d_mx, 0, sizeof(h_mx), stream) == cudaSuccess;
                 if (ok && v.channels == 1) {   // one float per voxel, uploaded from the caller's array
                     ok = upload(sc, v.data, n, &o.data1, &err) == 0;
                     raw = o.data1;
                 } else if (ok) {
                     void *tmp = nullptr;
                     ok = cudaMalloc(&tmp, sizeof(float) * 3 * n) == cudaSuccess &&
-                         h2d(tmp, v.data, sizeof(float) * 3 * n, ctx->stream, &err) == 0 &&
+                         h2d(tmp, v.data, sizeof(float) * 3 * n, stream, &err) == 0 &&
                          cudaMalloc((void **)&rgb, sizeof(float4) * n) == cudaSuccess;
                     if (rgb) {
                         sc->allocs.push_back(rgb);
@@ -741,11 +764,11 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
                     raw = (const float *)tmp;
                 }
                 if (ok) {
-                    k_grid_prep<<<gblocks, 256, 0, ctx->stream>>>(raw, n, v.channels, rgb, d_mx);
+                    k_grid_prep<<<gblocks, 256, 0, stream>>>(raw, n, v.channels, rgb, d_mx);
                     ok = cudaGetLastError() == cudaSuccess &&
-                         cudaMemcpyAsync(h_mx, d_mx, sizeof(h_mx), cudaMemcpyDeviceToHost, ctx->stream) ==
+                         cudaMemcpyAsync(h_mx, d_mx, sizeof(h_mx), cudaMemcpyDeviceToHost, stream) ==
                              cudaSuccess &&
-                         cudaStreamSynchronize(ctx->stream) == cudaSuccess;
+                         cudaStreamSynchronize(stream) == cudaSuccess;
                 }
                 if (v.channels == 3 && raw) cudaFree(const_cast<float *>(raw));
                 if (d_mx) cudaFree(d_mx);
@@ -774,12 +797,78 @@ int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
         ds.camera_medium = d->camera.medium_id;
         ds.max_null_collisions = d->options.max_null_collisions;
     }
-    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+    if (cudaStreamSynchronize(stream) != cudaSuccess) {
         err = "scene upload: stream synchronize failed";
         return fail(LJ_ERR_CUDA);
     }
+    sc->upload_stream = ctx->stream;   // later copies (none yet) go to the context's stream
+    *out = sc;
+    return LJ_OK;
+}
+
+constexpr int kCreateThreads = 8;   // host threads of one lj_gpu_scene_create_many call at most
+
+}  // namespace
+
+int lj_gpu_scene_create(lj_ctx *ctx, const lj_scene_desc *d, lj_scene **out) {
+    if (!ctx || !d || !out) return LJ_ERR_INVALID_ARG;
+    *out = nullptr;
+    std::string msg;
+    if (check_desc(d, msg)) return set_error(ctx, LJ_ERR_INVALID_ARG, msg);
+    lj_scene *sc = nullptr;
+    const int rc = create_scene(ctx, d, ctx->stream, &sc, msg);
+    if (rc != LJ_OK) return set_error(ctx, rc, msg);
     ctx->scenes.push_back(sc);
     *out = sc;
+    return LJ_OK;
+}
+
+int lj_gpu_scene_create_many(lj_ctx *ctx, int32_t n, const lj_scene_desc *const *descs, lj_scene **out) {
+    if (!ctx || n < 0 || (n > 0 && (!descs || !out))) return LJ_ERR_INVALID_ARG;
+    for (int i = 0; i < n; i++) out[i] = nullptr;
+    for (int i = 0; i < n; i++) {
+        std::string msg = "NULL description";
+        if (!descs[i] || check_desc(descs[i], msg))
+            return set_error(ctx, LJ_ERR_INVALID_ARG, "scene_create_many: description " + std::to_string(i) + ": " + msg);
+    }
+    if (n == 0) return LJ_OK;
+    cudaSetDevice(ctx->device);
+    std::vector<cudaStream_t> streams(n, nullptr);
+    for (int i = 0; i < n; i++) {
+        if (cudaStreamCreateWithFlags(&streams[i], cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            for (int k = 0; k < i; k++) cudaStreamDestroy(streams[k]);
+            return set_error(ctx, LJ_ERR_CUDA, "scene_create_many: stream creation failed");
+        }
+    }
+    std::vector<lj_scene *> made(n, nullptr);
+    std::vector<int> rc(n, LJ_OK);
+    std::vector<std::string> msg(n);
+    std::atomic<int> next{0};
+    auto work = [&]() {
+        for (int i = next++; i < n; i = next++) rc[i] = create_scene(ctx, descs[i], streams[i], &made[i], msg[i]);
+    };
+    std::vector<std::thread> helpers;
+    for (int t = 1; t < std::min(n, kCreateThreads); t++) {
+        try {
+            helpers.emplace_back(work);
+        } catch (...) {   // no more threads: the ones started (and this one) take the rest
+            break;
+        }
+    }
+    work();
+    for (std::thread &t : helpers) t.join();
+    for (cudaStream_t s : streams) cudaStreamDestroy(s);   // each creation synchronized its stream
+    for (int i = 0; i < n; i++) {
+        if (rc[i] == LJ_OK) continue;
+        for (lj_scene *sc : made)
+            if (sc) discard_scene(sc);
+        return set_error(ctx, rc[i], "scene_create_many: description " + std::to_string(i) + ": " + msg[i]);
+    }
+    for (int i = 0; i < n; i++) {
+        ctx->scenes.push_back(made[i]);
+        out[i] = made[i];
+    }
     return LJ_OK;
 }
 

@@ -33,6 +33,7 @@ struct PathBuffers {
 
 struct lj_scene {
     lj_ctx *ctx = nullptr;
+    cudaStream_t upload_stream = nullptr;   // the stream the scene's creation copies and builds on
     lj::DevScene dev{};
     std::vector<void *> allocs;   // device allocations freed on destroy
     lj_scene_info info{};

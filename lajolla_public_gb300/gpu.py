@@ -52,6 +52,7 @@ def lib():
                           % (L.lj_gpu_abi_version(), abi.LJ_GPU_ABI_VERSION))
         L.lj_gpu_scene_create.argtypes = [vp, C.POINTER(abi.lj_scene_desc), C.POINTER(vp)]
         L.lj_gpu_scene_validate.argtypes = [C.POINTER(abi.lj_scene_desc), C.c_char_p, C.c_int]
+        L.lj_gpu_scene_create_many.argtypes = [vp, i32, C.POINTER(C.POINTER(abi.lj_scene_desc)), C.POINTER(vp)]
         L.lj_gpu_scene_destroy.argtypes = [vp]
         L.lj_gpu_scene_update_mesh.argtypes = [vp, i32, vp, vp, i32, i32]
         L.lj_gpu_scene_info.argtypes = [vp, C.POINTER(abi.lj_scene_info)]
@@ -181,6 +182,28 @@ class Context:
         self.check(lib().lj_gpu_phase_batch(self.h, kind, g, _ptr(dir_in), _ptr(dir_out), _ptr(rnd),
                                             _ptr(val), _ptr(pdf), _ptr(d), n, stream))
         return val, pdf, d
+
+
+def create_scenes(ctx, scene_list):
+    """GpuScenes for several scenes.Scene descriptions at once
+    (lj_gpu_scene_create_many: the same scenes as one GpuScene each, their
+    copies, device builds and host tables overlapped)."""
+    scene_list = list(scene_list)
+    n = len(scene_list)
+    if not ctx.h:
+        raise LjError(abi.LJ_ERR_INVALID_ARG, "context is closed")
+    made = [s.desc() for s in scene_list]   # (desc, arrays it points into)
+    descs = (C.POINTER(abi.lj_scene_desc) * max(1, n))(*[C.pointer(d) for d, _ in made])
+    outs = (C.c_void_p * max(1, n))()
+    ctx.check(lib().lj_gpu_scene_create_many(ctx.h, n, descs, outs))
+    res = []
+    for s, h in zip(scene_list, outs[:n]):
+        g = GpuScene.__new__(GpuScene)
+        g.ctx, g.scene, g.h = ctx, s, C.c_void_p(h)
+        ctx._scenes.add(g)
+        res.append(g)
+    del made
+    return res
 
 
 class GpuScene:

@@ -31,7 +31,7 @@ def test_library_builds_and_loads():
     path = build.build()
     assert os.path.exists(path)
     L = gpu.lib()
-    assert L.lj_gpu_abi_version() == abi.LJ_GPU_ABI_VERSION == 3
+    assert L.lj_gpu_abi_version() == abi.LJ_GPU_ABI_VERSION == 4
 
 
 def test_every_declared_symbol_is_exported():
