@@ -417,25 +417,32 @@ void discard_scene(lj_scene *sc) {
     delete sc;
 }
 
+// A scene under construction: discarded on every way out but success
+// (an error code or an exception).
+struct SceneGuard {
+    lj_scene *sc = nullptr;
+    bool keep = false;
+    ~SceneGuard() {
+        if (sc && !keep) discard_scene(sc);
+    }
+};
+
 // One scene from a checked description, every copy and kernel on `stream`,
 // the host-side tables built on the calling thread.  Touches nothing of the
 // context but its device and stream-independent settings, so that several
 // run at once; on failure the scene's allocations are freed and msg says why.
-int create_scene(lj_ctx *ctx, const lj_scene_desc *d, cudaStream_t stream, lj_scene **out, std::string &msg) {
+int create_scene_body(lj_ctx *ctx, const lj_scene_desc *d, cudaStream_t stream, lj_scene **out, std::string &msg,
+                      SceneGuard &guard) {
     cudaSetDevice(ctx->device);
-    lj_scene *sc = new (std::nothrow) lj_scene();
-    if (!sc) {
-        msg = "host allocation failed";
-        return LJ_ERR_OUT_OF_MEMORY;
-    }
+    lj_scene *sc = new lj_scene();
+    guard.sc = sc;
     sc->ctx = ctx;
     sc->upload_stream = stream;
     sc->options = d->options;
     sc->width = d->camera.width;
     sc->height = d->camera.height;
     std::string err;
-    auto fail = [&](int code) {
-        discard_scene(sc);
+    auto fail = [&](int code) {   // the guard frees the scene
         msg = err.empty() ? "scene upload failed" : err;
         return code;
     };
@@ -802,8 +809,26 @@ int create_scene(lj_ctx *ctx, const lj_scene_desc *d, cudaStream_t stream, lj_sc
         return fail(LJ_ERR_CUDA);
     }
     sc->upload_stream = ctx->stream;   // later copies (none yet) go to the context's stream
+    guard.keep = true;
     *out = sc;
     return LJ_OK;
+}
+
+// create_scene_body with no exception leaving it (a host allocation that
+// fails becomes LJ_ERR_OUT_OF_MEMORY): it runs on threads of its own and
+// under the C ABI.
+int create_scene(lj_ctx *ctx, const lj_scene_desc *d, cudaStream_t stream, lj_scene **out, std::string &msg) {
+    *out = nullptr;
+    try {
+        SceneGuard guard;
+        return create_scene_body(ctx, d, stream, out, msg, guard);
+    } catch (const std::bad_alloc &) {
+        msg = "host allocation failed";
+        return LJ_ERR_OUT_OF_MEMORY;
+    } catch (...) {
+        msg = "scene creation failed";
+        return LJ_ERR_CUDA;
+    }
 }
 
 constexpr int kCreateThreads = 8;   // host threads of one lj_gpu_scene_create_many call at most
