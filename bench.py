@@ -540,6 +540,7 @@ def run_ours(args):
     sec, _, _ = serve_step(srv_e2e, g2, jobs)
     e2e_s = time.perf_counter() - t0
     srv_e2e.stop()
+    e2e_build_ms = [round(g.info().build_ms, 2) for g in g2]
     for g in g2:
         g.close()
     e2e_value = job_samples(jobs) * world / max_over_ranks(e2e_s, world) / 1e6
@@ -616,6 +617,7 @@ def run_ours(args):
         "clocks": ck,
         "e2e": {"value": round(e2e_value, 3), "unit": "Msamples/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "scene_upload_s": round(upload_s, 4),
+                "scene_build_ms": e2e_build_ms,
                 "what": "scene pool uploaded from host (lj_gpu_scene_create_many, BVH builds) + one step served, "
                         "images to host"},
         "scene_update": update,
