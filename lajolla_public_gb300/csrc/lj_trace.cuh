@@ -297,7 +297,8 @@ LJ_D bool trace_bvh(const DevBvh &bvh, V3 o, V3 d, float tnear, float tfar, Trac
     V3 dd = V3{fabsf(d.x) < tiny ? copysignf(tiny, d.x) : d.x,
                fabsf(d.y) < tiny ? copysignf(tiny, d.y) : d.y,
                fabsf(d.z) < tiny ? copysignf(tiny, d.z) : d.z};
-    V3 inv = V3{1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z};
+    // __frcp_rn: the correctly rounded reciprocal, the same bits as 1.0f / x
+    V3 inv = V3{__frcp_rn(dd.x), __frcp_rn(dd.y), __frcp_rn(dd.z)};
     const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
     const uint32_t oct_xor = 7u - oct;
     const uint32_t oct_inv4 = oct_xor * 0x01010101u;

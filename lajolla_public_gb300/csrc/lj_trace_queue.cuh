@@ -55,7 +55,7 @@ LJ_D void trav_init(Trav &s, const DevBvh &bvh, V3 o, V3 d, float tnear, float t
                fabsf(d.z) < tiny ? copysignf(tiny, d.z) : d.z};
     s.o = o;
     s.d = d;
-    s.inv = V3{1.0f / dd.x, 1.0f / dd.y, 1.0f / dd.z};
+    s.inv = V3{__frcp_rn(dd.x), __frcp_rn(dd.y), __frcp_rn(dd.z)};   // = 1.0f / x, correctly rounded
     s.tnear = tnear;
     s.tfar = tfar;
     const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);

@@ -82,7 +82,9 @@ LJ_D V3 vol_lookup(const VolRec &v, V3 p) {
 LJ_D bool vol_box_hit(const VolRec &v, V3 o, V3 d) {
     if (v.kind == 0) return true;
     float t0 = 0.f, t1 = __int_as_float(0x7f800000);
-    const float oo[3] = {o.x, o.y, o.z}, inv[3] = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+    // __frcp_rn: the correctly rounded reciprocal, the same bits as 1.0f / x
+    // without the division sequence (this test runs in the ratio-tracking loop)
+    const float oo[3] = {o.x, o.y, o.z}, inv[3] = {__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z)};
     for (int i = 0; i < 3; i++) {
         float tn = (v.pmin[i] - oo[i]) * inv[i];
         float tf = (v.pmax[i] - oo[i]) * inv[i];
