@@ -51,6 +51,17 @@ def test_scenes_created_together_equal_scenes_created_alone(ctx):
         g.close()
 
 
+def test_one_description_twice(ctx):
+    # both creations copy the same caller's density grid (8 MB, page-locked
+    # for its copy) at once: two equal scenes
+    sc = scenes.volume_scene(width=24, height=24, spp=2, grid=128)
+    a, b = gpu.create_scenes(ctx, [sc, sc])
+    assert a.info().num_wide_nodes == b.info().num_wide_nodes
+    np.testing.assert_array_equal(a.render(seed=3)[0], b.render(seed=3)[0])
+    a.close()
+    b.close()
+
+
 def test_a_bad_description_keeps_no_scene(ctx):
     scs = pool()[:3]
     bad = copy.deepcopy(scs[1])
